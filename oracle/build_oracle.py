@@ -1,0 +1,45 @@
+"""Build recipe for the oracle (TEST INFRASTRUCTURE ONLY).
+
+* ``lib/libvsl_oracle.so`` from ``vsl_oracle.c`` (the C restatement), always;
+* ``_ref/libvsl_ref.so`` from the reference's own kernel sources via ``ref/Makefile``, only
+  where the reference checkout is present (it is read in place, never copied).
+
+Both are built for the machine this runs on (x86 here, Arm on the GPU host).
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REFERENCE_KERNELS = "/root/reference/src/7_0_paper/2_0_Vesicle/CUDA_Code"
+
+CFLAGS = ["-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-std=c11", "-Wall"]
+
+
+def build_port(force: bool = False) -> str:
+    src = os.path.join(HERE, "vsl_oracle.c")
+    out = os.path.join(HERE, "lib", "libvsl_oracle.so")
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    if force or not os.path.exists(out) or os.path.getmtime(out) < max(
+        os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "vsl_oracle.h"))
+    ):
+        subprocess.run(["gcc", *CFLAGS, "-o", out, src, "-lm"], check=True)
+    return out
+
+
+def build_ref() -> str | None:
+    """Compile the reference kernels for the host; None when the checkout is absent."""
+    if not os.path.isdir(REFERENCE_KERNELS):
+        return None
+    subprocess.run(["make", "-s", "-j8", "-C", os.path.join(HERE, "ref"), f"REF={REFERENCE_KERNELS}"], check=True)
+    return os.path.join(HERE, "_ref", "libvsl_ref.so")
+
+
+def build() -> None:
+    build_port()
+    build_ref()
+
+
+if __name__ == "__main__":
+    build()

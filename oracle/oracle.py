@@ -1,0 +1,413 @@
+"""CPU oracle for the level-set hot path -- TEST INFRASTRUCTURE ONLY.
+
+Two interchangeable kernel sets with the reference kernels' names and argument order:
+
+* ``kernels("port")``  -- ``vsl_oracle.c``, this repository's C restatement;
+* ``kernels("ref")``   -- the reference's own ``.cu`` files compiled for the host by
+  ``oracle/ref/Makefile`` into ``oracle/_ref/`` (only where the reference checkout exists).
+
+On top of either set, the functions below restate the MATLAB glue of the reference's
+``SD.SDF3`` class (setDistance, the TVD-RK3 loops, the extension normals, the closest-point
+surface redistance, area/volume/surface integrals) with numpy float64 arithmetic.
+
+Arrays are numpy float64 of shape (rows, cols, pges) in Fortran (column-major) order, the
+reference's memory layout: element (i, j, k) = row (y), column (x), page (z).
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg use this
+module.  The product (the CUDA library) never imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_LIB = os.path.join(HERE, "lib", "libvsl_oracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libvsl_ref.so")
+
+_D = ctypes.c_double
+_I = ctypes.c_int
+_P = ctypes.c_void_p
+
+# name -> argument kinds ('p' pointer, 'i' int, 'd' double), reference prototype order
+SIGNATURES = {
+    "boundary_location": "pppppppiiiiddd",
+    "cubic_boundary_correction": "pppppppiiiiddd",
+    "re_step": "ppppppppppiiidddi",
+    "re_step_eno3": "ppppppppppiiidddi",
+    "upwind_normal": "ppppppppppiiidddi",
+    "upwind_normal_eno3": "ppppppppppiiidddi",
+    "boundary_interpolant": "pppppppppppppiiidddi",
+    "boundary_interpolate_eno3": "pppppppppppppiiidddi",
+    "extend_step": "ppppppppppppppppppiiidddi",
+    "extend_step_eno3": "ppppppppppppppppppiiidddi",
+    "advection_step": "pppppiiiddd",
+    "weno_derivative": "pppppppiiiddd",
+    "set_calculus_toolbox": "ppppppppppppppppppppiiiddddi",
+}
+_KIND = {"p": _P, "i": _I, "d": _D}
+
+
+class KernelSet:
+    """ctypes front end of one kernel library; methods take numpy arrays for pointers."""
+
+    def __init__(self, path: str, prefix: str):
+        if not os.path.exists(path):
+            raise FileNotFoundError(f"oracle library not built: {path}")
+        self.path = path
+        self.lib = ctypes.CDLL(path)
+        self._fns = {}
+        for name, sig in SIGNATURES.items():
+            fn = getattr(self.lib, prefix + name)
+            fn.argtypes = [_KIND[c] for c in sig]
+            fn.restype = None
+            self._fns[name] = (fn, sig)
+
+    def __getattr__(self, name):
+        if name.startswith("_") or name not in SIGNATURES:
+            raise AttributeError(name)
+        fn, sig = self._fns[name]
+
+        def call(*args):
+            if len(args) != len(sig):
+                raise TypeError(f"{name}: expected {len(sig)} arguments, got {len(args)}")
+            conv = []
+            for a, c in zip(args, sig):
+                if c == "p":
+                    if not (isinstance(a, np.ndarray) and a.flags.f_contiguous):
+                        raise TypeError(f"{name}: array arguments must be Fortran-ordered numpy arrays")
+                    conv.append(a.ctypes.data)
+                elif c == "i":
+                    conv.append(int(a))
+                else:
+                    conv.append(float(a))
+            fn(*conv)
+
+        return call
+
+
+_CACHE: dict = {}
+
+
+def kernels(which: str = "port") -> KernelSet:
+    """The restatement ("port") or the reference host build ("ref")."""
+    if which not in _CACHE:
+        if which == "port":
+            _CACHE[which] = KernelSet(PORT_LIB, "orc_")
+        elif which == "ref":
+            _CACHE[which] = KernelSet(REF_LIB, "ref_")
+        else:
+            raise ValueError(which)
+    return _CACHE[which]
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_LIB)
+
+
+# ---------------------------------------------------------------------------------------
+# grid metadata: V/+SD/@GD3/GD3.m:86-106
+# ---------------------------------------------------------------------------------------
+
+
+@dataclass
+class Grid:
+    rows: int
+    cols: int
+    pges: int
+    dx: float
+    dy: float
+    dz: float
+
+    @property
+    def ds(self) -> float:
+        return (self.dx + self.dy + self.dz) / 3
+
+    @property
+    def size(self):
+        return (self.rows, self.cols, self.pges)
+
+    @property
+    def num_ele(self) -> int:
+        return self.rows * self.cols * self.pges
+
+    def args(self):
+        return (self.rows, self.cols, self.pges, self.dx, self.dy, self.dz)
+
+
+def meshgrid(xv, yv, zv):
+    """MATLAB meshgrid(xv, yv, zv): arrays of shape (len(yv), len(xv), len(zv)), F order."""
+    x, y, z = np.meshgrid(np.asarray(xv, float), np.asarray(yv, float), np.asarray(zv, float))
+    return np.asfortranarray(x), np.asfortranarray(y), np.asfortranarray(z)
+
+
+def grid_from_mesh(x, y, z) -> Grid:
+    """Dx = X(1,2,1)-X(1,1,1), Dy = Y(2,1,1)-Y(1,1,1), Dz = Z(1,1,2)-Z(1,1,1)."""
+    r, c, p = x.shape
+    return Grid(r, c, p, float(x[0, 1, 0] - x[0, 0, 0]), float(y[1, 0, 0] - y[0, 0, 0]), float(z[0, 0, 1] - z[0, 0, 0]))
+
+
+def zeros(g: Grid):
+    return np.zeros(g.size, order="F")
+
+
+def full(g: Grid, v: float):
+    return np.full(g.size, v, order="F")
+
+
+def F64(a):
+    return np.asfortranarray(np.asarray(a, dtype=np.float64))
+
+
+# ---------------------------------------------------------------------------------------
+# setDistance: V/+SD/@SDF3/setDistance.m:5-21
+# ---------------------------------------------------------------------------------------
+
+
+@dataclass
+class Distances:
+    xpr: np.ndarray
+    xpl: np.ndarray
+    ypf: np.ndarray
+    ypb: np.ndarray
+    zpu: np.ndarray
+    zpd: np.ndarray
+
+    def six(self):
+        return (self.xpr, self.xpl, self.ypf, self.ypb, self.zpu, self.zpd)
+
+    @property
+    def min_dist(self):
+        return np.minimum(np.minimum(self.xpr, self.xpl), np.minimum(np.minimum(self.ypf, self.ypb), np.minimum(self.zpu, self.zpd)))
+
+
+def set_distance(K: KernelSet, g: Grid, F, cubic: bool = False) -> Distances:
+    """Distances to the interface along the six grid directions (Delta where none)."""
+    F = F64(F)
+    d = Distances(full(g, g.dx), full(g, g.dx), full(g, g.dy), full(g, g.dy), full(g, g.dz), full(g, g.dz))
+    fn = K.cubic_boundary_correction if cubic else K.boundary_location
+    fn(*d.six(), F, g.num_ele, *g.args())
+    return d
+
+
+# ---------------------------------------------------------------------------------------
+# TVD-RK3 reinitialization: V/+SD/@SDF3/WENO5RK3Reinitialization.m:3-43 and
+# V/+SD/@SDF3/WENORK3Reinitialization.m:3-61
+# ---------------------------------------------------------------------------------------
+
+
+def _rk3(F, stage):
+    """Shu-Osher TVD-RK3 exactly as the MATLAB loops combine the stages."""
+    step = stage(F)
+    t1 = F - step
+    step = stage(t1)
+    t2 = t1 - step
+    t05 = 3.0 / 4.0 * F + 1.0 / 4.0 * t2
+    step = stage(t05)
+    t15 = t05 - step
+    return 1.0 / 3.0 * F + 2.0 / 3.0 * t15
+
+
+def reinit_weno5(K, g: Grid, F, iteration: int, dist: Distances):
+    """WENO5RK3Reinitialization(F, iteration) with the object's cached distances."""
+    F = F64(F).copy(order="F")
+    mask = np.asfortranarray(F < 0)
+    deltat = F64(0.3 * dist.min_dist)
+    step = zeros(g)
+
+    def stage(Fs):
+        K.re_step(step, F64(Fs), mask, deltat, *dist.six(), *g.args(), g.num_ele)
+        return step.copy(order="F")
+
+    for _ in range(iteration):
+        F = F64(_rk3(F, stage))
+    return F
+
+
+def reinit_eno3(K, g: Grid, F, iteration: int):
+    """WENORK3Reinitialization(F, iteration): cubic distances recomputed from F."""
+    F = F64(F).copy(order="F")
+    mask = np.asfortranarray(F < 0)
+    dist = set_distance(K, g, F, cubic=True)
+    deltat = F64(0.3 * dist.min_dist)
+    step = zeros(g)
+
+    def stage(Fs):
+        K.re_step_eno3(step, F64(Fs), mask, deltat, *dist.six(), *g.args(), g.num_ele)
+        return step.copy(order="F")
+
+    for _ in range(iteration):
+        F = F64(_rk3(F, stage))
+    return F
+
+
+# ---------------------------------------------------------------------------------------
+# extension: V/+SD/@SDF3/WENO5RK3Extend.m:9-76 and V/+SD/@SDF3/WENORK3Extend.m:9-98
+# ---------------------------------------------------------------------------------------
+
+
+def extension_velocity(K, g: Grid, F, dist: Distances, eno3: bool = False, floor: float = 1e-6):
+    """v = sign(F) * n, n = upwind gradient / max(|gradient|, floor)."""
+    fx, fy, fz = zeros(g), zeros(g), zeros(g)
+    fn = K.upwind_normal_eno3 if eno3 else K.upwind_normal
+    fn(fx, fy, fz, F64(F), *dist.six(), *g.args(), g.num_ele)
+    grad = np.maximum(np.sqrt(fx ** 2 + fy ** 2 + fz ** 2), floor)
+    s = np.sign(F)
+    return F64(s * (fx / grad)), F64(s * (fy / grad)), F64(s * (fz / grad))
+
+
+def crossing_values(K, g: Grid, C, dist: Distances, eno3: bool = False):
+    cp = [zeros(g) for _ in range(6)]
+    fn = K.boundary_interpolate_eno3 if eno3 else K.boundary_interpolant
+    fn(*cp, *dist.six(), F64(C), *g.args(), g.num_ele)
+    return cp
+
+
+def extend_loop(K, g: Grid, C, iteration, dist: Distances, v, deltat, cp, eno3: bool = False):
+    step = zeros(g)
+    fn = K.extend_step_eno3 if eno3 else K.extend_step
+
+    def stage(Cs):
+        fn(step, deltat, F64(Cs), *v, *dist.six(), *cp, *g.args(), g.num_ele)
+        return step.copy(order="F")
+
+    C = F64(C).copy(order="F")
+    for _ in range(iteration):
+        C = F64(_rk3(C, stage))
+    return C
+
+
+def extend_weno5(K, g: Grid, F, dist: Distances, C, iteration: int):
+    """WENO5RK3Extend(C, iteration) with the object's cached distances of F."""
+    v = extension_velocity(K, g, F, dist)
+    cp = crossing_values(K, g, C, dist)
+    deltat = F64(0.3 * dist.min_dist)
+    return extend_loop(K, g, C, iteration, dist, v, deltat, cp)
+
+
+def extend_eno3(K, g: Grid, F, C, iteration: int):
+    """WENORK3Extend(C, iteration): cubic distances of F recomputed inside."""
+    dist = set_distance(K, g, F, cubic=True)
+    v = extension_velocity(K, g, F, dist, eno3=True)
+    cp = crossing_values(K, g, C, dist, eno3=True)
+    deltat = F64(0.3 * dist.min_dist)
+    return extend_loop(K, g, C, iteration, dist, v, deltat, cp, eno3=True)
+
+
+# ---------------------------------------------------------------------------------------
+# closest-point surface redistance: V/+SD/@SDF3/WENO5RK3ClosetPointSurfaceRedistance.m:4-157
+# ---------------------------------------------------------------------------------------
+
+
+def surface_redistance(K, g: Grid, F, A, iter1: int, iter2: int):
+    A = F64(A).copy(order="F")
+    dA = set_distance(K, g, A)
+    deltat = F64(0.3 * dA.min_dist)
+    mask = np.asfortranarray(A < 0)
+    dF = set_distance(K, g, F)
+    fdeltat = F64(0.3 * dF.min_dist)
+    v = extension_velocity(K, g, F, dF, floor=1e-14)
+    step = zeros(g)
+
+    def ext(C):
+        cp = crossing_values(K, g, C, dF)
+        return extend_loop(K, g, C, iter2, dF, v, fdeltat, cp)
+
+    def re(Cs):
+        K.re_step(step, F64(Cs), mask, deltat, *dA.six(), *g.args(), g.num_ele)
+        return step.copy(order="F")
+
+    new = A
+    for _ in range(iter1):
+        new = ext(new)
+        t1 = new - re(new)
+        t1 = ext(t1)
+        t2 = t1 - re(t1)
+        t05 = 3.0 / 4.0 * new + 1.0 / 4.0 * t2
+        t05 = ext(t05)
+        t15 = t05 - re(t05)
+        new = F64(1.0 / 3.0 * new + 2.0 / 3.0 * t15)
+    return ext(new)
+
+
+# ---------------------------------------------------------------------------------------
+# calculus toolbox and reductions: V/+SD/@SDF3/GPUsetCalculusToolBox.m:2-42, SDF3.m:73-85
+# ---------------------------------------------------------------------------------------
+
+TOOLBOX_FIELDS = ("Fx", "Fy", "Fz", "FGradMag", "Nx", "Ny", "Nz", "Fxx", "Fyy", "Fzz", "Fxy", "Fyz", "Fzx",
+                  "FLaplacian", "MeanCurvature", "GaussianCurvature", "Heaviside", "DiracDelta")
+
+
+def calculus_toolbox(K, g: Grid, F):
+    F = F64(F)
+    hp = F64(np.maximum(F, 0))
+    out = {n: zeros(g) for n in TOOLBOX_FIELDS}
+    K.set_calculus_toolbox(*[out[n] for n in TOOLBOX_FIELDS], F, hp, *g.args(), g.ds, g.num_ele)
+    return out
+
+
+def exact_sum(a) -> float:
+    """Correctly rounded sum (the oracle's reduction; any summation order approximates it)."""
+    return math.fsum(np.asarray(a, dtype=np.float64).ravel(order="F").tolist())
+
+
+def cal_area(g: Grid, F, delta) -> float:
+    mask = np.abs(F) < 2 * g.ds
+    return exact_sum(delta[mask]) * g.ds ** 3
+
+
+def cal_volume(g: Grid, F, heaviside) -> float:
+    mask = F < 2 * g.ds
+    return exact_sum(1 - heaviside[mask]) * g.ds ** 3
+
+
+def surface_integral(g: Grid, F, field, delta, gradmag) -> float:
+    mask = np.abs(F) < 2 * g.ds
+    return exact_sum(field[mask] * delta[mask] * gradmag[mask]) * g.ds ** 3
+
+
+# ---------------------------------------------------------------------------------------
+# WENO5 advection (GD3.WENODotGrad, V/+SD/@GD3/GD3.m:393-398) in a TVD-RK3 wrapper
+# ---------------------------------------------------------------------------------------
+
+
+def weno_dot_grad(K, g: Grid, vx, vy, vz, field):
+    out = zeros(g)
+    K.advection_step(out, F64(vx), F64(vy), F64(vz), F64(field), *g.args())
+    return out
+
+
+def advect_rk3(K, g: Grid, F, vx, vy, vz, dt: float, steps: int = 1):
+    """phi_t + v.grad(phi) = 0, each stage F_s - dt*(v.grad F_s), Shu-Osher combination."""
+    def stage(Fs):
+        return dt * weno_dot_grad(K, g, vx, vy, vz, Fs)
+
+    F = F64(F).copy(order="F")
+    for _ in range(steps):
+        F = F64(_rk3(F, stage))
+    return F
+
+
+# ---------------------------------------------------------------------------------------
+# composite vesicle step (order of V/p00_test_singlephase_relax.m:60-196)
+# ---------------------------------------------------------------------------------------
+
+
+def vesicle_step(K, g: Grid, F, dist: Distances, ext_iters=30, reinit_iters=20, cfl=0.5):
+    """One step: toolbox -> area/volume -> extend mean curvature -> dt -> WENO5 RK3 advection
+    along v = Vn*N -> setDistance -> WENO5 reinitialization.  Returns (F, dist, info)."""
+    tb = calculus_toolbox(K, g, F)
+    area = cal_area(g, F, tb["DiracDelta"])
+    volume = cal_volume(g, F, tb["Heaviside"])
+    vn = extend_weno5(K, g, F, dist, tb["MeanCurvature"], ext_iters)
+    band = np.abs(F) < 2 * g.ds
+    vmax = float(np.max(np.abs(vn[band])))
+    dt = cfl * g.ds / vmax
+    F = advect_rk3(K, g, F, vn * tb["Nx"], vn * tb["Ny"], vn * tb["Nz"], dt)
+    dist = set_distance(K, g, F)
+    F = reinit_weno5(K, g, F, reinit_iters, dist)
+    return F, dist, {"area": area, "volume": volume, "dt": dt, "vmax": vmax}
