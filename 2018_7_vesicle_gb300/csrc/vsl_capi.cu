@@ -1,0 +1,501 @@
+// vsl_capi.cu -- method-level entry points of the C ABI (include/vsl_gb300.h): argument
+// checks, workspace carving and the launch sequences of the TVD-RK3 loops.  Everything
+// is enqueued on the caller's stream; nothing here allocates or synchronises.
+#include <cmath>
+#include <type_traits>
+
+#include "vsl_internal.h"
+
+namespace vsl {
+namespace {
+
+// ---------------------------------------------------------------------------------------
+// workspace: a bump allocator over the caller's buffer (256-byte aligned pieces); with a
+// null base it only measures
+// ---------------------------------------------------------------------------------------
+struct Bump {
+    char *base;
+    size_t used = 0;
+    explicit Bump(void *b) : base(static_cast<char *>(b)) {}
+    template <typename U> U *take(long long n)
+    {
+        used = (used + 255) & ~size_t(255);
+        U *p = base ? reinterpret_cast<U *>(base + used) : nullptr;
+        used += sizeof(U) * (size_t)n;
+        return p;
+    }
+};
+
+template <typename T> struct ReinitWork {
+    T *b, *c;
+    uint8_t *flags;
+    Ptr6<T> dist;  // ENO3 only
+};
+template <typename T> ReinitWork<T> carve_reinit(Bump &w, const Grid &g, bool own_dist)
+{
+    ReinitWork<T> r{};
+    r.b = w.take<T>(g.num);
+    r.c = w.take<T>(g.num);
+    r.flags = w.take<uint8_t>(g.num);
+    for (int q = 0; q < 6; ++q) r.dist.p[q] = own_dist ? w.take<T>(g.num) : nullptr;
+    return r;
+}
+
+template <typename T> struct ExtendWork {
+    Ptr3<T> v;
+    Ptr6<T> cp;
+    T *b, *c;
+    uint8_t *flags;
+    Ptr6<T> dist;  // ENO3 only
+};
+template <typename T> ExtendWork<T> carve_extend(Bump &w, const Grid &g, bool own_dist)
+{
+    ExtendWork<T> e{};
+    for (int q = 0; q < 3; ++q) e.v.p[q] = w.take<T>(g.num);
+    for (int q = 0; q < 6; ++q) e.cp.p[q] = w.take<T>(g.num);
+    e.b = w.take<T>(g.num);
+    e.c = w.take<T>(g.num);
+    e.flags = w.take<uint8_t>(g.num);
+    for (int q = 0; q < 6; ++q) e.dist.p[q] = own_dist ? w.take<T>(g.num) : nullptr;
+    return e;
+}
+
+template <typename T> struct RedistWork {
+    ExtendWork<T> ext;  // F's distances in ext.dist
+    ReinitWork<T> re;   // A's distances in re.dist
+};
+template <typename T> RedistWork<T> carve_redist(Bump &w, const Grid &g)
+{
+    RedistWork<T> r;
+    r.ext = carve_extend<T>(w, g, true);
+    r.re = carve_reinit<T>(w, g, true);
+    return r;
+}
+
+struct ReduceWork {
+    double *partials;
+    double *scalars;  // dt, vmax
+};
+ReduceWork carve_reduce(Bump &w, const Grid &g, int ncomp)
+{
+    ReduceWork r;
+    r.partials = w.take<double>((long long)ncomp * toolbox_partial_blocks(g));
+    r.scalars = w.take<double>(4);
+    return r;
+}
+
+template <typename T> struct StepWork {
+    T *vn;
+    Ptr3<T> nrm;
+    ExtendWork<T> ext;
+    ReduceWork red;
+};
+template <typename T> StepWork<T> carve_step(Bump &w, const Grid &g)
+{
+    StepWork<T> s;
+    s.vn = w.take<T>(g.num);
+    for (int q = 0; q < 3; ++q) s.nrm.p[q] = w.take<T>(g.num);
+    s.ext = carve_extend<T>(w, g, false);
+    s.red = carve_reduce(w, g, 2);
+    return s;
+}
+
+size_t measure(int op, const Grid &g, int elem)
+{
+    Bump w(nullptr);
+    auto run = [&](auto tag) {
+        using T = decltype(tag);
+        switch (op) {
+        case VSL_OP_REINIT_WENO5: carve_reinit<T>(w, g, false); break;
+        case VSL_OP_REINIT_ENO3: carve_reinit<T>(w, g, true); break;
+        case VSL_OP_EXTEND_WENO5: carve_extend<T>(w, g, false); break;
+        case VSL_OP_EXTEND_ENO3: carve_extend<T>(w, g, true); break;
+        case VSL_OP_SURFACE_REDISTANCE: carve_redist<T>(w, g); break;
+        case VSL_OP_AREA_VOLUME: carve_reduce(w, g, 2); break;
+        case VSL_OP_ADVECTION: carve_reinit<T>(w, g, false); break;
+        case VSL_OP_VESICLE_STEP: carve_step<T>(w, g); break;
+        default: return false;
+        }
+        return true;
+    };
+    bool ok = elem == 8 ? run(double{}) : (elem == 4 ? run(float{}) : false);
+    return ok ? ((w.used + 255) & ~size_t(255)) : 0;
+}
+
+// ---------------------------------------------------------------------------------------
+// checks
+// ---------------------------------------------------------------------------------------
+template <typename... P> bool any_null(P... p) { return ((p == nullptr) || ...); }
+
+int check_ws(int op, const Grid &g, int elem, void *ws, size_t bytes)
+{
+    if (ws == nullptr) return VSL_ERR_WORKSPACE;
+    if (reinterpret_cast<uintptr_t>(ws) % 256 != 0) return VSL_ERR_WORKSPACE;
+    if (bytes < measure(op, g, elem)) return VSL_ERR_WORKSPACE;
+    return VSL_OK;
+}
+
+#define VSL_TRY(expr)                                                                                              \
+    do {                                                                                                           \
+        cudaError_t e_ = (expr);                                                                                   \
+        if (e_ != cudaSuccess) return VSL_ERR_CUDA;                                                                \
+    } while (0)
+
+template <typename T> constexpr bool fast_form() { return std::is_same<T, float>::value; }
+
+template <typename T> Ptr6<const T> cview(const Ptr6<T> &p)
+{
+    Ptr6<const T> r;
+    for (int q = 0; q < 6; ++q) r.p[q] = p.p[q];
+    return r;
+}
+template <typename T> Ptr3<const T> cview3(const Ptr3<T> &p)
+{
+    Ptr3<const T> r;
+    for (int q = 0; q < 3; ++q) r.p[q] = p.p[q];
+    return r;
+}
+
+// ---------------------------------------------------------------------------------------
+// loops
+// ---------------------------------------------------------------------------------------
+
+// `iters` TVD-RK3 reinitialization pseudo-steps of F in place (flags already classified)
+template <typename T>
+int reinit_loop(T *F, int iters, Ptr6<const T> d, const ReinitWork<T> &w, const Grid &g, bool eno3, cudaStream_t s)
+{
+    const bool fast = fast_form<T>();
+    for (int it = 0; it < iters; ++it) {
+        VSL_TRY(launch_reinit_stage<T>(F, F, w.b, w.flags, d, g, 0, eno3, fast, s));
+        VSL_TRY(launch_reinit_stage<T>(w.b, F, w.c, w.flags, d, g, 1, eno3, fast, s));
+        VSL_TRY(launch_reinit_stage<T>(w.c, F, F, w.flags, d, g, 2, eno3, fast, s));
+    }
+    return VSL_OK;
+}
+
+// velocity and node classes of an extension off the zero set of F (distances d)
+template <typename T>
+int extend_setup(const T *F, Ptr6<const T> d, const ExtendWork<T> &w, const Grid &g, bool eno3, double floor,
+                 cudaStream_t s)
+{
+    VSL_TRY(launch_extension_velocity<T>(F, d, w.v, g, eno3, floor, s));
+    VSL_TRY(launch_classify<T>(F, d, w.flags, g, s));
+    return VSL_OK;
+}
+
+// crossing values of C, then `iters` TVD-RK3 extension pseudo-steps of C in place
+template <typename T>
+int extend_loop(T *C, int iters, Ptr6<const T> d, const ExtendWork<T> &w, const Grid &g, bool eno3, cudaStream_t s)
+{
+    const bool fast = fast_form<T>();
+    VSL_TRY(launch_crossing<T>(C, d, w.cp, g, eno3, s));
+    Ptr6<const T> cp = cview(w.cp);
+    Ptr3<const T> v = cview3(w.v);
+    for (int it = 0; it < iters; ++it) {
+        VSL_TRY(launch_extend_stage<T>(C, C, w.b, w.flags, d, cp, v, g, 0, eno3, fast, s));
+        VSL_TRY(launch_extend_stage<T>(w.b, C, w.c, w.flags, d, cp, v, g, 1, eno3, fast, s));
+        VSL_TRY(launch_extend_stage<T>(w.c, C, C, w.flags, d, cp, v, g, 2, eno3, fast, s));
+    }
+    return VSL_OK;
+}
+
+template <typename T>
+int advect_loop(T *F, Ptr3<const T> v, const T *speed, const double *dt, int steps, const ReinitWork<T> &w,
+                const Grid &g, cudaStream_t s)
+{
+    const bool fast = fast_form<T>();
+    for (int it = 0; it < steps; ++it) {
+        VSL_TRY(launch_advect_stage<T>(F, F, w.b, v, speed, dt, g, 0, fast, s));
+        VSL_TRY(launch_advect_stage<T>(w.b, F, w.c, v, speed, dt, g, 1, fast, s));
+        VSL_TRY(launch_advect_stage<T>(w.c, F, F, v, speed, dt, g, 2, fast, s));
+    }
+    return VSL_OK;
+}
+
+template <typename T> Ptr6<const T> six(const T *a, const T *b, const T *c, const T *d, const T *e, const T *f)
+{
+    return Ptr6<const T>{{a, b, c, d, e, f}};
+}
+
+// ---------------------------------------------------------------------------------------
+// operations (templated on the field type)
+// ---------------------------------------------------------------------------------------
+
+template <typename T>
+int op_set_distance(const T *F, T *xpr, T *xpl, T *ypf, T *ypb, T *zpu, T *zpd, int rows, int cols, int pges,
+                    double dx, double dy, double dz, cudaStream_t s)
+{
+    if (any_null(F, xpr, xpl, ypf, ypb, zpu, zpd)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    VSL_TRY(launch_set_distance<T>(F, Ptr6<T>{{xpr, xpl, ypf, ypb, zpu, zpd}}, g, true, s));
+    return VSL_OK;
+}
+
+template <typename T>
+int op_reinit_weno5(T *F, int iteration, const T *xpr, const T *xpl, const T *ypf, const T *ypb, const T *zpu,
+                    const T *zpd, int rows, int cols, int pges, double dx, double dy, double dz, void *ws,
+                    size_t bytes, cudaStream_t s)
+{
+    if (any_null(F, xpr, xpl, ypf, ypb, zpu, zpd)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    if (iteration < 0) return VSL_ERR_VALUE;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    if (int st = check_ws(VSL_OP_REINIT_WENO5, g, sizeof(T), ws, bytes)) return st;
+    Bump b(ws);
+    ReinitWork<T> w = carve_reinit<T>(b, g, false);
+    Ptr6<const T> d = six(xpr, xpl, ypf, ypb, zpu, zpd);
+    VSL_TRY(launch_classify<T>(F, d, w.flags, g, s));
+    return reinit_loop<T>(F, iteration, d, w, g, false, s);
+}
+
+template <typename T>
+int op_reinit_eno3(T *F, int iteration, int rows, int cols, int pges, double dx, double dy, double dz, void *ws,
+                   size_t bytes, cudaStream_t s)
+{
+    if (any_null(F)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    if (iteration < 0) return VSL_ERR_VALUE;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    if (int st = check_ws(VSL_OP_REINIT_ENO3, g, sizeof(T), ws, bytes)) return st;
+    Bump b(ws);
+    ReinitWork<T> w = carve_reinit<T>(b, g, true);
+    VSL_TRY(launch_set_distance<T>(F, w.dist, g, false, s));
+    Ptr6<const T> d = cview(w.dist);
+    VSL_TRY(launch_classify<T>(F, d, w.flags, g, s));
+    return reinit_loop<T>(F, iteration, d, w, g, true, s);
+}
+
+template <typename T>
+int op_extend_weno5(T *C, int iteration, const T *F, const T *xpr, const T *xpl, const T *ypf, const T *ypb,
+                    const T *zpu, const T *zpd, int rows, int cols, int pges, double dx, double dy, double dz,
+                    void *ws, size_t bytes, cudaStream_t s)
+{
+    if (any_null(C, F, xpr, xpl, ypf, ypb, zpu, zpd)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    if (iteration < 0) return VSL_ERR_VALUE;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    if (int st = check_ws(VSL_OP_EXTEND_WENO5, g, sizeof(T), ws, bytes)) return st;
+    Bump b(ws);
+    ExtendWork<T> w = carve_extend<T>(b, g, false);
+    Ptr6<const T> d = six(xpr, xpl, ypf, ypb, zpu, zpd);
+    if (int st = extend_setup<T>(F, d, w, g, false, 1e-6, s)) return st;
+    return extend_loop<T>(C, iteration, d, w, g, false, s);
+}
+
+template <typename T>
+int op_extend_eno3(T *C, int iteration, const T *F, int rows, int cols, int pges, double dx, double dy, double dz,
+                   void *ws, size_t bytes, cudaStream_t s)
+{
+    if (any_null(C, F)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    if (iteration < 0) return VSL_ERR_VALUE;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    if (int st = check_ws(VSL_OP_EXTEND_ENO3, g, sizeof(T), ws, bytes)) return st;
+    Bump b(ws);
+    ExtendWork<T> w = carve_extend<T>(b, g, true);
+    VSL_TRY(launch_set_distance<T>(F, w.dist, g, false, s));
+    Ptr6<const T> d = cview(w.dist);
+    if (int st = extend_setup<T>(F, d, w, g, true, 1e-6, s)) return st;
+    return extend_loop<T>(C, iteration, d, w, g, true, s);
+}
+
+template <typename T>
+int op_redistance(T *A, int iter1, int iter2, const T *F, int rows, int cols, int pges, double dx, double dy,
+                  double dz, void *ws, size_t bytes, cudaStream_t s)
+{
+    if (any_null(A, F)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    if (iter1 < 0 || iter2 < 0) return VSL_ERR_VALUE;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    if (int st = check_ws(VSL_OP_SURFACE_REDISTANCE, g, sizeof(T), ws, bytes)) return st;
+    Bump b(ws);
+    RedistWork<T> w = carve_redist<T>(b, g);
+    // reinitialization part: distances of A, mask A < 0 (ClosetPointSurfaceRedistance.m:15-25)
+    VSL_TRY(launch_set_distance<T>(A, w.re.dist, g, true, s));
+    Ptr6<const T> dA = cview(w.re.dist);
+    VSL_TRY(launch_classify<T>(A, dA, w.re.flags, g, s));
+    // extension part: distances and upwind normals of F, floor 1e-14 (:37-74)
+    VSL_TRY(launch_set_distance<T>(F, w.ext.dist, g, true, s));
+    Ptr6<const T> dF = cview(w.ext.dist);
+    if (int st = extend_setup<T>(F, dF, w.ext, g, false, 1e-14, s)) return st;
+    const bool fast = fast_form<T>();
+    // the reinit stages need their own temporaries: the extension uses w.ext.b/c
+    T *t1 = w.re.b, *t2 = w.re.c;
+    for (int it = 0; it < iter1; ++it) {
+        if (int st = extend_loop<T>(A, iter2, dF, w.ext, g, false, s)) return st;
+        VSL_TRY(launch_reinit_stage<T>(A, A, t1, w.re.flags, dA, g, 0, false, fast, s));
+        if (int st = extend_loop<T>(t1, iter2, dF, w.ext, g, false, s)) return st;
+        VSL_TRY(launch_reinit_stage<T>(t1, A, t2, w.re.flags, dA, g, 1, false, fast, s));
+        if (int st = extend_loop<T>(t2, iter2, dF, w.ext, g, false, s)) return st;
+        VSL_TRY(launch_reinit_stage<T>(t2, A, A, w.re.flags, dA, g, 2, false, fast, s));
+    }
+    return extend_loop<T>(A, iter2, dF, w.ext, g, false, s);
+}
+
+template <typename T>
+int op_area_volume(const T *F, double *av, int rows, int cols, int pges, double dx, double dy, double dz, void *ws,
+                   size_t bytes, cudaStream_t s)
+{
+    if (any_null(F, av)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    if (int st = check_ws(VSL_OP_AREA_VOLUME, g, sizeof(T), ws, bytes)) return st;
+    Bump b(ws);
+    ReduceWork r = carve_reduce(b, g, 2);
+    const double ds = (dx + dy + dz) / 3;
+    ToolboxOut<T> none{};
+    int nb = 0;
+    VSL_TRY(launch_toolbox<T>(F, none, g, ds, r.partials, &nb, s));
+    VSL_TRY(launch_sum_partials(r.partials, nb, 2, std::pow(ds, 3), av, s));
+    return VSL_OK;
+}
+
+template <typename T>
+int op_advection(T *F, const T *vx, const T *vy, const T *vz, const double *dt, int steps, int rows, int cols,
+                 int pges, double dx, double dy, double dz, void *ws, size_t bytes, cudaStream_t s)
+{
+    if (any_null(F, vx, vy, vz, dt)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    if (steps < 0) return VSL_ERR_VALUE;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    if (int st = check_ws(VSL_OP_ADVECTION, g, sizeof(T), ws, bytes)) return st;
+    Bump b(ws);
+    ReinitWork<T> w = carve_reinit<T>(b, g, false);
+    return advect_loop<T>(F, Ptr3<const T>{{vx, vy, vz}}, nullptr, dt, steps, w, g, s);
+}
+
+template <typename T>
+int op_vesicle_step(T *F, T *xpr, T *xpl, T *ypf, T *ypb, T *zpu, T *zpd, int ext_iters, int reinit_iters,
+                    double cfl, double *info, int rows, int cols, int pges, double dx, double dy, double dz, void *ws,
+                    size_t bytes, cudaStream_t s)
+{
+    if (any_null(F, xpr, xpl, ypf, ypb, zpu, zpd, info)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    if (ext_iters < 0 || reinit_iters < 0 || !(cfl > 0)) return VSL_ERR_VALUE;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    if (int st = check_ws(VSL_OP_VESICLE_STEP, g, sizeof(T), ws, bytes)) return st;
+    Bump b(ws);
+    StepWork<T> w = carve_step<T>(b, g);
+    const double ds = (dx + dy + dz) / 3;
+    Ptr6<const T> d = six<T>(xpr, xpl, ypf, ypb, zpu, zpd);
+    // calculus toolbox: mean curvature (the normal speed), normals, area and volume
+    ToolboxOut<T> tb{};
+    tb.f[4] = w.nrm.p[0];
+    tb.f[5] = w.nrm.p[1];
+    tb.f[6] = w.nrm.p[2];
+    tb.f[14] = w.vn;
+    int nb = 0;
+    VSL_TRY(launch_toolbox<T>(F, tb, g, ds, w.red.partials, &nb, s));
+    VSL_TRY(launch_sum_partials(w.red.partials, nb, 2, std::pow(ds, 3), info, s));
+    // extend the normal speed off the interface (cached distances of F)
+    if (int st = extend_setup<T>(F, d, w.ext, g, false, 1e-6, s)) return st;
+    if (int st = extend_loop<T>(w.vn, ext_iters, d, w.ext, g, false, s)) return st;
+    // dt = cfl * Ds / max |Vn| over |F| < 2 Ds
+    VSL_TRY(launch_band_maxabs<T>(w.vn, F, 2 * ds, g, w.red.partials, &nb, s));
+    VSL_TRY(launch_time_step(w.red.partials, nb, cfl * ds, info + 2, info + 3, s));
+    // one WENO5 TVD-RK3 advection step along Vn * N
+    ReinitWork<T> tmp{};
+    tmp.b = w.ext.b;
+    tmp.c = w.ext.c;
+    if (int st = advect_loop<T>(F, cview3(w.nrm), w.vn, info + 2, 1, tmp, g, s)) return st;
+    // setDistance, then reinitialization
+    VSL_TRY(launch_set_distance<T>(F, Ptr6<T>{{xpr, xpl, ypf, ypb, zpu, zpd}}, g, true, s));
+    ReinitWork<T> rw{};
+    rw.b = w.ext.b;
+    rw.c = w.ext.c;
+    rw.flags = w.ext.flags;
+    VSL_TRY(launch_classify<T>(F, d, rw.flags, g, s));
+    return reinit_loop<T>(F, reinit_iters, d, rw, g, false, s);
+}
+
+}  // namespace
+}  // namespace vsl
+
+using namespace vsl;
+
+extern "C" {
+
+const char *vsl_status_string(int status)
+{
+    switch (status) {
+    case VSL_OK: return "ok";
+    case VSL_ERR_NULL: return "null pointer argument";
+    case VSL_ERR_SHAPE: return "bad grid shape";
+    case VSL_ERR_VALUE: return "argument value out of range";
+    case VSL_ERR_WORKSPACE: return "workspace missing, too small or not 256-byte aligned";
+    case VSL_ERR_CUDA: return "CUDA launch failed";
+    case VSL_ERR_OP: return "unknown operation";
+    default: return "unknown status";
+    }
+}
+
+int vsl_version(void) { return 1; }
+
+size_t vsl_workspace_bytes(int op, int rows, int cols, int pges, int elem_bytes)
+{
+    if (rows <= 0 || cols <= 0 || pges <= 0) return 0;
+    Grid g = make_grid(rows, cols, pges, 1.0, 1.0, 1.0);
+    return measure(op, g, elem_bytes);
+}
+
+#define VSL_TYPED(SUF, T)                                                                                          \
+    int vsl_set_distance_##SUF(const T *F, T *xpr, T *xpl, T *ypf, T *ypb, T *zpu, T *zpd, int rows, int cols,     \
+                               int pges, double dx, double dy, double dz, vsl_stream_t stream)                     \
+    {                                                                                                              \
+        return op_set_distance<T>(F, xpr, xpl, ypf, ypb, zpu, zpd, rows, cols, pges, dx, dy, dz, stream);          \
+    }                                                                                                              \
+    int vsl_weno5_rk3_reinitialization_##SUF(T *F, int iteration, const T *xpr, const T *xpl, const T *ypf,        \
+                                             const T *ypb, const T *zpu, const T *zpd, int rows, int cols,         \
+                                             int pges, double dx, double dy, double dz, void *ws, size_t bytes,    \
+                                             vsl_stream_t stream)                                                  \
+    {                                                                                                              \
+        return op_reinit_weno5<T>(F, iteration, xpr, xpl, ypf, ypb, zpu, zpd, rows, cols, pges, dx, dy, dz, ws,    \
+                                  bytes, stream);                                                                  \
+    }                                                                                                              \
+    int vsl_wenork3_reinitialization_##SUF(T *F, int iteration, int rows, int cols, int pges, double dx,           \
+                                           double dy, double dz, void *ws, size_t bytes, vsl_stream_t stream)      \
+    {                                                                                                              \
+        return op_reinit_eno3<T>(F, iteration, rows, cols, pges, dx, dy, dz, ws, bytes, stream);                   \
+    }                                                                                                              \
+    int vsl_weno5_rk3_extend_##SUF(T *C, int iteration, const T *F, const T *xpr, const T *xpl, const T *ypf,      \
+                                   const T *ypb, const T *zpu, const T *zpd, int rows, int cols, int pges,         \
+                                   double dx, double dy, double dz, void *ws, size_t bytes, vsl_stream_t stream)   \
+    {                                                                                                              \
+        return op_extend_weno5<T>(C, iteration, F, xpr, xpl, ypf, ypb, zpu, zpd, rows, cols, pges, dx, dy, dz, ws, \
+                                  bytes, stream);                                                                  \
+    }                                                                                                              \
+    int vsl_wenork3_extend_##SUF(T *C, int iteration, const T *F, int rows, int cols, int pges, double dx,         \
+                                 double dy, double dz, void *ws, size_t bytes, vsl_stream_t stream)                \
+    {                                                                                                              \
+        return op_extend_eno3<T>(C, iteration, F, rows, cols, pges, dx, dy, dz, ws, bytes, stream);                \
+    }                                                                                                              \
+    int vsl_weno5_rk3_surface_redistance_##SUF(T *A, int iter1, int iter2, const T *F, int rows, int cols,         \
+                                               int pges, double dx, double dy, double dz, void *ws, size_t bytes,  \
+                                               vsl_stream_t stream)                                                \
+    {                                                                                                              \
+        return op_redistance<T>(A, iter1, iter2, F, rows, cols, pges, dx, dy, dz, ws, bytes, stream);              \
+    }                                                                                                              \
+    int vsl_area_volume_##SUF(const T *F, double *area_volume, int rows, int cols, int pges, double dx, double dy, \
+                              double dz, void *ws, size_t bytes, vsl_stream_t stream)                              \
+    {                                                                                                              \
+        return op_area_volume<T>(F, area_volume, rows, cols, pges, dx, dy, dz, ws, bytes, stream);                 \
+    }                                                                                                              \
+    int vsl_weno5_rk3_advection_##SUF(T *F, const T *vx, const T *vy, const T *vz, const double *dt, int steps,    \
+                                      int rows, int cols, int pges, double dx, double dy, double dz, void *ws,     \
+                                      size_t bytes, vsl_stream_t stream)                                           \
+    {                                                                                                              \
+        return op_advection<T>(F, vx, vy, vz, dt, steps, rows, cols, pges, dx, dy, dz, ws, bytes, stream);         \
+    }                                                                                                              \
+    int vsl_vesicle_step_##SUF(T *F, T *xpr, T *xpl, T *ypf, T *ypb, T *zpu, T *zpd, int ext_iters,                \
+                               int reinit_iters, double cfl, double *info, int rows, int cols, int pges,           \
+                               double dx, double dy, double dz, void *ws, size_t bytes, vsl_stream_t stream)       \
+    {                                                                                                              \
+        return op_vesicle_step<T>(F, xpr, xpl, ypf, ypb, zpu, zpd, ext_iters, reinit_iters, cfl, info, rows, cols, \
+                                  pges, dx, dy, dz, ws, bytes, stream);                                            \
+    }
+
+VSL_TYPED(f64, double)
+VSL_TYPED(f32, float)
+
+}  // extern "C"

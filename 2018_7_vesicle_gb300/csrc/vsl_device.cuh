@@ -1,0 +1,577 @@
+// vsl_device.cuh -- device building blocks of the level-set hot path (sm_103a).
+//
+// Grid layout (the reference's MATLAB layout): ind = k*rows*cols + j*rows + i, with
+// i = row (y, stride 1), j = column (x, stride rows), k = page (z, stride rows*cols).
+// Neighbour coordinates outside the grid are clamped to the edge, as the reference's
+// sub2ind does (CUDA_Code/1_3_WENO5RK3_Reinitialization/shared_utilities.hpp:21-31).
+//
+// Stencil arithmetic is templated on the field type T (double for the plain form, float
+// for the mixed-precision form).  The sub-cell interface distances (polynomial fits and
+// their roots) are always computed in double.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace vsl {
+
+// ---------------------------------------------------------------------------------------
+// grid and indexing
+// ---------------------------------------------------------------------------------------
+
+struct Grid {
+    int rows, cols, pges;
+    long long plane;  // rows * cols
+    long long num;    // rows * cols * pges
+    double dx, dy, dz;
+};
+
+__host__ __device__ inline Grid make_grid(int rows, int cols, int pges, double dx, double dy, double dz)
+{
+    Grid g;
+    g.rows = rows;
+    g.cols = cols;
+    g.pges = pges;
+    g.plane = (long long)rows * cols;
+    g.num = g.plane * pges;
+    g.dx = dx;
+    g.dy = dy;
+    g.dz = dz;
+    return g;
+}
+
+enum Axis { AX_X = 0, AX_Y = 1, AX_Z = 2 };
+
+__device__ __forceinline__ int clampi(int v, int n) { return min(max(v, 0), n - 1); }
+
+__device__ __forceinline__ long long node_index(const Grid &g, int i, int j, int k)
+{
+    return (long long)k * g.plane + (long long)j * g.rows + i;
+}
+
+__device__ __forceinline__ long long clamped_index(const Grid &g, int i, int j, int k)
+{
+    return node_index(g, clampi(i, g.rows), clampi(j, g.cols), clampi(k, g.pges));
+}
+
+// Coordinate, extent and stride of (i,j,k) along an axis; `base` is the index with that
+// coordinate set to zero.
+struct AxisLine {
+    long long base;
+    long long stride;
+    int c, n;
+};
+
+__device__ __forceinline__ AxisLine axis_line(const Grid &g, int i, int j, int k, int ax)
+{
+    AxisLine L;
+    if (ax == AX_X) {
+        L.base = (long long)k * g.plane + i;
+        L.stride = g.rows;
+        L.c = j;
+        L.n = g.cols;
+    } else if (ax == AX_Y) {
+        L.base = (long long)k * g.plane + (long long)j * g.rows;
+        L.stride = 1;
+        L.c = i;
+        L.n = g.rows;
+    } else {
+        L.base = (long long)j * g.rows + i;
+        L.stride = g.plane;
+        L.c = k;
+        L.n = g.pges;
+    }
+    return L;
+}
+
+// Seven values f[c-3 .. c+3] along a line, clamped.
+template <typename T>
+__device__ __forceinline__ void load_line7(const T *__restrict__ f, const AxisLine &L, T p[7])
+{
+#pragma unroll
+    for (int s = -3; s <= 3; ++s) p[s + 3] = __ldg(f + L.base + (long long)clampi(L.c + s, L.n) * L.stride);
+}
+
+__device__ __forceinline__ double axis_h(const Grid &g, int ax) { return ax == AX_X ? g.dx : (ax == AX_Y ? g.dy : g.dz); }
+
+// ---------------------------------------------------------------------------------------
+// scalar helpers (shared_utilities.hpp:5-18): comparisons written as in the reference so
+// ties and signed zeros resolve the same way.
+// ---------------------------------------------------------------------------------------
+
+template <typename T> __device__ __forceinline__ T vmax(T x, T y) { return (x < y) ? y : x; }
+template <typename T> __device__ __forceinline__ T vmin(T x, T y) { return (x < y) ? x : y; }
+template <typename T> __device__ __forceinline__ T minmod(T x, T y)
+{
+    return (x * y < T(0)) ? T(0) : (fabs(x) < fabs(y) ? x : y);
+}
+template <typename T> __device__ __forceinline__ T minabs(T x, T y) { return (fabs(x) < fabs(y)) ? x : y; }
+__device__ __forceinline__ double sgn1(double x) { return (x > 0) ? 1.0 : -1.0; }
+template <typename T> __device__ __forceinline__ T sqr(T x) { return x * x; }
+
+// ---------------------------------------------------------------------------------------
+// sub-cell interface distances, always double
+// ---------------------------------------------------------------------------------------
+
+// Degree-n interpolant through (x[m], y[m]) in monomial form: expand each Lagrange basis
+// term factor by factor (highest power first) and sum per power.  Same construction as
+// Poly<n>::setInterpolation (shared_utilities.hpp:55-103).
+template <int N>
+__device__ __forceinline__ void lagrange_monomial(const double *x, const double *y, double *a)
+{
+    double scale[N + 1], ex[N + 1][N + 1];
+#pragma unroll
+    for (int m = 0; m <= N; ++m) {
+        scale[m] = y[m];
+        ex[m][0] = 1.0;
+#pragma unroll
+        for (int q = 1; q <= N; ++q) ex[m][q] = 0.0;
+        int r = 0;
+#pragma unroll
+        for (int q = 0; q <= N; ++q) {
+            if (q == m) continue;
+            scale[m] /= x[m] - x[q];
+            // multiply the running product by (t - x[q])
+#pragma unroll
+            for (int p = N; p >= 1; --p)
+                if (p <= r + 1) ex[m][p] = ex[m][p] - x[q] * ex[m][p - 1];
+            ++r;
+        }
+    }
+#pragma unroll
+    for (int p = 0; p <= N; ++p) {
+        double acc = 0.0;
+#pragma unroll
+        for (int m = 0; m <= N; ++m) acc += scale[m] * ex[m][N - p];
+        a[p] = acc;
+    }
+}
+
+// sum a[p] t^p, powers accumulated left to right (the reference sums a[p]*pow(t,p)).
+template <int N> __device__ __forceinline__ double poly_eval(const double *a, double t)
+{
+    double v = 0.0, tp = 1.0;
+#pragma unroll
+    for (int p = 0; p <= N; ++p) {
+        v += a[p] * tp;
+        tp *= t;
+    }
+    return v;
+}
+
+// Brent's root finder over [x1, x2] (tolerance tol, at most 100 iterations), the method
+// of zeroin (shared_utilities.hpp:109-173).
+template <int N> __device__ double brent_root(const double *a, double x1, double x2, double tol)
+{
+    double d = 0.0, e = 0.0;
+    double lo = x1, b = x2, c = x2;
+    double flo = poly_eval<N>(a, lo), fb = poly_eval<N>(a, b), fc = fb;
+    for (int it = 0; it < 100; ++it) {
+        if ((fb > 0.0 && fc > 0.0) || (fb < 0.0 && fc < 0.0)) {
+            c = lo;
+            fc = flo;
+            d = b - lo;
+            e = d;
+        }
+        if (fabs(fc) < fabs(fb)) {
+            lo = b;
+            b = c;
+            c = lo;
+            flo = fb;
+            fb = fc;
+            fc = flo;
+        }
+        double xm = 0.5 * (c - b);
+        if (fabs(xm) <= tol || fb == 0.0) return b;
+        if (fabs(e) < tol || fabs(flo) <= fabs(fb)) {
+            d = xm;
+            e = xm;
+        } else {
+            double s = fb / flo, p, q;
+            if (lo == c) {
+                p = 2.0 * xm * s;
+                q = 1.0 - s;
+            } else {
+                double qq = flo / fc, r = fb / fc;
+                p = s * (2.0 * xm * qq * (qq - r) - (b - lo) * (r - 1.0));
+                q = (qq - 1.0) * (r - 1.0) * (s - 1.0);
+            }
+            if (p > 0) q = -q;
+            p = fabs(p);
+            double lim1 = 3.0 * xm * q - fabs(tol * q);
+            double lim2 = fabs(e * q);
+            if (2.0 * p < vmin(lim1, lim2)) {
+                e = d;
+                d = p / q;
+            } else {
+                d = xm;
+                e = d;
+            }
+        }
+        lo = b;
+        flo = fb;
+        if (fabs(d) > tol)
+            b = b + d;
+        else
+            b += sgn1(xm) * tol;
+        fb = poly_eval<N>(a, b);
+    }
+    return b;
+}
+
+// Quadratic ENO distance from node b to the interface between b and c; a before b, d
+// after c (sp, boundary_location.cu:6-20).
+__device__ __forceinline__ double eno2_distance(double a, double b, double c, double d, double h)
+{
+    const double eps = 10e-10;
+    double d2 = minmod(c - 2.0 * b + a, d - 2.0 * c + b);
+    if (d2 > eps || d2 < -eps) {
+        double disc = sqr(0.5 * d2 - b - c) - 4. * b * c;
+        return h * (0.5 + (b - c - sgn1(b - c) * sqrt(disc)) / d2);
+    }
+    return h * b / (b - c);
+}
+
+// Degree-5 fit through samples at 0..5h with the crossing between 2h and 3h; quadratic
+// ENO next to a kink (six_distance, boundary_location.cu:53-80).
+__device__ inline double quintic_distance(const double v[6], double h)
+{
+    if (v[1] * v[2] < 0 || v[3] * v[4] < 0) return eno2_distance(v[1], v[2], v[3], v[4], h);
+    double xs[6] = {0.0, h, 2 * h, 3 * h, 4 * h, 5 * h};
+    double a[6];
+    lagrange_monomial<5>(xs, v, a);
+    double t = brent_root<5>(a, 2 * h, 3 * h, 3e-16);
+    t = vmin(vmax(t, 2 * h), 3 * h);
+    return t - 2 * h;
+}
+
+// Cubic through 0..3h, Newton from the linear guess, at most 50 steps (cubic_distance,
+// weno_rk3_reinitialization.cu:73-116).
+__device__ inline double cubic_newton_distance(double v0, double v1, double v2, double v3, double h)
+{
+    if (v0 * v1 < 0 || v2 * v3 < 0) return eno2_distance(v0, v1, v2, v3, h);
+    double a0 = v0;
+    double a1 = (3.0 * (v1 - v0) - 3.0 / 2.0 * (v2 - v0) + 1.0 / 3.0 * (v3 - v0)) / h;
+    double a2 = (-5.0 / 2.0 * (v1 - v0) + 2.0 * (v2 - v0) - 1.0 / 2.0 * (v3 - v0)) / (h * h);
+    double a3 = (1.0 / 2.0 * (v1 - v0) - 1.0 / 2.0 * (v2 - v0) + 1.0 / 6.0 * (v3 - v0)) / (h * h * h);
+    double t = h + h * v1 / (v1 - v2);
+    double change = 1.0;
+    for (int it = 0; change > 1e-14 && it < 50; ++it) {
+        double f = a0 + a1 * t + a2 * t * t + a3 * t * t * t;
+        double df = a1 + 2 * a2 * t + 3 * a3 * t * t;
+        double r = f / df;
+        change = fabs(r);
+        t = t - r;
+    }
+    t = vmin(vmax(t, h), 2 * h);
+    return t - h;
+}
+
+// Distance from the node at L.c to the interface between it and its +1 neighbour along
+// the line L, as the reference thread of that node computes it (double arithmetic on
+// the promoted samples): degree-5 fit (boundary_location.cu:84-132) or cubic Newton
+// (weno_rk3_reinitialization.cu:251-293).
+template <bool QUINTIC, typename T>
+__device__ __forceinline__ double fore_distance(const T *__restrict__ f, const AxisLine &L, double h)
+{
+    if (QUINTIC) {
+        double v[6];
+#pragma unroll
+        for (int s = -2; s <= 3; ++s) v[s + 2] = (double)__ldg(f + L.base + (long long)clampi(L.c + s, L.n) * L.stride);
+        return quintic_distance(v, h);
+    } else {
+        double v0 = (double)__ldg(f + L.base + (long long)clampi(L.c - 1, L.n) * L.stride);
+        double v1 = (double)__ldg(f + L.base + (long long)L.c * L.stride);
+        double v2 = (double)__ldg(f + L.base + (long long)clampi(L.c + 1, L.n) * L.stride);
+        double v3 = (double)__ldg(f + L.base + (long long)clampi(L.c + 2, L.n) * L.stride);
+        return cubic_newton_distance(v0, v1, v2, v3, h);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// one-sided derivatives
+// ---------------------------------------------------------------------------------------
+
+// Jiang-Shu WENO5 one-sided derivative from five first differences (biased toward v3),
+// in the reference's operation order (re_step.cu:11-37); squares by multiplication.
+template <typename T>
+__device__ __forceinline__ T weno5_plain(T v1, T v2, T v3, T v4, T v5)
+{
+    T q1 = T(1. / 3.) * v1 - T(7. / 6.) * v2 + T(11. / 6.) * v3;
+    T q2 = T(-1. / 6.) * v2 + T(5. / 6.) * v3 + T(1. / 3.) * v4;
+    T q3 = T(1. / 3.) * v3 + T(5. / 6.) * v4 - T(1. / 6.) * v5;
+    T s1 = T(13. / 12.) * sqr(v1 - 2 * v2 + v3) + T(1. / 4.) * sqr(v1 - 4 * v2 + 3 * v3);
+    T s2 = T(13. / 12.) * sqr(v2 - 2 * v3 + v4) + T(1. / 4.) * sqr(v2 - v4);
+    T s3 = T(13. / 12.) * sqr(v3 - 2 * v4 + v5) + T(1. / 4.) * sqr(3 * v3 - 4 * v4 + v5);
+    const T eps = T(1e-6);
+    T a1 = T(0.1) / sqr(s1 + eps);
+    T a2 = T(0.6) / sqr(s2 + eps);
+    T a3 = T(0.3) / sqr(s3 + eps);
+    T tot = a1 + a2 + a3;
+    return (a1 / tot) * q1 + (a2 / tot) * q2 + (a3 / tot) * q3;
+}
+
+// The same reconstruction from UNSCALED differences u = h*v with eps2 = eps*h^2, one
+// division instead of six: with Q_k = (S_k(u) + eps2)^2 the normalised weights are
+// d_k/Q_k / sum, i.e. d_k*Q_l*Q_m / (d_1 Q_2 Q_3 + d_2 Q_1 Q_3 + d_3 Q_1 Q_2); the result
+// is then multiplied by 1/h.  Algebraically identical to weno5_plain(u/h).
+template <typename T>
+__device__ __forceinline__ T weno5_fast(T u1, T u2, T u3, T u4, T u5, T eps2)
+{
+    T q1 = T(1. / 3.) * u1 - T(7. / 6.) * u2 + T(11. / 6.) * u3;
+    T q2 = T(-1. / 6.) * u2 + T(5. / 6.) * u3 + T(1. / 3.) * u4;
+    T q3 = T(1. / 3.) * u3 + T(5. / 6.) * u4 - T(1. / 6.) * u5;
+    T s1 = T(13. / 12.) * sqr(u1 - 2 * u2 + u3) + T(1. / 4.) * sqr(u1 - 4 * u2 + 3 * u3);
+    T s2 = T(13. / 12.) * sqr(u2 - 2 * u3 + u4) + T(1. / 4.) * sqr(u2 - u4);
+    T s3 = T(13. / 12.) * sqr(u3 - 2 * u4 + u5) + T(1. / 4.) * sqr(3 * u3 - 4 * u4 + u5);
+    T Q1 = sqr(s1 + eps2), Q2 = sqr(s2 + eps2), Q3 = sqr(s3 + eps2);
+    T w1 = T(0.1) * (Q2 * Q3), w2 = T(0.6) * (Q1 * Q3), w3 = T(0.3) * (Q1 * Q2);
+    return (w1 * q1 + w2 * q2 + w3 * q3) / (w1 + w2 + w3);
+}
+
+// Seven-point stencil with the interface inserted at r1 (forward) / l1 (backward) when
+// they are shorter than h, carrying the values hf / hb there (select_stencil,
+// re_step.cu:41-77 and shared_utilities.cup:211-247).
+template <typename T>
+__device__ __forceinline__ void insert_interface(const T p[7], T r1, T l1, T h, T hf, T hb, T xs[7], T hs[7])
+{
+    hs[3] = p[3];
+    xs[3] = T(0);
+    if (r1 < h) {
+        xs[4] = r1; xs[5] = h; xs[6] = 2 * h;
+        hs[4] = hf; hs[5] = p[4]; hs[6] = p[5];
+    } else {
+        xs[4] = h; xs[5] = 2 * h; xs[6] = 3 * h;
+        hs[4] = p[4]; hs[5] = p[5]; hs[6] = p[6];
+    }
+    if (l1 < h) {
+        xs[2] = -l1; xs[1] = -h; xs[0] = -2 * h;
+        hs[2] = hb; hs[1] = p[2]; hs[0] = p[1];
+    } else {
+        xs[2] = -h; xs[1] = -2 * h; xs[0] = -3 * h;
+        hs[2] = p[2]; hs[1] = p[1]; hs[0] = p[0];
+    }
+}
+
+// Smoothness indicators of the nonuniform WENO reconstruction for faces e[0..5] and
+// cell averages u[0..4] (re_step.cu:116-158; the same expressions serve both biases).
+template <typename T>
+__device__ __forceinline__ void nu_smoothness(const T e[6], const T u[5], T s[3])
+{
+    const T xm25 = e[0], xm15 = e[1], xm05 = e[2], x05 = e[3], x15 = e[4], x25 = e[5];
+    const T um2 = u[0], um1 = u[1], u0 = u[2], u1 = u[3], u2 = u[4];
+    const T w = x05 - xm05;
+    s[0] = T(4.0) * sqr(w / (x25 - xm05)) *
+           (sqr((u2 - u1) / (x25 - x05)) * (T(10.0) * sqr(w) + (x15 - xm05) * (x15 - x05)) +
+            (u2 - u1) * (u0 - u1) / ((x25 - x05) * (x15 - xm05)) *
+                (T(20.0) * sqr(w) + T(2.0) * (x15 - xm05) * (x15 - x05) + (x25 - xm05) * (T(2.0) * x15 - x05 - xm05)) +
+            sqr((u0 - u1) / (x15 - xm05)) * (T(10.0) * sqr(w) + (x25 + x15 - T(2.0) * xm05) * (x25 + x15 - x05 - xm05)));
+    s[1] = T(4.0) * sqr(w / (x15 - xm15)) *
+           (sqr((um1 - u0) / (x05 - xm15)) * (T(10.0) * sqr(w) + (x15 - xm05) * (x15 - x05)) +
+            (u1 - u0) * (um1 - u0) / ((x15 - xm05) * (x05 - xm15)) *
+                (T(20.0) * sqr(w) - (x15 - x05) * (xm05 - xm15) - (x15 - xm05) * (x05 - xm15)) +
+            sqr((u1 - u0) / (x15 - xm05)) * (T(10.0) * sqr(w) + (xm05 - xm15) * (x05 - xm15)));
+    s[2] = T(4.0) * sqr(w / (x05 - xm25)) *
+           (sqr((um2 - um1) / (xm05 - xm25)) * (T(10.0) * sqr(w) + (x05 - xm15) * (xm05 - xm15)) +
+            (u0 - um1) * (um2 - um1) / ((x05 - xm15) * (xm05 - xm25)) *
+                (T(20.0) * sqr(w) + T(2.0) * (x05 - xm15) * (xm05 - xm15) + (x05 - xm25) * (x05 + xm05 - T(2.0) * xm15)) +
+            sqr((u0 - um1) / (x05 - xm15)) * (T(10.0) * sqr(w) + (T(2.0) * x05 - xm25 - xm15) * (x05 + xm05 - xm15 - xm25)));
+}
+
+template <typename T> __device__ __forceinline__ T nu_combine(const T v[3], const T c[3], const T s[3])
+{
+    const T eps = T(1e-6);
+    T a0 = c[0] / sqr(s[0] + eps);
+    T a1 = c[1] / sqr(s[1] + eps);
+    T a2 = c[2] / sqr(s[2] + eps);
+    T tot = a0 + a1 + a2;
+    return v[0] * (a0 / tot) + v[1] * (a1 / tot) + v[2] * (a2 / tot);
+}
+
+// Nonuniform WENO forward/backward derivatives at xs[3] = 0 (weno_nonuniform,
+// re_step.cu:79-243).
+template <typename T>
+__device__ __noinline__ void weno_nonuniform_pair(const T xs[7], const T hs[7], T &d_fore, T &d_back)
+{
+    T dd[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) dd[m] = (hs[m + 1] - hs[m]) / (xs[m + 1] - xs[m]);
+    T e[6], u[5], v[3], c[3], s[3];
+    // forward bias: faces xs[1..6], cells dd[1..5], value at the face xs[3]
+#pragma unroll
+    for (int m = 0; m < 6; ++m) e[m] = xs[m + 1];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) u[m] = dd[m + 1];
+    {
+        const T xm25 = e[0], xm15 = e[1], xm05 = e[2], x05 = e[3], x15 = e[4], x25 = e[5];
+        const T um2 = u[0], um1 = u[1], u0 = u[2], u1 = u[3], u2 = u[4];
+        v[0] = u1 + (u0 - u1) * (T(1.0) + (x05 - xm05) / (x15 - xm05) + (x05 - xm05) / (x25 - xm05)) +
+               (u2 - u1) * ((x05 - xm05) / (x25 - xm05)) * ((x15 - xm05) / (x25 - x05));
+        v[1] = u0 + (um1 - u0) * ((x05 - xm05) / (x15 - xm15)) * ((x15 - xm05) / (x05 - xm15)) -
+               (u1 - u0) * ((x05 - xm05) / (x15 - xm15)) * ((xm05 - xm15) / (x15 - xm05));
+        v[2] = um1 + (u0 - um1) * ((xm05 - xm15) / (x05 - xm25)) * ((xm05 - xm25) / (x05 - xm15)) -
+               (um2 - um1) * ((xm05 - xm15) / (x05 - xm25)) * ((x05 - xm05) / (xm05 - xm25));
+        c[0] = ((xm05 - xm15) / (x25 - xm25)) * ((xm05 - xm25) / (x25 - xm15));
+        c[1] = ((xm05 - xm25) / (x25 - xm25)) * ((x25 - xm05) / (x25 - xm15)) * (T(1.0) + (x25 - xm15) / (x15 - xm25));
+        c[2] = ((x15 - xm05) / (x25 - xm25)) * ((x25 - xm05) / (x15 - xm25));
+    }
+    nu_smoothness(e, u, s);
+    d_fore = nu_combine(v, c, s);
+    // backward bias: faces xs[0..5], cells dd[0..4], value at the face xs[3]
+#pragma unroll
+    for (int m = 0; m < 6; ++m) e[m] = xs[m];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) u[m] = dd[m];
+    {
+        const T xm25 = e[0], xm15 = e[1], xm05 = e[2], x05 = e[3], x15 = e[4], x25 = e[5];
+        const T um2 = u[0], um1 = u[1], u0 = u[2], u1 = u[3], u2 = u[4];
+        v[0] = u1 + (u0 - u1) * ((x15 - x05) / (x25 - xm05)) * ((x25 - x05) / (x15 - xm05)) -
+               (u2 - u1) * ((x15 - x05) / (x25 - xm05)) * ((x05 - xm05) / (x25 - x05));
+        v[1] = u0 + (u1 - u0) * ((x05 - xm05) / (x15 - xm15)) * ((x05 - xm15) / (x15 - xm05)) -
+               (um1 - u0) * ((x05 - xm05) / (x15 - xm15)) * ((x15 - x05) / (x05 - xm15));
+        v[2] = um1 + (um2 - um1) * ((x05 - xm05) / (xm05 - xm25)) * ((x05 - xm15) / (x05 - xm25)) +
+               (u0 - um1) * (T(1.0) + (x05 - xm05) / (x05 - xm15) + (x05 - xm05) / (x05 - xm25));
+        c[0] = ((x05 - xm25) / (x25 - xm25)) * ((x05 - xm15) / (x25 - xm15));
+        c[1] = ((x05 - xm25) / (x25 - xm25)) * ((x25 - x05) / (x25 - xm15)) * (T(1.0) + (x25 - xm15) / (x15 - xm25));
+        c[2] = ((x15 - x05) / (x25 - xm25)) * ((x25 - x05) / (x15 - xm25));
+    }
+    nu_smoothness(e, u, s);
+    d_back = nu_combine(v, c, s);
+}
+
+// Nonuniform cubic ENO forward/backward derivatives at xs[3] = 0, the "ENO3" scheme
+// (ENO_cubic_derivative, weno_rk3_reinitialization.cu:189-222).
+template <typename T>
+__device__ __noinline__ void eno3_nonuniform_pair(const T xs[7], const T hs[7], T &d_fore, T &d_back)
+{
+    const T x3m = xs[0], x2m = xs[1], x1m = xs[2], x0 = xs[3], x1 = xs[4], x2 = xs[5], x3 = xs[6];
+    T f25 = (hs[6] - hs[5]) / (x3 - x2);
+    T f15 = (hs[5] - hs[4]) / (x2 - x1);
+    T f05 = (hs[4] - hs[3]) / (x1 - x0);
+    T fm05 = (hs[3] - hs[2]) / (x0 - x1m);
+    T fm15 = (hs[2] - hs[1]) / (x1m - x2m);
+    T fm25 = (hs[1] - hs[0]) / (x2m - x3m);
+    T g2 = (f25 - f15) / (x3 - x1);
+    T g1 = (f15 - f05) / (x2 - x0);
+    T g0 = (f05 - fm05) / (x1 - x1m);
+    T gm1 = (fm05 - fm15) / (x0 - x2m);
+    T gm2 = (fm15 - fm25) / (x1m - x3m);
+    T t15 = (g2 - g1) / (x3 - x0);
+    T t05 = (g1 - g0) / (x2 - x1m);
+    T tm05 = (g0 - gm1) / (x1 - x2m);
+    T tm15 = (gm1 - gm2) / (x0 - x3m);
+    T a1 = (x0 - x1m) * (x0 - x2m) * minabs(tm05, tm15);
+    T a2 = (x0 - x1m) * (x0 - x1) * minabs(tm05, t05);
+    T a = (fabs(gm1) < fabs(g0)) ? a1 : a2;
+    T b1 = (x0 - x1m) * (x0 - x1) * minabs(tm05, t05);
+    T b2 = (x0 - x1) * (x0 - x2) * minabs(t05, t15);
+    T b = (fabs(g0) < fabs(g1)) ? b1 : b2;
+    d_back = fm05 + minmod(gm1, g0) * (x0 - x1m) + a;
+    d_fore = f05 + minmod(g0, g1) * (x0 - x1) + b;
+}
+
+// Uniform WENO5 pair from the seven line values, plain (reference) numerics.
+template <typename T>
+__device__ __forceinline__ void weno5_pair_plain(const T p[7], T h, T &d_fore, T &d_back)
+{
+    T v[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) v[m] = (p[m + 1] - p[m]) / h;
+    d_back = weno5_plain(v[0], v[1], v[2], v[3], v[4]);
+    d_fore = weno5_plain(v[5], v[4], v[3], v[2], v[1]);
+}
+
+// Uniform WENO5 pair, fast numerics (unscaled differences, one division each).
+template <typename T>
+__device__ __forceinline__ void weno5_pair_fast(const T p[7], T inv_h, T eps2, T &d_fore, T &d_back)
+{
+    T u[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) u[m] = p[m + 1] - p[m];
+    d_back = weno5_fast(u[0], u[1], u[2], u[3], u[4], eps2) * inv_h;
+    d_fore = weno5_fast(u[5], u[4], u[3], u[2], u[1], eps2) * inv_h;
+}
+
+// Interface-aware pair: nonuniform WENO (eno3 = false) or cubic ENO (eno3 = true).
+template <typename T>
+__device__ __forceinline__ void interface_pair(const T p[7], T r1, T l1, T h, T hf, T hb, bool eno3, T &d_fore,
+                                               T &d_back)
+{
+    T xs[7], hs[7];
+    insert_interface(p, r1, l1, h, hf, hb, xs, hs);
+    if (eno3)
+        eno3_nonuniform_pair(xs, hs, d_fore, d_back);
+    else
+        weno_nonuniform_pair(xs, hs, d_fore, d_back);
+}
+
+// Godunov |grad phi| for the reinitialization Hamiltonian; `neg` is the mask (phi0 < 0)
+// (re_step.cu:382-392).
+template <typename T>
+__device__ __forceinline__ T godunov_norm(bool neg, T xR, T xL, T yF, T yB, T zU, T zD)
+{
+    const T z = T(0);
+    if (neg)
+        return sqrt(vmax(sqr(vmin(z, xL)), sqr(vmax(z, xR))) + vmax(sqr(vmin(z, yB)), sqr(vmax(z, yF))) +
+                    vmax(sqr(vmin(z, zD)), sqr(vmax(z, zU))));
+    return sqrt(vmax(sqr(vmax(z, xL)), sqr(vmin(z, xR))) + vmax(sqr(vmax(z, yB)), sqr(vmin(z, yF))) +
+                vmax(sqr(vmax(z, zD)), sqr(vmin(z, zU))));
+}
+
+// Upwind transport term sum_a min(0,v_a) D+_a + max(0,v_a) D-_a (extend_step.cu:121-123).
+template <typename T>
+__device__ __forceinline__ T upwind_dot(T vx, T vy, T vz, T xR, T xL, T yF, T yB, T zU, T zD)
+{
+    const T z = T(0);
+    return vmin(z, vx) * xR + vmax(z, vx) * xL + vmin(z, vy) * yF + vmax(z, vy) * yB + vmin(z, vz) * zU +
+           vmax(z, vz) * zD;
+}
+
+// Degree-5 value of the line at the crossing (sixth_interp, boundary_interpolant.cu:78-99)
+// and the cubic one (cubic_interp, wenork3_extend.cu:296-328); double throughout.
+__device__ inline void crossing_quintic(const double p[7], double dis_f, double dis_b, double h, double &cf,
+                                        double &cb)
+{
+    cf = 0.0;
+    cb = 0.0;
+    if (dis_f < h) {
+        double xs[6] = {h, 2 * h, 3 * h, 4 * h, 5 * h, 6 * h};
+        double a[6];
+        lagrange_monomial<5>(xs, p + 1, a);
+        cf = poly_eval<5>(a, 3 * h + dis_f);
+    }
+    if (dis_b < h) {
+        double xs[6] = {0.0, h, 2 * h, 3 * h, 4 * h, 5 * h};
+        double a[6];
+        lagrange_monomial<5>(xs, p, a);
+        cb = poly_eval<5>(a, 3 * h - dis_b);
+    }
+}
+
+__device__ __forceinline__ void cubic_fit(double v0, double v1, double v2, double v3, double h, double a[4])
+{
+    a[0] = v0;
+    a[1] = (3.0 * (v1 - v0) - 3.0 / 2.0 * (v2 - v0) + 1.0 / 3.0 * (v3 - v0)) / h;
+    a[2] = (-5.0 / 2.0 * (v1 - v0) + 2.0 * (v2 - v0) - 1.0 / 2.0 * (v3 - v0)) / (h * h);
+    a[3] = (1.0 / 2.0 * (v1 - v0) - 1.0 / 2.0 * (v2 - v0) + 1.0 / 6.0 * (v3 - v0)) / (h * h * h);
+}
+
+__device__ inline void crossing_cubic(const double p[7], double dis_f, double dis_b, double h, double &cf,
+                                      double &cb)
+{
+    cf = 0.0;
+    cb = 0.0;
+    double a[4];
+    if (dis_f < h) {
+        cubic_fit(p[2], p[3], p[4], p[5], h, a);
+        double t = h + dis_f;
+        cf = a[0] + a[1] * t + a[2] * (t * t) + a[3] * (t * t * t);
+    }
+    if (dis_b < h) {
+        cubic_fit(p[1], p[2], p[3], p[4], h, a);
+        double t = 2 * h - dis_b;
+        cb = a[0] + a[1] * t + a[2] * (t * t) + a[3] * (t * t * t);
+    }
+}
+
+}  // namespace vsl

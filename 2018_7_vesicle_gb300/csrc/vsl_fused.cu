@@ -1,0 +1,404 @@
+// vsl_fused.cu -- fused TVD-RK3 stage kernels of the method-level operations.
+//
+// One launch evaluates one Runge-Kutta stage of a whole pseudo-step AND its Shu-Osher
+// combination, writing the next stage field directly:
+//   stage 0: out = phi_s - step(phi_s)
+//   stage 1: out = 3/4 phi_n + 1/4 (phi_s - step(phi_s))
+//   stage 2: out = 1/3 phi_n + 2/3 (phi_s - step(phi_s))
+// which are the elementwise updates of WENO5RK3Reinitialization.m:15-39 (and of the
+// extension loops) folded into the stencil pass.
+//
+// Per node, a classification byte written once per call replaces the six distance reads:
+//   bits 0..5  distance xpr,xpl,ypf,ypb,zpu,zpd differs from the grid spacing (crossing)
+//   bit  6     mask (phi < 0 when the call started)
+//   bit  7     fixed node (a distance below 1e-6*dx: the reference's step-0 nodes)
+// Distances and crossing values are read only where a bit says they differ from the
+// defaults, so the dense per-stage traffic is phi_s (stencil), phi_n, flags and out.
+#include "vsl_internal.h"
+
+namespace vsl {
+namespace {
+
+constexpr uint8_t FIXED_BIT = 0x80;
+constexpr uint8_t MASK_BIT = 0x40;
+
+__device__ __forceinline__ bool fused_node(const Grid &g, int &i, int &j, int &k)
+{
+    i = blockIdx.x * BX + threadIdx.x;
+    j = blockIdx.y * BY + threadIdx.y;
+    k = blockIdx.z;
+    return i < g.rows && j < g.cols;
+}
+
+template <typename T> __device__ __forceinline__ T rk3_combine(int stage, T phi_n, T t)
+{
+    if (stage == 0) return t;
+    if (stage == 1) return T(3. / 4.) * phi_n + T(1. / 4.) * t;
+    return T(1. / 3.) * phi_n + T(2. / 3.) * t;
+}
+
+// distance of direction q (0..5) at node c: the stored value where the flag says it
+// differs from the spacing, the spacing otherwise
+template <typename T>
+__device__ __forceinline__ T flagged_distance(uint8_t fl, int q, const Ptr6<const T> &d, long long c, T h)
+{
+    return (fl & (1u << q)) ? __ldg(d.p[q] + c) : h;
+}
+
+// 0.3 * min over the six distances, as deltat = 0.3*min_dist of setDistance.m:17-21
+template <typename T>
+__device__ __forceinline__ T pseudo_dt(uint8_t fl, const Ptr6<const T> &d, long long c, T hx, T hy, T hz)
+{
+    T v[6];
+    const T h[3] = {hx, hy, hz};
+#pragma unroll
+    for (int q = 0; q < 6; ++q) v[q] = flagged_distance(fl, q, d, c, h[q / 2]);
+    T m = vmin(vmin(v[0], v[1]), vmin(vmin(v[2], v[3]), vmin(v[4], v[5])));
+    return T(0.3) * m;
+}
+
+template <typename T, bool FAST>
+__device__ __forceinline__ void uniform_pair(const T p[7], T h, T &df, T &db)
+{
+    if (FAST) {
+        const T inv_h = T(1) / h;
+        const T eps2 = T(1e-6) * h * h;
+        weno5_pair_fast(p, inv_h, eps2, df, db);
+    } else {
+        weno5_pair_plain(p, h, df, db);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// setDistance: all six distances written (spacing where no crossing)
+// ---------------------------------------------------------------------------------------
+template <typename T, bool QUINTIC>
+__global__ void __launch_bounds__(BX *BY) k_set_distance(const T *__restrict__ f, Ptr6<T> d, Grid g)
+{
+    int i, j, k;
+    if (!fused_node(g, i, j, k)) return;
+    const long long c = node_index(g, i, j, k);
+    const double f0 = (double)__ldg(f + c);
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        AxisLine L = axis_line(g, i, j, k, ax);
+        const double h = axis_h(g, ax);
+        const double fn = (double)__ldg(f + L.base + (long long)clampi(L.c + 1, L.n) * L.stride);
+        double fore = h, back = h;
+        if (f0 * fn < 0) fore = fore_distance<QUINTIC>(f, L, h);
+        if (L.c > 0) {
+            const double fp = (double)__ldg(f + L.base + (long long)(L.c - 1) * L.stride);
+            if (fp * f0 < 0) {
+                AxisLine Lp = L;
+                Lp.c = L.c - 1;
+                back = h - fore_distance<QUINTIC>(f, Lp, h);
+            }
+        }
+        d.p[2 * ax][c] = (T)fore;
+        d.p[2 * ax + 1][c] = (T)back;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BX *BY) k_classify(const T *__restrict__ phi0, Ptr6<const T> d, uint8_t *flags, Grid g)
+{
+    int i, j, k;
+    if (!fused_node(g, i, j, k)) return;
+    const long long c = node_index(g, i, j, k);
+    const T h[3] = {(T)g.dx, (T)g.dy, (T)g.dz};
+    const T tiny = (T)(1e-6 * g.dx);
+    uint8_t fl = 0;
+    bool fixed = false;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        const T v = __ldg(d.p[q] + c);
+        if (v != h[q / 2]) fl |= (uint8_t)(1u << q);
+        fixed |= v < tiny;
+    }
+    if (__ldg(phi0 + c) < T(0)) fl |= MASK_BIT;
+    if (fixed) fl |= FIXED_BIT;
+    flags[c] = fl;
+}
+
+// ---------------------------------------------------------------------------------------
+// reinitialization stage (re_step.cu:283-393 / weno_rk3_reinitialization.cu:295-406)
+// ---------------------------------------------------------------------------------------
+template <typename T, bool ENO3, bool FAST>
+__global__ void __launch_bounds__(BX *BY) k_reinit_stage(const T *__restrict__ phi_s, const T *__restrict__ phi_n,
+                                                           T *__restrict__ out, const uint8_t *__restrict__ flags,
+                                                           Ptr6<const T> d, Grid g, int stage)
+{
+    int i, j, k;
+    if (!fused_node(g, i, j, k)) return;
+    const long long c = node_index(g, i, j, k);
+    const uint8_t fl = __ldg(flags + c);
+    const T ps = __ldg(phi_s + c);
+    const T hx = (T)g.dx, hy = (T)g.dy, hz = (T)g.dz;
+    T step = T(0);
+    if (!(fl & FIXED_BIT)) {
+        T df[3], db[3];
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            T p[7];
+            load_line7(phi_s, axis_line(g, i, j, k, ax), p);
+            const T h = ax == 0 ? hx : (ax == 1 ? hy : hz);
+            if (p[2] * p[3] < T(0) || p[3] * p[4] < T(0)) {
+                const T r1 = flagged_distance(fl, 2 * ax, d, c, h);
+                const T l1 = flagged_distance(fl, 2 * ax + 1, d, c, h);
+                interface_pair(p, r1, l1, h, T(0), T(0), ENO3, df[ax], db[ax]);
+            } else {
+                uniform_pair<T, FAST>(p, h, df[ax], db[ax]);
+            }
+        }
+        const bool neg = fl & MASK_BIT;
+        const T gn = godunov_norm(neg, df[0], db[0], df[1], db[1], df[2], db[2]);
+        step = (gn - T(1)) * pseudo_dt(fl, d, c, hx, hy, hz) * (neg ? T(-1) : T(1));
+    }
+    const T pn = stage == 0 ? T(0) : __ldg(phi_n + c);
+    out[c] = rk3_combine(stage, pn, ps - step);
+}
+
+// ---------------------------------------------------------------------------------------
+// extension set-up: v = sign(F) * grad / max(|grad|, floor) with the upwind normal of
+// upwind_normal.cu:4-104 (WENORK3: wenork3_extend.cu:192-292) and the normalisation of
+// WENO5RK3Extend.m:23-31
+// ---------------------------------------------------------------------------------------
+template <typename T, bool ENO3>
+__global__ void __launch_bounds__(BX *BY) k_extension_velocity(const T *__restrict__ phi, Ptr6<const T> d, Ptr3<T> v,
+                                                                 Grid g, T floor)
+{
+    int i, j, k;
+    if (!fused_node(g, i, j, k)) return;
+    const long long c = node_index(g, i, j, k);
+    T n[3];
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        T p[7], df, db;
+        load_line7(phi, axis_line(g, i, j, k, ax), p);
+        const T h = (T)axis_h(g, ax);
+        const T r1 = __ldg(d.p[2 * ax] + c), l1 = __ldg(d.p[2 * ax + 1] + c);
+        if (r1 < h || l1 < h)
+            interface_pair(p, r1, l1, h, T(0), T(0), ENO3, df, db);
+        else
+            weno5_pair_plain(p, h, df, db);
+        n[ax] = (fabs(p[4]) < fabs(p[2])) ? df : db;
+    }
+    const T grad = vmax(sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]), floor);
+    const T f0 = __ldg(phi + c);
+    const T s = f0 > T(0) ? T(1) : (f0 < T(0) ? T(-1) : T(0));
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) v.p[ax][c] = s * (n[ax] / grad);
+}
+
+// crossing values (boundary_interpolant.cu:78-141 / wenork3_extend.cu:296-365), double
+template <typename T, bool CUBIC>
+__global__ void __launch_bounds__(BX *BY) k_crossing(const T *__restrict__ cfield, Ptr6<const T> d, Ptr6<T> cp, Grid g)
+{
+    int i, j, k;
+    if (!fused_node(g, i, j, k)) return;
+    const long long c = node_index(g, i, j, k);
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        const double h = axis_h(g, ax);
+        const double r1 = (double)__ldg(d.p[2 * ax] + c), l1 = (double)__ldg(d.p[2 * ax + 1] + c);
+        double cf = 0.0, cb = 0.0;
+        if (r1 < h || l1 < h) {
+            AxisLine L = axis_line(g, i, j, k, ax);
+            double p[7];
+#pragma unroll
+            for (int s = -3; s <= 3; ++s) p[s + 3] = (double)__ldg(cfield + L.base + (long long)clampi(L.c + s, L.n) * L.stride);
+            if (CUBIC)
+                crossing_cubic(p, r1, l1, h, cf, cb);
+            else
+                crossing_quintic(p, r1, l1, h, cf, cb);
+        }
+        cp.p[2 * ax][c] = (T)cf;
+        cp.p[2 * ax + 1][c] = (T)cb;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// extension stage (extend_step.cu:10-125 / wenork3_extend.cu:372-487)
+// ---------------------------------------------------------------------------------------
+template <typename T, bool ENO3, bool FAST>
+__global__ void __launch_bounds__(BX *BY) k_extend_stage(const T *__restrict__ c_s, const T *__restrict__ c_n,
+                                                           T *__restrict__ out, const uint8_t *__restrict__ flags,
+                                                           Ptr6<const T> d, Ptr6<const T> cp, Ptr3<const T> v, Grid g,
+                                                           int stage)
+{
+    int i, j, k;
+    if (!fused_node(g, i, j, k)) return;
+    const long long c = node_index(g, i, j, k);
+    const uint8_t fl = __ldg(flags + c);
+    const T cs = __ldg(c_s + c);
+    const T hx = (T)g.dx, hy = (T)g.dy, hz = (T)g.dz;
+    T step = T(0);
+    if (!(fl & FIXED_BIT)) {
+        T df[3], db[3];
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            T p[7];
+            load_line7(c_s, axis_line(g, i, j, k, ax), p);
+            const T h = ax == 0 ? hx : (ax == 1 ? hy : hz);
+            const T r1 = flagged_distance(fl, 2 * ax, d, c, h);
+            const T l1 = flagged_distance(fl, 2 * ax + 1, d, c, h);
+            if (r1 < h || l1 < h) {
+                const T hf = r1 < h ? __ldg(cp.p[2 * ax] + c) : T(0);
+                const T hb = l1 < h ? __ldg(cp.p[2 * ax + 1] + c) : T(0);
+                interface_pair(p, r1, l1, h, hf, hb, ENO3, df[ax], db[ax]);
+            } else {
+                uniform_pair<T, FAST>(p, h, df[ax], db[ax]);
+            }
+        }
+        step = upwind_dot(__ldg(v.p[0] + c), __ldg(v.p[1] + c), __ldg(v.p[2] + c), df[0], db[0], df[1], db[1], df[2],
+                          db[2]) *
+               pseudo_dt(fl, d, c, hx, hy, hz);
+    }
+    const T pn = stage == 0 ? T(0) : __ldg(c_n + c);
+    out[c] = rk3_combine(stage, pn, cs - step);
+}
+
+// ---------------------------------------------------------------------------------------
+// WENO5 advection stage: step = dt * (upwind v.grad phi) (advection_step.cu:30-56).
+// With `speed` non-null the velocity is speed * (v0, v1, v2) (normal speed times normal).
+// ---------------------------------------------------------------------------------------
+template <typename T, bool FAST>
+__global__ void __launch_bounds__(BX *BY) k_advect_stage(const T *__restrict__ phi_s, const T *__restrict__ phi_n,
+                                                           T *__restrict__ out, Ptr3<const T> v,
+                                                           const T *__restrict__ speed, const double *__restrict__ dt,
+                                                           Grid g, int stage)
+{
+    int i, j, k;
+    if (!fused_node(g, i, j, k)) return;
+    const long long c = node_index(g, i, j, k);
+    T df[3], db[3];
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        T p[7];
+        load_line7(phi_s, axis_line(g, i, j, k, ax), p);
+        uniform_pair<T, FAST>(p, (T)axis_h(g, ax), df[ax], db[ax]);
+    }
+    T vx = __ldg(v.p[0] + c), vy = __ldg(v.p[1] + c), vz = __ldg(v.p[2] + c);
+    if (speed) {
+        const T sp = __ldg(speed + c);
+        vx = sp * vx;
+        vy = sp * vy;
+        vz = sp * vz;
+    }
+    const T step = (T)__ldg(dt) * upwind_dot(vx, vy, vz, df[0], db[0], df[1], db[1], df[2], db[2]);
+    const T pn = stage == 0 ? T(0) : __ldg(phi_n + c);
+    out[c] = rk3_combine(stage, pn, __ldg(phi_s + c) - step);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------------------
+
+template <typename T>
+cudaError_t launch_set_distance(const T *phi, Ptr6<T> dist, const Grid &g, bool quintic, cudaStream_t s)
+{
+    if (quintic)
+        k_set_distance<T, true><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, dist, g);
+    else
+        k_set_distance<T, false><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, dist, g);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_classify(const T *phi0, Ptr6<const T> dist, uint8_t *flags, const Grid &g, cudaStream_t s)
+{
+    k_classify<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi0, dist, flags, g);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_reinit_stage(const T *phi_s, const T *phi_n, T *out, const uint8_t *flags, Ptr6<const T> dist,
+                                const Grid &g, int stage, bool eno3, bool fast, cudaStream_t s)
+{
+    dim3 gr = node_grid(g), bl(BX, BY);
+    if (eno3) {
+        if (fast)
+            k_reinit_stage<T, true, true><<<gr, bl, 0, s>>>(phi_s, phi_n, out, flags, dist, g, stage);
+        else
+            k_reinit_stage<T, true, false><<<gr, bl, 0, s>>>(phi_s, phi_n, out, flags, dist, g, stage);
+    } else {
+        if (fast)
+            k_reinit_stage<T, false, true><<<gr, bl, 0, s>>>(phi_s, phi_n, out, flags, dist, g, stage);
+        else
+            k_reinit_stage<T, false, false><<<gr, bl, 0, s>>>(phi_s, phi_n, out, flags, dist, g, stage);
+    }
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_extension_velocity(const T *phi, Ptr6<const T> dist, Ptr3<T> v, const Grid &g, bool eno3,
+                                      double floor, cudaStream_t s)
+{
+    if (eno3)
+        k_extension_velocity<T, true><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, dist, v, g, (T)floor);
+    else
+        k_extension_velocity<T, false><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, dist, v, g, (T)floor);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_crossing(const T *c, Ptr6<const T> dist, Ptr6<T> cp, const Grid &g, bool cubic, cudaStream_t s)
+{
+    if (cubic)
+        k_crossing<T, true><<<node_grid(g), dim3(BX, BY), 0, s>>>(c, dist, cp, g);
+    else
+        k_crossing<T, false><<<node_grid(g), dim3(BX, BY), 0, s>>>(c, dist, cp, g);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_extend_stage(const T *c_s, const T *c_n, T *out, const uint8_t *flags, Ptr6<const T> dist,
+                                Ptr6<const T> cp, Ptr3<const T> v, const Grid &g, int stage, bool eno3, bool fast,
+                                cudaStream_t s)
+{
+    dim3 gr = node_grid(g), bl(BX, BY);
+    if (eno3) {
+        if (fast)
+            k_extend_stage<T, true, true><<<gr, bl, 0, s>>>(c_s, c_n, out, flags, dist, cp, v, g, stage);
+        else
+            k_extend_stage<T, true, false><<<gr, bl, 0, s>>>(c_s, c_n, out, flags, dist, cp, v, g, stage);
+    } else {
+        if (fast)
+            k_extend_stage<T, false, true><<<gr, bl, 0, s>>>(c_s, c_n, out, flags, dist, cp, v, g, stage);
+        else
+            k_extend_stage<T, false, false><<<gr, bl, 0, s>>>(c_s, c_n, out, flags, dist, cp, v, g, stage);
+    }
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_advect_stage(const T *phi_s, const T *phi_n, T *out, Ptr3<const T> v, const T *speed,
+                                const double *dt, const Grid &g, int stage, bool fast, cudaStream_t s)
+{
+    if (fast)
+        k_advect_stage<T, true><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi_s, phi_n, out, v, speed, dt, g, stage);
+    else
+        k_advect_stage<T, false><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi_s, phi_n, out, v, speed, dt, g, stage);
+    return cudaGetLastError();
+}
+
+#define VSL_INSTANTIATE_FUSED(T)                                                                                   \
+    template cudaError_t launch_set_distance<T>(const T *, Ptr6<T>, const Grid &, bool, cudaStream_t);              \
+    template cudaError_t launch_classify<T>(const T *, Ptr6<const T>, uint8_t *, const Grid &, cudaStream_t);       \
+    template cudaError_t launch_reinit_stage<T>(const T *, const T *, T *, const uint8_t *, Ptr6<const T>,          \
+                                                const Grid &, int, bool, bool, cudaStream_t);                       \
+    template cudaError_t launch_extension_velocity<T>(const T *, Ptr6<const T>, Ptr3<T>, const Grid &, bool,        \
+                                                      double, cudaStream_t);                                        \
+    template cudaError_t launch_crossing<T>(const T *, Ptr6<const T>, Ptr6<T>, const Grid &, bool, cudaStream_t);   \
+    template cudaError_t launch_extend_stage<T>(const T *, const T *, T *, const uint8_t *, Ptr6<const T>,          \
+                                                Ptr6<const T>, Ptr3<const T>, const Grid &, int, bool, bool,        \
+                                                cudaStream_t);                                                      \
+    template cudaError_t launch_advect_stage<T>(const T *, const T *, T *, Ptr3<const T>, const T *,                \
+                                                const double *, const Grid &, int, bool, cudaStream_t);
+
+VSL_INSTANTIATE_FUSED(float)
+VSL_INSTANTIATE_FUSED(double)
+
+}  // namespace vsl

@@ -1,0 +1,76 @@
+// vsl_internal.h -- shared declarations between the translation units of the library.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/vsl_gb300.h"
+#include "vsl_device.cuh"
+
+namespace vsl {
+
+// thread block used by the node-parallel kernels: 32 rows x 8 columns of one page
+constexpr int BX = 32;
+constexpr int BY = 8;
+
+inline dim3 node_grid(const Grid &g) { return dim3((g.rows + BX - 1) / BX, (g.cols + BY - 1) / BY, g.pges); }
+
+// Validation shared by every entry point (status codes of vsl_gb300.h).
+inline int check_grid(int rows, int cols, int pges, double dx, double dy, double dz)
+{
+    if (rows <= 0 || cols <= 0 || pges <= 0) return VSL_ERR_SHAPE;
+    if ((long long)rows * cols * pges > (long long)VSL_MAX_NODES) return VSL_ERR_SHAPE;
+    if (pges > 65535) return VSL_ERR_SHAPE;
+    if (!(dx > 0) || !(dy > 0) || !(dz > 0)) return VSL_ERR_VALUE;
+    return VSL_OK;
+}
+
+inline int launch_status(cudaError_t e) { return e == cudaSuccess ? VSL_OK : VSL_ERR_CUDA; }
+
+template <typename T> struct Ptr6 {
+    T *p[6];
+};
+template <typename T> struct Ptr3 {
+    T *p[3];
+};
+
+// ---- fused kernels (vsl_fused.cu), T in {float, double} --------------------------------
+template <typename T>
+cudaError_t launch_set_distance(const T *phi, Ptr6<T> dist, const Grid &g, bool quintic, cudaStream_t s);
+template <typename T>
+cudaError_t launch_classify(const T *phi0, Ptr6<const T> dist, uint8_t *flags, const Grid &g, cudaStream_t s);
+template <typename T>
+cudaError_t launch_reinit_stage(const T *phi_s, const T *phi_n, T *out, const uint8_t *flags, Ptr6<const T> dist,
+                                const Grid &g, int stage, bool eno3, bool fast, cudaStream_t s);
+template <typename T>
+cudaError_t launch_extension_velocity(const T *phi, Ptr6<const T> dist, Ptr3<T> v, const Grid &g, bool eno3,
+                                      double floor, cudaStream_t s);
+template <typename T>
+cudaError_t launch_crossing(const T *c, Ptr6<const T> dist, Ptr6<T> cp, const Grid &g, bool cubic, cudaStream_t s);
+template <typename T>
+cudaError_t launch_extend_stage(const T *c_s, const T *c_n, T *out, const uint8_t *flags, Ptr6<const T> dist,
+                                Ptr6<const T> cp, Ptr3<const T> v, const Grid &g, int stage, bool eno3, bool fast,
+                                cudaStream_t s);
+template <typename T>
+cudaError_t launch_advect_stage(const T *phi_s, const T *phi_n, T *out, Ptr3<const T> v, const T *speed,
+                                const double *dt, const Grid &g, int stage, bool fast, cudaStream_t s);
+
+// ---- toolbox and reductions (vsl_toolbox.cu) ------------------------------------------
+// Fields of the calculus toolbox a caller may ask for (null pointers are skipped).
+template <typename T> struct ToolboxOut {
+    T *f[18];
+};
+template <typename T>
+cudaError_t launch_toolbox(const T *phi, ToolboxOut<T> out, const Grid &g, double ds, double *partials,
+                           int *nblocks, cudaStream_t s);
+cudaError_t launch_sum_partials(const double *partials, int nblocks, int ncomp, double scale, double *result,
+                                cudaStream_t s);
+template <typename T>
+cudaError_t launch_band_maxabs(const T *f, const T *phi, double band, const Grid &g, double *partials,
+                               int *nblocks, cudaStream_t s);
+cudaError_t launch_time_step(const double *partials, int nblocks, double cfl_ds, double *dt, double *vmax,
+                             cudaStream_t s);
+int toolbox_partial_blocks(const Grid &g);
+
+}  // namespace vsl

@@ -1,0 +1,233 @@
+// vsl_toolbox.cu -- calculus toolbox fused with the FP64 area/volume reductions, the
+// band maximum of the normal speed and the time step, all reductions in a fixed order
+// (per-block warp-shuffle trees, then one block summing the block partials in index
+// order), so a result is bitwise reproducible for a given grid.
+#include "vsl_internal.h"
+
+namespace vsl {
+namespace {
+
+constexpr int NT = BX * BY;  // threads per node block
+constexpr int NW = NT / 32;
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__device__ __forceinline__ long long block_linear() { return blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z); }
+
+// set_calculus_toolbox (set_calculus_toolbox.cu:9-107) in double from the promoted field,
+// HPrimal = max(F, 0) formed on the fly (GPUsetCalculusToolBox.m:4); per block the sums
+// of DiracDelta over |F| < 2Ds and of 1 - Heaviside over F < 2Ds (SDF3.m:73-80).
+template <typename T>
+__global__ void __launch_bounds__(NT) k_toolbox(const T *__restrict__ f, ToolboxOut<T> o, Grid g, double ds,
+                                                double *__restrict__ partials)
+{
+    const int i = blockIdx.x * BX + threadIdx.x;
+    const int j = blockIdx.y * BY + threadIdx.y;
+    const int k = blockIdx.z;
+    double area = 0.0, vol = 0.0;
+    if (i < g.rows && j < g.cols) {
+        const long long c = node_index(g, i, j, k);
+        auto F = [&](int a, int b, int e) { return (double)__ldg(f + clamped_index(g, a, b, e)); };
+        auto H = [&](int a, int b, int e) { return fmax((double)__ldg(f + clamped_index(g, a, b, e)), 0.0); };
+        const double dx = g.dx, dy = g.dy, dz = g.dz;
+        const double fc = (double)__ldg(f + c);
+        const double fxp = F(i, j + 1, k), fxm = F(i, j - 1, k), fyp = F(i + 1, j, k), fym = F(i - 1, j, k);
+        const double fzp = F(i, j, k + 1), fzm = F(i, j, k - 1);
+        double fx = (fxp - fxm) / (2 * dx);
+        double fy = (fyp - fym) / (2 * dy);
+        double fz = (fzp - fzm) / (2 * dz);
+        double gm = vmax(sqrt(fx * fx + fy * fy + fz * fz), 1e-14);
+        double fxx = (fxp - 2 * fc + fxm) / (dx * dx);
+        double fyy = (fyp - 2 * fc + fym) / (dy * dy);
+        double fzz = (fzp - 2 * fc + fzm) / (dz * dz);
+        double fxy = (F(i + 1, j + 1, k) + F(i - 1, j - 1, k) - F(i + 1, j - 1, k) - F(i - 1, j + 1, k)) / (4 * ds * ds);
+        double fyz = (F(i + 1, j, k + 1) + F(i - 1, j, k - 1) - F(i + 1, j, k - 1) - F(i - 1, j, k + 1)) / (4 * ds * ds);
+        double fzx = (F(i, j + 1, k + 1) + F(i, j - 1, k - 1) - F(i, j + 1, k - 1) - F(i, j - 1, k + 1)) / (4 * ds * ds);
+        double lap = fxx + fyy + fzz;
+        double r1 = fxx * fx + fxy * fy + fzx * fz;
+        double r2 = fxy * fx + fyy * fy + fyz * fz;
+        double r3 = fzx * fx + fyz * fy + fzz * fz;
+        double gm2 = gm * gm;
+        double mean = -lap / gm + (fx * r1 + fy * r2 + fz * r3) / (gm2 * gm);
+        double hc = fmax(fc, 0.0);
+        double hxp = H(i, j + 1, k), hxm = H(i, j - 1, k), hyp = H(i + 1, j, k), hym = H(i - 1, j, k);
+        double hzp = H(i, j, k + 1), hzm = H(i, j, k - 1);
+        double px = (hxp - hxm) / (2 * dx), py = (hyp - hym) / (2 * dy), pz = (hzp - hzm) / (2 * dz);
+        double dot = px * fx + py * fy + pz * fz;
+        double pxx = (hxp - 2 * hc + hxm) / (dx * dx);
+        double pyy = (hyp - 2 * hc + hym) / (dy * dy);
+        double pzz = (hzp - 2 * hc + hzm) / (dz * dz);
+        double plap = pxx + pyy + pzz;
+        double heav = dot / gm2;
+        double delta = plap / gm2 - dot * lap / (gm2 * gm2);
+        if (fabs(fc) < 2 * ds) area = delta;
+        if (fc < 2 * ds) vol = 1 - heav;
+        if (o.f[0]) o.f[0][c] = (T)fx;
+        if (o.f[1]) o.f[1][c] = (T)fy;
+        if (o.f[2]) o.f[2][c] = (T)fz;
+        if (o.f[3]) o.f[3][c] = (T)gm;
+        if (o.f[4]) o.f[4][c] = (T)(fx / gm);
+        if (o.f[5]) o.f[5][c] = (T)(fy / gm);
+        if (o.f[6]) o.f[6][c] = (T)(fz / gm);
+        if (o.f[7]) o.f[7][c] = (T)fxx;
+        if (o.f[8]) o.f[8][c] = (T)fyy;
+        if (o.f[9]) o.f[9][c] = (T)fzz;
+        if (o.f[10]) o.f[10][c] = (T)fxy;
+        if (o.f[11]) o.f[11][c] = (T)fyz;
+        if (o.f[12]) o.f[12][c] = (T)fzx;
+        if (o.f[13]) o.f[13][c] = (T)lap;
+        if (o.f[14]) o.f[14][c] = (T)mean;
+        if (o.f[15]) {
+            double q1 = (fyy * fzz - fyz * fyz) * fx + (fzx * fyz - fxy * fzz) * fy + (fxy * fyz - fzx * fyy) * fz;
+            double q2 = (fyz * fzx - fxy * fzz) * fx + (fxx * fzz - fzx * fzx) * fy + (fzx * fxy - fxx * fyz) * fz;
+            double q3 = (fxy * fyz - fyy * fzx) * fx + (fzx * fxy - fxx * fyz) * fy + (fxx * fyy - fxy * fxy) * fz;
+            o.f[15][c] = (T)((fx * q1 + fy * q2 + fz * q3) / (gm2 * gm2));
+        }
+        if (o.f[16]) o.f[16][c] = (T)heav;
+        if (o.f[17]) o.f[17][c] = (T)delta;
+    }
+    if (!partials) return;
+    __shared__ double sa[NW], sv[NW];
+    const int t = threadIdx.y * BX + threadIdx.x;
+    area = warp_sum(area);
+    vol = warp_sum(vol);
+    if ((t & 31) == 0) {
+        sa[t >> 5] = area;
+        sv[t >> 5] = vol;
+    }
+    __syncthreads();
+    if (t == 0) {
+        double a = 0.0, v = 0.0;
+        for (int w = 0; w < NW; ++w) {
+            a += sa[w];
+            v += sv[w];
+        }
+        const long long b = block_linear();
+        partials[2 * b] = a;
+        partials[2 * b + 1] = v;
+    }
+}
+
+// result[q] = scale * sum_b partials[ncomp*b + q], fixed order (one block of 1024)
+__global__ void __launch_bounds__(1024) k_sum_partials(const double *__restrict__ partials, int nblocks, int ncomp,
+                                                       double scale, double *__restrict__ result)
+{
+    __shared__ double s[32];
+    for (int q = 0; q < ncomp; ++q) {
+        double acc = 0.0;
+        for (int b = threadIdx.x; b < nblocks; b += blockDim.x) acc += partials[(long long)ncomp * b + q];
+        acc = warp_sum(acc);
+        if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double tot = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) tot += s[w];
+            result[q] = tot * scale;
+        }
+        __syncthreads();
+    }
+}
+
+// per-block max |f| over the band |phi| < band (p00_test_singlephase_relax.m:86-89)
+template <typename T>
+__global__ void __launch_bounds__(NT) k_band_maxabs(const T *__restrict__ f, const T *__restrict__ phi, double band,
+                                                    Grid g, double *__restrict__ partials)
+{
+    const int i = blockIdx.x * BX + threadIdx.x;
+    const int j = blockIdx.y * BY + threadIdx.y;
+    const int k = blockIdx.z;
+    double m = 0.0;
+    if (i < g.rows && j < g.cols) {
+        const long long c = node_index(g, i, j, k);
+        if (fabs((double)__ldg(phi + c)) < band) m = fabs((double)__ldg(f + c));
+    }
+    __shared__ double s[NW];
+    const int t = threadIdx.y * BX + threadIdx.x;
+    m = warp_max(m);
+    if ((t & 31) == 0) s[t >> 5] = m;
+    __syncthreads();
+    if (t == 0) {
+        double r = 0.0;
+        for (int w = 0; w < NW; ++w) r = fmax(r, s[w]);
+        partials[block_linear()] = r;
+    }
+}
+
+__global__ void __launch_bounds__(1024) k_time_step(const double *__restrict__ partials, int nblocks, double cfl_ds,
+                                                    double *__restrict__ dt, double *__restrict__ vmax)
+{
+    __shared__ double s[32];
+    double m = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) m = fmax(m, partials[b]);
+    m = warp_max(m);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, s[w]);
+        if (vmax) *vmax = r;
+        *dt = r > 0.0 ? cfl_ds / r : 0.0;
+    }
+}
+
+}  // namespace
+
+int toolbox_partial_blocks(const Grid &g)
+{
+    dim3 gr = node_grid(g);
+    return (int)((long long)gr.x * gr.y * gr.z);
+}
+
+template <typename T>
+cudaError_t launch_toolbox(const T *phi, ToolboxOut<T> out, const Grid &g, double ds, double *partials,
+                           int *nblocks, cudaStream_t s)
+{
+    if (nblocks) *nblocks = toolbox_partial_blocks(g);
+    k_toolbox<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, out, g, ds, partials);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sum_partials(const double *partials, int nblocks, int ncomp, double scale, double *result,
+                                cudaStream_t s)
+{
+    k_sum_partials<<<1, 1024, 0, s>>>(partials, nblocks, ncomp, scale, result);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_band_maxabs(const T *f, const T *phi, double band, const Grid &g, double *partials,
+                               int *nblocks, cudaStream_t s)
+{
+    if (nblocks) *nblocks = toolbox_partial_blocks(g);
+    k_band_maxabs<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(f, phi, band, g, partials);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_time_step(const double *partials, int nblocks, double cfl_ds, double *dt, double *vmax,
+                             cudaStream_t s)
+{
+    k_time_step<<<1, 1024, 0, s>>>(partials, nblocks, cfl_ds, dt, vmax);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_toolbox<float>(const float *, ToolboxOut<float>, const Grid &, double, double *, int *,
+                                           cudaStream_t);
+template cudaError_t launch_toolbox<double>(const double *, ToolboxOut<double>, const Grid &, double, double *,
+                                            int *, cudaStream_t);
+template cudaError_t launch_band_maxabs<float>(const float *, const float *, double, const Grid &, double *, int *,
+                                               cudaStream_t);
+template cudaError_t launch_band_maxabs<double>(const double *, const double *, double, const Grid &, double *,
+                                                int *, cudaStream_t);
+
+}  // namespace vsl

@@ -1,0 +1,277 @@
+"""Host-side mirror of the reference's level-set classes SD.GD3 and SD.SDF3.
+
+Same method names, argument meaning and order as the MATLAB classes
+(src/7_0_paper/2_0_Vesicle/+SD/@GD3/GD3.m, +SD/@SDF3/*.m); the arithmetic runs in the
+CUDA library through the C ABI (``_lib``).  Fields are torch tensors on the current CUDA
+device with the MATLAB layout: shape (rows, cols, pges) = (y, x, z), column-major
+storage (strides 1, rows, rows*cols).
+
+``precision="f64"`` is the plain form (FP64 everywhere); ``precision="f32"`` is the
+mixed-precision form (FP32 fields and stencils, FP64 interface roots and reductions).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import torch
+
+from ._lib import lib
+
+_DTYPES = {"f64": torch.float64, "f32": torch.float32}
+
+
+# ---------------------------------------------------------------------------------------
+# column-major field helpers
+# ---------------------------------------------------------------------------------------
+
+
+def is_colmajor(t: torch.Tensor) -> bool:
+    return t.dim() == 3 and t.permute(2, 1, 0).is_contiguous()
+
+
+def colmajor_empty(size, dtype, device=None) -> torch.Tensor:
+    r, c, p = size
+    return torch.empty((p, c, r), dtype=dtype, device=device or "cuda").permute(2, 1, 0)
+
+
+def colmajor_full(size, value, dtype, device=None) -> torch.Tensor:
+    t = colmajor_empty(size, dtype, device)
+    t.fill_(value)
+    return t
+
+
+def as_field(a, dtype, device=None) -> torch.Tensor:
+    """A (rows, cols, pges) column-major CUDA tensor of `dtype` holding `a` (numpy array in
+    any order, or tensor)."""
+    device = device or "cuda"
+    if isinstance(a, np.ndarray):
+        r, c, p = a.shape
+        flat = np.asarray(a, dtype=np.float64).ravel(order="F")
+        t = torch.from_numpy(flat.copy()).view(p, c, r).permute(2, 1, 0)
+    else:
+        t = a
+    t = t.to(device=device, dtype=dtype)
+    if not is_colmajor(t):
+        t = t.permute(2, 1, 0).contiguous().permute(2, 1, 0)
+    return t
+
+
+def to_numpy(t: torch.Tensor) -> np.ndarray:
+    """Fortran-ordered float64 numpy copy of a column-major field."""
+    return np.asfortranarray(t.detach().to("cpu", torch.float64).numpy())
+
+
+def _ptr(t) -> int:
+    return 0 if t is None else t.data_ptr()
+
+
+def _stream() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+# ---------------------------------------------------------------------------------------
+# SD.GD3: grid metadata (GD3.m:86-106)
+# ---------------------------------------------------------------------------------------
+
+
+class GD3:
+    """Meshgrid metadata: X, Y, Z of shape (rows, cols, pges) as MATLAB meshgrid(xv,yv,zv)."""
+
+    def __init__(self, Xm, Ym, Zm, spacing=None, device=None):
+        self.X = as_field(Xm, torch.float64, device)
+        self.Y = as_field(Ym, torch.float64, device)
+        self.Z = as_field(Zm, torch.float64, device)
+        self.Size = tuple(self.X.shape)
+        self.mrows, self.ncols, self.lshts = self.Size
+        self.NumElt = self.mrows * self.ncols * self.lshts
+        if spacing is None:
+            X, Y, Z = (to_numpy(v) for v in (self.X, self.Y, self.Z))
+            spacing = (float(X[0, 1, 0] - X[0, 0, 0]), float(Y[1, 0, 0] - Y[0, 0, 0]), float(Z[0, 0, 1] - Z[0, 0, 0]))
+        self.Dx, self.Dy, self.Dz = (float(s) for s in spacing)
+        self.Ds = (self.Dx + self.Dy + self.Dz) / 3
+
+    @staticmethod
+    def meshgrid(xv, yv, zv, device=None):
+        """MATLAB [x,y,z] = meshgrid(xv,yv,zv) as column-major CUDA tensors."""
+        x, y, z = np.meshgrid(np.asarray(xv, float), np.asarray(yv, float), np.asarray(zv, float))
+        return as_field(x, torch.float64, device), as_field(y, torch.float64, device), as_field(z, torch.float64, device)
+
+    def args(self):
+        return (self.mrows, self.ncols, self.lshts, self.Dx, self.Dy, self.Dz)
+
+    def WENODotGrad(self, vx, vy, vz, field):
+        """Upwind WENO5 v.grad(field) (GD3.m:393-398), FP64."""
+        f = as_field(field, torch.float64)
+        v = [as_field(a, torch.float64) for a in (vx, vy, vz)]
+        out = colmajor_empty(self.Size, torch.float64)
+        lib().call("vsl_advection_step", _ptr(out), *map(_ptr, v), _ptr(f), *self.args(), _stream())
+        return out
+
+    def GPUWENODerivative(self, field):
+        """Six one-sided WENO5 derivatives [back_x, fore_x, back_y, fore_y, back_z, fore_z]."""
+        f = as_field(field, torch.float64)
+        outs = [colmajor_empty(self.Size, torch.float64) for _ in range(6)]
+        lib().call("vsl_weno_derivative", *map(_ptr, outs), _ptr(f), *self.args(), _stream())
+        return outs
+
+
+# ---------------------------------------------------------------------------------------
+# SD.SDF3: the level-set object
+# ---------------------------------------------------------------------------------------
+
+TOOLBOX_FIELDS = ("Fx", "Fy", "Fz", "FGradMag", "Nx", "Ny", "Nz", "Fxx", "Fyy", "Fzz", "Fxy", "Fyz", "Fzx",
+                  "FLaplacian", "MeanCurvature", "GaussianCurvature", "Heaviside", "DiracDelta")
+
+
+class SDF3:
+    """Signed distance function on a GD3 grid (SDF3.m)."""
+
+    def __init__(self, grid: GD3, Xm=None, Ym=None, Zm=None, Val=None, precision: str = "f64"):
+        if precision not in _DTYPES:
+            raise ValueError(f"precision must be one of {sorted(_DTYPES)}")
+        self.GD3 = grid
+        self.precision = precision
+        self.dtype = _DTYPES[precision]
+        self.elem = 8 if precision == "f64" else 4
+        self.F = None if Val is None else as_field(Val, self.dtype)
+        self.xpr = self.xpl = self.ypf = self.ypb = self.zpu = self.zpd = None
+        self._ws = {}
+
+    # -- plumbing ----------------------------------------------------------------------
+    def _fn(self, base: str) -> str:
+        return f"{base}_{self.precision}"
+
+    def _field(self, a) -> torch.Tensor:
+        return as_field(a, self.dtype)
+
+    def workspace(self, op: str) -> torch.Tensor:
+        n = lib().workspace_bytes(op, *self.GD3.Size, self.elem)
+        ws = self._ws.get(op)
+        if ws is None or ws.numel() < n:
+            ws = torch.empty(max(n, 256), dtype=torch.uint8, device="cuda")
+            self._ws[op] = ws
+        return ws
+
+    def _dist(self):
+        if self.xpr is None:
+            raise RuntimeError("setDistance must be called before any use of the distances")
+        return (self.xpr, self.xpl, self.ypf, self.ypb, self.zpu, self.zpd)
+
+    @property
+    def min_dist(self):
+        xpr, xpl, ypf, ypb, zpu, zpd = self._dist()
+        return torch.minimum(torch.minimum(xpr, xpl), torch.minimum(torch.minimum(ypf, ypb), torch.minimum(zpu, zpd)))
+
+    # -- setDistance.m:3-33 -----------------------------------------------------------------
+    def setDistance(self):
+        size = self.GD3.Size
+        d = [colmajor_empty(size, self.dtype) for _ in range(6)]
+        lib().call(self._fn("vsl_set_distance"), _ptr(self.F), *map(_ptr, d), *self.GD3.args(), _stream())
+        self.xpr, self.xpl, self.ypf, self.ypb, self.zpu, self.zpd = d
+
+    # -- reinitialization ------------------------------------------------------------------
+    def WENO5RK3Reinitialization(self, F, iteration: int):
+        """WENO5RK3Reinitialization.m:3-43 (cached distances of setDistance)."""
+        out = self._field(F).clone()
+        ws = self.workspace("reinit_weno5")
+        lib().call(self._fn("vsl_weno5_rk3_reinitialization"), _ptr(out), int(iteration), *map(_ptr, self._dist()),
+                   *self.GD3.args(), _ptr(ws), ws.numel(), _stream())
+        return out
+
+    def WENORK3Reinitialization(self, F, iteration: int):
+        """WENORK3Reinitialization.m:3-61 (cubic distances recomputed from F)."""
+        out = self._field(F).clone()
+        ws = self.workspace("reinit_eno3")
+        lib().call(self._fn("vsl_wenork3_reinitialization"), _ptr(out), int(iteration), *self.GD3.args(), _ptr(ws),
+                   ws.numel(), _stream())
+        return out
+
+    # -- extension ---------------------------------------------------------------------------
+    def WENO5RK3Extend(self, C, iteration: int):
+        """WENO5RK3Extend.m:9-76."""
+        out = self._field(C).clone()
+        ws = self.workspace("extend_weno5")
+        lib().call(self._fn("vsl_weno5_rk3_extend"), _ptr(out), int(iteration), _ptr(self.F), *map(_ptr, self._dist()),
+                   *self.GD3.args(), _ptr(ws), ws.numel(), _stream())
+        return out
+
+    def WENORK3Extend(self, C, iteration: int):
+        """WENORK3Extend.m:9-98."""
+        out = self._field(C).clone()
+        ws = self.workspace("extend_eno3")
+        lib().call(self._fn("vsl_wenork3_extend"), _ptr(out), int(iteration), _ptr(self.F), *self.GD3.args(), _ptr(ws),
+                   ws.numel(), _stream())
+        return out
+
+    # -- surface redistance -------------------------------------------------------------------
+    def WENO5RK3ClosetPointSurfaceRedistance(self, A, iter1: int, iter2: int):
+        """WENO5RK3ClosetPointSurfaceRedistance.m:4-157."""
+        out = self._field(A).clone()
+        ws = self.workspace("surface_redistance")
+        lib().call(self._fn("vsl_weno5_rk3_surface_redistance"), _ptr(out), int(iter1), int(iter2), _ptr(self.F),
+                   *self.GD3.args(), _ptr(ws), ws.numel(), _stream())
+        return out
+
+    # -- calculus toolbox and integrals ----------------------------------------------------
+    def GPUsetCalculusToolBox(self):
+        """GPUsetCalculusToolBox.m:2-42: the 18 toolbox fields (computed in FP64)."""
+        f64 = as_field(self.F, torch.float64)
+        hp = torch.clamp(f64, min=0)  # HPrimal = max(F, 0)
+        outs = [colmajor_empty(self.GD3.Size, torch.float64) for _ in TOOLBOX_FIELDS]
+        lib().call("vsl_set_calculus_toolbox", *map(_ptr, outs), _ptr(f64), _ptr(hp), *self.GD3.args(), self.GD3.Ds,
+                   self.GD3.NumElt, _stream())
+        for name, t in zip(TOOLBOX_FIELDS, outs):
+            setattr(self, name, t if self.dtype == torch.float64 else t.to(self.dtype))
+        self.HPrimal = hp
+
+    def area_volume(self) -> torch.Tensor:
+        """Device tensor [area, volume] (SDF3.m:73-80), FP64 fixed-order sums."""
+        out = torch.empty(2, dtype=torch.float64, device="cuda")
+        ws = self.workspace("area_volume")
+        lib().call(self._fn("vsl_area_volume"), _ptr(self.F), _ptr(out), *self.GD3.args(), _ptr(ws), ws.numel(),
+                   _stream())
+        return out
+
+    def calArea(self) -> float:
+        return float(self.area_volume()[0])
+
+    def calVolume(self) -> float:
+        return float(self.area_volume()[1])
+
+    def surfaceIntegral(self, field) -> float:
+        """SDF3.m:82-85; uses the toolbox fields of the last GPUsetCalculusToolBox."""
+        F = as_field(self.F, torch.float64)
+        mask = F.abs() < 2 * self.GD3.Ds
+        f = as_field(field, torch.float64)
+        return float((f[mask] * self.DiracDelta.double()[mask] * self.FGradMag.double()[mask]).sum()) * self.GD3.Ds ** 3
+
+    # -- advection and the composite step ----------------------------------------------------
+    def WENO5RK3Advection(self, F, vx, vy, vz, dt, steps: int = 1):
+        """F advanced `steps` WENO5 TVD-RK3 steps of phi_t + v.grad(phi) = 0 with time step dt."""
+        out = self._field(F).clone()
+        v = [self._field(a) for a in (vx, vy, vz)]
+        dtt = dt if isinstance(dt, torch.Tensor) else torch.tensor([float(dt)], dtype=torch.float64, device="cuda")
+        ws = self.workspace("advection")
+        lib().call(self._fn("vsl_weno5_rk3_advection"), _ptr(out), *map(_ptr, v), _ptr(dtt), int(steps),
+                   *self.GD3.args(), _ptr(ws), ws.numel(), _stream())
+        return out
+
+    def vesicle_step(self, ext_iters: int = 30, reinit_iters: int = 20, cfl: float = 0.5, info=None) -> torch.Tensor:
+        """One vesicle step in place on self.F and its cached distances; returns the device
+        tensor [area, volume, dt, max|Vn|]."""
+        info = torch.empty(4, dtype=torch.float64, device="cuda") if info is None else info
+        ws = self.workspace("vesicle_step")
+        lib().call(self._fn("vsl_vesicle_step"), _ptr(self.F), *map(_ptr, self._dist()), int(ext_iters),
+                   int(reinit_iters), float(cfl), _ptr(info), *self.GD3.args(), _ptr(ws), ws.numel(), _stream())
+        return info
+
+
+def ellipsoid_phi(x, y, z, a: float, b: float, c: float):
+    """sqrt(x^2/a^2 + y^2/b^2 + z^2/c^2) - 1 (Ellipsoid.m:45)."""
+    return torch.sqrt(x**2 / a**2 + y**2 / b**2 + z**2 / c**2) - 1
+
+
+def reduced_volume(area: float, volume: float) -> float:
+    """(3V/4pi) (4pi/A)^(3/2) (p00_test_singlephase_relax.m:32)."""
+    return (3 * volume / 4 / math.pi) * (4 * math.pi / area) ** 1.5

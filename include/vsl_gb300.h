@@ -1,0 +1,243 @@
+/*
+ * vsl_gb300.h -- C ABI of the GB300 level-set hot path (vesicle code).
+ *
+ * Layout of every field (the reference's MATLAB gpuArray layout): a rows x cols x pges
+ * column-major array, element (i, j, k) at k*rows*cols + j*rows + i, with i = row (y),
+ * j = column (x), k = page (z); dx is the column spacing, dy the row spacing, dz the page
+ * spacing.  Neighbours outside the grid are clamped to the edge.
+ *
+ * All pointers are DEVICE pointers on the current CUDA device, the work is enqueued on
+ * `stream` (NULL = legacy default stream) and the call returns once it is enqueued.  No
+ * entry point allocates memory: callers pass outputs and, for the composite operations,
+ * a workspace of at least vsl_workspace_bytes(...) bytes (256-byte aligned).
+ *
+ * Return value: VSL_OK or one of the VSL_ERR_* codes below.
+ *
+ * Citations "ref: file:line" name the reference function each entry point replaces,
+ * relative to src/7_0_paper/2_0_Vesicle/ of tiankuizhang/2018_7_Vesicle.
+ */
+#ifndef VSL_GB300_H
+#define VSL_GB300_H
+
+#include <stdbool.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *vsl_stream_t; /* same type as cudaStream_t */
+
+enum {
+    VSL_OK = 0,
+    VSL_ERR_NULL = 1,      /* a required pointer is NULL */
+    VSL_ERR_SHAPE = 2,     /* rows/cols/pges not positive, too large, or != num_ele */
+    VSL_ERR_VALUE = 3,     /* a spacing, iteration count or CFL number out of range */
+    VSL_ERR_WORKSPACE = 4, /* workspace missing, too small or misaligned */
+    VSL_ERR_CUDA = 5,      /* a kernel launch failed (cudaGetLastError) */
+    VSL_ERR_OP = 6         /* unknown operation id */
+};
+
+/* largest grid accepted (nodes); indices are 64-bit inside the kernels */
+#define VSL_MAX_NODES 2147483647LL
+
+const char *vsl_status_string(int status);
+int vsl_version(void);
+
+/* ===================================================================================== */
+/* Drop-in kernels: FP64, the reference kernel's argument order, MATLAB in/out semantics */
+/* (non-const pointers are in/out; entries a kernel does not write keep their values).   */
+/* ===================================================================================== */
+
+/* ref: CUDA_Code/1_3_WENO5RK3_Reinitialization/boundary_location.cu:84-132 (boundary_location) */
+int vsl_boundary_location(double *xpr, double *xpl, double *ypf, double *ypb, double *zpu, double *zpd,
+                          const double *lsf, int num_ele, int rows, int cols, int pges, double dx, double dy,
+                          double dz, vsl_stream_t stream);
+
+/* ref: CUDA_Code/1_1_WENORK3_Reinitialization/weno_rk3_reinitialization.cu:251-293 (boundary_correction) */
+int vsl_cubic_boundary_correction(double *xpr, double *xpl, double *ypf, double *ypb, double *zpu, double *zpd,
+                                  const double *lsf, int num_ele, int rows, int cols, int pges, double dx,
+                                  double dy, double dz, vsl_stream_t stream);
+
+/* ref: CUDA_Code/1_3_WENO5RK3_Reinitialization/re_step.cu:283-393 (re_step) */
+int vsl_re_step(double *step, const double *lsf, const bool *mask, const double *deltat, const double *xpr,
+                const double *xpl, const double *ypf, const double *ypb, const double *zpu, const double *zpd,
+                int rows, int cols, int pges, double dx, double dy, double dz, int num_ele, vsl_stream_t stream);
+
+/* ref: CUDA_Code/1_1_WENORK3_Reinitialization/weno_rk3_reinitialization.cu:295-406 (re_step) */
+int vsl_re_step_eno3(double *step, const double *lsf, const bool *mask, const double *deltat, const double *xpr,
+                     const double *xpl, const double *ypf, const double *ypb, const double *zpu, const double *zpd,
+                     int rows, int cols, int pges, double dx, double dy, double dz, int num_ele,
+                     vsl_stream_t stream);
+
+/* ref: CUDA_Code/2_2_WENO5RK3_Extend/upwind_normal.cu:14-104 (upwind_normal) */
+int vsl_upwind_normal(double *nx, double *ny, double *nz, const double *lsf, const double *xpr, const double *xpl,
+                      const double *ypf, const double *ypb, const double *zpu, const double *zpd, int rows, int cols,
+                      int pges, double dx, double dy, double dz, int num_ele, vsl_stream_t stream);
+
+/* ref: CUDA_Code/2_1_WENORK3_Extend/wenork3_extend.cu:202-292 (upwind_normal) */
+int vsl_upwind_normal_eno3(double *nx, double *ny, double *nz, const double *lsf, const double *xpr,
+                           const double *xpl, const double *ypf, const double *ypb, const double *zpu,
+                           const double *zpd, int rows, int cols, int pges, double dx, double dy, double dz,
+                           int num_ele, vsl_stream_t stream);
+
+/* ref: CUDA_Code/2_2_WENO5RK3_Extend/boundary_interpolant.cu:102-141 (boundary_interpolant) */
+int vsl_boundary_interpolant(double *cpr, double *cpl, double *cpf, double *cpb, double *cpu, double *cpd,
+                             const double *xpr, const double *xpl, const double *ypf, const double *ypb,
+                             const double *zpu, const double *zpd, const double *lsf, int rows, int cols, int pges,
+                             double dx, double dy, double dz, int num_ele, vsl_stream_t stream);
+
+/* ref: CUDA_Code/2_1_WENORK3_Extend/wenork3_extend.cu:331-365 (boundary_interpolate) */
+int vsl_boundary_interpolate_eno3(double *cpr, double *cpl, double *cpf, double *cpb, double *cpu, double *cpd,
+                                  const double *xpr, const double *xpl, const double *ypf, const double *ypb,
+                                  const double *zpu, const double *zpd, const double *lsf, int rows, int cols,
+                                  int pges, double dx, double dy, double dz, int num_ele, vsl_stream_t stream);
+
+/* ref: CUDA_Code/2_2_WENO5RK3_Extend/extend_step.cu:10-125 (extend_step) */
+int vsl_extend_step(double *step, const double *deltat, const double *lsf, const double *vx, const double *vy,
+                    const double *vz, const double *xpr, const double *xpl, const double *ypf, const double *ypb,
+                    const double *zpu, const double *zpd, const double *cpr, const double *cpl, const double *cpf,
+                    const double *cpb, const double *cpu, const double *cpd, int rows, int cols, int pges,
+                    double dx, double dy, double dz, int num_ele, vsl_stream_t stream);
+
+/* ref: CUDA_Code/2_1_WENORK3_Extend/wenork3_extend.cu:372-487 (extend_step) */
+int vsl_extend_step_eno3(double *step, const double *deltat, const double *lsf, const double *vx, const double *vy,
+                         const double *vz, const double *xpr, const double *xpl, const double *ypf,
+                         const double *ypb, const double *zpu, const double *zpd, const double *cpr,
+                         const double *cpl, const double *cpf, const double *cpb, const double *cpu,
+                         const double *cpd, int rows, int cols, int pges, double dx, double dy, double dz,
+                         int num_ele, vsl_stream_t stream);
+
+/* ref: CUDA_Code/4_0_Calculus_ToolBox/set_calculus_toolbox.cu:9-107 (set_calculus_toolbox) */
+int vsl_set_calculus_toolbox(double *Fx, double *Fy, double *Fz, double *FGradMag, double *Nx, double *Ny,
+                             double *Nz, double *Fxx, double *Fyy, double *Fzz, double *Fxy, double *Fyz,
+                             double *Fzx, double *FLaplacian, double *MeanCurvature, double *GaussianCurvature,
+                             double *Heaviside, double *DiracDelta, const double *lsf, const double *HPrimal,
+                             int rows, int cols, int pges, double dx, double dy, double dz, double ds, int num_ele,
+                             vsl_stream_t stream);
+
+/* ref: CUDA_Code/4_0_Calculus_ToolBox/advection_step.cu:30-56 (advection_step) */
+int vsl_advection_step(double *astep, const double *vx, const double *vy, const double *vz, const double *lsf,
+                       int rows, int cols, int pges, double dx, double dy, double dz, vsl_stream_t stream);
+
+/* ref: CUDA_Code/5_0_Nonoscillating_Reconstruction/nonoscillating_interpolant.cu:59-122 (weno_derivative) */
+int vsl_weno_derivative(double *WENO_back_x, double *WENO_fore_x, double *WENO_back_y, double *WENO_fore_y,
+                        double *WENO_back_z, double *WENO_fore_z, const double *lsf, int rows, int cols, int pges,
+                        double dx, double dy, double dz, vsl_stream_t stream);
+
+/* ===================================================================================== */
+/* Method-level operations of the level-set object (SD.SDF3), fused GB300 kernels.        */
+/* _f64: the plain form, FP64 throughout.  _f32: the mixed-precision form, FP32 fields    */
+/* and stencils with the sub-cell interface roots and all reductions in FP64.             */
+/* ===================================================================================== */
+
+/* workspace operation ids for vsl_workspace_bytes */
+enum {
+    VSL_OP_REINIT_WENO5 = 1,
+    VSL_OP_REINIT_ENO3 = 2,
+    VSL_OP_EXTEND_WENO5 = 3,
+    VSL_OP_EXTEND_ENO3 = 4,
+    VSL_OP_SURFACE_REDISTANCE = 5,
+    VSL_OP_AREA_VOLUME = 6,
+    VSL_OP_ADVECTION = 7,
+    VSL_OP_VESICLE_STEP = 8
+};
+
+/* Bytes of workspace operation `op` needs on a rows x cols x pges grid of elements of
+ * `elem_bytes` (8 for _f64, 4 for _f32); 0 for an unknown op or bad shape. */
+size_t vsl_workspace_bytes(int op, int rows, int cols, int pges, int elem_bytes);
+
+/* ref: +SD/@SDF3/setDistance.m:3-33.  Writes all six distance fields (Delta where no
+ * interface crosses the edge). */
+int vsl_set_distance_f64(const double *F, double *xpr, double *xpl, double *ypf, double *ypb, double *zpu,
+                         double *zpd, int rows, int cols, int pges, double dx, double dy, double dz,
+                         vsl_stream_t stream);
+int vsl_set_distance_f32(const float *F, float *xpr, float *xpl, float *ypf, float *ypb, float *zpu, float *zpd,
+                         int rows, int cols, int pges, double dx, double dy, double dz, vsl_stream_t stream);
+
+/* ref: +SD/@SDF3/WENO5RK3Reinitialization.m:3-43.  F is advanced in place `iteration`
+ * TVD-RK3 pseudo-steps with the cached distances of setDistance (mask = F<0 at entry,
+ * dt = 0.3 * min distance). */
+int vsl_weno5_rk3_reinitialization_f64(double *F, int iteration, const double *xpr, const double *xpl,
+                                       const double *ypf, const double *ypb, const double *zpu, const double *zpd,
+                                       int rows, int cols, int pges, double dx, double dy, double dz,
+                                       void *workspace, size_t workspace_bytes, vsl_stream_t stream);
+int vsl_weno5_rk3_reinitialization_f32(float *F, int iteration, const float *xpr, const float *xpl,
+                                       const float *ypf, const float *ypb, const float *zpu, const float *zpd,
+                                       int rows, int cols, int pges, double dx, double dy, double dz,
+                                       void *workspace, size_t workspace_bytes, vsl_stream_t stream);
+
+/* ref: +SD/@SDF3/WENORK3Reinitialization.m:3-61 (cubic distances recomputed from F). */
+int vsl_wenork3_reinitialization_f64(double *F, int iteration, int rows, int cols, int pges, double dx, double dy,
+                                     double dz, void *workspace, size_t workspace_bytes, vsl_stream_t stream);
+int vsl_wenork3_reinitialization_f32(float *F, int iteration, int rows, int cols, int pges, double dx, double dy,
+                                     double dz, void *workspace, size_t workspace_bytes, vsl_stream_t stream);
+
+/* ref: +SD/@SDF3/WENO5RK3Extend.m:9-76.  C is extended in place off the zero set of F
+ * with F's cached distances. */
+int vsl_weno5_rk3_extend_f64(double *C, int iteration, const double *F, const double *xpr, const double *xpl,
+                             const double *ypf, const double *ypb, const double *zpu, const double *zpd, int rows,
+                             int cols, int pges, double dx, double dy, double dz, void *workspace,
+                             size_t workspace_bytes, vsl_stream_t stream);
+int vsl_weno5_rk3_extend_f32(float *C, int iteration, const float *F, const float *xpr, const float *xpl,
+                             const float *ypf, const float *ypb, const float *zpu, const float *zpd, int rows,
+                             int cols, int pges, double dx, double dy, double dz, void *workspace,
+                             size_t workspace_bytes, vsl_stream_t stream);
+
+/* ref: +SD/@SDF3/WENORK3Extend.m:9-98 (cubic distances of F recomputed inside). */
+int vsl_wenork3_extend_f64(double *C, int iteration, const double *F, int rows, int cols, int pges, double dx,
+                           double dy, double dz, void *workspace, size_t workspace_bytes, vsl_stream_t stream);
+int vsl_wenork3_extend_f32(float *C, int iteration, const float *F, int rows, int cols, int pges, double dx,
+                           double dy, double dz, void *workspace, size_t workspace_bytes, vsl_stream_t stream);
+
+/* ref: +SD/@SDF3/WENO5RK3ClosetPointSurfaceRedistance.m:4-157.  A is redistanced in
+ * place on the zero set of F: iter1 RK3 steps, each stage preceded by iter2 extension
+ * steps of A off the interface. */
+int vsl_weno5_rk3_surface_redistance_f64(double *A, int iter1, int iter2, const double *F, int rows, int cols,
+                                         int pges, double dx, double dy, double dz, void *workspace,
+                                         size_t workspace_bytes, vsl_stream_t stream);
+int vsl_weno5_rk3_surface_redistance_f32(float *A, int iter1, int iter2, const float *F, int rows, int cols,
+                                         int pges, double dx, double dy, double dz, void *workspace,
+                                         size_t workspace_bytes, vsl_stream_t stream);
+
+/* ref: +SD/@SDF3/SDF3.m:73-80 (calArea, calVolume) after GPUsetCalculusToolBox.m:2-42.
+ * area_volume: device pointer to 2 doubles, written with the FP64 sums
+ * area = Ds^3 * sum(DiracDelta where |F| < 2Ds), volume = Ds^3 * sum(1 - Heaviside where
+ * F < 2Ds), summed in a fixed order (bitwise reproducible for a given grid). */
+int vsl_area_volume_f64(const double *F, double *area_volume, int rows, int cols, int pges, double dx, double dy,
+                        double dz, void *workspace, size_t workspace_bytes, vsl_stream_t stream);
+int vsl_area_volume_f32(const float *F, double *area_volume, int rows, int cols, int pges, double dx, double dy,
+                        double dz, void *workspace, size_t workspace_bytes, vsl_stream_t stream);
+
+/* WENO5 advection phi_t + v.grad(phi) = 0 (the upwind operator of
+ * CUDA_Code/4_0_Calculus_ToolBox/advection_step.cu:30-56 / +SD/@GD3/GD3.m:393-398) in the
+ * TVD-RK3 combination of WENO5RK3Reinitialization.m:15-39; `steps` steps of the device
+ * time step *dt. */
+int vsl_weno5_rk3_advection_f64(double *F, const double *vx, const double *vy, const double *vz, const double *dt,
+                                int steps, int rows, int cols, int pges, double dx, double dy, double dz,
+                                void *workspace, size_t workspace_bytes, vsl_stream_t stream);
+int vsl_weno5_rk3_advection_f32(float *F, const float *vx, const float *vy, const float *vz, const double *dt,
+                                int steps, int rows, int cols, int pges, double dx, double dy, double dz,
+                                void *workspace, size_t workspace_bytes, vsl_stream_t stream);
+
+/* One vesicle step in the order of p00_test_singlephase_relax.m:60-196 with the normal
+ * speed set to the mean curvature: calculus toolbox -> area/volume -> extend the mean
+ * curvature (ext_iters WENO5 RK3 pseudo-steps) -> dt = cfl*Ds/max|Vn| over |F|<2Ds ->
+ * one WENO5 RK3 advection step along Vn*N -> setDistance -> reinit_iters WENO5 RK3
+ * pseudo-steps.  F and its cached distances (xpr..zpd) are updated in place.
+ * info: device pointer to 4 doubles {area, volume, dt, max|Vn|} (area/volume measured
+ * before the step). */
+int vsl_vesicle_step_f64(double *F, double *xpr, double *xpl, double *ypf, double *ypb, double *zpu, double *zpd,
+                         int ext_iters, int reinit_iters, double cfl, double *info, int rows, int cols, int pges,
+                         double dx, double dy, double dz, void *workspace, size_t workspace_bytes,
+                         vsl_stream_t stream);
+int vsl_vesicle_step_f32(float *F, float *xpr, float *xpl, float *ypf, float *ypb, float *zpu, float *zpd,
+                         int ext_iters, int reinit_iters, double cfl, double *info, int rows, int cols, int pges,
+                         double dx, double dy, double dz, void *workspace, size_t workspace_bytes,
+                         vsl_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

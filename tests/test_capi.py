@@ -1,0 +1,104 @@
+"""The C ABI library without a GPU: it loads, exports every entry point declared in
+include/vsl_gb300.h with the declared arity, and rejects bad arguments with the documented
+status before launching anything."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "vsl_gb300.h")
+
+
+def declared():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(?:int|size_t|const char \*)\s*(vsl_\w+)\s*\(([^;]*?)\);", text, flags=re.S):
+        params = [p for p in m.group(2).split(",") if p.strip() and p.strip() != "void"]
+        out[m.group(1)] = len(params)
+    return out
+
+
+def test_header_declares_entry_points():
+    d = declared()
+    assert "vsl_re_step" in d and "vsl_vesicle_step_f32" in d
+    assert len(d) >= 30
+
+
+def test_library_exports_every_declared_symbol(vsl):
+    lib = ctypes.CDLL(vsl.path)
+    for name in declared():
+        assert hasattr(lib, name), f"{name} not exported"
+
+
+def test_bindings_match_header_arity(pkg):
+    from importlib import import_module
+
+    sigs = import_module(pkg.__name__ + "._lib").SIGNATURES
+    d = declared()
+    for name, sig in sigs.items():
+        assert name in d, f"{name} bound but not declared"
+        assert len(sig) == d[name], f"{name}: {len(sig)} bound vs {d[name]} declared"
+    for name in d:
+        if name not in ("vsl_status_string", "vsl_version", "vsl_workspace_bytes"):
+            assert name in sigs, f"{name} declared but not bound"
+
+
+def test_status_strings(vsl):
+    assert vsl.status_string(0) == "ok"
+    for st in range(1, 7):
+        assert vsl.status_string(st) != "unknown status"
+    assert vsl.lib.vsl_version() == 1
+
+
+FAKE = 0x1000  # never dereferenced: every call below fails its checks first
+
+
+def test_null_pointer_rejected(vsl):
+    st = vsl.raw("vsl_re_step", 0, FAKE, FAKE, FAKE, *[FAKE] * 6, 8, 8, 8, 0.1, 0.1, 0.1, 512, None)
+    assert st == 1
+    st = vsl.raw("vsl_weno5_rk3_reinitialization_f32", 0, 3, *[FAKE] * 6, 8, 8, 8, 0.1, 0.1, 0.1, FAKE, 1 << 20, None)
+    assert st == 1
+
+
+def test_shape_checks(vsl):
+    # num_ele inconsistent with rows*cols*pges
+    st = vsl.raw("vsl_boundary_location", *[FAKE] * 7, 511, 8, 8, 8, 0.1, 0.1, 0.1, None)
+    assert st == 2
+    st = vsl.raw("vsl_boundary_location", *[FAKE] * 7, 0, 0, 8, 8, 0.1, 0.1, 0.1, None)
+    assert st == 2
+    st = vsl.raw("vsl_set_distance_f64", *[FAKE] * 7, 8, -1, 8, 0.1, 0.1, 0.1, None)
+    assert st == 2
+    # non-positive spacing
+    st = vsl.raw("vsl_set_distance_f64", *[FAKE] * 7, 8, 8, 8, 0.1, 0.0, 0.1, None)
+    assert st == 3
+
+
+def test_value_and_workspace_checks(vsl):
+    n = vsl.workspace_bytes("reinit_weno5", 8, 8, 8, 8)
+    st = vsl.raw("vsl_weno5_rk3_reinitialization_f64", FAKE, -1, *[FAKE] * 6, 8, 8, 8, 0.1, 0.1, 0.1, FAKE, n, None)
+    assert st == 3
+    st = vsl.raw("vsl_weno5_rk3_reinitialization_f64", FAKE, 2, *[FAKE] * 6, 8, 8, 8, 0.1, 0.1, 0.1, 0, n, None)
+    assert st == 4
+    st = vsl.raw("vsl_weno5_rk3_reinitialization_f64", FAKE, 2, *[FAKE] * 6, 8, 8, 8, 0.1, 0.1, 0.1, FAKE, n - 1, None)
+    assert st == 4
+    st = vsl.raw("vsl_weno5_rk3_reinitialization_f64", FAKE, 2, *[FAKE] * 6, 8, 8, 8, 0.1, 0.1, 0.1, FAKE + 8, n, None)
+    assert st == 4
+    st = vsl.raw("vsl_vesicle_step_f32", *[FAKE] * 7, 3, 3, -0.5, FAKE, 8, 8, 8, 0.1, 0.1, 0.1, FAKE, 1 << 30, None)
+    assert st == 3
+
+
+def test_workspace_sizes(vsl):
+    for op, per_node_min in (("reinit_weno5", 2 * 8 + 1), ("reinit_eno3", 8 * 8 + 1), ("extend_weno5", 11 * 8 + 1),
+                             ("surface_redistance", 25 * 8 + 2), ("advection", 2 * 8), ("vesicle_step", 15 * 8 + 1)):
+        n = vsl.workspace_bytes(op, 32, 24, 16, 8)
+        assert n >= per_node_min * 32 * 24 * 16, op
+        assert n % 256 == 0
+        assert vsl.workspace_bytes(op, 32, 24, 16, 4) < n
+    assert vsl.workspace_bytes("area_volume", 64, 64, 64, 8) >= 16 * (64 // 32) * (64 // 8) * 64
+    assert vsl.lib.vsl_workspace_bytes(99, 8, 8, 8, 8) == 0
+    assert vsl.lib.vsl_workspace_bytes(1, 8, 8, 8, 2) == 0
+    assert vsl.lib.vsl_workspace_bytes(1, 0, 8, 8, 8) == 0

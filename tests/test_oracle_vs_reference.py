@@ -1,0 +1,40 @@
+"""Where the reference checkout is present (development container), its kernels compiled
+for the host must give bit-identical results to the C restatement on fresh seeded
+inputs.  Skipped where the reference host build is absent.  CPU only."""
+import numpy as np
+import pytest
+
+
+@pytest.fixture(scope="module")
+def both(oracle_mod):
+    from oracle import build_oracle
+
+    if build_oracle.build_ref() is None or not oracle_mod.ref_available():
+        pytest.skip("reference checkout not present")
+    return oracle_mod, oracle_mod.kernels("port"), oracle_mod.kernels("ref")
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_bit_identical_on_seeded_inputs(both, seed):
+    O, P, R = both
+    rng = np.random.default_rng(seed)
+    shape = tuple(int(v) for v in rng.integers(9, 17, size=3))
+    xv = np.linspace(-1, 1, shape[1])
+    yv = np.linspace(-1, 1, shape[0]) * rng.uniform(0.7, 1.2)
+    zv = np.linspace(-1, 1, shape[2]) * rng.uniform(0.7, 1.2)
+    x, y, z = O.meshgrid(xv, yv, zv)
+    g = O.grid_from_mesh(x, y, z)
+    c = rng.uniform(-0.2, 0.2, 3)
+    F = O.F64((np.sqrt((x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2) - 0.55) * (0.2 + rng.uniform() * x**2))
+    C = O.F64(np.sin(2 * x + seed) * np.cos(y) + z)
+    d = O.set_distance(P, g, F)
+    assert all(np.array_equal(a, b) for a, b in zip(d.six(), O.set_distance(R, g, F).six()))
+    assert np.array_equal(O.reinit_weno5(P, g, F, 2, d), O.reinit_weno5(R, g, F, 2, d))
+    assert np.array_equal(O.reinit_eno3(P, g, F, 2), O.reinit_eno3(R, g, F, 2))
+    assert np.array_equal(O.extend_weno5(P, g, F, d, C, 2), O.extend_weno5(R, g, F, d, C, 2))
+    assert np.array_equal(O.extend_eno3(P, g, F, C, 2), O.extend_eno3(R, g, F, C, 2))
+    tp, tr = O.calculus_toolbox(P, g, F), O.calculus_toolbox(R, g, F)
+    assert all(np.array_equal(tp[k], tr[k]) for k in O.TOOLBOX_FIELDS)
+    v = [O.F64(rng.standard_normal(g.size)) for _ in range(3)]
+    assert np.array_equal(O.weno_dot_grad(P, g, *v, F), O.weno_dot_grad(R, g, *v, F))
+    assert np.array_equal(O.surface_redistance(P, g, F, C, 1, 2), O.surface_redistance(R, g, F, C, 1, 2))
