@@ -20,8 +20,8 @@ def build(force: bool = False) -> str:
 
 
 def __getattr__(name):
-    if name in ("GD3", "SDF3", "sdf3"):
-        from . import sdf3
+    if name in ("GD3", "SDF3"):
+        import importlib
 
-        return sdf3 if name == "sdf3" else getattr(sdf3, name)
+        return getattr(importlib.import_module(__name__ + ".sdf3"), name)
     raise AttributeError(name)

@@ -18,6 +18,13 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE]
+# The plain FP64 form rounds every product and sum separately, as the reference's kernels
+# (and the host oracle) do, so it can match them to the last bit: no mul+add contraction.
+FILE_FLAGS = {
+    "vsl_plain.cu": ["-fmad=false"],
+    "vsl_fused_f64.cu": ["-fmad=false"],
+    "vsl_toolbox.cu": ["-fmad=false"],
+}
 
 
 def nvcc() -> str:
@@ -46,7 +53,8 @@ def _stale(target: str, deps) -> bool:
 def _compile(src: str, extra) -> str:
     obj = os.path.join(OUT_DIR, "obj", os.path.basename(src)[:-3] + ".o")
     if _stale(obj, [src, *headers()]):
-        cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-c", src, "-o", obj]
+        per_file = FILE_FLAGS.get(os.path.basename(src), [])
+        cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *per_file, *extra, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")

@@ -109,6 +109,25 @@ template <typename T> __device__ __forceinline__ T minabs(T x, T y) { return (fa
 __device__ __forceinline__ double sgn1(double x) { return (x > 0) ? 1.0 : -1.0; }
 template <typename T> __device__ __forceinline__ T sqr(T x) { return x * x; }
 
+// t^p rounded once: the running product is carried as an unevaluated double-double
+// (hi + lo, error-free products via fma), so the result is the correctly rounded power
+// except in cases within ~2^-100 of a rounding midpoint -- what a correctly rounded
+// pow(t, p) returns.  The reference's polynomial and curvature code calls pow(t, p).
+template <int P> __device__ __forceinline__ double pow_cr(double t)
+{
+    if (P == 0) return 1.0;
+    if (P == 1) return t;
+    double hi = t, lo = 0.0;
+#pragma unroll
+    for (int k = 2; k <= P; ++k) {
+        const double p1 = hi * t;
+        const double e1 = fma(hi, t, -p1);
+        lo = fma(lo, t, e1);
+        hi = p1;
+    }
+    return hi + lo;
+}
+
 // ---------------------------------------------------------------------------------------
 // sub-cell interface distances, always double
 // ---------------------------------------------------------------------------------------
@@ -147,15 +166,16 @@ __device__ __forceinline__ void lagrange_monomial(const double *x, const double 
     }
 }
 
-// sum a[p] t^p, powers accumulated left to right (the reference sums a[p]*pow(t,p)).
+// sum of a[p] t^p, terms added from p = 0 (Poly<n>::operator(), shared_utilities.hpp:47-53)
 template <int N> __device__ __forceinline__ double poly_eval(const double *a, double t)
 {
-    double v = 0.0, tp = 1.0;
-#pragma unroll
-    for (int p = 0; p <= N; ++p) {
-        v += a[p] * tp;
-        tp *= t;
-    }
+    double v = 0.0;
+    v += a[0] * 1.0;
+    if (N >= 1) v += a[1] * t;
+    if (N >= 2) v += a[2] * (t * t);
+    if (N >= 3) v += a[3] * pow_cr<3>(t);
+    if (N >= 4) v += a[4] * pow_cr<4>(t);
+    if (N >= 5) v += a[5] * pow_cr<5>(t);
     return v;
 }
 
@@ -253,7 +273,7 @@ __device__ inline double cubic_newton_distance(double v0, double v1, double v2, 
     double a0 = v0;
     double a1 = (3.0 * (v1 - v0) - 3.0 / 2.0 * (v2 - v0) + 1.0 / 3.0 * (v3 - v0)) / h;
     double a2 = (-5.0 / 2.0 * (v1 - v0) + 2.0 * (v2 - v0) - 1.0 / 2.0 * (v3 - v0)) / (h * h);
-    double a3 = (1.0 / 2.0 * (v1 - v0) - 1.0 / 2.0 * (v2 - v0) + 1.0 / 6.0 * (v3 - v0)) / (h * h * h);
+    double a3 = (1.0 / 2.0 * (v1 - v0) - 1.0 / 2.0 * (v2 - v0) + 1.0 / 6.0 * (v3 - v0)) / pow_cr<3>(h);
     double t = h + h * v1 / (v1 - v2);
     double change = 1.0;
     for (int it = 0; change > 1e-14 && it < 50; ++it) {
@@ -553,7 +573,7 @@ __device__ __forceinline__ void cubic_fit(double v0, double v1, double v2, doubl
     a[0] = v0;
     a[1] = (3.0 * (v1 - v0) - 3.0 / 2.0 * (v2 - v0) + 1.0 / 3.0 * (v3 - v0)) / h;
     a[2] = (-5.0 / 2.0 * (v1 - v0) + 2.0 * (v2 - v0) - 1.0 / 2.0 * (v3 - v0)) / (h * h);
-    a[3] = (1.0 / 2.0 * (v1 - v0) - 1.0 / 2.0 * (v2 - v0) + 1.0 / 6.0 * (v3 - v0)) / (h * h * h);
+    a[3] = (1.0 / 2.0 * (v1 - v0) - 1.0 / 2.0 * (v2 - v0) + 1.0 / 6.0 * (v3 - v0)) / pow_cr<3>(h);
 }
 
 __device__ inline void crossing_cubic(const double p[7], double dis_f, double dis_b, double h, double &cf,
@@ -565,12 +585,12 @@ __device__ inline void crossing_cubic(const double p[7], double dis_f, double di
     if (dis_f < h) {
         cubic_fit(p[2], p[3], p[4], p[5], h, a);
         double t = h + dis_f;
-        cf = a[0] + a[1] * t + a[2] * (t * t) + a[3] * (t * t * t);
+        cf = a[0] + a[1] * t + a[2] * (t * t) + a[3] * pow_cr<3>(t);
     }
     if (dis_b < h) {
         cubic_fit(p[1], p[2], p[3], p[4], h, a);
         double t = 2 * h - dis_b;
-        cb = a[0] + a[1] * t + a[2] * (t * t) + a[3] * (t * t * t);
+        cb = a[0] + a[1] * t + a[2] * (t * t) + a[3] * pow_cr<3>(t);
     }
 }
 

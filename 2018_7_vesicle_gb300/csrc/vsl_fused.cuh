@@ -1,4 +1,6 @@
-// vsl_fused.cu -- fused TVD-RK3 stage kernels of the method-level operations.
+// vsl_fused.cuh -- fused TVD-RK3 stage kernels of the method-level operations, included
+// by vsl_fused_f64.cu (plain form, compiled without multiply-add contraction so that the
+// FP64 arithmetic rounds like the reference's) and vsl_fused_f32.cu (mixed form).
 //
 // One launch evaluates one Runge-Kutta stage of a whole pseudo-step AND its Shu-Osher
 // combination, writing the next stage field directly:
@@ -14,6 +16,8 @@
 //   bit  7     fixed node (a distance below 1e-6*dx: the reference's step-0 nodes)
 // Distances and crossing values are read only where a bit says they differ from the
 // defaults, so the dense per-stage traffic is phi_s (stencil), phi_n, flags and out.
+#pragma once
+
 #include "vsl_internal.h"
 
 namespace vsl {
@@ -397,8 +401,5 @@ cudaError_t launch_advect_stage(const T *phi_s, const T *phi_n, T *out, Ptr3<con
                                                 cudaStream_t);                                                      \
     template cudaError_t launch_advect_stage<T>(const T *, const T *, T *, Ptr3<const T>, const T *,                \
                                                 const double *, const Grid &, int, bool, cudaStream_t);
-
-VSL_INSTANTIATE_FUSED(float)
-VSL_INSTANTIATE_FUSED(double)
 
 }  // namespace vsl

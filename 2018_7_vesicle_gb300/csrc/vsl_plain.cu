@@ -239,12 +239,13 @@ __global__ void __launch_bounds__(BX *BY) k_set_calculus_toolbox(Fields18 o, con
     double r1 = fxx * fx + fxy * fy + fzx * fz;
     double r2 = fxy * fx + fyy * fy + fyz * fz;
     double r3 = fzx * fx + fyz * fy + fzz * fz;
-    double mean = -lap / gm + (fx * r1 + fy * r2 + fz * r3) / (gm * gm * gm);
+    double mean = -lap / gm + (fx * r1 + fy * r2 + fz * r3) / pow_cr<3>(gm);
     r1 = (fyy * fzz - fyz * fyz) * fx + (fzx * fyz - fxy * fzz) * fy + (fxy * fyz - fzx * fyy) * fz;
     r2 = (fyz * fzx - fxy * fzz) * fx + (fxx * fzz - fzx * fzx) * fy + (fzx * fxy - fxx * fyz) * fz;
     r3 = (fxy * fyz - fyy * fzx) * fx + (fzx * fxy - fxx * fyz) * fy + (fxx * fyy - fxy * fxy) * fz;
     double gm2 = gm * gm;
-    double gauss = (fx * r1 + fy * r2 + fz * r3) / (gm2 * gm2);
+    const double gm4 = pow_cr<4>(gm);
+    double gauss = (fx * r1 + fy * r2 + fz * r3) / gm4;
     double px = (__ldg(hp + xp) - __ldg(hp + xm)) / (2 * dx);
     double py = (__ldg(hp + yp) - __ldg(hp + ym)) / (2 * dy);
     double pz = (__ldg(hp + zp) - __ldg(hp + zm)) / (2 * dz);
@@ -255,7 +256,7 @@ __global__ void __launch_bounds__(BX *BY) k_set_calculus_toolbox(Fields18 o, con
     double pzz = (__ldg(hp + zp) - 2 * hc + __ldg(hp + zm)) / (dz * dz);
     double plap = pxx + pyy + pzz;
     const double vals[18] = {fx,  fy,  fz,  gm,  fx / gm, fy / gm, fz / gm, fxx, fyy, fzz, fxy, fyz, fzx, lap, mean,
-                             gauss, dot / gm2, plap / gm2 - dot * lap / (gm2 * gm2)};
+                             gauss, dot / gm2, plap / gm2 - dot * lap / gm4};
 #pragma unroll
     for (int q = 0; q < 18; ++q) o.p[q][c] = vals[q];
 }

@@ -59,7 +59,8 @@ __global__ void __launch_bounds__(NT) k_toolbox(const T *__restrict__ f, Toolbox
         double r2 = fxy * fx + fyy * fy + fyz * fz;
         double r3 = fzx * fx + fyz * fy + fzz * fz;
         double gm2 = gm * gm;
-        double mean = -lap / gm + (fx * r1 + fy * r2 + fz * r3) / (gm2 * gm);
+        double mean = -lap / gm + (fx * r1 + fy * r2 + fz * r3) / pow_cr<3>(gm);
+        const double gm4 = pow_cr<4>(gm);
         double hc = fmax(fc, 0.0);
         double hxp = H(i, j + 1, k), hxm = H(i, j - 1, k), hyp = H(i + 1, j, k), hym = H(i - 1, j, k);
         double hzp = H(i, j, k + 1), hzm = H(i, j, k - 1);
@@ -70,7 +71,7 @@ __global__ void __launch_bounds__(NT) k_toolbox(const T *__restrict__ f, Toolbox
         double pzz = (hzp - 2 * hc + hzm) / (dz * dz);
         double plap = pxx + pyy + pzz;
         double heav = dot / gm2;
-        double delta = plap / gm2 - dot * lap / (gm2 * gm2);
+        double delta = plap / gm2 - dot * lap / gm4;
         if (fabs(fc) < 2 * ds) area = delta;
         if (fc < 2 * ds) vol = 1 - heav;
         if (o.f[0]) o.f[0][c] = (T)fx;
@@ -92,7 +93,7 @@ __global__ void __launch_bounds__(NT) k_toolbox(const T *__restrict__ f, Toolbox
             double q1 = (fyy * fzz - fyz * fyz) * fx + (fzx * fyz - fxy * fzz) * fy + (fxy * fyz - fzx * fyy) * fz;
             double q2 = (fyz * fzx - fxy * fzz) * fx + (fxx * fzz - fzx * fzx) * fy + (fzx * fxy - fxx * fyz) * fz;
             double q3 = (fxy * fyz - fyy * fzx) * fx + (fzx * fxy - fxx * fyz) * fy + (fxx * fyy - fxy * fxy) * fz;
-            o.f[15][c] = (T)((fx * q1 + fy * q2 + fz * q3) / (gm2 * gm2));
+            o.f[15][c] = (T)((fx * q1 + fy * q2 + fz * q3) / gm4);
         }
         if (o.f[16]) o.f[16][c] = (T)heav;
         if (o.f[17]) o.f[17][c] = (T)delta;

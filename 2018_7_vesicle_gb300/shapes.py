@@ -1,8 +1,9 @@
 """Initial level-set fields of the benchmark and test workloads (host-side numpy setup,
 the role of the reference's SD.Shape package, src/7_0_paper/2_0_Vesicle/+SD/+Shape/).
 
-All fields are float64 numpy arrays of shape (rows, cols, pges) = (y, x, z) in Fortran
-order, the MATLAB meshgrid layout.
+All fields have shape (rows, cols, pges) = (y, x, z), the MATLAB meshgrid layout:
+float64 numpy arrays in Fortran order, or, where a torch device is given, float64 torch
+tensors computed on that device (same values, the pointwise formulas run on the GPU).
 """
 from __future__ import annotations
 
@@ -11,9 +12,36 @@ import math
 import numpy as np
 
 
-def meshgrid(xv, yv, zv):
+def meshgrid(xv, yv, zv, device=None):
+    if device is not None:
+        import torch
+
+        t = [torch.as_tensor(np.asarray(v, float), device=device) for v in (xv, yv, zv)]
+        return torch.meshgrid(t[0], t[1], t[2], indexing="xy")
     x, y, z = np.meshgrid(np.asarray(xv, float), np.asarray(yv, float), np.asarray(zv, float))
     return np.asfortranarray(x), np.asfortranarray(y), np.asfortranarray(z)
+
+
+class _Ops:
+    """The few array functions the shape formulas need, for numpy arrays or torch tensors."""
+
+    def __init__(self, a):
+        self.torch = not isinstance(a, np.ndarray)
+        if self.torch:
+            import torch
+
+            self.m = torch
+        else:
+            self.m = np
+
+    def atan2(self, y, x):
+        return self.m.atan2(y, x) if self.torch else np.arctan2(y, x)
+
+    def fortran(self, a):
+        return a if self.torch else np.asfortranarray(a)
+
+    def __getattr__(self, name):
+        return getattr(self.m, name)
 
 
 def cube_grid(n: int, lo: float, hi: float):
@@ -52,9 +80,9 @@ def oblate_c_for_reduced_volume(rv: float) -> float:
 
 def _legendre_all(lmax: int, t):
     """Associated Legendre P_l^m(t), 0 <= m <= l <= lmax, (no Condon-Shortley phase)."""
-    s = np.sqrt(np.maximum(0.0, 1 - t * t))
-    P = {}
-    P[(0, 0)] = np.ones_like(t)
+    xp = _Ops(t)
+    s = xp.sqrt(xp.clamp(1 - t * t, min=0.0)) if xp.torch else np.sqrt(np.maximum(0.0, 1 - t * t))
+    P = {(0, 0): xp.ones_like(t)}
     for m in range(1, lmax + 1):
         P[(m, m)] = (2 * m - 1) * s * P[(m - 1, m - 1)]
     for m in range(0, lmax):
@@ -65,38 +93,53 @@ def _legendre_all(lmax: int, t):
     return P
 
 
-def sh_noise(x, y, z, lmax: int, seed: int):
-    """Real spherical-harmonic series sum_{l<=lmax, |m|<=l} a_lm Y_lm(theta, phi) with
-    a_lm ~ N(0, 1) from numpy's default_rng(seed), normalised to max |.| = 1 on the grid."""
-    rng = np.random.default_rng(seed)
-    r = np.sqrt(x**2 + y**2 + z**2)
-    t = np.where(r > 0, z / np.where(r > 0, r, 1), 1.0)
-    ph = np.arctan2(y, x)
+def _sh_series(coef, lmax, t, ph):
+    xp = _Ops(t)
     P = _legendre_all(lmax, t)
-    out = np.zeros_like(x)
+    out = xp.zeros_like(t)
+    q = 0
     for l in range(lmax + 1):
         for m in range(-l, l + 1):
             am = abs(m)
             norm = math.sqrt((2 * l + 1) / (4 * math.pi) * math.factorial(l - am) / math.factorial(l + am))
-            ang = np.cos(am * ph) if m >= 0 else np.sin(am * ph)
+            ang = xp.cos(am * ph) if m >= 0 else xp.sin(am * ph)
             if m != 0:
                 norm *= math.sqrt(2)
-            out += rng.standard_normal() * norm * P[(l, am)] * ang
-    return np.asfortranarray(out / np.max(np.abs(out)))
+            out = out + float(coef[q]) * norm * P[(l, am)] * ang
+            q += 1
+    return out
+
+
+def sh_noise(x, y, z, lmax: int, seed: int):
+    """Real spherical-harmonic series sum_{l<=lmax, |m|<=l} a_lm Y_lm(theta, phi) of the
+    direction of (x, y, z), a_lm ~ N(0, 1) from numpy's default_rng(seed), normalised to
+    max |.| = 1 over a 1-degree sphere grid (so any sub-grid sees the same field)."""
+    coef = np.random.default_rng(seed).standard_normal((lmax + 1) ** 2)
+    th, phs = np.meshgrid(np.linspace(0, np.pi, 181), np.linspace(-np.pi, np.pi, 361), indexing="ij")
+    scale = float(np.max(np.abs(_sh_series(coef, lmax, np.cos(th), phs))))
+    xp = _Ops(x)
+    r = xp.sqrt(x**2 + y**2 + z**2)
+    safe = xp.where(r > 0, r, xp.ones_like(r))
+    t = xp.where(r > 0, z / safe, xp.ones_like(r))
+    return xp.fortran(_sh_series(coef, lmax, t, xp.atan2(y, x)) / scale)
 
 
 def noisy_oblate(x, y, z, axes=(1.0, 1.0, 0.55), amplitude: float = 0.02, lmax: int = 6, seed: int = 0):
     """Oblate ellipsoid sqrt(x^2/a^2+y^2/b^2+z^2/c^2) - 1 (Ellipsoid.m:45) with its radius
     perturbed by `amplitude` times a seeded spherical-harmonic series (l <= lmax)."""
     a, b, c = axes
-    base = np.sqrt(x**2 / a**2 + y**2 / b**2 + z**2 / c**2)
-    return np.asfortranarray(base - 1 - amplitude * sh_noise(x, y, z, lmax, seed))
+    xp = _Ops(x)
+    base = xp.sqrt(x**2 / a**2 + y**2 / b**2 + z**2 / c**2)
+    return xp.fortran(base - 1 - amplitude * sh_noise(x, y, z, lmax, seed))
 
 
-def vesicle_256(n: int = 256, seed: int = 0, reduced_volume: float = 0.65):
+def vesicle_256(n: int = 256, seed: int = 0, reduced_volume: float = 0.65, pages=None, device=None):
     """The mixed-precision vesicle workload: n^3 on [-1.5, 1.5]^3, oblate ellipsoid with
-    half axes (1, 1, c(reduced volume)) plus l <= 6 spherical-harmonic noise of 0.02."""
-    x, y, z = cube_grid(n, -1.5, 1.5)
+    half axes (1, 1, c(reduced volume)) plus l <= 6 spherical-harmonic noise of 0.02.
+    `pages` (a slice of z indices) restricts it to a slab of the same field; `device`
+    computes it as torch tensors on that device."""
+    v = np.linspace(-1.5, 1.5, n)
+    x, y, z = meshgrid(v, v, v if pages is None else v[pages], device=device)
     c = oblate_c_for_reduced_volume(reduced_volume)
     return x, y, z, noisy_oblate(x, y, z, axes=(1.0, 1.0, c), seed=seed)
 

@@ -1,0 +1,367 @@
+"""Benchmark of the level-set hot path: the mixed-precision vesicle step at 256^3.
+
+Workload (one "step"): one vesicle step on a 256^3 grid over [-1.5, 1.5]^3, the oblate
+vesicle of reduced volume 0.65 with l <= 6 spherical-harmonic noise: calculus toolbox and
+FP64 area/volume -> 30 WENO5 TVD-RK3 extension pseudo-steps of the mean curvature -> time
+step (CFL 0.5) -> one WENO5 TVD-RK3 advection step -> setDistance -> 20 WENO5 TVD-RK3
+reinitialization pseudo-steps.  FP32 stencils with FP64 interface roots and reductions.
+Grid-point updates per step = 256^3 * (30 + 1 + 20).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  With torchrun, every rank advances its own vesicle (a
+different noise seed): independent replicas, no data exchange; `value` is the sum over
+ranks of the per-rank throughput measured over the max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PKG = "2018_7_vesicle_gb300"
+N = 256
+EXT, ADV, RE = 30, 1, 20
+GPT_PER_NODE = EXT + ADV + RE
+CFL = 0.5
+METRIC = "Gpt-updates/s"
+UNIT = "Gpt/s"
+W32 = 4
+# algorithmic bytes per grid-point update of each operator (reference dataflow, w = 4)
+BYTES_REINIT = 29 * W32 + 3
+BYTES_EXTEND = 56 * W32
+BYTES_ADVECT = 17 * W32
+# per-node setup bytes counted once per step (distances 7w, normals 10w, crossings 13w,
+# toolbox + reductions 1w, plus a second setDistance 7w)
+BYTES_SETUP = (7 + 10 + 13 + 1 + 7) * W32
+BYTES_PER_NODE_STEP = EXT * BYTES_EXTEND + ADV * BYTES_ADVECT + RE * BYTES_REINIT + BYTES_SETUP
+# kernels launched per vesicle step: toolbox, sum, velocity, classify, crossing,
+# 3*EXT extension stages, band max, time step, 3 advection stages, setDistance,
+# classify, 3*RE reinitialization stages
+LAUNCHES_PER_STEP = 1 + 1 + 1 + 1 + 1 + 3 * EXT + 1 + 1 + 3 * ADV + 1 + 1 + 3 * RE
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "extend_stage_f32_256.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch_256:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.out = out
+        else:
+            self.out = ""
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_sample(seconds: float = 10.0, seed: int = 0):
+    """The oracle on a bounded sample of the workload: full vesicle steps on a 32-page slab
+    through the middle of the 256^3 field, all host threads, repeated for >= `seconds`."""
+    from oracle import build_oracle
+    from oracle import oracle as O
+
+    build_oracle.build_port()
+    S = importlib.import_module(PKG + ".shapes")
+    K = O.kernels("port")
+    x, y, z, F = S.vesicle_256(N, seed=seed, pages=slice(N // 2 - 16, N // 2 + 16))
+    F = O.F64(F)
+    g = O.Grid(F.shape[0], F.shape[1], F.shape[2], 3.0 / (N - 1), 3.0 / (N - 1), 3.0 / (N - 1))
+    d = O.set_distance(K, g, F)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        F, d, _ = O.vesicle_step(K, g, F, d, EXT, RE, CFL)
+        steps += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    nodes = g.num_ele
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {
+        "value": GPT_PER_NODE * nodes * steps / el / 1e9,
+        "unit": UNIT,
+        "cores": cores,
+        "kind": "port",
+        "sample": f"{steps} full vesicle step(s) (30 ext + 1 adv + 20 reinit) on a 256x256x32 slab "
+                  f"of the 256^3 field, oracle C restatement, OpenMP over pages, {el:.1f} s",
+    }
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference's CPU kernels (oracle/_ref where it was compiled
+    here, else the oracle restatement) on the host cores, rank 0 only."""
+    if rank != 0:
+        return
+    per = []
+    base = None
+    for i in range(args.warmup + args.steps):
+        s = cpu_sample(seconds=max(2.0, 20.0 / max(1, args.steps + args.warmup)), seed=0)
+        if i >= args.warmup:
+            per.append(s["value"])
+        base = s
+    v = statistics.median(per)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args.gpus),
+        "cpu_baseline": {**base, "value": v},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def profile_case(which, m, torch):
+    """A handful of launches of one operator on the full 256^3 field (ncu capture case)."""
+    C = m.F.clone()
+    for _ in range(2):
+        if which == "extend":
+            m.WENO5RK3Extend(C, 2)
+        elif which == "reinit":
+            m.WENO5RK3Reinitialization(m.F, 2)
+        elif which == "advect":
+            v = m.F.clone().fill_(0.5)
+            m.WENO5RK3Advection(m.F, v, v, v, 1e-3, steps=2)
+        else:
+            m.vesicle_step(2, 2, CFL)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": which, "ok": True}))
+
+
+def workload_config(ngpus):
+    return {"workload": f"vesicle step {N}^3 mixed precision (FP32 stencils, FP64 roots/reductions): "
+                        f"{EXT} WENO5-RK3 extension + {ADV} WENO5-RK3 advection + {RE} WENO5-RK3 reinit "
+                        "pseudo-steps, oblate rv 0.65 + SH noise on [-1.5,1.5]^3",
+            "grid": [N, N, N], "gpt_per_step": GPT_PER_NODE * N**3, "parallelism": f"replicas x{ngpus}",
+            "l2": "working set ~1.4 GB per GPU, larger than the 129 MB L2"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--profile", choices=["extend", "reinit", "advect", "step"],
+                    help="run only a few launches of one operator at 256^3 (the ncu capture case)")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    pkg = importlib.import_module(PKG)
+    pkg.build()
+    S = importlib.import_module(PKG + ".shapes")
+    x, y, z, F0 = S.vesicle_256(N, seed=rank, device="cuda")
+    h = 3.0 / (N - 1)
+    grid = pkg.GD3(x, y, z, spacing=(h, h, h))
+    m = pkg.SDF3(grid, Val=F0, precision="f32")
+    m.setDistance()
+    # only the level-set object stays on the device (coordinates are not needed)
+    del x, y, z, F0
+    grid.X = grid.Y = grid.Z = None
+    torch.cuda.empty_cache()
+    stream = torch.cuda.current_stream()
+    if args.profile:
+        return profile_case(args.profile, m, torch)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        m.vesicle_step(EXT, RE, CFL)
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            info = m.vesicle_step(EXT, RE, CFL)
+        ev1.record(stream)
+        barrier()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    gpt_step = GPT_PER_NODE * N**3
+    value = world * gpt_step / (ms / 1e3) / 1e9
+    info_h = info.cpu().tolist()
+
+    # dominant kernel: the FP32 extension stage, timed live on the launching stream as
+    # (extension with 30 pseudo-steps) - (extension with 0 pseudo-steps) over 90 launches
+    C = m.F.clone()
+    for _ in range(2):
+        m.WENO5RK3Extend(C, EXT)
+    def t_ext(iters, reps=3):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            m.WENO5RK3Extend(C, iters)
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+    stage_ms = (t_ext(EXT) - t_ext(0)) / (3 * EXT)
+    hbm, peak_kind = peaks()
+    alg_bytes_launch = BYTES_EXTEND / 3 * N**3
+    achieved = alg_bytes_launch / (stage_ms / 1e3) / 1e9
+    traffic = profiled_traffic()
+
+    # end to end through the public API with host buffers: H2D of F, setDistance, one
+    # vesicle step, D2H of F and of [area, volume, dt, max|Vn|]
+    F_host = torch.empty(N**3, dtype=torch.float32, pin_memory=True)
+    F_host.copy_(m.F.permute(2, 1, 0).reshape(-1).cpu())
+    F_out = torch.empty_like(F_host, pin_memory=True)
+    info_out = torch.empty(4, dtype=torch.float64, pin_memory=True)
+    Fv = m.F.permute(2, 1, 0).reshape(-1)  # column-major storage as a flat view
+    e2e_steps = max(2, args.steps // 2)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        Fv.copy_(F_host, non_blocking=True)
+        m.setDistance()
+        inf = m.vesicle_step(EXT, RE, CFL)
+        F_out.copy_(Fv, non_blocking=True)
+        info_out.copy_(inf, non_blocking=True)
+    barrier()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_val = world * gpt_step / e2e_s / 1e9
+
+    # the plain FP64 form of the same step, for the FP32/FP64 throughput ratio
+    fp64 = None
+    if not args.no_fp64:
+        F0 = S.vesicle_256(N, seed=rank, device="cuda")[3]
+        m64 = pkg.SDF3(grid, Val=F0, precision="f64")
+        del F0
+        m64.setDistance()
+        m64.vesicle_step(EXT, RE, CFL)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        m64.vesicle_step(EXT, RE, CFL)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms64 = a.elapsed_time(b)
+        fp64 = {"value": gpt_step / (ms64 / 1e3) / 1e9, "unit": UNIT, "ms_per_step": ms64,
+                "ratio_fp32_over_fp64": (gpt_step / (ms / 1e3)) / (gpt_step / (ms64 / 1e3))}
+        del m64
+
+    if rank != 0:
+        if dist is not None:
+            dist.barrier()
+        return
+    cpu = None if args.no_cpu_baseline else cpu_sample(seconds=10.0)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(world),
+        "roofline": {"bound": "hbm", "kernel": "k_extend_stage<float> (one WENO5 RK3 extension stage)",
+                     "achieved": achieved, "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic, "stage_ms": stage_ms,
+                     "algorithmic_bytes_per_launch": alg_bytes_launch,
+                     "effective": "fused stage reads fewer bytes than the reference dataflow counts"},
+        "step_hbm": {"algorithmic_bytes_per_step": BYTES_PER_NODE_STEP * N**3,
+                     "achieved_gbs": BYTES_PER_NODE_STEP * N**3 / (ms / 1e3) / 1e9,
+                     "frac": BYTES_PER_NODE_STEP * N**3 / (ms / 1e3) / 1e9 / hbm},
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 4 * N**3,
+                "d2h_bytes_per_step": 4 * N**3 + 32, "ms_per_step": e2e_s * 1e3},
+        "gpu_launches": LAUNCHES_PER_STEP * args.steps,
+        "clocks": clk.summary(),
+        "fp64_plain": fp64,
+        "last_info": {"area": info_h[0], "volume": info_h[1], "dt": info_h[2], "max_speed": info_h[3]},
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

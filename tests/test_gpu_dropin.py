@@ -83,8 +83,9 @@ def test_normals_crossings_extend_step(case, oracle_mod):
         ref = O.zeros(g)
         (K.extend_step_eno3 if e3 else K.extend_step)(ref, dt, O.F64(G["C"]), *v, *dd.six(), *cpo, *g.args(), g.num_ele)
         step = empty(shape, fill=np.nan)
-        vsl.call("vsl_extend_step_eno3" if e3 else "vsl_extend_step", ptr(step), ptr(dev(dt)), ptr(C),
-                 *[ptr(dev(a)) for a in v], *map(ptr, d), *[ptr(dev(a)) for a in cpo], *shape, *h, n, stream())
+        dt_d, v_d, cp_d = dev(dt), [dev(a) for a in v], [dev(a) for a in cpo]  # kept alive across the call
+        vsl.call("vsl_extend_step_eno3" if e3 else "vsl_extend_step", ptr(step), ptr(dt_d), ptr(C),
+                 *map(ptr, v_d), *map(ptr, d), *map(ptr, cp_d), *shape, *h, n, stream())
         assert max_rel(host(step), ref, scale=max(1e-300, float(np.max(np.abs(ref))))) <= 1e-11
 
 
