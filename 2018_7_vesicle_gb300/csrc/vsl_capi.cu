@@ -26,10 +26,26 @@ struct Bump {
     }
 };
 
+// band queue of the tiled FP32 kernels (allocated for FP32 only) and its stage count
+struct Band {
+    BandQueue q{nullptr, nullptr};
+    int seq = 0;
+};
+template <typename T> Band carve_band(Bump &w, const Grid &g)
+{
+    Band b;
+    if (std::is_same<T, float>::value) {
+        b.q.queue = w.take<unsigned>(g.num);
+        b.q.counter = w.take<unsigned>(2);
+    }
+    return b;
+}
+
 template <typename T> struct ReinitWork {
     T *b, *c;
     uint8_t *flags;
     Ptr6<T> dist;  // ENO3 only
+    Band band;
 };
 template <typename T> ReinitWork<T> carve_reinit(Bump &w, const Grid &g, bool own_dist)
 {
@@ -38,6 +54,7 @@ template <typename T> ReinitWork<T> carve_reinit(Bump &w, const Grid &g, bool ow
     r.c = w.take<T>(g.num);
     r.flags = w.take<uint8_t>(g.num);
     for (int q = 0; q < 6; ++q) r.dist.p[q] = own_dist ? w.take<T>(g.num) : nullptr;
+    r.band = carve_band<T>(w, g);
     return r;
 }
 
@@ -47,6 +64,7 @@ template <typename T> struct ExtendWork {
     T *b, *c;
     uint8_t *flags;
     Ptr6<T> dist;  // ENO3 only
+    Band band;
 };
 template <typename T> ExtendWork<T> carve_extend(Bump &w, const Grid &g, bool own_dist)
 {
@@ -57,7 +75,16 @@ template <typename T> ExtendWork<T> carve_extend(Bump &w, const Grid &g, bool ow
     e.c = w.take<T>(g.num);
     e.flags = w.take<uint8_t>(g.num);
     for (int q = 0; q < 6; ++q) e.dist.p[q] = own_dist ? w.take<T>(g.num) : nullptr;
+    e.band = carve_band<T>(w, g);
     return e;
+}
+
+// zero the band counters before the first tiled stage of an operation
+int band_reset(Band &b, cudaStream_t s)
+{
+    b.seq = 0;
+    if (b.q.counter == nullptr) return VSL_OK;
+    return cudaMemsetAsync(b.q.counter, 0, 2 * sizeof(unsigned), s) == cudaSuccess ? VSL_OK : VSL_ERR_CUDA;
 }
 
 template <typename T> struct RedistWork {
@@ -160,11 +187,31 @@ template <typename T> Ptr3<const T> cview3(const Ptr3<T> &p)
 // loops
 // ---------------------------------------------------------------------------------------
 
+// one stage through the tiled FP32 kernels (stage input s_in, RK3 base n_in, output out)
+inline cudaError_t tiled(int kind, bool eno3, Band &band, const float *s_in, const float *n_in, float *out,
+                         const uint8_t *flags, Ptr6<const float> d, Ptr6<const float> cp, Ptr3<const float> v,
+                         const float *speed, const double *dt, int stage, const Grid &g, cudaStream_t s)
+{
+    TiledStage st{s_in, n_in, out, flags, d, cp, v, speed, dt, band.q, stage, band.seq++};
+    return launch_tiled_stage(kind, eno3, st, g, s);
+}
+
 // `iters` TVD-RK3 reinitialization pseudo-steps of F in place (flags already classified)
 template <typename T>
-int reinit_loop(T *F, int iters, Ptr6<const T> d, const ReinitWork<T> &w, const Grid &g, bool eno3, cudaStream_t s)
+int reinit_loop(T *F, int iters, Ptr6<const T> d, ReinitWork<T> &w, const Grid &g, bool eno3, cudaStream_t s)
 {
     const bool fast = fast_form<T>();
+    if constexpr (std::is_same<T, float>::value) {
+        if (int st = band_reset(w.band, s)) return st;
+        const Ptr6<const float> none6{};
+        const Ptr3<const float> none3{};
+        for (int it = 0; it < iters; ++it) {
+            VSL_TRY(tiled(0, eno3, w.band, F, F, w.b, w.flags, d, none6, none3, nullptr, nullptr, 0, g, s));
+            VSL_TRY(tiled(0, eno3, w.band, w.b, F, w.c, w.flags, d, none6, none3, nullptr, nullptr, 1, g, s));
+            VSL_TRY(tiled(0, eno3, w.band, w.c, F, F, w.flags, d, none6, none3, nullptr, nullptr, 2, g, s));
+        }
+        return VSL_OK;
+    }
     for (int it = 0; it < iters; ++it) {
         VSL_TRY(launch_reinit_stage<T>(F, F, w.b, w.flags, d, g, 0, eno3, fast, s));
         VSL_TRY(launch_reinit_stage<T>(w.b, F, w.c, w.flags, d, g, 1, eno3, fast, s));
@@ -185,12 +232,21 @@ int extend_setup(const T *F, Ptr6<const T> d, const ExtendWork<T> &w, const Grid
 
 // crossing values of C, then `iters` TVD-RK3 extension pseudo-steps of C in place
 template <typename T>
-int extend_loop(T *C, int iters, Ptr6<const T> d, const ExtendWork<T> &w, const Grid &g, bool eno3, cudaStream_t s)
+int extend_loop(T *C, int iters, Ptr6<const T> d, ExtendWork<T> &w, const Grid &g, bool eno3, cudaStream_t s)
 {
     const bool fast = fast_form<T>();
     VSL_TRY(launch_crossing<T>(C, d, w.cp, g, eno3, s));
     Ptr6<const T> cp = cview(w.cp);
     Ptr3<const T> v = cview3(w.v);
+    if constexpr (std::is_same<T, float>::value) {
+        if (int st = band_reset(w.band, s)) return st;
+        for (int it = 0; it < iters; ++it) {
+            VSL_TRY(tiled(1, eno3, w.band, C, C, w.b, w.flags, d, cp, v, nullptr, nullptr, 0, g, s));
+            VSL_TRY(tiled(1, eno3, w.band, w.b, C, w.c, w.flags, d, cp, v, nullptr, nullptr, 1, g, s));
+            VSL_TRY(tiled(1, eno3, w.band, w.c, C, C, w.flags, d, cp, v, nullptr, nullptr, 2, g, s));
+        }
+        return VSL_OK;
+    }
     for (int it = 0; it < iters; ++it) {
         VSL_TRY(launch_extend_stage<T>(C, C, w.b, w.flags, d, cp, v, g, 0, eno3, fast, s));
         VSL_TRY(launch_extend_stage<T>(w.b, C, w.c, w.flags, d, cp, v, g, 1, eno3, fast, s));
@@ -200,10 +256,19 @@ int extend_loop(T *C, int iters, Ptr6<const T> d, const ExtendWork<T> &w, const 
 }
 
 template <typename T>
-int advect_loop(T *F, Ptr3<const T> v, const T *speed, const double *dt, int steps, const ReinitWork<T> &w,
-                const Grid &g, cudaStream_t s)
+int advect_loop(T *F, Ptr3<const T> v, const T *speed, const double *dt, int steps, ReinitWork<T> &w, const Grid &g,
+                cudaStream_t s)
 {
     const bool fast = fast_form<T>();
+    if constexpr (std::is_same<T, float>::value) {
+        const Ptr6<const float> none6{};
+        for (int it = 0; it < steps; ++it) {
+            VSL_TRY(tiled(2, false, w.band, F, F, w.b, nullptr, none6, none6, v, speed, dt, 0, g, s));
+            VSL_TRY(tiled(2, false, w.band, w.b, F, w.c, nullptr, none6, none6, v, speed, dt, 1, g, s));
+            VSL_TRY(tiled(2, false, w.band, w.c, F, F, nullptr, none6, none6, v, speed, dt, 2, g, s));
+        }
+        return VSL_OK;
+    }
     for (int it = 0; it < steps; ++it) {
         VSL_TRY(launch_advect_stage<T>(F, F, w.b, v, speed, dt, g, 0, fast, s));
         VSL_TRY(launch_advect_stage<T>(w.b, F, w.c, v, speed, dt, g, 1, fast, s));
@@ -320,15 +385,24 @@ int op_redistance(T *A, int iter1, int iter2, const T *F, int rows, int cols, in
     Ptr6<const T> dF = cview(w.ext.dist);
     if (int st = extend_setup<T>(F, dF, w.ext, g, false, 1e-14, s)) return st;
     const bool fast = fast_form<T>();
+    if (int st = band_reset(w.re.band, s)) return st;
+    // one reinitialization stage of A's pseudo-time loop (tiled kernels for FP32)
+    auto re_stage = [&](const T *in, T *out, int stage) -> cudaError_t {
+        if constexpr (std::is_same<T, float>::value)
+            return tiled(0, false, w.re.band, in, A, out, w.re.flags, dA, Ptr6<const float>{}, Ptr3<const float>{},
+                         nullptr, nullptr, stage, g, s);
+        else
+            return launch_reinit_stage<T>(in, A, out, w.re.flags, dA, g, stage, false, fast, s);
+    };
     // the reinit stages need their own temporaries: the extension uses w.ext.b/c
     T *t1 = w.re.b, *t2 = w.re.c;
     for (int it = 0; it < iter1; ++it) {
         if (int st = extend_loop<T>(A, iter2, dF, w.ext, g, false, s)) return st;
-        VSL_TRY(launch_reinit_stage<T>(A, A, t1, w.re.flags, dA, g, 0, false, fast, s));
+        VSL_TRY(re_stage(A, t1, 0));
         if (int st = extend_loop<T>(t1, iter2, dF, w.ext, g, false, s)) return st;
-        VSL_TRY(launch_reinit_stage<T>(t1, A, t2, w.re.flags, dA, g, 1, false, fast, s));
+        VSL_TRY(re_stage(t1, t2, 1));
         if (int st = extend_loop<T>(t2, iter2, dF, w.ext, g, false, s)) return st;
-        VSL_TRY(launch_reinit_stage<T>(t2, A, A, w.re.flags, dA, g, 2, false, fast, s));
+        VSL_TRY(re_stage(t2, A, 2));
     }
     return extend_loop<T>(A, iter2, dF, w.ext, g, false, s);
 }
@@ -398,6 +472,7 @@ int op_vesicle_step(T *F, T *xpr, T *xpl, T *ypf, T *ypb, T *zpu, T *zpd, int ex
     ReinitWork<T> tmp{};
     tmp.b = w.ext.b;
     tmp.c = w.ext.c;
+    tmp.band = w.ext.band;
     if (int st = advect_loop<T>(F, cview3(w.nrm), w.vn, info + 2, 1, tmp, g, s)) return st;
     // setDistance, then reinitialization
     VSL_TRY(launch_set_distance<T>(F, Ptr6<T>{{xpr, xpl, ypf, ypb, zpu, zpd}}, g, true, s));
@@ -405,6 +480,7 @@ int op_vesicle_step(T *F, T *xpr, T *xpl, T *ypf, T *ypb, T *zpu, T *zpd, int ex
     rw.b = w.ext.b;
     rw.c = w.ext.c;
     rw.flags = w.ext.flags;
+    rw.band = w.ext.band;
     VSL_TRY(launch_classify<T>(F, d, rw.flags, g, s));
     return reinit_loop<T>(F, reinit_iters, d, rw, g, false, s);
 }

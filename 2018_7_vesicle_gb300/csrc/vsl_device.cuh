@@ -331,10 +331,14 @@ __device__ __forceinline__ T weno5_plain(T v1, T v2, T v3, T v4, T v5)
     return (a1 / tot) * q1 + (a2 / tot) * q2 + (a3 / tot) * q3;
 }
 
-// The same reconstruction from UNSCALED differences u = h*v with eps2 = eps*h^2, one
-// division instead of six: with Q_k = (S_k(u) + eps2)^2 the normalised weights are
-// d_k/Q_k / sum, i.e. d_k*Q_l*Q_m / (d_1 Q_2 Q_3 + d_2 Q_1 Q_3 + d_3 Q_1 Q_2); the result
-// is then multiplied by 1/h.  Algebraically identical to weno5_plain(u/h).
+// a / b: the hardware reciprocal-based quotient for float (about 2 ulp), IEEE for double
+__device__ __forceinline__ float fast_div(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double fast_div(double a, double b) { return a / b; }
+
+// The same reconstruction from UNSCALED differences u = h*v with eps2 = eps*h^2 and the
+// 1/h factor applied once at the end (S_k(u) = h^2 S_k(v), so the normalised weights are
+// unchanged); the weights use the fast quotient.  Algebraically identical to
+// weno5_plain(u/h) * h; used by the mixed-precision form only.
 template <typename T>
 __device__ __forceinline__ T weno5_fast(T u1, T u2, T u3, T u4, T u5, T eps2)
 {
@@ -344,9 +348,10 @@ __device__ __forceinline__ T weno5_fast(T u1, T u2, T u3, T u4, T u5, T eps2)
     T s1 = T(13. / 12.) * sqr(u1 - 2 * u2 + u3) + T(1. / 4.) * sqr(u1 - 4 * u2 + 3 * u3);
     T s2 = T(13. / 12.) * sqr(u2 - 2 * u3 + u4) + T(1. / 4.) * sqr(u2 - u4);
     T s3 = T(13. / 12.) * sqr(u3 - 2 * u4 + u5) + T(1. / 4.) * sqr(3 * u3 - 4 * u4 + u5);
-    T Q1 = sqr(s1 + eps2), Q2 = sqr(s2 + eps2), Q3 = sqr(s3 + eps2);
-    T w1 = T(0.1) * (Q2 * Q3), w2 = T(0.6) * (Q1 * Q3), w3 = T(0.3) * (Q1 * Q2);
-    return (w1 * q1 + w2 * q2 + w3 * q3) / (w1 + w2 + w3);
+    T a1 = fast_div(T(0.1), sqr(s1 + eps2));
+    T a2 = fast_div(T(0.6), sqr(s2 + eps2));
+    T a3 = fast_div(T(0.3), sqr(s3 + eps2));
+    return fast_div(a1 * q1 + a2 * q2 + a3 * q3, a1 + a2 + a3);
 }
 
 // Seven-point stencil with the interface inserted at r1 (forward) / l1 (backward) when

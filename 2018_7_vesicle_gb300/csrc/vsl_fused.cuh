@@ -127,13 +127,12 @@ __global__ void __launch_bounds__(BX *BY) k_classify(const T *__restrict__ phi0,
 // ---------------------------------------------------------------------------------------
 // reinitialization stage (re_step.cu:283-393 / weno_rk3_reinitialization.cu:295-406)
 // ---------------------------------------------------------------------------------------
+// one node of a reinitialization stage, all reads from global memory (clamped)
 template <typename T, bool ENO3, bool FAST>
-__global__ void __launch_bounds__(BX *BY) k_reinit_stage(const T *__restrict__ phi_s, const T *__restrict__ phi_n,
-                                                           T *__restrict__ out, const uint8_t *__restrict__ flags,
-                                                           Ptr6<const T> d, Grid g, int stage)
+__device__ __forceinline__ void reinit_node(const T *__restrict__ phi_s, const T *__restrict__ phi_n,
+                                            T *__restrict__ out, const uint8_t *__restrict__ flags,
+                                            const Ptr6<const T> &d, const Grid &g, int stage, int i, int j, int k)
 {
-    int i, j, k;
-    if (!fused_node(g, i, j, k)) return;
     const long long c = node_index(g, i, j, k);
     const uint8_t fl = __ldg(flags + c);
     const T ps = __ldg(phi_s + c);
@@ -160,6 +159,16 @@ __global__ void __launch_bounds__(BX *BY) k_reinit_stage(const T *__restrict__ p
     }
     const T pn = stage == 0 ? T(0) : __ldg(phi_n + c);
     out[c] = rk3_combine(stage, pn, ps - step);
+}
+
+template <typename T, bool ENO3, bool FAST>
+__global__ void __launch_bounds__(BX *BY) k_reinit_stage(const T *__restrict__ phi_s, const T *__restrict__ phi_n,
+                                                           T *__restrict__ out, const uint8_t *__restrict__ flags,
+                                                           Ptr6<const T> d, Grid g, int stage)
+{
+    int i, j, k;
+    if (!fused_node(g, i, j, k)) return;
+    reinit_node<T, ENO3, FAST>(phi_s, phi_n, out, flags, d, g, stage, i, j, k);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -224,14 +233,13 @@ __global__ void __launch_bounds__(BX *BY) k_crossing(const T *__restrict__ cfiel
 // ---------------------------------------------------------------------------------------
 // extension stage (extend_step.cu:10-125 / wenork3_extend.cu:372-487)
 // ---------------------------------------------------------------------------------------
+// one node of an extension stage, all reads from global memory (clamped)
 template <typename T, bool ENO3, bool FAST>
-__global__ void __launch_bounds__(BX *BY) k_extend_stage(const T *__restrict__ c_s, const T *__restrict__ c_n,
-                                                           T *__restrict__ out, const uint8_t *__restrict__ flags,
-                                                           Ptr6<const T> d, Ptr6<const T> cp, Ptr3<const T> v, Grid g,
-                                                           int stage)
+__device__ __forceinline__ void extend_node(const T *__restrict__ c_s, const T *__restrict__ c_n, T *__restrict__ out,
+                                            const uint8_t *__restrict__ flags, const Ptr6<const T> &d,
+                                            const Ptr6<const T> &cp, const Ptr3<const T> &v, const Grid &g, int stage,
+                                            int i, int j, int k)
 {
-    int i, j, k;
-    if (!fused_node(g, i, j, k)) return;
     const long long c = node_index(g, i, j, k);
     const uint8_t fl = __ldg(flags + c);
     const T cs = __ldg(c_s + c);
@@ -260,6 +268,17 @@ __global__ void __launch_bounds__(BX *BY) k_extend_stage(const T *__restrict__ c
     }
     const T pn = stage == 0 ? T(0) : __ldg(c_n + c);
     out[c] = rk3_combine(stage, pn, cs - step);
+}
+
+template <typename T, bool ENO3, bool FAST>
+__global__ void __launch_bounds__(BX *BY) k_extend_stage(const T *__restrict__ c_s, const T *__restrict__ c_n,
+                                                           T *__restrict__ out, const uint8_t *__restrict__ flags,
+                                                           Ptr6<const T> d, Ptr6<const T> cp, Ptr3<const T> v, Grid g,
+                                                           int stage)
+{
+    int i, j, k;
+    if (!fused_node(g, i, j, k)) return;
+    extend_node<T, ENO3, FAST>(c_s, c_n, out, flags, d, cp, v, g, stage, i, j, k);
 }
 
 // ---------------------------------------------------------------------------------------

@@ -56,6 +56,30 @@ template <typename T>
 cudaError_t launch_advect_stage(const T *phi_s, const T *phi_n, T *out, Ptr3<const T> v, const T *speed,
                                 const double *dt, const Grid &g, int stage, bool fast, cudaStream_t s);
 
+// ---- tiled FP32 stage kernels (vsl_tiled.cuh, built into vsl_fused_f32.cu) ----------
+// compact queue of the nodes that need the interface-aware stencil, two counters used
+// alternately by consecutive stages (zeroed at the start of an operation)
+struct BandQueue {
+    unsigned *queue;
+    unsigned *counter;
+};
+struct TiledStage {
+    const float *phi_s;
+    const float *phi_n;
+    float *out;
+    const uint8_t *flags;
+    Ptr6<const float> d;
+    Ptr6<const float> cp;
+    Ptr3<const float> v;
+    const float *speed;
+    const double *dt;
+    BandQueue band;
+    int stage;  // 0, 1, 2 within the RK3 step
+    int seq;    // running stage count since the counters were zeroed
+};
+// kind: 0 reinitialization, 1 extension, 2 advection
+cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const Grid &g, cudaStream_t s);
+
 // ---- toolbox and reductions (vsl_toolbox.cu) ------------------------------------------
 // Fields of the calculus toolbox a caller may ask for (null pointers are skipped).
 template <typename T> struct ToolboxOut {

@@ -1,0 +1,256 @@
+// vsl_tiled.cuh -- 2.5D-tiled stage kernels of the mixed-precision (FP32) form.
+//
+// A block of 32 x 8 threads owns a tile of 32 rows x 8 columns and marches KZ pages along
+// z.  The x and y stencils of page k come from a ring of 5 shared-memory planes holding
+// the tile with a 3-node halo (clamped at the grid edge when loaded, so the stencil reads
+// need no clamping); the z stencil comes from a 7-deep register queue per thread.  One
+// barrier per page: at page k the block loads page k+4 into the slot page k-1 vacated and
+// takes the centre of page k+3 into the queue.
+//
+// Nodes whose update needs the interface-aware (nonuniform) stencil -- the "band" -- are
+// not computed here: their indices go to a compact queue (warp-aggregated atomics) and
+// band_stage_kernel processes them with the generic per-node code, so the uniform WENO5
+// path runs without divergence.  A node is band when, for the reinitialization, the sign
+// of phi changes on one of its stencil edges (the reference's trigger), and for the
+// extension when one of its distances differs from the spacing (a superset of the
+// reference's trigger r1 < h || l1 < h; the band kernel applies the exact test).
+#pragma once
+
+#include "vsl_fused.cuh"
+
+namespace vsl {
+namespace {
+
+constexpr int TY = 32;  // rows per tile (threadIdx.x)
+constexpr int TX = 8;   // columns per tile (threadIdx.y)
+constexpr int KZ = 32;  // pages per block
+constexpr int HALO = 3;
+constexpr int SW = TY + 2 * HALO;  // smem row extent (fastest)
+constexpr int SH = TX + 2 * HALO;
+constexpr int PLANE = SW * SH;
+constexpr int RING = 5;
+
+enum StageKind { SK_REINIT = 0, SK_EXTEND = 1, SK_ADVECT = 2 };
+
+struct TiledArgs {
+    const float *phi_s;
+    const float *phi_n;
+    float *out;
+    const uint8_t *flags;
+    Ptr6<const float> d;
+    Ptr3<const float> v;
+    const float *speed;
+    const double *dt;
+    unsigned *queue;
+    unsigned *counter;
+    Grid g;
+    int stage;
+    float h[3], inv_h[3], eps2[3];
+    float dt_uniform;  // 0.3 * min spacing: the pseudo time step of a node with no crossing
+};
+
+template <int KIND>
+__global__ void __launch_bounds__(TY *TX) k_stage_tiled(TiledArgs a)
+{
+    __shared__ float sm[RING][SH][SW];
+    const Grid &g = a.g;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int tid = ty * TY + tx;
+    const int i0 = blockIdx.x * TY, j0 = blockIdx.y * TX;
+    const int i = i0 + tx, j = j0 + ty;
+    const int k0 = blockIdx.z * KZ;
+    const int k1 = min(k0 + KZ, g.pges);
+    const bool active = i < g.rows && j < g.cols;
+
+    // load page p (clamped) of the tile with its halo into ring slot p % RING
+    auto load_plane = [&](int p) {
+        const int pc = clampi(p, g.pges);
+        float *dst = &sm[((p % RING) + RING) % RING][0][0];
+        const float *src = a.phi_s + (long long)pc * g.plane;
+        for (int e = tid; e < PLANE; e += TY * TX) {
+            const int sy = e / SW, sx = e - sy * SW;
+            const int gi = clampi(i0 + sx - HALO, g.rows), gj = clampi(j0 + sy - HALO, g.cols);
+            dst[e] = __ldg(src + (long long)gj * g.rows + gi);
+        }
+    };
+    auto slot = [&](int p) { return ((p % RING) + RING) % RING; };
+
+    float q[7];  // phi_s(i, j, k-3 .. k+3)
+    for (int p = k0; p < k0 + 4; ++p) load_plane(p);
+    {
+        const int ic = clampi(i, g.rows), jc = clampi(j, g.cols);
+        const float *col = a.phi_s + (long long)jc * g.rows + ic;
+#pragma unroll
+        for (int s = 0; s < 3; ++s) q[s] = __ldg(col + (long long)clampi(k0 - 3 + s, g.pges) * g.plane);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 3; s < 6; ++s) q[s] = sm[slot(k0 + s - 3)][ty + HALO][tx + HALO];
+
+    const unsigned lane = tid & 31;
+    for (int k = k0; k < k1; ++k) {
+        __syncthreads();
+        load_plane(k + 4);
+        q[6] = sm[slot(k + 3)][ty + HALO][tx + HALO];
+        const float(*P)[SW] = sm[slot(k)];
+
+        bool band = false;
+        if (active) {
+            const long long c = (long long)k * g.plane + (long long)j * g.rows + i;
+            float px[7], py[7];
+#pragma unroll
+            for (int s = 0; s < 7; ++s) {
+                px[s] = P[ty + s][tx + HALO];
+                py[s] = P[ty + HALO][tx + s];
+            }
+            const float ps = q[3];
+            uint8_t fl = 0;
+            if (KIND != SK_ADVECT) fl = __ldg(a.flags + c);
+            float step = 0.f;
+            bool compute = true;
+            if (KIND != SK_ADVECT && (fl & FIXED_BIT)) compute = false;
+            if (compute && KIND == SK_REINIT) {
+                band = px[2] * px[3] < 0.f || px[3] * px[4] < 0.f || py[2] * py[3] < 0.f || py[3] * py[4] < 0.f ||
+                       q[2] * q[3] < 0.f || q[3] * q[4] < 0.f;
+            } else if (compute && KIND == SK_EXTEND) {
+                band = (fl & 0x3F) != 0;
+            }
+            if (compute && !band) {
+                float dxf, dxb, dyf, dyb, dzf, dzb;
+                weno5_pair_fast(px, a.inv_h[0], a.eps2[0], dxf, dxb);
+                weno5_pair_fast(py, a.inv_h[1], a.eps2[1], dyf, dyb);
+                weno5_pair_fast(q, a.inv_h[2], a.eps2[2], dzf, dzb);
+                if (KIND == SK_REINIT) {
+                    const bool neg = fl & MASK_BIT;
+                    const float dtn = (fl & 0x3F) ? pseudo_dt(fl, a.d, c, a.h[0], a.h[1], a.h[2]) : a.dt_uniform;
+                    const float gn = godunov_norm(neg, dxf, dxb, dyf, dyb, dzf, dzb);
+                    step = (gn - 1.f) * dtn * (neg ? -1.f : 1.f);
+                } else if (KIND == SK_EXTEND) {
+                    step = upwind_dot(__ldg(a.v.p[0] + c), __ldg(a.v.p[1] + c), __ldg(a.v.p[2] + c), dxf, dxb, dyf,
+                                      dyb, dzf, dzb) *
+                           a.dt_uniform;
+                } else {
+                    float vx = __ldg(a.v.p[0] + c), vy = __ldg(a.v.p[1] + c), vz = __ldg(a.v.p[2] + c);
+                    if (a.speed) {
+                        const float sp = __ldg(a.speed + c);
+                        vx *= sp;
+                        vy *= sp;
+                        vz *= sp;
+                    }
+                    step = (float)__ldg(a.dt) * upwind_dot(vx, vy, vz, dxf, dxb, dyf, dyb, dzf, dzb);
+                }
+            }
+            if (!band) {
+                const float pn = a.stage == 0 ? 0.f : __ldg(a.phi_n + c);
+                a.out[c] = rk3_combine(a.stage, pn, ps - step);
+            }
+        }
+        if (KIND != SK_ADVECT) {
+            const unsigned m = __ballot_sync(0xffffffffu, band);
+            if (m) {
+                unsigned base = 0;
+                const int leader = __ffs(m) - 1;
+                if ((int)lane == leader) base = atomicAdd(a.counter, (unsigned)__popc(m));
+                base = __shfl_sync(0xffffffffu, base, leader);
+                if (band) {
+                    const unsigned rank = __popc(m & ((1u << lane) - 1u));
+                    a.queue[base + rank] = (unsigned)((long long)k * g.plane + (long long)j * g.rows + i);
+                }
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < 6; ++s) q[s] = q[s + 1];
+    }
+}
+
+// Band nodes of one stage: the generic per-node update (interface-aware stencils),
+// grid-stride over the queue.  Also clears the other stage's counter for its next use.
+template <int KIND, bool ENO3>
+__global__ void __launch_bounds__(128) k_band_stage(TiledArgs a, Ptr6<const float> cp, unsigned *next_counter)
+{
+    const unsigned n = *a.counter;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *next_counter = 0u;
+    const Grid &g = a.g;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const long long c = a.queue[t];
+        const int k = (int)(c / g.plane);
+        const long long r = c - (long long)k * g.plane;
+        const int j = (int)(r / g.rows);
+        const int i = (int)(r - (long long)j * g.rows);
+        if (KIND == SK_REINIT)
+            reinit_node<float, ENO3, true>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
+        else
+            extend_node<float, ENO3, true>(a.phi_s, a.phi_n, a.out, a.flags, a.d, cp, a.v, g, a.stage, i, j, k);
+    }
+}
+
+}  // namespace
+
+inline TiledArgs tiled_args(const Grid &g)
+{
+    TiledArgs a{};
+    a.g = g;
+    const double hh[3] = {g.dx, g.dy, g.dz};
+    for (int q = 0; q < 3; ++q) {
+        a.h[q] = (float)hh[q];
+        a.inv_h[q] = 1.0f / (float)hh[q];
+        a.eps2[q] = 1e-6f * (float)hh[q] * (float)hh[q];
+    }
+    const float hx = (float)g.dx, hy = (float)g.dy, hz = (float)g.dz;
+    a.dt_uniform = 0.3f * fminf(fminf(hx, hx), fminf(fminf(hy, hy), fminf(hz, hz)));
+    return a;
+}
+
+inline int band_blocks()
+{
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        n = (sms > 0 ? sms : 132) * 4;
+    }
+    return n;
+}
+
+inline dim3 tiled_grid(const Grid &g) { return dim3((g.rows + TY - 1) / TY, (g.cols + TX - 1) / TX, (g.pges + KZ - 1) / KZ); }
+
+cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const Grid &g, cudaStream_t s)
+{
+    TiledArgs a = tiled_args(g);
+    a.phi_s = st.phi_s;
+    a.phi_n = st.phi_n;
+    a.out = st.out;
+    a.flags = st.flags;
+    a.d = st.d;
+    a.v = st.v;
+    a.speed = st.speed;
+    a.dt = st.dt;
+    a.queue = st.band.queue;
+    a.counter = st.band.counter + (st.seq & 1);
+    a.stage = st.stage;
+    dim3 gr = tiled_grid(g), bl(TY, TX);
+    if (kind == SK_REINIT)
+        k_stage_tiled<SK_REINIT><<<gr, bl, 0, s>>>(a);
+    else if (kind == SK_EXTEND)
+        k_stage_tiled<SK_EXTEND><<<gr, bl, 0, s>>>(a);
+    else
+        k_stage_tiled<SK_ADVECT><<<gr, bl, 0, s>>>(a);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || kind == SK_ADVECT) return e;
+    unsigned *next = st.band.counter + ((st.seq + 1) & 1);
+    if (kind == SK_REINIT) {
+        if (eno3)
+            k_band_stage<SK_REINIT, true><<<band_blocks(), 128, 0, s>>>(a, st.cp, next);
+        else
+            k_band_stage<SK_REINIT, false><<<band_blocks(), 128, 0, s>>>(a, st.cp, next);
+    } else {
+        if (eno3)
+            k_band_stage<SK_EXTEND, true><<<band_blocks(), 128, 0, s>>>(a, st.cp, next);
+        else
+            k_band_stage<SK_EXTEND, false><<<band_blocks(), 128, 0, s>>>(a, st.cp, next);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace vsl

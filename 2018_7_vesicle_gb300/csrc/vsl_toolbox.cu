@@ -25,11 +25,19 @@ __device__ __forceinline__ double warp_max(double v)
 
 __device__ __forceinline__ long long block_linear() { return blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z); }
 
-// set_calculus_toolbox (set_calculus_toolbox.cu:9-107) in double from the promoted field,
-// HPrimal = max(F, 0) formed on the fly (GPUsetCalculusToolBox.m:4); per block the sums
-// of DiracDelta over |F| < 2Ds and of 1 - Heaviside over F < 2Ds (SDF3.m:73-80).
+// set_calculus_toolbox (set_calculus_toolbox.cu:9-107) in the field's precision T (the
+// plain form is FP64 throughout; the mixed form computes these stencils in FP32), with
+// HPrimal = max(F, 0) formed on the fly (GPUsetCalculusToolBox.m:4); per block the FP64
+// sums of DiracDelta over |F| < 2Ds and of 1 - Heaviside over F < 2Ds (SDF3.m:73-80).
+template <typename T> __device__ __forceinline__ T cube(T x);
+template <> __device__ __forceinline__ double cube<double>(double x) { return pow_cr<3>(x); }
+template <> __device__ __forceinline__ float cube<float>(float x) { return x * x * x; }
+template <typename T> __device__ __forceinline__ T fourth(T x);
+template <> __device__ __forceinline__ double fourth<double>(double x) { return pow_cr<4>(x); }
+template <> __device__ __forceinline__ float fourth<float>(float x) { return (x * x) * (x * x); }
+
 template <typename T>
-__global__ void __launch_bounds__(NT) k_toolbox(const T *__restrict__ f, ToolboxOut<T> o, Grid g, double ds,
+__global__ void __launch_bounds__(NT) k_toolbox(const T *__restrict__ f, ToolboxOut<T> o, Grid g, double ds_,
                                                 double *__restrict__ partials)
 {
     const int i = blockIdx.x * BX + threadIdx.x;
@@ -38,65 +46,65 @@ __global__ void __launch_bounds__(NT) k_toolbox(const T *__restrict__ f, Toolbox
     double area = 0.0, vol = 0.0;
     if (i < g.rows && j < g.cols) {
         const long long c = node_index(g, i, j, k);
-        auto F = [&](int a, int b, int e) { return (double)__ldg(f + clamped_index(g, a, b, e)); };
-        auto H = [&](int a, int b, int e) { return fmax((double)__ldg(f + clamped_index(g, a, b, e)), 0.0); };
-        const double dx = g.dx, dy = g.dy, dz = g.dz;
-        const double fc = (double)__ldg(f + c);
-        const double fxp = F(i, j + 1, k), fxm = F(i, j - 1, k), fyp = F(i + 1, j, k), fym = F(i - 1, j, k);
-        const double fzp = F(i, j, k + 1), fzm = F(i, j, k - 1);
-        double fx = (fxp - fxm) / (2 * dx);
-        double fy = (fyp - fym) / (2 * dy);
-        double fz = (fzp - fzm) / (2 * dz);
-        double gm = vmax(sqrt(fx * fx + fy * fy + fz * fz), 1e-14);
-        double fxx = (fxp - 2 * fc + fxm) / (dx * dx);
-        double fyy = (fyp - 2 * fc + fym) / (dy * dy);
-        double fzz = (fzp - 2 * fc + fzm) / (dz * dz);
-        double fxy = (F(i + 1, j + 1, k) + F(i - 1, j - 1, k) - F(i + 1, j - 1, k) - F(i - 1, j + 1, k)) / (4 * ds * ds);
-        double fyz = (F(i + 1, j, k + 1) + F(i - 1, j, k - 1) - F(i + 1, j, k - 1) - F(i - 1, j, k + 1)) / (4 * ds * ds);
-        double fzx = (F(i, j + 1, k + 1) + F(i, j - 1, k - 1) - F(i, j + 1, k - 1) - F(i, j - 1, k + 1)) / (4 * ds * ds);
-        double lap = fxx + fyy + fzz;
-        double r1 = fxx * fx + fxy * fy + fzx * fz;
-        double r2 = fxy * fx + fyy * fy + fyz * fz;
-        double r3 = fzx * fx + fyz * fy + fzz * fz;
-        double gm2 = gm * gm;
-        double mean = -lap / gm + (fx * r1 + fy * r2 + fz * r3) / pow_cr<3>(gm);
-        const double gm4 = pow_cr<4>(gm);
-        double hc = fmax(fc, 0.0);
-        double hxp = H(i, j + 1, k), hxm = H(i, j - 1, k), hyp = H(i + 1, j, k), hym = H(i - 1, j, k);
-        double hzp = H(i, j, k + 1), hzm = H(i, j, k - 1);
-        double px = (hxp - hxm) / (2 * dx), py = (hyp - hym) / (2 * dy), pz = (hzp - hzm) / (2 * dz);
-        double dot = px * fx + py * fy + pz * fz;
-        double pxx = (hxp - 2 * hc + hxm) / (dx * dx);
-        double pyy = (hyp - 2 * hc + hym) / (dy * dy);
-        double pzz = (hzp - 2 * hc + hzm) / (dz * dz);
-        double plap = pxx + pyy + pzz;
-        double heav = dot / gm2;
-        double delta = plap / gm2 - dot * lap / gm4;
-        if (fabs(fc) < 2 * ds) area = delta;
-        if (fc < 2 * ds) vol = 1 - heav;
-        if (o.f[0]) o.f[0][c] = (T)fx;
-        if (o.f[1]) o.f[1][c] = (T)fy;
-        if (o.f[2]) o.f[2][c] = (T)fz;
-        if (o.f[3]) o.f[3][c] = (T)gm;
-        if (o.f[4]) o.f[4][c] = (T)(fx / gm);
-        if (o.f[5]) o.f[5][c] = (T)(fy / gm);
-        if (o.f[6]) o.f[6][c] = (T)(fz / gm);
-        if (o.f[7]) o.f[7][c] = (T)fxx;
-        if (o.f[8]) o.f[8][c] = (T)fyy;
-        if (o.f[9]) o.f[9][c] = (T)fzz;
-        if (o.f[10]) o.f[10][c] = (T)fxy;
-        if (o.f[11]) o.f[11][c] = (T)fyz;
-        if (o.f[12]) o.f[12][c] = (T)fzx;
-        if (o.f[13]) o.f[13][c] = (T)lap;
-        if (o.f[14]) o.f[14][c] = (T)mean;
+        auto F = [&](int a, int b, int e) { return __ldg(f + clamped_index(g, a, b, e)); };
+        auto H = [&](int a, int b, int e) { return vmax(__ldg(f + clamped_index(g, a, b, e)), T(0)); };
+        const T dx = (T)g.dx, dy = (T)g.dy, dz = (T)g.dz, ds = (T)ds_;
+        const T fc = __ldg(f + c);
+        const T fxp = F(i, j + 1, k), fxm = F(i, j - 1, k), fyp = F(i + 1, j, k), fym = F(i - 1, j, k);
+        const T fzp = F(i, j, k + 1), fzm = F(i, j, k - 1);
+        T fx = (fxp - fxm) / (2 * dx);
+        T fy = (fyp - fym) / (2 * dy);
+        T fz = (fzp - fzm) / (2 * dz);
+        T gm = vmax(sqrt(fx * fx + fy * fy + fz * fz), T(1e-14));
+        T fxx = (fxp - 2 * fc + fxm) / (dx * dx);
+        T fyy = (fyp - 2 * fc + fym) / (dy * dy);
+        T fzz = (fzp - 2 * fc + fzm) / (dz * dz);
+        T fxy = (F(i + 1, j + 1, k) + F(i - 1, j - 1, k) - F(i + 1, j - 1, k) - F(i - 1, j + 1, k)) / (4 * ds * ds);
+        T fyz = (F(i + 1, j, k + 1) + F(i - 1, j, k - 1) - F(i + 1, j, k - 1) - F(i - 1, j, k + 1)) / (4 * ds * ds);
+        T fzx = (F(i, j + 1, k + 1) + F(i, j - 1, k - 1) - F(i, j + 1, k - 1) - F(i, j - 1, k + 1)) / (4 * ds * ds);
+        T lap = fxx + fyy + fzz;
+        T r1 = fxx * fx + fxy * fy + fzx * fz;
+        T r2 = fxy * fx + fyy * fy + fyz * fz;
+        T r3 = fzx * fx + fyz * fy + fzz * fz;
+        T gm2 = gm * gm;
+        T mean = -lap / gm + (fx * r1 + fy * r2 + fz * r3) / cube(gm);
+        const T gm4 = fourth(gm);
+        T hc = vmax(fc, T(0));
+        T hxp = H(i, j + 1, k), hxm = H(i, j - 1, k), hyp = H(i + 1, j, k), hym = H(i - 1, j, k);
+        T hzp = H(i, j, k + 1), hzm = H(i, j, k - 1);
+        T px = (hxp - hxm) / (2 * dx), py = (hyp - hym) / (2 * dy), pz = (hzp - hzm) / (2 * dz);
+        T dot = px * fx + py * fy + pz * fz;
+        T pxx = (hxp - 2 * hc + hxm) / (dx * dx);
+        T pyy = (hyp - 2 * hc + hym) / (dy * dy);
+        T pzz = (hzp - 2 * hc + hzm) / (dz * dz);
+        T plap = pxx + pyy + pzz;
+        T heav = dot / gm2;
+        T delta = plap / gm2 - dot * lap / gm4;
+        if (fabs((double)fc) < 2 * ds_) area = (double)delta;
+        if ((double)fc < 2 * ds_) vol = 1 - (double)heav;
+        if (o.f[0]) o.f[0][c] = fx;
+        if (o.f[1]) o.f[1][c] = fy;
+        if (o.f[2]) o.f[2][c] = fz;
+        if (o.f[3]) o.f[3][c] = gm;
+        if (o.f[4]) o.f[4][c] = fx / gm;
+        if (o.f[5]) o.f[5][c] = fy / gm;
+        if (o.f[6]) o.f[6][c] = fz / gm;
+        if (o.f[7]) o.f[7][c] = fxx;
+        if (o.f[8]) o.f[8][c] = fyy;
+        if (o.f[9]) o.f[9][c] = fzz;
+        if (o.f[10]) o.f[10][c] = fxy;
+        if (o.f[11]) o.f[11][c] = fyz;
+        if (o.f[12]) o.f[12][c] = fzx;
+        if (o.f[13]) o.f[13][c] = lap;
+        if (o.f[14]) o.f[14][c] = mean;
         if (o.f[15]) {
-            double q1 = (fyy * fzz - fyz * fyz) * fx + (fzx * fyz - fxy * fzz) * fy + (fxy * fyz - fzx * fyy) * fz;
-            double q2 = (fyz * fzx - fxy * fzz) * fx + (fxx * fzz - fzx * fzx) * fy + (fzx * fxy - fxx * fyz) * fz;
-            double q3 = (fxy * fyz - fyy * fzx) * fx + (fzx * fxy - fxx * fyz) * fy + (fxx * fyy - fxy * fxy) * fz;
-            o.f[15][c] = (T)((fx * q1 + fy * q2 + fz * q3) / gm4);
+            T q1 = (fyy * fzz - fyz * fyz) * fx + (fzx * fyz - fxy * fzz) * fy + (fxy * fyz - fzx * fyy) * fz;
+            T q2 = (fyz * fzx - fxy * fzz) * fx + (fxx * fzz - fzx * fzx) * fy + (fzx * fxy - fxx * fyz) * fz;
+            T q3 = (fxy * fyz - fyy * fzx) * fx + (fzx * fxy - fxx * fyz) * fy + (fxx * fyy - fxy * fxy) * fz;
+            o.f[15][c] = (fx * q1 + fy * q2 + fz * q3) / gm4;
         }
-        if (o.f[16]) o.f[16][c] = (T)heav;
-        if (o.f[17]) o.f[17][c] = (T)delta;
+        if (o.f[16]) o.f[16][c] = heav;
+        if (o.f[17]) o.f[17][c] = delta;
     }
     if (!partials) return;
     __shared__ double sa[NW], sv[NW];

@@ -1,0 +1,149 @@
+"""Mixed-precision form (FP32 fields and stencils, FP64 interface roots and reductions)
+against the FP64 oracle.  Tolerances, written per test:
+
+* reinitialization: max error over the interface band |phi| < 3dx below 1e-5*dx (the
+  target of the mixed form), after 1, 20 and 100 pseudo-steps at the full 64^3 size;
+* extension and advection (fields of arbitrary scale): max error below 5e-5 of the
+  field's scale, i.e. a few hundred FP32 ulps after 30 pseudo-steps;
+* area and volume: relative error below 1e-6.
+
+GPU only; everything goes through the C ABI."""
+import importlib
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, load_golden
+from gpu_util import dev, host
+
+pytestmark = pytest.mark.gpu
+
+S = importlib.import_module("2018_7_vesicle_gb300.shapes")
+
+
+def band_err(a, ref, phi, dx, width=3):
+    m = np.abs(phi) < width * dx
+    return float(np.max(np.abs(a[m] - ref[m]))) / dx
+
+
+def rel_err(a, ref):
+    return float(np.max(np.abs(a - ref))) / max(1.0, float(np.max(np.abs(ref))))
+
+
+@pytest.fixture(scope="module")
+def config1(pkg, vsl, oracle_mod):
+    O = oracle_mod
+    x, y, z = S.cube_grid(64, -1.0, 1.0)
+    F = S.perturbed_sphere(x, y, z)
+    g = O.grid_from_mesh(x, y, z)
+    return x, y, z, F, g, O.kernels("port")
+
+
+def f32(pkg, x, y, z, F):
+    m = pkg.SDF3(pkg.GD3(x, y, z), Val=F, precision="f32")
+    m.setDistance()
+    return m
+
+
+@pytest.mark.parametrize("iters", [1, 20, 100])
+def test_reinit_weno5_band_error(pkg, oracle_mod, config1, iters):
+    O = oracle_mod
+    x, y, z, F, g, K = config1
+    ref = O.reinit_weno5(K, g, F, iters, O.set_distance(K, g, F))
+    m = f32(pkg, x, y, z, F)
+    got = host(m.WENO5RK3Reinitialization(m.F, iters))
+    assert band_err(got, ref, ref, g.dx) <= 1e-5
+    assert rel_err(got, ref) <= 5e-5
+
+
+def test_reinit_eno3_band_error(pkg, oracle_mod, config1):
+    O = oracle_mod
+    x, y, z, F, g, K = config1
+    ref = O.reinit_eno3(K, g, F, 100)
+    m = f32(pkg, x, y, z, F)
+    got = host(m.WENORK3Reinitialization(m.F, 100))
+    assert band_err(got, ref, ref, g.dx) <= 1e-5
+
+
+@pytest.mark.parametrize("eno3", [False, True])
+def test_extend(pkg, oracle_mod, config1, eno3):
+    O = oracle_mod
+    x, y, z, F, g, K = config1
+    C = S.surface_field(x, y, z)
+    m = f32(pkg, x, y, z, F)
+    if eno3:
+        ref = O.extend_eno3(K, g, F, C, 30)
+        got = host(m.WENORK3Extend(dev(C), 30))
+    else:
+        ref = O.extend_weno5(K, g, F, O.set_distance(K, g, F), C, 30)
+        got = host(m.WENO5RK3Extend(dev(C), 30))
+    assert rel_err(got, ref) <= 5e-5
+
+
+def test_advection(pkg, oracle_mod, config1):
+    O = oracle_mod
+    x, y, z, F, g, K = config1
+    vx = np.asfortranarray(-y + 0.3 * np.sin(2 * z))
+    vy = np.asfortranarray(x.copy())
+    vz = np.asfortranarray(0.5 * np.cos(3 * x) * y)
+    dt = 0.5 * g.ds / 1.5
+    ref = O.advect_rk3(K, g, F, vx, vy, vz, dt, steps=3)
+    m = f32(pkg, x, y, z, F)
+    got = host(m.WENO5RK3Advection(m.F, dev(vx), dev(vy), dev(vz), dt, steps=3))
+    assert rel_err(got, ref) <= 5e-5
+
+
+def test_area_volume(pkg, oracle_mod, config1):
+    O = oracle_mod
+    x, y, z, F, g, K = config1
+    tb = O.calculus_toolbox(K, g, F)
+    m = f32(pkg, x, y, z, F)
+    av = m.area_volume().cpu().numpy()
+    a, v = O.cal_area(g, F, tb["DiracDelta"]), O.cal_volume(g, F, tb["Heaviside"])
+    assert abs(av[0] - a) <= 1e-6 * a
+    assert abs(av[1] - v) <= 1e-6 * v
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_golden_cases_fp32(pkg, vsl, name):
+    """The reference's own outputs on the golden inputs (kinks, nodes on the interface,
+    grids smaller than the stencil), within FP32 tolerance."""
+    G = load_golden(name)
+    r, c, p, dx, dy, dz = G["grid"]
+    x = np.zeros((int(r), int(c), int(p)), order="F")
+    m = pkg.SDF3(pkg.GD3(x, x, x, spacing=(dx, dy, dz)), Val=G["F"], precision="f32")
+    m.setDistance()
+    C = dev(G["C"])
+    assert rel_err(host(m.WENO5RK3Reinitialization(m.F, 4)), G["reinit5_it4"]) <= 5e-5
+    assert rel_err(host(m.WENORK3Reinitialization(m.F, 4)), G["reinit3_it4"]) <= 5e-5
+    assert rel_err(host(m.WENO5RK3Extend(C, 3)), G["extend5_it3"]) <= 5e-5
+    assert rel_err(host(m.WENORK3Extend(C, 3)), G["extend3_it3"]) <= 5e-5
+
+
+def test_surface_redistance(pkg, oracle_mod):
+    O = oracle_mod
+    x, y, z = S.cube_grid(28, -1.0, 1.0)
+    F = np.asfortranarray(np.sqrt(x**2 + y**2 + z**2) - 0.6)
+    A = np.asfortranarray(np.exp(z) - 1)
+    m = f32(pkg, x, y, z, F)
+    got = host(m.WENO5RK3ClosetPointSurfaceRedistance(dev(A), 3, 6))
+    ref = O.surface_redistance(O.kernels("port"), O.grid_from_mesh(x, y, z), F, A, 3, 6)
+    assert rel_err(got, ref) <= 5e-5
+
+
+def test_vesicle_steps(pkg, oracle_mod):
+    """Three composite steps at 48^3: interface-band error and area/volume per step."""
+    O = oracle_mod
+    x, y, z = S.cube_grid(48, -1.5, 1.5)
+    F = S.noisy_oblate(x, y, z, seed=3)
+    g = O.grid_from_mesh(x, y, z)
+    K = O.kernels("port")
+    m = f32(pkg, x, y, z, F)
+    Fo, do = F, O.set_distance(K, g, F)
+    for _ in range(3):
+        info = m.vesicle_step(30, 20, 0.5).cpu().numpy()
+        Fo, do, oi = O.vesicle_step(K, g, Fo, do, 30, 20, 0.5)
+        assert abs(info[0] - oi["area"]) <= 1e-6 * oi["area"]
+        assert abs(info[1] - oi["volume"]) <= 1e-6 * oi["volume"]
+        assert abs(info[2] - oi["dt"]) <= 1e-4 * oi["dt"]
+        assert band_err(host(m.F), Fo, Fo, g.dx) <= 2e-4
