@@ -18,13 +18,15 @@ CFLAGS = ["-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-std=c11"
 
 
 def build_port(force: bool = False) -> str:
+    """lib/libvsl_oracle.so (pow from libm, as the reference) and
+    lib/libvsl_oracle_crpow.so (integer powers rounded once, as the CUDA plain form)."""
     src = os.path.join(HERE, "vsl_oracle.c")
+    deps = max(os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "vsl_oracle.h")))
     out = os.path.join(HERE, "lib", "libvsl_oracle.so")
     os.makedirs(os.path.dirname(out), exist_ok=True)
-    if force or not os.path.exists(out) or os.path.getmtime(out) < max(
-        os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "vsl_oracle.h"))
-    ):
-        subprocess.run(["gcc", *CFLAGS, "-o", out, src, "-lm"], check=True)
+    for path, extra in ((out, []), (os.path.join(HERE, "lib", "libvsl_oracle_crpow.so"), ["-DVSL_ORACLE_CR_POW"])):
+        if force or not os.path.exists(path) or os.path.getmtime(path) < deps:
+            subprocess.run(["gcc", *CFLAGS, *extra, "-o", path, src, "-lm"], check=True)
     return out
 
 

@@ -3,6 +3,7 @@
 Two interchangeable kernel sets with the reference kernels' names and argument order:
 
 * ``kernels("port")``  -- ``vsl_oracle.c``, this repository's C restatement;
+* ``kernels("port_crpow")`` -- the same with integer powers rounded once;
 * ``kernels("ref")``   -- the reference's own ``.cu`` files compiled for the host by
   ``oracle/ref/Makefile`` into ``oracle/_ref/`` (only where the reference checkout exists).
 
@@ -27,6 +28,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "lib", "libvsl_oracle.so")
+PORT_CRPOW_LIB = os.path.join(HERE, "lib", "libvsl_oracle_crpow.so")
 REF_LIB = os.path.join(HERE, "_ref", "libvsl_ref.so")
 
 _D = ctypes.c_double
@@ -94,10 +96,13 @@ _CACHE: dict = {}
 
 
 def kernels(which: str = "port") -> KernelSet:
-    """The restatement ("port") or the reference host build ("ref")."""
+    """The restatement ("port"), the restatement with integer powers rounded once
+    ("port_crpow", the rounding of the CUDA plain form) or the reference host build ("ref")."""
     if which not in _CACHE:
         if which == "port":
             _CACHE[which] = KernelSet(PORT_LIB, "orc_")
+        elif which == "port_crpow":
+            _CACHE[which] = KernelSet(PORT_CRPOW_LIB, "orc_")
         elif which == "ref":
             _CACHE[which] = KernelSet(REF_LIB, "ref_")
         else:

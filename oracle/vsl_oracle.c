@@ -17,7 +17,7 @@
  *   5_0_Nonoscillating_Reconstruction/nonoscillating_interpolant.cu
  *
  * Arithmetic is kept in the reference's operation order (same association, same
- * constants, same pow() calls) so that, built with -ffp-contract=off, it agrees with the
+ * constants, same POW() calls) so that, built with -ffp-contract=off, it agrees with the
  * reference compiled for the host to the last bit or within a few ulps.  The grid layout
  * is ind = k*rows*cols + j*rows + i with i = row (y, stride 1), j = column (x), k = page
  * (z); neighbour indices outside the grid are clamped to the edge.
@@ -28,6 +28,33 @@
 #include <string.h>
 
 #include "vsl_oracle.h"
+
+/* The reference calls pow(t, n) for small integer n.  Built with VSL_ORACLE_CR_POW the
+ * oracle instead rounds those powers once (the running product kept exactly as a
+ * double-double via fma), which is how the CUDA plain form forms them; glibc's pow is
+ * accurate to 0.52 ulp but not always correctly rounded, so the two builds can differ in
+ * the last bit of a power.  Comparing the CUDA form with this build isolates everything
+ * else to the bit. */
+#ifdef VSL_ORACLE_CR_POW
+static double cr_pow(double t, double pd)
+{
+    int n = (int)pd;
+    if ((double)n != pd || n < 0 || n > 8) return pow(t, pd);
+    if (n == 0) return 1.0;
+    if (n == 1) return t;
+    double hi = t, lo = 0.0;
+    for (int k = 2; k <= n; ++k) {
+        double p1 = hi * t;
+        double e1 = fma(hi, t, -p1);
+        lo = fma(lo, t, e1);
+        hi = p1;
+    }
+    return hi + lo;
+}
+#define POW cr_pow
+#else
+#define POW pow
+#endif
 
 /* ------------------------------------------------------------------------------------ */
 /* indexing                                                                              */
@@ -106,11 +133,11 @@ static void lagrange_monomial(int n, const double *x, const double *y, double *a
     }
 }
 
-/* Poly<n>::operator(), shared_utilities.hpp:47-53: sum of a[p] * pow(t, p). */
+/* Poly<n>::operator(), shared_utilities.hpp:47-53: sum of a[p] * POW(t, p). */
 static double poly_at(int n, const double *a, double t)
 {
     double v = 0;
-    for (int p = 0; p <= n; ++p) v += a[p] * pow(t, p);
+    for (int p = 0; p <= n; ++p) v += a[p] * POW(t, p);
     return v;
 }
 
@@ -188,7 +215,7 @@ static double eno2_distance(double a, double b, double c, double d, double h)
     double d2r = d - 2.0 * c + b;
     double d2 = minmod(d2l, d2r);
     if (d2 > eps || d2 < -eps) {
-        double disc = pow((0.5 * d2 - b - c), 2) - 4. * b * c;
+        double disc = POW((0.5 * d2 - b - c), 2) - 4. * b * c;
         return h * (0.5 + (b - c - sgn(b - c) * sqrt(disc)) / d2);
     }
     return (h * b / (b - c));
@@ -215,8 +242,8 @@ static double cubic_newton_distance(double v0, double v1, double v2, double v3, 
     if (v0 * v1 < 0 || v2 * v3 < 0) return eno2_distance(v0, v1, v2, v3, h);
     double a0 = v0;
     double a1 = (3.0 * (v1 - v0) - 3.0 / 2.0 * (v2 - v0) + 1.0 / 3.0 * (v3 - v0)) / h;
-    double a2 = (-5.0 / 2.0 * (v1 - v0) + 2.0 * (v2 - v0) - 1.0 / 2.0 * (v3 - v0)) / pow(h, 2);
-    double a3 = (1.0 / 2.0 * (v1 - v0) - 1.0 / 2.0 * (v2 - v0) + 1.0 / 6.0 * (v3 - v0)) / pow(h, 3);
+    double a2 = (-5.0 / 2.0 * (v1 - v0) + 2.0 * (v2 - v0) - 1.0 / 2.0 * (v3 - v0)) / POW(h, 2);
+    double a3 = (1.0 / 2.0 * (v1 - v0) - 1.0 / 2.0 * (v2 - v0) + 1.0 / 6.0 * (v3 - v0)) / POW(h, 3);
     double t = h + h * v1 / (v1 - v2);
     int it = 0;
     double change = 1;
@@ -245,13 +272,13 @@ static double weno5_ref_order(double v1, double v2, double v3, double v4, double
     double q1 = 1. / 3. * v1 - 7. / 6. * v2 + 11. / 6. * v3;
     double q2 = -1. / 6. * v2 + 5. / 6. * v3 + 1. / 3. * v4;
     double q3 = 1. / 3. * v3 + 5. / 6. * v4 - 1. / 6. * v5;
-    double s1 = 13. / 12. * pow((v1 - 2 * v2 + v3), 2) + 1. / 4. * pow((v1 - 4 * v2 + 3 * v3), 2);
-    double s2 = 13. / 12. * pow((v2 - 2 * v3 + v4), 2) + 1. / 4. * pow((v2 - v4), 2);
-    double s3 = 13. / 12. * pow((v3 - 2 * v4 + v5), 2) + 1. / 4. * pow((3 * v3 - 4 * v4 + v5), 2);
+    double s1 = 13. / 12. * POW((v1 - 2 * v2 + v3), 2) + 1. / 4. * POW((v1 - 4 * v2 + 3 * v3), 2);
+    double s2 = 13. / 12. * POW((v2 - 2 * v3 + v4), 2) + 1. / 4. * POW((v2 - v4), 2);
+    double s3 = 13. / 12. * POW((v3 - 2 * v4 + v5), 2) + 1. / 4. * POW((3 * v3 - 4 * v4 + v5), 2);
     double eps = 1e-6;
-    double a1 = 0.1 / pow((s1 + eps), 2);
-    double a2 = 0.6 / pow((s2 + eps), 2);
-    double a3 = 0.3 / pow((s3 + eps), 2);
+    double a1 = 0.1 / POW((s1 + eps), 2);
+    double a2 = 0.6 / POW((s2 + eps), 2);
+    double a3 = 0.3 / POW((s3 + eps), 2);
     double tot = a1 + a2 + a3;
     double o1 = a1 / tot, o2 = a2 / tot, o3 = a3 / tot;
     return (o1 * q1 + o2 * q2 + o3 * q3);
@@ -291,29 +318,29 @@ static void nu_smoothness(const double e[6], const double u[5], double s[3])
 {
     double xm25 = e[0], xm15 = e[1], xm05 = e[2], x05 = e[3], x15 = e[4], x25 = e[5];
     double um2 = u[0], um1 = u[1], u0 = u[2], u1 = u[3], u2 = u[4];
-    s[0] = 4.0 * pow((x05 - xm05) / (x25 - xm05), 2) *
-           (pow((u2 - u1) / (x25 - x05), 2) * (10.0 * pow(x05 - xm05, 2) + (x15 - xm05) * (x15 - x05)) +
+    s[0] = 4.0 * POW((x05 - xm05) / (x25 - xm05), 2) *
+           (POW((u2 - u1) / (x25 - x05), 2) * (10.0 * POW(x05 - xm05, 2) + (x15 - xm05) * (x15 - x05)) +
             (u2 - u1) * (u0 - u1) / ((x25 - x05) * (x15 - xm05)) *
-                (20.0 * pow(x05 - xm05, 2) + 2.0 * (x15 - xm05) * (x15 - x05) + (x25 - xm05) * (2.0 * x15 - x05 - xm05)) +
-            pow((u0 - u1) / (x15 - xm05), 2) * (10.0 * pow(x05 - xm05, 2) + (x25 + x15 - 2.0 * xm05) * (x25 + x15 - x05 - xm05)));
-    s[1] = 4.0 * pow((x05 - xm05) / (x15 - xm15), 2) *
-           (pow((um1 - u0) / (x05 - xm15), 2) * (10.0 * pow(x05 - xm05, 2) + (x15 - xm05) * (x15 - x05)) +
+                (20.0 * POW(x05 - xm05, 2) + 2.0 * (x15 - xm05) * (x15 - x05) + (x25 - xm05) * (2.0 * x15 - x05 - xm05)) +
+            POW((u0 - u1) / (x15 - xm05), 2) * (10.0 * POW(x05 - xm05, 2) + (x25 + x15 - 2.0 * xm05) * (x25 + x15 - x05 - xm05)));
+    s[1] = 4.0 * POW((x05 - xm05) / (x15 - xm15), 2) *
+           (POW((um1 - u0) / (x05 - xm15), 2) * (10.0 * POW(x05 - xm05, 2) + (x15 - xm05) * (x15 - x05)) +
             (u1 - u0) * (um1 - u0) / ((x15 - xm05) * (x05 - xm15)) *
-                (20.0 * pow(x05 - xm05, 2) - (x15 - x05) * (xm05 - xm15) - (x15 - xm05) * (x05 - xm15)) +
-            pow((u1 - u0) / (x15 - xm05), 2) * (10.0 * pow(x05 - xm05, 2) + (xm05 - xm15) * (x05 - xm15)));
-    s[2] = 4.0 * pow((x05 - xm05) / (x05 - xm25), 2) *
-           (pow((um2 - um1) / (xm05 - xm25), 2) * (10.0 * pow(x05 - xm05, 2) + (x05 - xm15) * (xm05 - xm15)) +
+                (20.0 * POW(x05 - xm05, 2) - (x15 - x05) * (xm05 - xm15) - (x15 - xm05) * (x05 - xm15)) +
+            POW((u1 - u0) / (x15 - xm05), 2) * (10.0 * POW(x05 - xm05, 2) + (xm05 - xm15) * (x05 - xm15)));
+    s[2] = 4.0 * POW((x05 - xm05) / (x05 - xm25), 2) *
+           (POW((um2 - um1) / (xm05 - xm25), 2) * (10.0 * POW(x05 - xm05, 2) + (x05 - xm15) * (xm05 - xm15)) +
             (u0 - um1) * (um2 - um1) / ((x05 - xm15) * (xm05 - xm25)) *
-                (20.0 * pow(x05 - xm05, 2) + 2.0 * (x05 - xm15) * (xm05 - xm15) + (x05 - xm25) * (x05 + xm05 - 2.0 * xm15)) +
-            pow((u0 - um1) / (x05 - xm15), 2) * (10.0 * pow(x05 - xm05, 2) + (2.0 * x05 - xm25 - xm15) * (x05 + xm05 - xm15 - xm25)));
+                (20.0 * POW(x05 - xm05, 2) + 2.0 * (x05 - xm15) * (xm05 - xm15) + (x05 - xm25) * (x05 + xm05 - 2.0 * xm15)) +
+            POW((u0 - um1) / (x05 - xm15), 2) * (10.0 * POW(x05 - xm05, 2) + (2.0 * x05 - xm25 - xm15) * (x05 + xm05 - xm15 - xm25)));
 }
 
 static double nu_combine(const double v[3], const double c[3], const double s[3])
 {
     double eps = 1e-6;
-    double a0 = c[0] / pow((s[0] + eps), 2);
-    double a1 = c[1] / pow((s[1] + eps), 2);
-    double a2 = c[2] / pow((s[2] + eps), 2);
+    double a0 = c[0] / POW((s[0] + eps), 2);
+    double a1 = c[1] / POW((s[1] + eps), 2);
+    double a2 = c[2] / POW((s[2] + eps), 2);
     double tot = a0 + a1 + a2;
     double o0 = a0 / tot, o1 = a1 / tot, o2 = a2 / tot;
     return v[0] * o0 + v[1] * o1 + v[2] * o2;
@@ -513,13 +540,13 @@ static void re_step_impl(double *step, const double *lsf, const bool *mask, cons
         }
         double xR = df[0], xL = db[0], yF = df[1], yB = db[1], zU = df[2], zD = db[2];
         if (mask[c]) {
-            step[c] = (sqrt(dmax(pow(dmin(0.0, xL), 2), pow(dmax(0.0, xR), 2)) +
-                            dmax(pow(dmin(0.0, yB), 2), pow(dmax(0.0, yF), 2)) +
-                            dmax(pow(dmin(0.0, zD), 2), pow(dmax(0.0, zU), 2))) - 1) * deltat[c] * (-1.);
+            step[c] = (sqrt(dmax(POW(dmin(0.0, xL), 2), POW(dmax(0.0, xR), 2)) +
+                            dmax(POW(dmin(0.0, yB), 2), POW(dmax(0.0, yF), 2)) +
+                            dmax(POW(dmin(0.0, zD), 2), POW(dmax(0.0, zU), 2))) - 1) * deltat[c] * (-1.);
         } else {
-            step[c] = (sqrt(dmax(pow(dmax(0.0, xL), 2), pow(dmin(0.0, xR), 2)) +
-                            dmax(pow(dmax(0.0, yB), 2), pow(dmin(0.0, yF), 2)) +
-                            dmax(pow(dmax(0.0, zD), 2), pow(dmin(0.0, zU), 2))) - 1) * deltat[c] * (1.);
+            step[c] = (sqrt(dmax(POW(dmax(0.0, xL), 2), POW(dmin(0.0, xR), 2)) +
+                            dmax(POW(dmax(0.0, yB), 2), POW(dmin(0.0, yF), 2)) +
+                            dmax(POW(dmax(0.0, zD), 2), POW(dmin(0.0, zU), 2))) - 1) * deltat[c] * (1.);
         }
     }
 }
@@ -615,8 +642,8 @@ static void cubic_coefficients(double v0, double v1, double v2, double v3, doubl
 {
     a[0] = v0;
     a[1] = (3.0 * (v1 - v0) - 3.0 / 2.0 * (v2 - v0) + 1.0 / 3.0 * (v3 - v0)) / h;
-    a[2] = (-5.0 / 2.0 * (v1 - v0) + 2.0 * (v2 - v0) - 1.0 / 2.0 * (v3 - v0)) / pow(h, 2);
-    a[3] = (1.0 / 2.0 * (v1 - v0) - 1.0 / 2.0 * (v2 - v0) + 1.0 / 6.0 * (v3 - v0)) / pow(h, 3);
+    a[2] = (-5.0 / 2.0 * (v1 - v0) + 2.0 * (v2 - v0) - 1.0 / 2.0 * (v3 - v0)) / POW(h, 2);
+    a[3] = (1.0 / 2.0 * (v1 - v0) - 1.0 / 2.0 * (v2 - v0) + 1.0 / 6.0 * (v3 - v0)) / POW(h, 3);
 }
 
 static void crossing_values_cubic(const double p[7], double dis_f, double dis_b, double h, double *cf, double *cb)
@@ -627,12 +654,12 @@ static void crossing_values_cubic(const double p[7], double dis_f, double dis_b,
     if (dis_f < h) {
         cubic_coefficients(p[2], p[3], p[4], p[5], h, a);
         double t = h + dis_f;
-        *cf = a[0] + a[1] * t + a[2] * pow(t, 2) + a[3] * pow(t, 3);
+        *cf = a[0] + a[1] * t + a[2] * POW(t, 2) + a[3] * POW(t, 3);
     }
     if (dis_b < h) {
         cubic_coefficients(p[1], p[2], p[3], p[4], h, a);
         double t = 2 * h - dis_b;
-        *cb = a[0] + a[1] * t + a[2] * pow(t, 2) + a[3] * pow(t, 3);
+        *cb = a[0] + a[1] * t + a[2] * POW(t, 2) + a[3] * POW(t, 3);
     }
 }
 
@@ -831,24 +858,24 @@ void orc_set_calculus_toolbox(double *Fx, double *Fy, double *Fz, double *FGradM
         double r1 = fxx * fx + fxy * fy + fzx * fz;
         double r2 = fxy * fx + fyy * fy + fyz * fz;
         double r3 = fzx * fx + fyz * fy + fzz * fz;
-        MeanCurvature[c] = -lap / gm + (fx * r1 + fy * r2 + fz * r3) / pow(gm, 3);
+        MeanCurvature[c] = -lap / gm + (fx * r1 + fy * r2 + fz * r3) / POW(gm, 3);
 
         r1 = (fyy * fzz - fyz * fyz) * fx + (fzx * fyz - fxy * fzz) * fy + (fxy * fyz - fzx * fyy) * fz;
         r2 = (fyz * fzx - fxy * fzz) * fx + (fxx * fzz - fzx * fzx) * fy + (fzx * fxy - fxx * fyz) * fz;
         r3 = (fxy * fyz - fyy * fzx) * fx + (fzx * fxy - fxx * fyz) * fy + (fxx * fyy - fxy * fxy) * fz;
-        GaussianCurvature[c] = (fx * r1 + fy * r2 + fz * r3) / pow(gm, 4);
+        GaussianCurvature[c] = (fx * r1 + fy * r2 + fz * r3) / POW(gm, 4);
 
         double px = (HPrimal[xp] - HPrimal[xm]) / (2 * dx);
         double py = (HPrimal[yp] - HPrimal[ym]) / (2 * dy);
         double pz = (HPrimal[zp] - HPrimal[zm]) / (2 * dz);
         double dot = px * fx + py * fy + pz * fz;
-        Heaviside[c] = dot / pow(gm, 2);
+        Heaviside[c] = dot / POW(gm, 2);
 
         double pxx = (HPrimal[xp] - 2 * HPrimal[c] + HPrimal[xm]) / (dx * dx);
         double pyy = (HPrimal[yp] - 2 * HPrimal[c] + HPrimal[ym]) / (dy * dy);
         double pzz = (HPrimal[zp] - 2 * HPrimal[c] + HPrimal[zm]) / (dz * dz);
         double plap = pxx + pyy + pzz;
-        DiracDelta[c] = plap / pow(gm, 2) - dot * lap / pow(gm, 4);
+        DiracDelta[c] = plap / POW(gm, 2) - dot * lap / POW(gm, 4);
     }
 }
 
