@@ -24,6 +24,9 @@ FILE_FLAGS = {
     "vsl_plain.cu": ["-fmad=false"],
     "vsl_fused_f64.cu": ["-fmad=false"],
     "vsl_toolbox.cu": ["-fmad=false"],
+    # The mixed form's FP32 stencils use the hardware-approximate quotient and square root
+    # (FP64 code in the same file keeps IEEE division and square root).
+    "vsl_fused_f32.cu": ["-prec-div=false", "-prec-sqrt=false"],
 }
 
 

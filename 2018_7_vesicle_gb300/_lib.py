@@ -34,7 +34,7 @@ SIGNATURES = {
 for _suf in ("f64", "f32"):
     SIGNATURES.update(
         {
-            f"vsl_set_distance_{_suf}": "ppppppp" + _G + "s",
+            f"vsl_set_distance_{_suf}": "ppppppp" + _G + "pz" + "s",
             f"vsl_weno5_rk3_reinitialization_{_suf}": "pi" + "pppppp" + _G + "pz" + "s",
             f"vsl_wenork3_reinitialization_{_suf}": "pi" + _G + "pz" + "s",
             f"vsl_weno5_rk3_extend_{_suf}": "pip" + "pppppp" + _G + "pz" + "s",
@@ -55,6 +55,7 @@ OP = {
     "area_volume": 6,
     "advection": 7,
     "vesicle_step": 8,
+    "set_distance": 9,
 }
 
 

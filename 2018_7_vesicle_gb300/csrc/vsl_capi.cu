@@ -41,10 +41,26 @@ template <typename T> Band carve_band(Bump &w, const Grid &g)
     return b;
 }
 
+EdgeLists carve_edges(Bump &w, const Grid &g)
+{
+    EdgeLists e;
+    for (int q = 0; q < 3; ++q) e.idx[q] = w.take<unsigned>(g.num);
+    e.count = w.take<unsigned>(4);
+    return e;
+}
+NodeList carve_list(Bump &w, const Grid &g)
+{
+    NodeList l;
+    l.idx = w.take<unsigned>(g.num);
+    l.count = w.take<unsigned>(1);
+    return l;
+}
+
 template <typename T> struct ReinitWork {
     T *b, *c;
     uint8_t *flags;
-    Ptr6<T> dist;  // ENO3 only
+    Ptr6<T> dist;     // ENO3 only
+    EdgeLists edges;  // ENO3 only (its setDistance)
     Band band;
 };
 template <typename T> ReinitWork<T> carve_reinit(Bump &w, const Grid &g, bool own_dist)
@@ -54,6 +70,7 @@ template <typename T> ReinitWork<T> carve_reinit(Bump &w, const Grid &g, bool ow
     r.c = w.take<T>(g.num);
     r.flags = w.take<uint8_t>(g.num);
     for (int q = 0; q < 6; ++q) r.dist.p[q] = own_dist ? w.take<T>(g.num) : nullptr;
+    r.edges = own_dist ? carve_edges(w, g) : EdgeLists{};
     r.band = carve_band<T>(w, g);
     return r;
 }
@@ -63,7 +80,9 @@ template <typename T> struct ExtendWork {
     Ptr6<T> cp;
     T *b, *c;
     uint8_t *flags;
-    Ptr6<T> dist;  // ENO3 only
+    NodeList flagged;  // nodes with a distance flag: crossing values and the band
+    Ptr6<T> dist;      // ENO3 only
+    EdgeLists edges;   // ENO3 only (its setDistance)
     Band band;
 };
 template <typename T> ExtendWork<T> carve_extend(Bump &w, const Grid &g, bool own_dist)
@@ -74,7 +93,9 @@ template <typename T> ExtendWork<T> carve_extend(Bump &w, const Grid &g, bool ow
     e.b = w.take<T>(g.num);
     e.c = w.take<T>(g.num);
     e.flags = w.take<uint8_t>(g.num);
+    e.flagged = carve_list(w, g);
     for (int q = 0; q < 6; ++q) e.dist.p[q] = own_dist ? w.take<T>(g.num) : nullptr;
+    e.edges = own_dist ? carve_edges(w, g) : EdgeLists{};
     e.band = carve_band<T>(w, g);
     return e;
 }
@@ -116,6 +137,7 @@ template <typename T> struct StepWork {
     Ptr3<T> nrm;
     ExtendWork<T> ext;
     ReduceWork red;
+    EdgeLists edges;
 };
 template <typename T> StepWork<T> carve_step(Bump &w, const Grid &g)
 {
@@ -124,6 +146,7 @@ template <typename T> StepWork<T> carve_step(Bump &w, const Grid &g)
     for (int q = 0; q < 3; ++q) s.nrm.p[q] = w.take<T>(g.num);
     s.ext = carve_extend<T>(w, g, false);
     s.red = carve_reduce(w, g, 2);
+    s.edges = carve_edges(w, g);
     return s;
 }
 
@@ -141,6 +164,7 @@ size_t measure(int op, const Grid &g, int elem)
         case VSL_OP_AREA_VOLUME: carve_reduce(w, g, 2); break;
         case VSL_OP_ADVECTION: carve_reinit<T>(w, g, false); break;
         case VSL_OP_VESICLE_STEP: carve_step<T>(w, g); break;
+        case VSL_OP_SET_DISTANCE: carve_edges(w, g); break;
         default: return false;
         }
         return true;
@@ -190,9 +214,10 @@ template <typename T> Ptr3<const T> cview3(const Ptr3<T> &p)
 // one stage through the tiled FP32 kernels (stage input s_in, RK3 base n_in, output out)
 inline cudaError_t tiled(int kind, bool eno3, Band &band, const float *s_in, const float *n_in, float *out,
                          const uint8_t *flags, Ptr6<const float> d, Ptr6<const float> cp, Ptr3<const float> v,
-                         const float *speed, const double *dt, int stage, const Grid &g, cudaStream_t s)
+                         const float *speed, const double *dt, int stage, const Grid &g, cudaStream_t s,
+                         NodeList flagged = NodeList{nullptr, nullptr})
 {
-    TiledStage st{s_in, n_in, out, flags, d, cp, v, speed, dt, band.q, stage, band.seq++};
+    TiledStage st{s_in, n_in, out, flags, d, cp, v, speed, dt, band.q, flagged, stage, band.seq++};
     return launch_tiled_stage(kind, eno3, st, g, s);
 }
 
@@ -226,7 +251,7 @@ int extend_setup(const T *F, Ptr6<const T> d, const ExtendWork<T> &w, const Grid
                  cudaStream_t s)
 {
     VSL_TRY(launch_extension_velocity<T>(F, d, w.v, g, eno3, floor, s));
-    VSL_TRY(launch_classify<T>(F, d, w.flags, g, s));
+    VSL_TRY(launch_classify<T>(F, d, w.flags, w.flagged, g, s));
     return VSL_OK;
 }
 
@@ -235,15 +260,15 @@ template <typename T>
 int extend_loop(T *C, int iters, Ptr6<const T> d, ExtendWork<T> &w, const Grid &g, bool eno3, cudaStream_t s)
 {
     const bool fast = fast_form<T>();
-    VSL_TRY(launch_crossing<T>(C, d, w.cp, g, eno3, s));
+    VSL_TRY(launch_crossing<T>(C, d, w.cp, w.flagged, g, eno3, s));
     Ptr6<const T> cp = cview(w.cp);
     Ptr3<const T> v = cview3(w.v);
     if constexpr (std::is_same<T, float>::value) {
         if (int st = band_reset(w.band, s)) return st;
         for (int it = 0; it < iters; ++it) {
-            VSL_TRY(tiled(1, eno3, w.band, C, C, w.b, w.flags, d, cp, v, nullptr, nullptr, 0, g, s));
-            VSL_TRY(tiled(1, eno3, w.band, w.b, C, w.c, w.flags, d, cp, v, nullptr, nullptr, 1, g, s));
-            VSL_TRY(tiled(1, eno3, w.band, w.c, C, C, w.flags, d, cp, v, nullptr, nullptr, 2, g, s));
+            VSL_TRY(tiled(1, eno3, w.band, C, C, w.b, w.flags, d, cp, v, nullptr, nullptr, 0, g, s, w.flagged));
+            VSL_TRY(tiled(1, eno3, w.band, w.b, C, w.c, w.flags, d, cp, v, nullptr, nullptr, 1, g, s, w.flagged));
+            VSL_TRY(tiled(1, eno3, w.band, w.c, C, C, w.flags, d, cp, v, nullptr, nullptr, 2, g, s, w.flagged));
         }
         return VSL_OK;
     }
@@ -288,12 +313,15 @@ template <typename T> Ptr6<const T> six(const T *a, const T *b, const T *c, cons
 
 template <typename T>
 int op_set_distance(const T *F, T *xpr, T *xpl, T *ypf, T *ypb, T *zpu, T *zpd, int rows, int cols, int pges,
-                    double dx, double dy, double dz, cudaStream_t s)
+                    double dx, double dy, double dz, void *ws, size_t bytes, cudaStream_t s)
 {
     if (any_null(F, xpr, xpl, ypf, ypb, zpu, zpd)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     Grid g = make_grid(rows, cols, pges, dx, dy, dz);
-    VSL_TRY(launch_set_distance<T>(F, Ptr6<T>{{xpr, xpl, ypf, ypb, zpu, zpd}}, g, true, s));
+    if (int st = check_ws(VSL_OP_SET_DISTANCE, g, sizeof(T), ws, bytes)) return st;
+    Bump b(ws);
+    EdgeLists e = carve_edges(b, g);
+    VSL_TRY(launch_set_distance<T>(F, Ptr6<T>{{xpr, xpl, ypf, ypb, zpu, zpd}}, g, true, e, s));
     return VSL_OK;
 }
 
@@ -310,7 +338,7 @@ int op_reinit_weno5(T *F, int iteration, const T *xpr, const T *xpl, const T *yp
     Bump b(ws);
     ReinitWork<T> w = carve_reinit<T>(b, g, false);
     Ptr6<const T> d = six(xpr, xpl, ypf, ypb, zpu, zpd);
-    VSL_TRY(launch_classify<T>(F, d, w.flags, g, s));
+    VSL_TRY(launch_classify<T>(F, d, w.flags, NodeList{nullptr, nullptr}, g, s));
     return reinit_loop<T>(F, iteration, d, w, g, false, s);
 }
 
@@ -325,9 +353,9 @@ int op_reinit_eno3(T *F, int iteration, int rows, int cols, int pges, double dx,
     if (int st = check_ws(VSL_OP_REINIT_ENO3, g, sizeof(T), ws, bytes)) return st;
     Bump b(ws);
     ReinitWork<T> w = carve_reinit<T>(b, g, true);
-    VSL_TRY(launch_set_distance<T>(F, w.dist, g, false, s));
+    VSL_TRY(launch_set_distance<T>(F, w.dist, g, false, w.edges, s));
     Ptr6<const T> d = cview(w.dist);
-    VSL_TRY(launch_classify<T>(F, d, w.flags, g, s));
+    VSL_TRY(launch_classify<T>(F, d, w.flags, NodeList{nullptr, nullptr}, g, s));
     return reinit_loop<T>(F, iteration, d, w, g, true, s);
 }
 
@@ -359,7 +387,7 @@ int op_extend_eno3(T *C, int iteration, const T *F, int rows, int cols, int pges
     if (int st = check_ws(VSL_OP_EXTEND_ENO3, g, sizeof(T), ws, bytes)) return st;
     Bump b(ws);
     ExtendWork<T> w = carve_extend<T>(b, g, true);
-    VSL_TRY(launch_set_distance<T>(F, w.dist, g, false, s));
+    VSL_TRY(launch_set_distance<T>(F, w.dist, g, false, w.edges, s));
     Ptr6<const T> d = cview(w.dist);
     if (int st = extend_setup<T>(F, d, w, g, true, 1e-6, s)) return st;
     return extend_loop<T>(C, iteration, d, w, g, true, s);
@@ -377,11 +405,11 @@ int op_redistance(T *A, int iter1, int iter2, const T *F, int rows, int cols, in
     Bump b(ws);
     RedistWork<T> w = carve_redist<T>(b, g);
     // reinitialization part: distances of A, mask A < 0 (ClosetPointSurfaceRedistance.m:15-25)
-    VSL_TRY(launch_set_distance<T>(A, w.re.dist, g, true, s));
+    VSL_TRY(launch_set_distance<T>(A, w.re.dist, g, true, w.re.edges, s));
     Ptr6<const T> dA = cview(w.re.dist);
-    VSL_TRY(launch_classify<T>(A, dA, w.re.flags, g, s));
+    VSL_TRY(launch_classify<T>(A, dA, w.re.flags, NodeList{nullptr, nullptr}, g, s));
     // extension part: distances and upwind normals of F, floor 1e-14 (:37-74)
-    VSL_TRY(launch_set_distance<T>(F, w.ext.dist, g, true, s));
+    VSL_TRY(launch_set_distance<T>(F, w.ext.dist, g, true, w.ext.edges, s));
     Ptr6<const T> dF = cview(w.ext.dist);
     if (int st = extend_setup<T>(F, dF, w.ext, g, false, 1e-14, s)) return st;
     const bool fast = fast_form<T>();
@@ -475,13 +503,13 @@ int op_vesicle_step(T *F, T *xpr, T *xpl, T *ypf, T *ypb, T *zpu, T *zpd, int ex
     tmp.band = w.ext.band;
     if (int st = advect_loop<T>(F, cview3(w.nrm), w.vn, info + 2, 1, tmp, g, s)) return st;
     // setDistance, then reinitialization
-    VSL_TRY(launch_set_distance<T>(F, Ptr6<T>{{xpr, xpl, ypf, ypb, zpu, zpd}}, g, true, s));
+    VSL_TRY(launch_set_distance<T>(F, Ptr6<T>{{xpr, xpl, ypf, ypb, zpu, zpd}}, g, true, w.edges, s));
     ReinitWork<T> rw{};
     rw.b = w.ext.b;
     rw.c = w.ext.c;
     rw.flags = w.ext.flags;
     rw.band = w.ext.band;
-    VSL_TRY(launch_classify<T>(F, d, rw.flags, g, s));
+    VSL_TRY(launch_classify<T>(F, d, rw.flags, NodeList{nullptr, nullptr}, g, s));
     return reinit_loop<T>(F, reinit_iters, d, rw, g, false, s);
 }
 
@@ -517,9 +545,11 @@ size_t vsl_workspace_bytes(int op, int rows, int cols, int pges, int elem_bytes)
 
 #define VSL_TYPED(SUF, T)                                                                                          \
     int vsl_set_distance_##SUF(const T *F, T *xpr, T *xpl, T *ypf, T *ypb, T *zpu, T *zpd, int rows, int cols,     \
-                               int pges, double dx, double dy, double dz, vsl_stream_t stream)                     \
+                               int pges, double dx, double dy, double dz, void *ws, size_t bytes,                  \
+                               vsl_stream_t stream)                                                                \
     {                                                                                                              \
-        return op_set_distance<T>(F, xpr, xpl, ypf, ypb, zpu, zpd, rows, cols, pges, dx, dy, dz, stream);          \
+        return op_set_distance<T>(F, xpr, xpl, ypf, ypb, zpu, zpd, rows, cols, pges, dx, dy, dz, ws, bytes,        \
+                                  stream);                                                                         \
     }                                                                                                              \
     int vsl_weno5_rk3_reinitialization_##SUF(T *F, int iteration, const T *xpr, const T *xpl, const T *ypf,        \
                                              const T *ypb, const T *zpu, const T *zpd, int rows, int cols,         \

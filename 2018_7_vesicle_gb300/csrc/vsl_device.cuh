@@ -354,6 +354,33 @@ __device__ __forceinline__ T weno5_fast(T u1, T u2, T u3, T u4, T u5, T eps2)
     return fast_div(a1 * q1 + a2 * q2 + a3 * q3, a1 + a2 + a3);
 }
 
+// Smoothness indicators of the three candidate stencils of a WENO5 window of five first
+// differences (unscaled), returned as the reciprocal squares 1/(S_k + eps2)^2.  A window
+// serves two derivatives: the backward one at its fourth node and, reversed, the forward
+// one at its third node, since S_1(a,b,c) = S_3(c,b,a) and S_2 is symmetric.
+__device__ __forceinline__ void weno5_window_weights(float u1, float u2, float u3, float u4, float u5, float eps2,
+                                                     float &r1, float &r2, float &r3)
+{
+    const float s1 = (13.f / 12.f) * sqr(u1 - 2 * u2 + u3) + 0.25f * sqr(u1 - 4 * u2 + 3 * u3);
+    const float s2 = (13.f / 12.f) * sqr(u2 - 2 * u3 + u4) + 0.25f * sqr(u2 - u4);
+    const float s3 = (13.f / 12.f) * sqr(u3 - 2 * u4 + u5) + 0.25f * sqr(3 * u3 - 4 * u4 + u5);
+    r1 = __fdividef(1.f, sqr(s1 + eps2));
+    r2 = __fdividef(1.f, sqr(s2 + eps2));
+    r3 = __fdividef(1.f, sqr(s3 + eps2));
+}
+
+// WENO5 one-sided derivative (unscaled differences, biased toward u3) with the reciprocal
+// weights of its window given: weno5_fast with the smoothness part precomputed.
+__device__ __forceinline__ float weno5_with_weights(float u1, float u2, float u3, float u4, float u5, float r1,
+                                                    float r2, float r3)
+{
+    const float q1 = (1.f / 3.f) * u1 - (7.f / 6.f) * u2 + (11.f / 6.f) * u3;
+    const float q2 = (-1.f / 6.f) * u2 + (5.f / 6.f) * u3 + (1.f / 3.f) * u4;
+    const float q3 = (1.f / 3.f) * u3 + (5.f / 6.f) * u4 - (1.f / 6.f) * u5;
+    const float a1 = 0.1f * r1, a2 = 0.6f * r2, a3 = 0.3f * r3;
+    return __fdividef(a1 * q1 + a2 * q2 + a3 * q3, a1 + a2 + a3);
+}
+
 // Seven-point stencil with the interface inserted at r1 (forward) / l1 (backward) when
 // they are shorter than h, carrying the values hf / hb there (select_stencil,
 // re_step.cu:41-77 and shared_utilities.cup:211-247).

@@ -73,55 +73,97 @@ __device__ __forceinline__ void uniform_pair(const T p[7], T h, T &df, T &db)
     }
 }
 
-// ---------------------------------------------------------------------------------------
-// setDistance: all six distances written (spacing where no crossing)
-// ---------------------------------------------------------------------------------------
-template <typename T, bool QUINTIC>
-__global__ void __launch_bounds__(BX *BY) k_set_distance(const T *__restrict__ f, Ptr6<T> d, Grid g)
+// warp-aggregated append of `value` to a device list where `pred` holds (all 32 lanes of
+// the warp must call it)
+__device__ __forceinline__ void warp_append(bool pred, unsigned value, unsigned *list, unsigned *count)
 {
-    int i, j, k;
-    if (!fused_node(g, i, j, k)) return;
-    const long long c = node_index(g, i, j, k);
-    const double f0 = (double)__ldg(f + c);
+    const unsigned m = __ballot_sync(0xffffffffu, pred);
+    if (!m) return;
+    const unsigned lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31u;
+    const int leader = __ffs(m) - 1;
+    unsigned base = 0;
+    if ((int)lane == leader) base = atomicAdd(count, (unsigned)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (pred) list[base + __popc(m & ((1u << lane) - 1u))] = value;
+}
+
+__device__ __forceinline__ void node_of(const Grid &g, long long c, int &i, int &j, int &k)
+{
+    k = (int)(c / g.plane);
+    const long long r = c - (long long)k * g.plane;
+    j = (int)(r / g.rows);
+    i = (int)(r - (long long)j * g.rows);
+}
+
+// ---------------------------------------------------------------------------------------
+// setDistance (setDistance.m:5-15 with boundary_location.cu:84-132 / boundary_correction):
+// pass 1 writes the spacing everywhere and lists every edge (c, c+1) the zero set crosses;
+// pass 2 solves one root per listed edge and writes both of its endpoint distances
+// (h minus it on the far side), the values of the reference's scatter form.
+// ---------------------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(BX *BY) k_dist_scan(const T *__restrict__ f, Ptr6<T> d, EdgeLists e, Grid g)
+{
+    const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y, k = blockIdx.z;
+    const bool in = i < g.rows && j < g.cols;
+    const long long c = in ? node_index(g, i, j, k) : 0;
+    const double f0 = in ? (double)__ldg(f + c) : 0.0;
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax) {
-        AxisLine L = axis_line(g, i, j, k, ax);
-        const double h = axis_h(g, ax);
-        const double fn = (double)__ldg(f + L.base + (long long)clampi(L.c + 1, L.n) * L.stride);
-        double fore = h, back = h;
-        if (f0 * fn < 0) fore = fore_distance<QUINTIC>(f, L, h);
-        if (L.c > 0) {
-            const double fp = (double)__ldg(f + L.base + (long long)(L.c - 1) * L.stride);
-            if (fp * f0 < 0) {
-                AxisLine Lp = L;
-                Lp.c = L.c - 1;
-                back = h - fore_distance<QUINTIC>(f, Lp, h);
-            }
+        bool cross = false;
+        if (in) {
+            AxisLine L = axis_line(g, i, j, k, ax);
+            const T h = (T)axis_h(g, ax);
+            d.p[2 * ax][c] = h;
+            d.p[2 * ax + 1][c] = h;
+            const double fn = (double)__ldg(f + L.base + (long long)clampi(L.c + 1, L.n) * L.stride);
+            cross = f0 * fn < 0;
         }
-        d.p[2 * ax][c] = (T)fore;
-        d.p[2 * ax + 1][c] = (T)back;
+        warp_append(cross, (unsigned)c, e.idx[ax], e.count + ax);
+    }
+}
+
+template <typename T, bool QUINTIC>
+__global__ void __launch_bounds__(128) k_dist_roots(const T *__restrict__ f, Ptr6<T> d, EdgeLists e, Grid g)
+{
+    for (int ax = 0; ax < 3; ++ax) {
+        const unsigned n = *(e.count + ax);
+        const double h = axis_h(g, ax);
+        for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+            const long long c = e.idx[ax][t];
+            int i, j, k;
+            node_of(g, c, i, j, k);
+            const AxisLine L = axis_line(g, i, j, k, ax);
+            const double dist = fore_distance<QUINTIC>(f, L, h);
+            d.p[2 * ax][c] = (T)dist;
+            d.p[2 * ax + 1][c + L.stride] = (T)(h - dist);
+        }
     }
 }
 
 template <typename T>
-__global__ void __launch_bounds__(BX *BY) k_classify(const T *__restrict__ phi0, Ptr6<const T> d, uint8_t *flags, Grid g)
+__global__ void __launch_bounds__(BX *BY) k_classify(const T *__restrict__ phi0, Ptr6<const T> d, uint8_t *flags,
+                                                      NodeList list, Grid g)
 {
-    int i, j, k;
-    if (!fused_node(g, i, j, k)) return;
-    const long long c = node_index(g, i, j, k);
-    const T h[3] = {(T)g.dx, (T)g.dy, (T)g.dz};
-    const T tiny = (T)(1e-6 * g.dx);
+    const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y, k = blockIdx.z;
+    const bool in = i < g.rows && j < g.cols;
+    const long long c = in ? node_index(g, i, j, k) : 0;
     uint8_t fl = 0;
-    bool fixed = false;
+    if (in) {
+        const T h[3] = {(T)g.dx, (T)g.dy, (T)g.dz};
+        const T tiny = (T)(1e-6 * g.dx);
+        bool fixed = false;
 #pragma unroll
-    for (int q = 0; q < 6; ++q) {
-        const T v = __ldg(d.p[q] + c);
-        if (v != h[q / 2]) fl |= (uint8_t)(1u << q);
-        fixed |= v < tiny;
+        for (int q = 0; q < 6; ++q) {
+            const T v = __ldg(d.p[q] + c);
+            if (v != h[q / 2]) fl |= (uint8_t)(1u << q);
+            fixed |= v < tiny;
+        }
+        if (__ldg(phi0 + c) < T(0)) fl |= MASK_BIT;
+        if (fixed) fl |= FIXED_BIT;
+        flags[c] = fl;
     }
-    if (__ldg(phi0 + c) < T(0)) fl |= MASK_BIT;
-    if (fixed) fl |= FIXED_BIT;
-    flags[c] = fl;
+    if (list.idx) warp_append((fl & 0x3F) != 0, (unsigned)c, list.idx, list.count);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -203,30 +245,37 @@ __global__ void __launch_bounds__(BX *BY) k_extension_velocity(const T *__restri
     for (int ax = 0; ax < 3; ++ax) v.p[ax][c] = s * (n[ax] / grad);
 }
 
-// crossing values (boundary_interpolant.cu:78-141 / wenork3_extend.cu:296-365), double
+// crossing values (boundary_interpolant.cu:78-141 / wenork3_extend.cu:296-365) in double,
+// at the listed nodes only (a node without a distance flag has no crossing, and its
+// entries are never read)
 template <typename T, bool CUBIC>
-__global__ void __launch_bounds__(BX *BY) k_crossing(const T *__restrict__ cfield, Ptr6<const T> d, Ptr6<T> cp, Grid g)
+__global__ void __launch_bounds__(128) k_crossing(const T *__restrict__ cfield, Ptr6<const T> d, Ptr6<T> cp,
+                                                  NodeList list, Grid g)
 {
-    int i, j, k;
-    if (!fused_node(g, i, j, k)) return;
-    const long long c = node_index(g, i, j, k);
+    const unsigned n = *list.count;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const long long c = list.idx[t];
+        int i, j, k;
+        node_of(g, c, i, j, k);
 #pragma unroll
-    for (int ax = 0; ax < 3; ++ax) {
-        const double h = axis_h(g, ax);
-        const double r1 = (double)__ldg(d.p[2 * ax] + c), l1 = (double)__ldg(d.p[2 * ax + 1] + c);
-        double cf = 0.0, cb = 0.0;
-        if (r1 < h || l1 < h) {
-            AxisLine L = axis_line(g, i, j, k, ax);
-            double p[7];
+        for (int ax = 0; ax < 3; ++ax) {
+            const double h = axis_h(g, ax);
+            const double r1 = (double)__ldg(d.p[2 * ax] + c), l1 = (double)__ldg(d.p[2 * ax + 1] + c);
+            double cf = 0.0, cb = 0.0;
+            if (r1 < h || l1 < h) {
+                AxisLine L = axis_line(g, i, j, k, ax);
+                double p[7];
 #pragma unroll
-            for (int s = -3; s <= 3; ++s) p[s + 3] = (double)__ldg(cfield + L.base + (long long)clampi(L.c + s, L.n) * L.stride);
-            if (CUBIC)
-                crossing_cubic(p, r1, l1, h, cf, cb);
-            else
-                crossing_quintic(p, r1, l1, h, cf, cb);
+                for (int s = -3; s <= 3; ++s)
+                    p[s + 3] = (double)__ldg(cfield + L.base + (long long)clampi(L.c + s, L.n) * L.stride);
+                if (CUBIC)
+                    crossing_cubic(p, r1, l1, h, cf, cb);
+                else
+                    crossing_quintic(p, r1, l1, h, cf, cb);
+            }
+            cp.p[2 * ax][c] = (T)cf;
+            cp.p[2 * ax + 1][c] = (T)cb;
         }
-        cp.p[2 * ax][c] = (T)cf;
-        cp.p[2 * ax + 1][c] = (T)cb;
     }
 }
 
@@ -319,20 +368,40 @@ __global__ void __launch_bounds__(BX *BY) k_advect_stage(const T *__restrict__ p
 // launchers
 // ---------------------------------------------------------------------------------------
 
-template <typename T>
-cudaError_t launch_set_distance(const T *phi, Ptr6<T> dist, const Grid &g, bool quintic, cudaStream_t s)
+inline int list_blocks()
 {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        n = (sms > 0 ? sms : 132) * 4;
+    }
+    return n;
+}
+
+template <typename T>
+cudaError_t launch_set_distance(const T *phi, Ptr6<T> dist, const Grid &g, bool quintic, EdgeLists e, cudaStream_t s)
+{
+    cudaError_t err = cudaMemsetAsync(e.count, 0, 3 * sizeof(unsigned), s);
+    if (err != cudaSuccess) return err;
+    k_dist_scan<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, dist, e, g);
     if (quintic)
-        k_set_distance<T, true><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, dist, g);
+        k_dist_roots<T, true><<<list_blocks(), 128, 0, s>>>(phi, dist, e, g);
     else
-        k_set_distance<T, false><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, dist, g);
+        k_dist_roots<T, false><<<list_blocks(), 128, 0, s>>>(phi, dist, e, g);
     return cudaGetLastError();
 }
 
 template <typename T>
-cudaError_t launch_classify(const T *phi0, Ptr6<const T> dist, uint8_t *flags, const Grid &g, cudaStream_t s)
+cudaError_t launch_classify(const T *phi0, Ptr6<const T> dist, uint8_t *flags, NodeList list, const Grid &g,
+                            cudaStream_t s)
 {
-    k_classify<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi0, dist, flags, g);
+    if (list.idx) {
+        cudaError_t err = cudaMemsetAsync(list.count, 0, sizeof(unsigned), s);
+        if (err != cudaSuccess) return err;
+    }
+    k_classify<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi0, dist, flags, list, g);
     return cudaGetLastError();
 }
 
@@ -367,12 +436,13 @@ cudaError_t launch_extension_velocity(const T *phi, Ptr6<const T> dist, Ptr3<T> 
 }
 
 template <typename T>
-cudaError_t launch_crossing(const T *c, Ptr6<const T> dist, Ptr6<T> cp, const Grid &g, bool cubic, cudaStream_t s)
+cudaError_t launch_crossing(const T *c, Ptr6<const T> dist, Ptr6<T> cp, NodeList list, const Grid &g, bool cubic,
+                            cudaStream_t s)
 {
     if (cubic)
-        k_crossing<T, true><<<node_grid(g), dim3(BX, BY), 0, s>>>(c, dist, cp, g);
+        k_crossing<T, true><<<list_blocks(), 128, 0, s>>>(c, dist, cp, list, g);
     else
-        k_crossing<T, false><<<node_grid(g), dim3(BX, BY), 0, s>>>(c, dist, cp, g);
+        k_crossing<T, false><<<list_blocks(), 128, 0, s>>>(c, dist, cp, list, g);
     return cudaGetLastError();
 }
 
@@ -408,13 +478,15 @@ cudaError_t launch_advect_stage(const T *phi_s, const T *phi_n, T *out, Ptr3<con
 }
 
 #define VSL_INSTANTIATE_FUSED(T)                                                                                   \
-    template cudaError_t launch_set_distance<T>(const T *, Ptr6<T>, const Grid &, bool, cudaStream_t);              \
-    template cudaError_t launch_classify<T>(const T *, Ptr6<const T>, uint8_t *, const Grid &, cudaStream_t);       \
+    template cudaError_t launch_set_distance<T>(const T *, Ptr6<T>, const Grid &, bool, EdgeLists, cudaStream_t);   \
+    template cudaError_t launch_classify<T>(const T *, Ptr6<const T>, uint8_t *, NodeList, const Grid &,            \
+                                            cudaStream_t);                                                          \
     template cudaError_t launch_reinit_stage<T>(const T *, const T *, T *, const uint8_t *, Ptr6<const T>,          \
                                                 const Grid &, int, bool, bool, cudaStream_t);                       \
     template cudaError_t launch_extension_velocity<T>(const T *, Ptr6<const T>, Ptr3<T>, const Grid &, bool,        \
                                                       double, cudaStream_t);                                        \
-    template cudaError_t launch_crossing<T>(const T *, Ptr6<const T>, Ptr6<T>, const Grid &, bool, cudaStream_t);   \
+    template cudaError_t launch_crossing<T>(const T *, Ptr6<const T>, Ptr6<T>, NodeList, const Grid &, bool,        \
+                                            cudaStream_t);                                                          \
     template cudaError_t launch_extend_stage<T>(const T *, const T *, T *, const uint8_t *, Ptr6<const T>,          \
                                                 Ptr6<const T>, Ptr3<const T>, const Grid &, int, bool, bool,        \
                                                 cudaStream_t);                                                      \

@@ -35,19 +35,36 @@ template <typename T> struct Ptr3 {
     T *p[3];
 };
 
-// ---- fused kernels (vsl_fused.cu), T in {float, double} --------------------------------
+// compact lists built on the device: node indices and their count (zeroed by the launcher)
+struct NodeList {
+    unsigned *idx;
+    unsigned *count;
+};
+// one list of crossed edges per axis (the node at the edge's lower end), counts [3]
+struct EdgeLists {
+    unsigned *idx[3];
+    unsigned *count;
+};
+
+// ---- fused kernels (vsl_fused.cuh), T in {float, double} -------------------------------
+// setDistance: defaults plus a list of crossed edges, then one root per listed edge
 template <typename T>
-cudaError_t launch_set_distance(const T *phi, Ptr6<T> dist, const Grid &g, bool quintic, cudaStream_t s);
+cudaError_t launch_set_distance(const T *phi, Ptr6<T> dist, const Grid &g, bool quintic, EdgeLists e,
+                                cudaStream_t s);
+// classification bytes; with list.idx non-null also the list of nodes with a distance flag
 template <typename T>
-cudaError_t launch_classify(const T *phi0, Ptr6<const T> dist, uint8_t *flags, const Grid &g, cudaStream_t s);
+cudaError_t launch_classify(const T *phi0, Ptr6<const T> dist, uint8_t *flags, NodeList list, const Grid &g,
+                            cudaStream_t s);
 template <typename T>
 cudaError_t launch_reinit_stage(const T *phi_s, const T *phi_n, T *out, const uint8_t *flags, Ptr6<const T> dist,
                                 const Grid &g, int stage, bool eno3, bool fast, cudaStream_t s);
 template <typename T>
 cudaError_t launch_extension_velocity(const T *phi, Ptr6<const T> dist, Ptr3<T> v, const Grid &g, bool eno3,
                                       double floor, cudaStream_t s);
+// crossing values at the listed (flagged) nodes only; other entries of cp are not written
 template <typename T>
-cudaError_t launch_crossing(const T *c, Ptr6<const T> dist, Ptr6<T> cp, const Grid &g, bool cubic, cudaStream_t s);
+cudaError_t launch_crossing(const T *c, Ptr6<const T> dist, Ptr6<T> cp, NodeList list, const Grid &g, bool cubic,
+                            cudaStream_t s);
 template <typename T>
 cudaError_t launch_extend_stage(const T *c_s, const T *c_n, T *out, const uint8_t *flags, Ptr6<const T> dist,
                                 Ptr6<const T> cp, Ptr3<const T> v, const Grid &g, int stage, bool eno3, bool fast,
@@ -73,9 +90,10 @@ struct TiledStage {
     Ptr3<const float> v;
     const float *speed;
     const double *dt;
-    BandQueue band;
-    int stage;  // 0, 1, 2 within the RK3 step
-    int seq;    // running stage count since the counters were zeroed
+    BandQueue band;   // reinitialization: nodes queued by the stage kernel
+    NodeList flagged; // extension: the static list of nodes with a distance flag
+    int stage;        // 0, 1, 2 within the RK3 step
+    int seq;          // running stage count since the counters were zeroed
 };
 // kind: 0 reinitialization, 1 extension, 2 advection
 cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const Grid &g, cudaStream_t s);

@@ -4,8 +4,10 @@
 // z.  The x and y stencils of page k come from a ring of 5 shared-memory planes holding
 // the tile with a 3-node halo (clamped at the grid edge when loaded, so the stencil reads
 // need no clamping); the z stencil comes from a 7-deep register queue per thread.  One
-// barrier per page: at page k the block loads page k+4 into the slot page k-1 vacated and
-// takes the centre of page k+3 into the queue.
+// barrier per page: at page k the block issues the loads of page k+4 into registers,
+// computes page k, then stores page k+4 into the slot page k-1 vacated; the centre of
+// page k+3 enters the queue.  In z, the smoothness weights of the window of page k+1 serve
+// both the forward derivative at k and the backward derivative at k+1.
 //
 // Nodes whose update needs the interface-aware (nonuniform) stencil -- the "band" -- are
 // not computed here: their indices go to a compact queue (warp-aggregated atomics) and
@@ -49,8 +51,10 @@ struct TiledArgs {
     float dt_uniform;  // 0.3 * min spacing: the pseudo time step of a node with no crossing
 };
 
+constexpr int PER_THREAD = (PLANE + TY * TX - 1) / (TY * TX);  // halo elements per thread
+
 template <int KIND>
-__global__ void __launch_bounds__(TY *TX) k_stage_tiled(TiledArgs a)
+__global__ void __launch_bounds__(TY *TX, 5) k_stage_tiled(TiledArgs a)
 {
     __shared__ float sm[RING][SH][SW];
     const Grid &g = a.g;
@@ -61,22 +65,38 @@ __global__ void __launch_bounds__(TY *TX) k_stage_tiled(TiledArgs a)
     const int k0 = blockIdx.z * KZ;
     const int k1 = min(k0 + KZ, g.pges);
     const bool active = i < g.rows && j < g.cols;
+    auto slot = [](int p) { return ((p % RING) + RING) % RING; };
 
-    // load page p (clamped) of the tile with its halo into ring slot p % RING
-    auto load_plane = [&](int p) {
-        const int pc = clampi(p, g.pges);
-        float *dst = &sm[((p % RING) + RING) % RING][0][0];
-        const float *src = a.phi_s + (long long)pc * g.plane;
-        for (int e = tid; e < PLANE; e += TY * TX) {
-            const int sy = e / SW, sx = e - sy * SW;
-            const int gi = clampi(i0 + sx - HALO, g.rows), gj = clampi(j0 + sy - HALO, g.cols);
-            dst[e] = __ldg(src + (long long)gj * g.rows + gi);
-        }
+    // this thread's share of a tile plane (with halo): smem index and in-page offset of up
+    // to PER_THREAD elements; the same for every page, only the page base changes
+    // element tid + r*TY*TX of the plane; offsets are within one page (< 2^31)
+    int e_off[PER_THREAD];
+#pragma unroll
+    for (int r = 0; r < PER_THREAD; ++r) {
+        const int e = tid + r * TY * TX;
+        const int sy = e / SW, sx = e - sy * SW;
+        e_off[r] = clampi(j0 + sy - HALO, g.cols) * g.rows + clampi(i0 + sx - HALO, g.rows);
+    }
+    auto page_base = [&](int p) { return a.phi_s + (long long)clampi(p, g.pges) * g.plane; };
+    float pre[PER_THREAD];
+    auto fetch = [&](int p) {
+        const float *src = page_base(p);
+#pragma unroll
+        for (int r = 0; r < PER_THREAD; ++r)
+            if (tid + r * TY * TX < PLANE) pre[r] = __ldg(src + e_off[r]);
     };
-    auto slot = [&](int p) { return ((p % RING) + RING) % RING; };
+    auto store = [&](int p) {
+        float *dst = &sm[slot(p)][0][0];
+#pragma unroll
+        for (int r = 0; r < PER_THREAD; ++r)
+            if (tid + r * TY * TX < PLANE) dst[tid + r * TY * TX] = pre[r];
+    };
 
     float q[7];  // phi_s(i, j, k-3 .. k+3)
-    for (int p = k0; p < k0 + 4; ++p) load_plane(p);
+    for (int p = k0; p < k0 + 4; ++p) {
+        fetch(p);
+        store(p);
+    }
     {
         const int ic = clampi(i, g.rows), jc = clampi(j, g.cols);
         const float *col = a.phi_s + (long long)jc * g.rows + ic;
@@ -86,13 +106,24 @@ __global__ void __launch_bounds__(TY *TX) k_stage_tiled(TiledArgs a)
     __syncthreads();
 #pragma unroll
     for (int s = 3; s < 6; ++s) q[s] = sm[slot(k0 + s - 3)][ty + HALO][tx + HALO];
+    // reciprocal smoothness weights of the z window of page k0 (backward derivative)
+    float zr1, zr2, zr3;
+    weno5_window_weights(q[1] - q[0], q[2] - q[1], q[3] - q[2], q[4] - q[3], q[5] - q[4], a.eps2[2], zr1, zr2, zr3);
 
     const unsigned lane = tid & 31;
     for (int k = k0; k < k1; ++k) {
+        // every warp has finished page k-1 and stored page k+3
         __syncthreads();
-        load_plane(k + 4);
         q[6] = sm[slot(k + 3)][ty + HALO][tx + HALO];
+        fetch(k + 4);  // loads in flight during this page's arithmetic, stored at its end
         const float(*P)[SW] = sm[slot(k)];
+
+        // z window of page k+1: its weights give the forward derivative here and the
+        // backward derivative at the next page
+        const float v1 = q[1] - q[0], v2 = q[2] - q[1], v3 = q[3] - q[2], v4 = q[4] - q[3], v5 = q[5] - q[4],
+                    v6 = q[6] - q[5];
+        float nr1, nr2, nr3;
+        weno5_window_weights(v2, v3, v4, v5, v6, a.eps2[2], nr1, nr2, nr3);
 
         bool band = false;
         if (active) {
@@ -116,10 +147,11 @@ __global__ void __launch_bounds__(TY *TX) k_stage_tiled(TiledArgs a)
                 band = (fl & 0x3F) != 0;
             }
             if (compute && !band) {
-                float dxf, dxb, dyf, dyb, dzf, dzb;
+                float dxf, dxb, dyf, dyb;
                 weno5_pair_fast(px, a.inv_h[0], a.eps2[0], dxf, dxb);
                 weno5_pair_fast(py, a.inv_h[1], a.eps2[1], dyf, dyb);
-                weno5_pair_fast(q, a.inv_h[2], a.eps2[2], dzf, dzb);
+                const float dzb = weno5_with_weights(v1, v2, v3, v4, v5, zr1, zr2, zr3) * a.inv_h[2];
+                const float dzf = weno5_with_weights(v6, v5, v4, v3, v2, nr3, nr2, nr1) * a.inv_h[2];
                 if (KIND == SK_REINIT) {
                     const bool neg = fl & MASK_BIT;
                     const float dtn = (fl & 0x3F) ? pseudo_dt(fl, a.d, c, a.h[0], a.h[1], a.h[2]) : a.dt_uniform;
@@ -145,7 +177,7 @@ __global__ void __launch_bounds__(TY *TX) k_stage_tiled(TiledArgs a)
                 a.out[c] = rk3_combine(a.stage, pn, ps - step);
             }
         }
-        if (KIND != SK_ADVECT) {
+        if (KIND == SK_REINIT) {  // the extension's band is the static list of flagged nodes
             const unsigned m = __ballot_sync(0xffffffffu, band);
             if (m) {
                 unsigned base = 0;
@@ -158,18 +190,24 @@ __global__ void __launch_bounds__(TY *TX) k_stage_tiled(TiledArgs a)
                 }
             }
         }
+        // page k+4 goes to the slot of page k-1, which no warp reads any more
+        store(k + 4);
+        zr1 = nr1;
+        zr2 = nr2;
+        zr3 = nr3;
 #pragma unroll
         for (int s = 0; s < 6; ++s) q[s] = q[s + 1];
     }
 }
 
 // Band nodes of one stage: the generic per-node update (interface-aware stencils),
-// grid-stride over the queue.  Also clears the other stage's counter for its next use.
+// grid-stride over the queue (reinitialization: also clears the other stage's counter for
+// its next use) or over the static flagged list (extension).
 template <int KIND, bool ENO3>
 __global__ void __launch_bounds__(128) k_band_stage(TiledArgs a, Ptr6<const float> cp, unsigned *next_counter)
 {
     const unsigned n = *a.counter;
-    if (blockIdx.x == 0 && threadIdx.x == 0) *next_counter = 0u;
+    if (next_counter && blockIdx.x == 0 && threadIdx.x == 0) *next_counter = 0u;
     const Grid &g = a.g;
     for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         const long long c = a.queue[t];
@@ -201,17 +239,7 @@ inline TiledArgs tiled_args(const Grid &g)
     return a;
 }
 
-inline int band_blocks()
-{
-    static int n = 0;
-    if (n == 0) {
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        n = (sms > 0 ? sms : 132) * 4;
-    }
-    return n;
-}
+inline int band_blocks() { return list_blocks(); }
 
 inline dim3 tiled_grid(const Grid &g) { return dim3((g.rows + TY - 1) / TY, (g.cols + TX - 1) / TX, (g.pges + KZ - 1) / KZ); }
 
@@ -226,8 +254,15 @@ cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const 
     a.v = st.v;
     a.speed = st.speed;
     a.dt = st.dt;
-    a.queue = st.band.queue;
-    a.counter = st.band.counter + (st.seq & 1);
+    unsigned *next = nullptr;
+    if (kind == SK_EXTEND) {
+        a.queue = st.flagged.idx;
+        a.counter = st.flagged.count;
+    } else {
+        a.queue = st.band.queue;
+        a.counter = st.band.counter + (st.seq & 1);
+        next = st.band.counter + ((st.seq + 1) & 1);
+    }
     a.stage = st.stage;
     dim3 gr = tiled_grid(g), bl(TY, TX);
     if (kind == SK_REINIT)
@@ -238,7 +273,6 @@ cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const 
         k_stage_tiled<SK_ADVECT><<<gr, bl, 0, s>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || kind == SK_ADVECT) return e;
-    unsigned *next = st.band.counter + ((st.seq + 1) & 1);
     if (kind == SK_REINIT) {
         if (eno3)
             k_band_stage<SK_REINIT, true><<<band_blocks(), 128, 0, s>>>(a, st.cp, next);

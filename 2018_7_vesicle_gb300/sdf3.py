@@ -167,7 +167,9 @@ class SDF3:
     def setDistance(self):
         size = self.GD3.Size
         d = [colmajor_empty(size, self.dtype) for _ in range(6)]
-        lib().call(self._fn("vsl_set_distance"), _ptr(self.F), *map(_ptr, d), *self.GD3.args(), _stream())
+        ws = self.workspace("set_distance")
+        lib().call(self._fn("vsl_set_distance"), _ptr(self.F), *map(_ptr, d), *self.GD3.args(), _ptr(ws), ws.numel(),
+                   _stream())
         self.xpr, self.xpl, self.ypf, self.ypb, self.zpu, self.zpd = d
 
     # -- reinitialization ------------------------------------------------------------------

@@ -140,7 +140,8 @@ enum {
     VSL_OP_SURFACE_REDISTANCE = 5,
     VSL_OP_AREA_VOLUME = 6,
     VSL_OP_ADVECTION = 7,
-    VSL_OP_VESICLE_STEP = 8
+    VSL_OP_VESICLE_STEP = 8,
+    VSL_OP_SET_DISTANCE = 9
 };
 
 /* Bytes of workspace operation `op` needs on a rows x cols x pges grid of elements of
@@ -148,12 +149,13 @@ enum {
 size_t vsl_workspace_bytes(int op, int rows, int cols, int pges, int elem_bytes);
 
 /* ref: +SD/@SDF3/setDistance.m:3-33.  Writes all six distance fields (Delta where no
- * interface crosses the edge). */
+ * interface crosses the edge); the workspace holds the list of crossed edges. */
 int vsl_set_distance_f64(const double *F, double *xpr, double *xpl, double *ypf, double *ypb, double *zpu,
-                         double *zpd, int rows, int cols, int pges, double dx, double dy, double dz,
-                         vsl_stream_t stream);
+                         double *zpd, int rows, int cols, int pges, double dx, double dy, double dz, void *workspace,
+                         size_t workspace_bytes, vsl_stream_t stream);
 int vsl_set_distance_f32(const float *F, float *xpr, float *xpl, float *ypf, float *ypb, float *zpu, float *zpd,
-                         int rows, int cols, int pges, double dx, double dy, double dz, vsl_stream_t stream);
+                         int rows, int cols, int pges, double dx, double dy, double dz, void *workspace,
+                         size_t workspace_bytes, vsl_stream_t stream);
 
 /* ref: +SD/@SDF3/WENO5RK3Reinitialization.m:3-43.  F is advanced in place `iteration`
  * TVD-RK3 pseudo-steps with the cached distances of setDistance (mask = F<0 at entry,

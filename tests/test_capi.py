@@ -70,11 +70,14 @@ def test_shape_checks(vsl):
     assert st == 2
     st = vsl.raw("vsl_boundary_location", *[FAKE] * 7, 0, 0, 8, 8, 0.1, 0.1, 0.1, None)
     assert st == 2
-    st = vsl.raw("vsl_set_distance_f64", *[FAKE] * 7, 8, -1, 8, 0.1, 0.1, 0.1, None)
+    st = vsl.raw("vsl_set_distance_f64", *[FAKE] * 7, 8, -1, 8, 0.1, 0.1, 0.1, FAKE, 1 << 20, None)
     assert st == 2
     # non-positive spacing
-    st = vsl.raw("vsl_set_distance_f64", *[FAKE] * 7, 8, 8, 8, 0.1, 0.0, 0.1, None)
+    st = vsl.raw("vsl_set_distance_f64", *[FAKE] * 7, 8, 8, 8, 0.1, 0.0, 0.1, FAKE, 1 << 20, None)
     assert st == 3
+    # workspace too small for the edge lists
+    st = vsl.raw("vsl_set_distance_f32", *[FAKE] * 7, 8, 8, 8, 0.1, 0.1, 0.1, FAKE, 64, None)
+    assert st == 4
 
 
 def test_value_and_workspace_checks(vsl):
