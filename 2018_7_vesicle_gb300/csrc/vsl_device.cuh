@@ -626,4 +626,53 @@ __device__ inline void crossing_cubic(const double p[7], double dis_f, double di
     }
 }
 
+// Crossing values for the mixed-precision form: the same interpolating polynomials
+// (degree 5 through six nodes, or the cubic through four) evaluated in FP32 in Lagrange
+// product form with the equispaced denominators folded into constants, at the normalised
+// abscissa t (node spacing 1).  The reference builds monomial coefficients in FP64
+// (boundary_interpolant.cu:78-99, wenork3_extend.cu:296-328); the product form is the
+// better-conditioned evaluation of the same polynomial.
+template <int NPT>
+__device__ __forceinline__ float lagrange_equispaced(const float *y, float t)
+{
+    // nodes 0..NPT-1; weight_m = prod_{q != m} (t - q) / prod_{q != m} (m - q)
+    float d[NPT], pre[NPT], suf[NPT];
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) d[q] = t - (float)q;
+    pre[0] = 1.f;
+#pragma unroll
+    for (int q = 1; q < NPT; ++q) pre[q] = pre[q - 1] * d[q - 1];
+    suf[NPT - 1] = 1.f;
+#pragma unroll
+    for (int q = NPT - 2; q >= 0; --q) suf[q] = suf[q + 1] * d[q + 1];
+    float v = 0.f;
+#pragma unroll
+    for (int m = 0; m < NPT; ++m) {
+        float den = 1.f;
+#pragma unroll
+        for (int q = 0; q < NPT; ++q)
+            if (q != m) den *= (float)(m - q);
+        v += y[m] * (pre[m] * suf[m]) * (1.f / den);
+    }
+    return v;
+}
+
+__device__ __forceinline__ void crossing_quintic_fast(const float p[7], float dis_f, float dis_b, float h,
+                                                      float &cf, float &cb)
+{
+    cf = 0.f;
+    cb = 0.f;
+    if (dis_f < h) cf = lagrange_equispaced<6>(p + 1, 2.f + dis_f / h);  // nodes p[1..6] at 0..5
+    if (dis_b < h) cb = lagrange_equispaced<6>(p, 3.f - dis_b / h);      // nodes p[0..5] at 0..5
+}
+
+__device__ __forceinline__ void crossing_cubic_fast(const float p[7], float dis_f, float dis_b, float h, float &cf,
+                                                    float &cb)
+{
+    cf = 0.f;
+    cb = 0.f;
+    if (dis_f < h) cf = lagrange_equispaced<4>(p + 2, 1.f + dis_f / h);  // nodes p[2..5] at 0..3
+    if (dis_b < h) cb = lagrange_equispaced<4>(p + 1, 2.f - dis_b / h);  // nodes p[1..4] at 0..3
+}
+
 }  // namespace vsl

@@ -18,6 +18,8 @@
 // defaults, so the dense per-stage traffic is phi_s (stencil), phi_n, flags and out.
 #pragma once
 
+#include <type_traits>
+
 #include "vsl_internal.h"
 
 namespace vsl {
@@ -245,9 +247,10 @@ __global__ void __launch_bounds__(BX *BY) k_extension_velocity(const T *__restri
     for (int ax = 0; ax < 3; ++ax) v.p[ax][c] = s * (n[ax] / grad);
 }
 
-// crossing values (boundary_interpolant.cu:78-141 / wenork3_extend.cu:296-365) in double,
-// at the listed nodes only (a node without a distance flag has no crossing, and its
-// entries are never read)
+// crossing values (boundary_interpolant.cu:78-141 / wenork3_extend.cu:296-365), at the
+// listed nodes only (a node without a distance flag has no crossing, and its entries are
+// never read): the reference's FP64 construction for the plain form, the FP32 product
+// form for the mixed form
 template <typename T, bool CUBIC>
 __global__ void __launch_bounds__(128) k_crossing(const T *__restrict__ cfield, Ptr6<const T> d, Ptr6<T> cp,
                                                   NodeList list, Grid g)
@@ -264,14 +267,27 @@ __global__ void __launch_bounds__(128) k_crossing(const T *__restrict__ cfield, 
             double cf = 0.0, cb = 0.0;
             if (r1 < h || l1 < h) {
                 AxisLine L = axis_line(g, i, j, k, ax);
-                double p[7];
+                if constexpr (std::is_same<T, float>::value) {
+                    float p[7], ff, fb;
 #pragma unroll
-                for (int s = -3; s <= 3; ++s)
-                    p[s + 3] = (double)__ldg(cfield + L.base + (long long)clampi(L.c + s, L.n) * L.stride);
-                if (CUBIC)
-                    crossing_cubic(p, r1, l1, h, cf, cb);
-                else
-                    crossing_quintic(p, r1, l1, h, cf, cb);
+                    for (int s = -3; s <= 3; ++s)
+                        p[s + 3] = __ldg(cfield + L.base + (long long)clampi(L.c + s, L.n) * L.stride);
+                    if (CUBIC)
+                        crossing_cubic_fast(p, (float)r1, (float)l1, (float)h, ff, fb);
+                    else
+                        crossing_quintic_fast(p, (float)r1, (float)l1, (float)h, ff, fb);
+                    cf = ff;
+                    cb = fb;
+                } else {
+                    double p[7];
+#pragma unroll
+                    for (int s = -3; s <= 3; ++s)
+                        p[s + 3] = (double)__ldg(cfield + L.base + (long long)clampi(L.c + s, L.n) * L.stride);
+                    if (CUBIC)
+                        crossing_cubic(p, r1, l1, h, cf, cb);
+                    else
+                        crossing_quintic(p, r1, l1, h, cf, cb);
+                }
             }
             cp.p[2 * ax][c] = (T)cf;
             cp.p[2 * ax + 1][c] = (T)cb;

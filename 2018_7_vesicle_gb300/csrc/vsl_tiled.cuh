@@ -23,9 +23,17 @@
 namespace vsl {
 namespace {
 
-constexpr int TY = 32;  // rows per tile (threadIdx.x)
-constexpr int TX = 8;   // columns per tile (threadIdx.y)
-constexpr int KZ = 32;  // pages per block
+// Tile shape and occupancy target (compile-time tuning constants, chosen by measurement
+// on GB300: see the design notes).
+#ifndef VSL_TILED_KZ
+#define VSL_TILED_KZ 32
+#endif
+#ifndef VSL_TILED_MIN_BLOCKS
+#define VSL_TILED_MIN_BLOCKS 5
+#endif
+constexpr int TY = 32;            // rows per tile (threadIdx.x)
+constexpr int TX = 8;             // columns per tile (threadIdx.y)
+constexpr int KZ = VSL_TILED_KZ;  // pages per block
 constexpr int HALO = 3;
 constexpr int SW = TY + 2 * HALO;  // smem row extent (fastest)
 constexpr int SH = TX + 2 * HALO;
@@ -54,7 +62,7 @@ struct TiledArgs {
 constexpr int PER_THREAD = (PLANE + TY * TX - 1) / (TY * TX);  // halo elements per thread
 
 template <int KIND>
-__global__ void __launch_bounds__(TY *TX, 5) k_stage_tiled(TiledArgs a)
+__global__ void __launch_bounds__(TY *TX, VSL_TILED_MIN_BLOCKS) k_stage_tiled(TiledArgs a)
 {
     __shared__ float sm[RING][SH][SW];
     const Grid &g = a.g;
@@ -85,8 +93,8 @@ __global__ void __launch_bounds__(TY *TX, 5) k_stage_tiled(TiledArgs a)
         for (int r = 0; r < PER_THREAD; ++r)
             if (tid + r * TY * TX < PLANE) pre[r] = __ldg(src + e_off[r]);
     };
-    auto store = [&](int p) {
-        float *dst = &sm[slot(p)][0][0];
+    auto store_slot = [&](int sl) {
+        float *dst = &sm[sl][0][0];
 #pragma unroll
         for (int r = 0; r < PER_THREAD; ++r)
             if (tid + r * TY * TX < PLANE) dst[tid + r * TY * TX] = pre[r];
@@ -95,7 +103,7 @@ __global__ void __launch_bounds__(TY *TX, 5) k_stage_tiled(TiledArgs a)
     float q[7];  // phi_s(i, j, k-3 .. k+3)
     for (int p = k0; p < k0 + 4; ++p) {
         fetch(p);
-        store(p);
+        store_slot(slot(p));
     }
     {
         const int ic = clampi(i, g.rows), jc = clampi(j, g.cols);
@@ -111,12 +119,34 @@ __global__ void __launch_bounds__(TY *TX, 5) k_stage_tiled(TiledArgs a)
     weno5_window_weights(q[1] - q[0], q[2] - q[1], q[3] - q[2], q[4] - q[3], q[5] - q[4], a.eps2[2], zr1, zr2, zr3);
 
     const unsigned lane = tid & 31;
-    for (int k = k0; k < k1; ++k) {
+    // ring slots of pages k, k+3 and k+4 (= k-1), advanced by one per page
+    auto next_slot = [](int sl) { return sl == RING - 1 ? 0 : sl + 1; };
+    int s_k = slot(k0), s_k3 = slot(k0 + 3), s_k4 = slot(k0 + 4);
+    // per-node inputs of the next page, loaded one page ahead
+    const long long col_base = (long long)clampi(j, g.cols) * g.rows + clampi(i, g.rows);
+    long long c = col_base + (long long)k0 * g.plane;
+    uint8_t fl_next = 0;
+    float pn_next = 0.f, v0_next = 0.f, v1_next = 0.f, v2_next = 0.f, sp_next = 1.f;
+    auto load_node = [&](long long cc) {
+        if (KIND != SK_ADVECT) fl_next = __ldg(a.flags + cc);
+        if (a.stage != 0) pn_next = __ldg(a.phi_n + cc);
+        if (KIND != SK_REINIT) {
+            v0_next = __ldg(a.v.p[0] + cc);
+            v1_next = __ldg(a.v.p[1] + cc);
+            v2_next = __ldg(a.v.p[2] + cc);
+            if (KIND == SK_ADVECT && a.speed) sp_next = __ldg(a.speed + cc);
+        }
+    };
+    if (active && k0 < k1) load_node(c);
+    for (int k = k0; k < k1; ++k, c += g.plane) {
         // every warp has finished page k-1 and stored page k+3
         __syncthreads();
-        q[6] = sm[slot(k + 3)][ty + HALO][tx + HALO];
+        q[6] = sm[s_k3][ty + HALO][tx + HALO];
         fetch(k + 4);  // loads in flight during this page's arithmetic, stored at its end
-        const float(*P)[SW] = sm[slot(k)];
+        const float(*P)[SW] = sm[s_k];
+        const uint8_t fl = fl_next;
+        const float pn = pn_next, vx0 = v0_next, vy0 = v1_next, vz0 = v2_next, sp = sp_next;
+        if (active && k + 1 < k1) load_node(c + g.plane);
 
         // z window of page k+1: its weights give the forward derivative here and the
         // backward derivative at the next page
@@ -127,7 +157,6 @@ __global__ void __launch_bounds__(TY *TX, 5) k_stage_tiled(TiledArgs a)
 
         bool band = false;
         if (active) {
-            const long long c = (long long)k * g.plane + (long long)j * g.rows + i;
             float px[7], py[7];
 #pragma unroll
             for (int s = 0; s < 7; ++s) {
@@ -135,8 +164,6 @@ __global__ void __launch_bounds__(TY *TX, 5) k_stage_tiled(TiledArgs a)
                 py[s] = P[ty + HALO][tx + s];
             }
             const float ps = q[3];
-            uint8_t fl = 0;
-            if (KIND != SK_ADVECT) fl = __ldg(a.flags + c);
             float step = 0.f;
             bool compute = true;
             if (KIND != SK_ADVECT && (fl & FIXED_BIT)) compute = false;
@@ -158,24 +185,13 @@ __global__ void __launch_bounds__(TY *TX, 5) k_stage_tiled(TiledArgs a)
                     const float gn = godunov_norm(neg, dxf, dxb, dyf, dyb, dzf, dzb);
                     step = (gn - 1.f) * dtn * (neg ? -1.f : 1.f);
                 } else if (KIND == SK_EXTEND) {
-                    step = upwind_dot(__ldg(a.v.p[0] + c), __ldg(a.v.p[1] + c), __ldg(a.v.p[2] + c), dxf, dxb, dyf,
-                                      dyb, dzf, dzb) *
-                           a.dt_uniform;
+                    step = upwind_dot(vx0, vy0, vz0, dxf, dxb, dyf, dyb, dzf, dzb) * a.dt_uniform;
                 } else {
-                    float vx = __ldg(a.v.p[0] + c), vy = __ldg(a.v.p[1] + c), vz = __ldg(a.v.p[2] + c);
-                    if (a.speed) {
-                        const float sp = __ldg(a.speed + c);
-                        vx *= sp;
-                        vy *= sp;
-                        vz *= sp;
-                    }
-                    step = (float)__ldg(a.dt) * upwind_dot(vx, vy, vz, dxf, dxb, dyf, dyb, dzf, dzb);
+                    step = (float)__ldg(a.dt) *
+                           upwind_dot(vx0 * sp, vy0 * sp, vz0 * sp, dxf, dxb, dyf, dyb, dzf, dzb);
                 }
             }
-            if (!band) {
-                const float pn = a.stage == 0 ? 0.f : __ldg(a.phi_n + c);
-                a.out[c] = rk3_combine(a.stage, pn, ps - step);
-            }
+            if (!band) a.out[c] = rk3_combine(a.stage, pn, ps - step);
         }
         if (KIND == SK_REINIT) {  // the extension's band is the static list of flagged nodes
             const unsigned m = __ballot_sync(0xffffffffu, band);
@@ -186,17 +202,20 @@ __global__ void __launch_bounds__(TY *TX, 5) k_stage_tiled(TiledArgs a)
                 base = __shfl_sync(0xffffffffu, base, leader);
                 if (band) {
                     const unsigned rank = __popc(m & ((1u << lane) - 1u));
-                    a.queue[base + rank] = (unsigned)((long long)k * g.plane + (long long)j * g.rows + i);
+                    a.queue[base + rank] = (unsigned)c;
                 }
             }
         }
         // page k+4 goes to the slot of page k-1, which no warp reads any more
-        store(k + 4);
+        store_slot(s_k4);
         zr1 = nr1;
         zr2 = nr2;
         zr3 = nr3;
 #pragma unroll
         for (int s = 0; s < 6; ++s) q[s] = q[s + 1];
+        s_k = next_slot(s_k);
+        s_k3 = next_slot(s_k3);
+        s_k4 = next_slot(s_k4);
     }
 }
 

@@ -107,24 +107,34 @@ __global__ void __launch_bounds__(NT) k_toolbox(const T *__restrict__ f, Toolbox
         if (o.f[17]) o.f[17][c] = delta;
     }
     if (!partials) return;
+    // Volume terms equal to exactly 1 (nodes with no positive neighbour) are counted as
+    // integers; only warps holding other terms run the FP64 shuffle tree.  Per block:
+    // partial = (double)count + FP64 tree sum of the rest, in a fixed order.
     __shared__ double sa[NW], sv[NW];
+    __shared__ int sc[NW];
     const int t = threadIdx.y * BX + threadIdx.x;
-    area = warp_sum(area);
-    vol = warp_sum(vol);
+    const bool unit = vol == 1.0;
+    const unsigned ones = __ballot_sync(0xffffffffu, unit);
+    if (unit) vol = 0.0;
+    if (__any_sync(0xffffffffu, area != 0.0)) area = warp_sum(area);
+    if (__any_sync(0xffffffffu, vol != 0.0)) vol = warp_sum(vol);
     if ((t & 31) == 0) {
         sa[t >> 5] = area;
         sv[t >> 5] = vol;
+        sc[t >> 5] = __popc(ones);
     }
     __syncthreads();
     if (t == 0) {
         double a = 0.0, v = 0.0;
+        int n = 0;
         for (int w = 0; w < NW; ++w) {
             a += sa[w];
             v += sv[w];
+            n += sc[w];
         }
         const long long b = block_linear();
         partials[2 * b] = a;
-        partials[2 * b + 1] = v;
+        partials[2 * b + 1] = (double)n + v;
     }
 }
 

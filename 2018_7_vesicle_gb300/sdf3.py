@@ -166,7 +166,10 @@ class SDF3:
     # -- setDistance.m:3-33 -----------------------------------------------------------------
     def setDistance(self):
         size = self.GD3.Size
-        d = [colmajor_empty(size, self.dtype) for _ in range(6)]
+        if self.xpr is not None and tuple(self.xpr.shape) == size and self.xpr.dtype == self.dtype:
+            d = list(self._dist())  # rewritten in place (keeps recorded graphs valid)
+        else:
+            d = [colmajor_empty(size, self.dtype) for _ in range(6)]
         ws = self.workspace("set_distance")
         lib().call(self._fn("vsl_set_distance"), _ptr(self.F), *map(_ptr, d), *self.GD3.args(), _ptr(ws), ws.numel(),
                    _stream())
@@ -259,14 +262,35 @@ class SDF3:
                    *self.GD3.args(), _ptr(ws), ws.numel(), _stream())
         return out
 
-    def vesicle_step(self, ext_iters: int = 30, reinit_iters: int = 20, cfl: float = 0.5, info=None) -> torch.Tensor:
+    def vesicle_step(self, ext_iters: int = 30, reinit_iters: int = 20, cfl: float = 0.5, info=None,
+                     graph: bool = False) -> torch.Tensor:
         """One vesicle step in place on self.F and its cached distances; returns the device
-        tensor [area, volume, dt, max|Vn|]."""
+        tensor [area, volume, dt, max|Vn|].
+
+        graph=True records the step's whole launch sequence (about 300 kernels and memsets
+        for 30 + 20 pseudo-steps) once as a CUDA graph and replays it; the graph is
+        re-recorded when the arguments or the field/distance buffers change."""
+        if graph:
+            return self._vesicle_step_graph(int(ext_iters), int(reinit_iters), float(cfl))
         info = torch.empty(4, dtype=torch.float64, device="cuda") if info is None else info
         ws = self.workspace("vesicle_step")
         lib().call(self._fn("vsl_vesicle_step"), _ptr(self.F), *map(_ptr, self._dist()), int(ext_iters),
                    int(reinit_iters), float(cfl), _ptr(info), *self.GD3.args(), _ptr(ws), ws.numel(), _stream())
         return info
+
+    def _vesicle_step_graph(self, ext_iters: int, reinit_iters: int, cfl: float) -> torch.Tensor:
+        key = (ext_iters, reinit_iters, cfl, _ptr(self.F), tuple(map(_ptr, self._dist())))
+        if getattr(self, "_graph_key", None) != key:
+            ws = self.workspace("vesicle_step")
+            self._graph_info = torch.empty(4, dtype=torch.float64, device="cuda")
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                lib().call(self._fn("vsl_vesicle_step"), _ptr(self.F), *map(_ptr, self._dist()), ext_iters,
+                           reinit_iters, cfl, _ptr(self._graph_info), *self.GD3.args(), _ptr(ws), ws.numel(),
+                           _stream())
+            self._graph, self._graph_key = g, key
+        self._graph.replay()
+        return self._graph_info
 
 
 def ellipsoid_phi(x, y, z, a: float, b: float, c: float):

@@ -140,18 +140,46 @@ def test_surface_redistance(pkg, oracle_mod):
 
 
 def test_vesicle_steps(pkg, oracle_mod):
-    """Three composite steps at 48^3: interface-band error and area/volume per step."""
+    """The composite step, one step at a time from the FP64 oracle's state (field and its
+    cached distances rounded to FP32), three steps of the noisy oblate vesicle at 48^3.
+
+    Per step: interface-band error below 1e-4*dx at the worst node and 5e-6*dx RMS, area
+    and volume within 1e-6, dt within 1e-4 (dt = CFL*Ds/max|Vn| is a maximum over the band
+    and the most sensitive output).  Consecutive FP32 steps are not compared with
+    consecutive FP64 steps: the two trajectories drift apart through dt."""
     O = oracle_mod
     x, y, z = S.cube_grid(48, -1.5, 1.5)
     F = S.noisy_oblate(x, y, z, seed=3)
     g = O.grid_from_mesh(x, y, z)
     K = O.kernels("port")
-    m = f32(pkg, x, y, z, F)
     Fo, do = F, O.set_distance(K, g, F)
     for _ in range(3):
+        m = f32(pkg, x, y, z, Fo)
+        for t, a in zip(m._dist(), do.six()):
+            t.copy_(dev(a, t.dtype))
         info = m.vesicle_step(30, 20, 0.5).cpu().numpy()
-        Fo, do, oi = O.vesicle_step(K, g, Fo, do, 30, 20, 0.5)
+        Fn, dn, oi = O.vesicle_step(K, g, Fo, do, 30, 20, 0.5)
         assert abs(info[0] - oi["area"]) <= 1e-6 * oi["area"]
         assert abs(info[1] - oi["volume"]) <= 1e-6 * oi["volume"]
         assert abs(info[2] - oi["dt"]) <= 1e-4 * oi["dt"]
-        assert band_err(host(m.F), Fo, Fo, g.dx) <= 2e-4
+        got = host(m.F)
+        band = np.abs(Fn) < 3 * g.dx
+        e = np.abs(got[band] - Fn[band]) / g.dx
+        assert e.max() <= 1e-4 and np.sqrt(np.mean(e**2)) <= 5e-6
+        Fo, do = Fn, dn
+
+
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_vesicle_step_graph_replay(pkg, precision):
+    """The CUDA-graph replay of a vesicle step gives bitwise the result of direct launches."""
+    x, y, z = S.cube_grid(40, -1.5, 1.5)
+    F = S.noisy_oblate(x, y, z, seed=5)
+    runs = []
+    for graph in (False, True):
+        m = pkg.SDF3(pkg.GD3(x, y, z), Val=F, precision=precision)
+        m.setDistance()
+        infos = [m.vesicle_step(10, 6, 0.5, graph=graph).cpu().numpy().copy() for _ in range(3)]
+        runs.append((host(m.F), infos))
+    assert np.array_equal(runs[0][0], runs[1][0])
+    for a, b in zip(runs[0][1], runs[1][1]):
+        assert np.array_equal(a, b)
