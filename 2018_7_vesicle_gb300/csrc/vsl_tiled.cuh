@@ -23,13 +23,15 @@
 namespace vsl {
 namespace {
 
-// Tile shape and occupancy target (compile-time tuning constants, chosen by measurement
-// on GB300: see the design notes).
+// Pages per block and occupancy target (compile-time tuning constants).  Measured on
+// GB300 at 256^3 (vesicle step with graph replay): KZ 16/32/64 x 4/5 blocks per SM gave
+// 46.6/47.5/47.9 ms at 4 blocks (64 registers, no spills) and 49.5/51.4/53.0 ms at 5
+// blocks (48 registers with spills); 16 pages and 4 blocks is the default.
 #ifndef VSL_TILED_KZ
-#define VSL_TILED_KZ 32
+#define VSL_TILED_KZ 16
 #endif
 #ifndef VSL_TILED_MIN_BLOCKS
-#define VSL_TILED_MIN_BLOCKS 5
+#define VSL_TILED_MIN_BLOCKS 4
 #endif
 constexpr int TY = 32;            // rows per tile (threadIdx.x)
 constexpr int TX = 8;             // columns per tile (threadIdx.y)
