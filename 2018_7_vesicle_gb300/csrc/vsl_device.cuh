@@ -626,6 +626,74 @@ __device__ inline void crossing_cubic(const double p[7], double dis_f, double di
     }
 }
 
+// ---------------------------------------------------------------------------------------
+// Packed FP32 pairs (sm_100+ dual-lane FMA/MUL/ADD): the backward and forward WENO5
+// reconstructions of a node are the same arithmetic on mirrored differences, so the
+// mixed-precision form evaluates them as the .x (backward) and .y (forward) lanes of
+// float2 operations.
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 f2s(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 fdiv2(float2 a, float2 b) { return f2(__fdividef(a.x, b.x), __fdividef(a.y, b.y)); }
+
+// Candidate values of the three stencils for packed differences u1..u5.
+__device__ __forceinline__ void weno5_candidates2(float2 u1, float2 u2, float2 u3, float2 u4, float2 u5, float2 &q1,
+                                                  float2 &q2, float2 &q3)
+{
+    q1 = fma2(f2s(1.f / 3.f), u1, fma2(f2s(-7.f / 6.f), u2, mul2(f2s(11.f / 6.f), u3)));
+    q2 = fma2(f2s(-1.f / 6.f), u2, fma2(f2s(5.f / 6.f), u3, mul2(f2s(1.f / 3.f), u4)));
+    q3 = fma2(f2s(1.f / 3.f), u3, fma2(f2s(5.f / 6.f), u4, mul2(f2s(-1.f / 6.f), u5)));
+}
+
+// Reciprocal weights 1/(S_k + eps2)^2 of packed windows.
+__device__ __forceinline__ void weno5_weights2(float2 u1, float2 u2, float2 u3, float2 u4, float2 u5, float2 eps2,
+                                               float2 &r1, float2 &r2, float2 &r3)
+{
+    const float2 c13 = f2s(13.f / 12.f), c14 = f2s(0.25f);
+    const float2 t1 = fma2(f2s(-2.f), u2, add2(u1, u3));
+    const float2 t2 = fma2(f2s(-4.f), u2, fma2(f2s(3.f), u3, u1));
+    const float2 t3 = fma2(f2s(-2.f), u3, add2(u2, u4));
+    const float2 t4 = fma2(f2s(-1.f), u4, u2);
+    const float2 t5 = fma2(f2s(-2.f), u4, add2(u3, u5));
+    const float2 t6 = fma2(f2s(-4.f), u4, fma2(f2s(3.f), u3, u5));
+    const float2 s1 = fma2(c13, mul2(t1, t1), mul2(c14, mul2(t2, t2)));
+    const float2 s2 = fma2(c13, mul2(t3, t3), mul2(c14, mul2(t4, t4)));
+    const float2 s3 = fma2(c13, mul2(t5, t5), mul2(c14, mul2(t6, t6)));
+    const float2 e1 = add2(s1, eps2), e2 = add2(s2, eps2), e3 = add2(s3, eps2);
+    const float2 one = f2s(1.f);
+    r1 = fdiv2(one, mul2(e1, e1));
+    r2 = fdiv2(one, mul2(e2, e2));
+    r3 = fdiv2(one, mul2(e3, e3));
+}
+
+// Weighted combination sum(d_k r_k q_k) / sum(d_k r_k), d = (0.1, 0.6, 0.3).
+__device__ __forceinline__ float2 weno5_combine2(float2 q1, float2 q2, float2 q3, float2 r1, float2 r2, float2 r3)
+{
+    const float2 a1 = mul2(f2s(0.1f), r1), a2 = mul2(f2s(0.6f), r2), a3 = mul2(f2s(0.3f), r3);
+    return fdiv2(fma2(a1, q1, fma2(a2, q2, mul2(a3, q3))), add2(a1, add2(a2, a3)));
+}
+
+// Backward (.x) and forward (.y) WENO5 derivatives from the seven line values.
+__device__ __forceinline__ void weno5_pair_fast2(const float p[7], float inv_h, float eps2, float &d_fore,
+                                                 float &d_back)
+{
+    float u[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) u[m] = p[m + 1] - p[m];
+    // backward window u0..u4, forward window u5..u1
+    const float2 U1 = f2(u[0], u[5]), U2 = f2(u[1], u[4]), U3 = f2(u[2], u[3]), U4 = f2(u[3], u[2]),
+                 U5 = f2(u[4], u[1]);
+    float2 q1, q2, q3, r1, r2, r3;
+    weno5_candidates2(U1, U2, U3, U4, U5, q1, q2, q3);
+    weno5_weights2(U1, U2, U3, U4, U5, f2s(eps2), r1, r2, r3);
+    const float2 d = mul2(weno5_combine2(q1, q2, q3, r1, r2, r3), f2s(inv_h));
+    d_back = d.x;
+    d_fore = d.y;
+}
+
 // Crossing values for the mixed-precision form: the same interpolating polynomials
 // (degree 5 through six nodes, or the cubic through four) evaluated in FP32 in Lagrange
 // product form with the equispaced denominators folded into constants, at the normalised

@@ -177,10 +177,14 @@ __global__ void __launch_bounds__(TY *TX, VSL_TILED_MIN_BLOCKS) k_stage_tiled(Ti
             }
             if (compute && !band) {
                 float dxf, dxb, dyf, dyb;
-                weno5_pair_fast(px, a.inv_h[0], a.eps2[0], dxf, dxb);
-                weno5_pair_fast(py, a.inv_h[1], a.eps2[1], dyf, dyb);
-                const float dzb = weno5_with_weights(v1, v2, v3, v4, v5, zr1, zr2, zr3) * a.inv_h[2];
-                const float dzf = weno5_with_weights(v6, v5, v4, v3, v2, nr3, nr2, nr1) * a.inv_h[2];
+                weno5_pair_fast2(px, a.inv_h[0], a.eps2[0], dxf, dxb);
+                weno5_pair_fast2(py, a.inv_h[1], a.eps2[1], dyf, dyb);
+                // z: backward window of page k (weights carried), forward = reversed window of k+1
+                float2 q1, q2, q3;
+                weno5_candidates2(f2(v1, v6), f2(v2, v5), f2(v3, v4), f2(v4, v3), f2(v5, v2), q1, q2, q3);
+                const float2 dz = mul2(weno5_combine2(q1, q2, q3, f2(zr1, nr3), f2(zr2, nr2), f2(zr3, nr1)),
+                                       f2s(a.inv_h[2]));
+                const float dzb = dz.x, dzf = dz.y;
                 if (KIND == SK_REINIT) {
                     const bool neg = fl & MASK_BIT;
                     const float dtn = (fl & 0x3F) ? pseudo_dt(fl, a.d, c, a.h[0], a.h[1], a.h[2]) : a.dt_uniform;
