@@ -147,3 +147,30 @@ def vesicle_256(n: int = 256, seed: int = 0, reduced_volume: float = 0.65, pages
 def surface_field(x, y, z):
     """The scalar field redistanced on the interface: sin(3x) cos(2y) + 0.5 z^2."""
     return np.asfortranarray(np.sin(3 * x) * np.cos(2 * y) + 0.5 * z**2)
+
+
+EDGE_CHOICES = (48, 64, 96, 128, 160)
+
+
+def random_vesicles(count: int = 64, seed: int = 0, half_width: float = 1.2, edges=EDGE_CHOICES):
+    """The batched workload: `count` ellipsoids sqrt(x^2/a^2+y^2/b^2+z^2/c^2) - 1 with half
+    axes a, b, c ~ U[0.4, 1.0], each on its own box [-half_width, half_width]^3 with node
+    counts per axis drawn uniformly from `edges` (anisotropic grids).  Returns a list of
+    (xv, yv, zv, axes) -- the coordinate vectors of the columns (x), rows (y) and pages
+    (z) and the half axes; `ellipsoid_field` turns one into a field."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        nx, ny, nz = (int(v) for v in rng.choice(edges, size=3))
+        axes = tuple(float(v) for v in rng.uniform(0.4, 1.0, size=3))
+        out.append((np.linspace(-half_width, half_width, nx), np.linspace(-half_width, half_width, ny),
+                    np.linspace(-half_width, half_width, nz), axes))
+    return out
+
+
+def ellipsoid_field(xv, yv, zv, axes, device=None):
+    """Mesh (x, y, z) and field of one batched vesicle (see random_vesicles)."""
+    x, y, z = meshgrid(xv, yv, zv, device=device)
+    a, b, c = axes
+    xp = _Ops(x)
+    return x, y, z, xp.fortran(xp.sqrt(x**2 / a**2 + y**2 / b**2 + z**2 / c**2) - 1)

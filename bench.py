@@ -44,9 +44,10 @@ BYTES_ADVECT = 17 * W32
 BYTES_SETUP = (7 + 10 + 13 + 1 + 7) * W32
 BYTES_PER_NODE_STEP = EXT * BYTES_EXTEND + ADV * BYTES_ADVECT + RE * BYTES_REINIT + BYTES_SETUP
 # kernels launched per vesicle step: toolbox, sum, velocity, classify, crossing,
-# 3*EXT extension stages, band max, time step, 3 advection stages, setDistance,
-# classify, 3*RE reinitialization stages
-LAUNCHES_PER_STEP = 1 + 1 + 1 + 1 + 1 + 3 * EXT + 1 + 1 + 3 * ADV + 1 + 1 + 3 * RE
+# 3*EXT extension stages each with its band kernel, band max, time step, 3 advection
+# stages, setDistance (scan + roots), classify, 3*RE reinitialization stages each with
+# its band kernel (memsets of the list counters are not kernels)
+LAUNCHES_PER_STEP = 1 + 1 + 1 + 1 + 1 + 2 * 3 * EXT + 1 + 1 + 3 * ADV + 2 + 1 + 2 * 3 * RE
 
 
 def peaks():
@@ -197,6 +198,42 @@ def profile_case(which, m, torch):
     print(json.dumps({"profile_case": which, "ok": True}))
 
 
+def batched_measure(torch, pkg, S, steps: int, seed: int = 0):
+    """The batched workload: 64 vesicles with node counts per axis drawn from
+    {48, 64, 96, 128, 160} and half axes U[0.4, 1.0], FP32, advanced `steps` vesicle steps
+    as one CUDA graph per batch step (parallel branches) and, for comparison, by the
+    per-vesicle launch loop."""
+    B = importlib.import_module(PKG + ".batch")
+    maps = []
+    for xv, yv, zv, axes in S.random_vesicles(64, seed=seed):
+        x, y, z, F = S.ellipsoid_field(xv, yv, zv, axes, device="cuda")
+        spacing = (float(xv[1] - xv[0]), float(yv[1] - yv[0]), float(zv[1] - zv[0]))
+        g = pkg.GD3(x, y, z, spacing=spacing)
+        g.X = g.Y = g.Z = None
+        m = pkg.SDF3(g, Val=F, precision="f32")
+        m.setDistance()
+        maps.append(m)
+        del x, y, z, F
+    batch = B.VesicleBatch(maps, streams=16)
+    nodes = batch.nodes()
+    out = {"vesicles": len(maps), "nodes": nodes, "steps": steps}
+    for name, fn in (("graph", batch.step), ("loop", batch.step_loop)):
+        fn(EXT, RE, CFL)  # warm-up (records the graph)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(steps):
+            fn(EXT, RE, CFL)
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / steps
+        out[name] = {"ms_per_step": ms, "value": GPT_PER_NODE * nodes / (ms / 1e3) / 1e9, "unit": UNIT}
+    out["speedup_graph_over_loop"] = out["loop"]["ms_per_step"] / out["graph"]["ms_per_step"]
+    del batch, maps
+    torch.cuda.empty_cache()
+    return out
+
+
 def workload_config(ngpus):
     return {"workload": f"vesicle step {N}^3 mixed precision (FP32 stencils, FP64 roots/reductions): "
                         f"{EXT} WENO5-RK3 extension + {ADV} WENO5-RK3 advection + {RE} WENO5-RK3 reinit "
@@ -214,6 +251,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--profile", choices=["extend", "reinit", "advect", "step"],
                     help="run only a few launches of one operator at 256^3 (the ncu capture case)")
     args = ap.parse_args()
@@ -334,6 +372,12 @@ def main():
                 "ratio_fp32_over_fp64": (gpt_step / (ms / 1e3)) / (gpt_step / (ms64 / 1e3))}
         del m64
 
+    batched = None
+    if not args.no_batched and rank == 0:
+        del m
+        torch.cuda.empty_cache()
+        batched = batched_measure(torch, pkg, S, steps=5)
+
     if rank != 0:
         if dist is not None:
             dist.barrier()
@@ -356,6 +400,7 @@ def main():
         "gpu_launches": LAUNCHES_PER_STEP * args.steps,
         "clocks": clk.summary(),
         "fp64_plain": fp64,
+        "batched": batched,
         "last_info": {"area": info_h[0], "volume": info_h[1], "dt": info_h[2], "max_speed": info_h[3]},
         "cpu_baseline": cpu,
     }
