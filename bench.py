@@ -246,7 +246,7 @@ def workload_config(ngpus):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -387,9 +387,12 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(world),
-        "roofline": {"bound": "hbm", "kernel": "k_extend_stage<float> (one WENO5 RK3 extension stage)",
+        "roofline": {"bound": "hbm",
+                     "kernel": "one FP32 WENO5 RK3 extension stage: k_stage_tiled<SK_EXTEND> + k_band_stage<SK_EXTEND>",
                      "achieved": achieved, "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": traffic, "stage_ms": stage_ms,
+                     "frac": achieved / hbm, "traffic": traffic,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_stage_tiled<SK_EXTEND> at 256^3 (band launch not included)",
+                     "stage_ms": stage_ms,
                      "algorithmic_bytes_per_launch": alg_bytes_launch,
                      "effective": "fused stage reads fewer bytes than the reference dataflow counts"},
         "step_hbm": {"algorithmic_bytes_per_step": BYTES_PER_NODE_STEP * N**3,
