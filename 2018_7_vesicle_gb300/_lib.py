@@ -30,6 +30,8 @@ SIGNATURES = {
     "vsl_set_calculus_toolbox": "p" * 18 + "pp" + _G + "d" + "i" + "s",
     "vsl_advection_step": "ppppp" + _G + "s",
     "vsl_weno_derivative": "ppppppp" + _G + "s",
+    # no-allocation variant (static device scratch, no workspace argument)
+    "vsl_area_volume_noalloc_f64": "pp" + _G + "s",
 }
 for _suf in ("f64", "f32"):
     SIGNATURES.update(

@@ -530,6 +530,7 @@ const char *vsl_status_string(int status)
     case VSL_ERR_WORKSPACE: return "workspace missing, too small or not 256-byte aligned";
     case VSL_ERR_CUDA: return "CUDA launch failed";
     case VSL_ERR_OP: return "unknown operation";
+    case VSL_ERR_SCRATCH_LIMIT: return "grid too large for the static scratch of a no-allocation entry point";
     default: return "unknown status";
     }
 }

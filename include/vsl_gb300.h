@@ -35,7 +35,8 @@ enum {
     VSL_ERR_VALUE = 3,     /* a spacing, iteration count or CFL number out of range */
     VSL_ERR_WORKSPACE = 4, /* workspace missing, too small or misaligned */
     VSL_ERR_CUDA = 5,      /* a kernel launch failed (cudaGetLastError) */
-    VSL_ERR_OP = 6         /* unknown operation id */
+    VSL_ERR_OP = 6,        /* unknown operation id */
+    VSL_ERR_SCRATCH_LIMIT = 7 /* grid needs more than the static scratch of a no-allocation entry point */
 };
 
 /* largest grid accepted (nodes); indices are 64-bit inside the kernels */
@@ -210,6 +211,22 @@ int vsl_area_volume_f64(const double *F, double *area_volume, int rows, int cols
                         double dz, void *workspace, size_t workspace_bytes, vsl_stream_t stream);
 int vsl_area_volume_f32(const float *F, double *area_volume, int rows, int cols, int pges, double dx, double dy,
                         double dz, void *workspace, size_t workspace_bytes, vsl_stream_t stream);
+
+/* No counterpart in the reference.  vsl_area_volume_f64 for callers that cannot allocate
+ * device memory (a MEX function working on MATLAB-owned gpuArrays, a framework whose
+ * allocator must not be bypassed, code that must not take cudaMalloc's implicit
+ * synchronisation): no workspace argument, and the call allocates nothing.  Its scratch
+ * is one static device array of VSL_NOALLOC_SCRATCH_BYTES, held by every device that loads
+ * the library until the process exits.  Limit: ceil(rows/32) * ceil(cols/8) * pges <=
+ * VSL_NOALLOC_SCRATCH_BYTES / 16 = 65536 (every grid up to 256^3); larger grids return
+ * VSL_ERR_SCRATCH_LIMIT before anything is launched.  The first call on a device looks up
+ * the array's address with that device current (make that first call before any stream
+ * capture).  All calls on a device share the array: calls that can overlap on the GPU
+ * race, so order them (one stream, or events).  Results are bitwise those of
+ * vsl_area_volume_f64. */
+#define VSL_NOALLOC_SCRATCH_BYTES 1048576
+int vsl_area_volume_noalloc_f64(const double *F, double *area_volume, int rows, int cols, int pges, double dx,
+                                double dy, double dz, vsl_stream_t stream);
 
 /* WENO5 advection phi_t + v.grad(phi) = 0 (the upwind operator of
  * CUDA_Code/4_0_Calculus_ToolBox/advection_step.cu:30-56 / +SD/@GD3/GD3.m:393-398) in the
