@@ -45,6 +45,8 @@ for _suf in ("f64", "f32"):
             f"vsl_area_volume_{_suf}": "pp" + _G + "pz" + "s",
             f"vsl_weno5_rk3_advection_{_suf}": "pppppi" + _G + "pz" + "s",
             f"vsl_vesicle_step_{_suf}": "p" + "pppppp" + "iid" + "p" + _G + "pz" + "s",
+            f"vsl_weno5_rk3_advection_adjoint_{_suf}": "ppppp" + "pppp" + _G + "pz" + "s",
+            f"vsl_weno5_rk3_reinitialization_adjoint_{_suf}": "pipp" + _G + "pz" + "s",
         }
     )
 
@@ -58,6 +60,8 @@ OP = {
     "advection": 7,
     "vesicle_step": 8,
     "set_distance": 9,
+    "advection_adjoint": 10,
+    "reinit_adjoint": 11,
 }
 
 

@@ -150,6 +150,25 @@ template <typename T> StepWork<T> carve_step(Bump &w, const Grid &g)
     return s;
 }
 
+// adjoint sweeps: recomputed stage fields b, c (inside `re`), the 21 Jacobian slots,
+// the running adjoint x, the RK3 base accumulator and (reinitialization) the six
+// distance adjoints
+template <typename T> struct AdjWork {
+    ReinitWork<T> re;
+    T *W, *x, *acc;
+    Ptr6<T> mu;
+};
+template <typename T> AdjWork<T> carve_adj(Bump &w, const Grid &g, bool reinit)
+{
+    AdjWork<T> a{};
+    a.re = carve_reinit<T>(w, g, reinit);
+    a.W = w.take<T>((long long)ADJ_SLOTS * g.num);
+    a.x = w.take<T>(g.num);
+    a.acc = w.take<T>(g.num);
+    for (int q = 0; q < 6; ++q) a.mu.p[q] = reinit ? w.take<T>(g.num) : nullptr;
+    return a;
+}
+
 size_t measure(int op, const Grid &g, int elem)
 {
     Bump w(nullptr);
@@ -165,6 +184,8 @@ size_t measure(int op, const Grid &g, int elem)
         case VSL_OP_ADVECTION: carve_reinit<T>(w, g, false); break;
         case VSL_OP_VESICLE_STEP: carve_step<T>(w, g); break;
         case VSL_OP_SET_DISTANCE: carve_edges(w, g); break;
+        case VSL_OP_ADVECTION_ADJOINT: carve_adj<T>(w, g, false); break;
+        case VSL_OP_REINIT_ADJOINT: carve_adj<T>(w, g, true); break;
         default: return false;
         }
         return true;
@@ -513,6 +534,123 @@ int op_vesicle_step(T *F, T *xpr, T *xpl, T *ypf, T *ypb, T *zpu, T *zpd, int ex
     return reinit_loop<T>(F, reinit_iters, d, rw, g, false, s);
 }
 
+// ---------------------------------------------------------------------------------------
+// adjoints (no counterpart in the reference)
+// ---------------------------------------------------------------------------------------
+
+// Reverse sweep through the three stages of one RK3 step whose stage inputs are
+// s0 (= the step input), s1, s2.  `jac(ps, lam, coef)` fills W (and the parameter
+// adjoints) for the stage with input ps and output adjoint lam; on return lam holds the
+// adjoint of s0.
+template <typename T, typename Jac>
+int rk3_reverse(const T *s0, const T *s1, const T *s2, T *lam, AdjWork<T> &w, const Grid &g, cudaStream_t s, Jac jac)
+{
+    // stage 2: out = 1/3 s0 + 2/3 (s2 - step(s2))
+    VSL_TRY(jac(s2, lam, 2.0 / 3.0));
+    VSL_TRY(launch_adj_axpy<T>(w.acc, lam, 1.0 / 3.0, true, g, s));
+    VSL_TRY(launch_adj_gather<T>(w.W, lam, 2.0 / 3.0, nullptr, w.x, g, s));
+    // stage 1: s2 = 3/4 s0 + 1/4 (s1 - step(s1))
+    VSL_TRY(jac(s1, w.x, 0.25));
+    VSL_TRY(launch_adj_axpy<T>(w.acc, w.x, 0.75, false, g, s));
+    VSL_TRY(launch_adj_gather<T>(w.W, w.x, 0.25, nullptr, w.x, g, s));
+    // stage 0: s1 = s0 - step(s0)
+    VSL_TRY(jac(s0, w.x, 1.0));
+    VSL_TRY(launch_adj_gather<T>(w.W, w.x, 1.0, w.acc, lam, g, s));
+    return VSL_OK;
+}
+
+// stage inputs s1, s2 of one advection step from its input F, by the forward kernels
+template <typename T>
+int advect_stages(const T *F, Ptr3<const T> v, const double *dt, ReinitWork<T> &w, const Grid &g, cudaStream_t s)
+{
+    if constexpr (std::is_same<T, float>::value) {
+        const Ptr6<const float> none6{};
+        VSL_TRY(tiled(2, false, w.band, F, F, w.b, nullptr, none6, none6, v, nullptr, dt, 0, g, s));
+        VSL_TRY(tiled(2, false, w.band, w.b, F, w.c, nullptr, none6, none6, v, nullptr, dt, 1, g, s));
+    } else {
+        VSL_TRY(launch_advect_stage<T>(F, F, w.b, v, nullptr, dt, g, 0, false, s));
+        VSL_TRY(launch_advect_stage<T>(w.b, F, w.c, v, nullptr, dt, g, 1, false, s));
+    }
+    return VSL_OK;
+}
+
+// stage inputs s1, s2 of one reinitialization pseudo-step from its input F
+template <typename T>
+int reinit_stages(const T *F, Ptr6<const T> d, ReinitWork<T> &w, const Grid &g, cudaStream_t s)
+{
+    if constexpr (std::is_same<T, float>::value) {
+        if (int st = band_reset(w.band, s)) return st;
+        const Ptr6<const float> none6{};
+        const Ptr3<const float> none3{};
+        VSL_TRY(tiled(0, false, w.band, F, F, w.b, w.flags, d, none6, none3, nullptr, nullptr, 0, g, s));
+        VSL_TRY(tiled(0, false, w.band, w.b, F, w.c, w.flags, d, none6, none3, nullptr, nullptr, 1, g, s));
+    } else {
+        VSL_TRY(launch_reinit_stage<T>(F, F, w.b, w.flags, d, g, 0, false, false, s));
+        VSL_TRY(launch_reinit_stage<T>(w.b, F, w.c, w.flags, d, g, 1, false, false, s));
+    }
+    return VSL_OK;
+}
+
+template <typename T>
+int op_advection_adjoint(const T *F, const T *vx, const T *vy, const T *vz, const double *dt, T *lam, T *gvx, T *gvy,
+                         T *gvz, int rows, int cols, int pges, double dx, double dy, double dz, void *ws, size_t bytes,
+                         cudaStream_t s)
+{
+    if (any_null(F, vx, vy, vz, dt, lam, gvx, gvy, gvz)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    if (int st = check_ws(VSL_OP_ADVECTION_ADJOINT, g, sizeof(T), ws, bytes)) return st;
+    Bump b(ws);
+    AdjWork<T> w = carve_adj<T>(b, g, false);
+    const Ptr3<const T> v{{vx, vy, vz}};
+    const Ptr3<T> gv{{gvx, gvy, gvz}};
+    if (int st = advect_stages<T>(F, v, dt, w.re, g, s)) return st;
+    auto jac = [&](const T *ps, const T *l, double coef) {
+        return launch_adj_advect_jac<T>(ps, v, dt, l, coef, w.W, gv, g, s);
+    };
+    return rk3_reverse<T>(F, w.re.b, w.re.c, lam, w, g, s, jac);
+}
+
+template <typename T>
+int op_reinit_adjoint(const T *F0, int iteration, T *lam, T *tape, int rows, int cols, int pges, double dx, double dy,
+                      double dz, void *ws, size_t bytes, cudaStream_t s)
+{
+    if (any_null(F0, lam, tape)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    if (iteration < 0) return VSL_ERR_VALUE;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    if (int st = check_ws(VSL_OP_REINIT_ADJOINT, g, sizeof(T), ws, bytes)) return st;
+    if (iteration == 0) return VSL_OK;
+    Bump b(ws);
+    AdjWork<T> w = carve_adj<T>(b, g, true);
+    ReinitWork<T> &re = w.re;
+    // the forward set-up of WENO5RK3Reinitialization: distances of F0 (degree-5 roots),
+    // classification, then the pseudo-step inputs phi^0 .. phi^{K-1} into the tape
+    VSL_TRY(launch_set_distance<T>(F0, re.dist, g, true, re.edges, s));
+    const Ptr6<const T> d = cview(re.dist);
+    VSL_TRY(launch_classify<T>(F0, d, re.flags, NodeList{nullptr, nullptr}, g, s));
+    const size_t field = sizeof(T) * (size_t)g.num;
+    VSL_TRY(cudaMemcpyAsync(tape, F0, field, cudaMemcpyDeviceToDevice, s));
+    for (int k = 1; k < iteration; ++k) {
+        T *cur = tape + (size_t)k * g.num;
+        VSL_TRY(cudaMemcpyAsync(cur, cur - g.num, field, cudaMemcpyDeviceToDevice, s));
+        if (int st = reinit_loop<T>(cur, 1, d, re, g, false, s)) return st;
+    }
+    for (int q = 0; q < 6; ++q) VSL_TRY(cudaMemsetAsync(w.mu.p[q], 0, field, s));
+    auto jac = [&](const T *ps, const T *l, double coef) {
+        return launch_adj_reinit_jac<T>(ps, re.flags, d, l, coef, w.W, w.mu, g, s);
+    };
+    for (int k = iteration - 1; k >= 0; --k) {
+        const T *phik = tape + (size_t)k * g.num;
+        if (int st = reinit_stages<T>(phik, d, re, g, s)) return st;
+        if (int st = rk3_reverse<T>(phik, re.b, re.c, lam, w, g, s, jac)) return st;
+    }
+    // the distances' dependence on F0
+    VSL_TRY(launch_adj_dist_edges<T>(F0, re.edges, cview(w.mu), w.W, g, s));
+    VSL_TRY(launch_adj_gather<T>(w.W, lam, 1.0, nullptr, lam, g, s));
+    return VSL_OK;
+}
+
 }  // namespace
 }  // namespace vsl
 
@@ -600,6 +738,20 @@ size_t vsl_workspace_bytes(int op, int rows, int cols, int pges, int elem_bytes)
     {                                                                                                              \
         return op_vesicle_step<T>(F, xpr, xpl, ypf, ypb, zpu, zpd, ext_iters, reinit_iters, cfl, info, rows, cols, \
                                   pges, dx, dy, dz, ws, bytes, stream);                                            \
+    }                                                                                                              \
+    int vsl_weno5_rk3_advection_adjoint_##SUF(const T *F, const T *vx, const T *vy, const T *vz, const double *dt, \
+                                              T *lam, T *gvx, T *gvy, T *gvz, int rows, int cols, int pges,        \
+                                              double dx, double dy, double dz, void *ws, size_t bytes,             \
+                                              vsl_stream_t stream)                                                 \
+    {                                                                                                              \
+        return op_advection_adjoint<T>(F, vx, vy, vz, dt, lam, gvx, gvy, gvz, rows, cols, pges, dx, dy, dz, ws,    \
+                                       bytes, stream);                                                             \
+    }                                                                                                              \
+    int vsl_weno5_rk3_reinitialization_adjoint_##SUF(const T *F0, int iteration, T *lam, T *tape, int rows,        \
+                                                     int cols, int pges, double dx, double dy, double dz,          \
+                                                     void *ws, size_t bytes, vsl_stream_t stream)                  \
+    {                                                                                                              \
+        return op_reinit_adjoint<T>(F0, iteration, lam, tape, rows, cols, pges, dx, dy, dz, ws, bytes, stream);    \
     }
 
 VSL_TYPED(f64, double)

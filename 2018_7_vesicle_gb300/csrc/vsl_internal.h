@@ -115,4 +115,21 @@ cudaError_t launch_time_step(const double *partials, int nblocks, double cfl_ds,
                              cudaStream_t s);
 int toolbox_partial_blocks(const Grid &g);
 
+// ---- adjoint kernels (vsl_adjoint.cu), T in {float, double} ------------------------
+// W: 21 slot fields of g.num values each (slot ax*7 + o: line offset o - 3 along ax)
+template <typename T>
+cudaError_t launch_adj_advect_jac(const T *ps, Ptr3<const T> v, const double *dt, const T *lam, double coef, T *W,
+                                  Ptr3<T> gv, const Grid &g, cudaStream_t s);
+template <typename T>
+cudaError_t launch_adj_reinit_jac(const T *ps, const uint8_t *flags, Ptr6<const T> d, const T *lam, double coef, T *W,
+                                  Ptr6<T> mu, const Grid &g, cudaStream_t s);
+template <typename T>
+cudaError_t launch_adj_gather(const T *W, const T *lam, double alpha, const T *acc, T *out, const Grid &g,
+                              cudaStream_t s);
+template <typename T>
+cudaError_t launch_adj_axpy(T *acc, const T *lam, double a, bool init, const Grid &g, cudaStream_t s);
+template <typename T>
+cudaError_t launch_adj_dist_edges(const T *f, EdgeLists e, Ptr6<const T> mu, T *W, const Grid &g, cudaStream_t s);
+constexpr int ADJ_SLOTS = 21;
+
 }  // namespace vsl

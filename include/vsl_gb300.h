@@ -142,7 +142,9 @@ enum {
     VSL_OP_AREA_VOLUME = 6,
     VSL_OP_ADVECTION = 7,
     VSL_OP_VESICLE_STEP = 8,
-    VSL_OP_SET_DISTANCE = 9
+    VSL_OP_SET_DISTANCE = 9,
+    VSL_OP_ADVECTION_ADJOINT = 10,
+    VSL_OP_REINIT_ADJOINT = 11
 };
 
 /* Bytes of workspace operation `op` needs on a rows x cols x pges grid of elements of
@@ -254,6 +256,38 @@ int vsl_vesicle_step_f32(float *F, float *xpr, float *xpl, float *ypf, float *yp
                          int ext_iters, int reinit_iters, double cfl, double *info, int rows, int cols, int pges,
                          double dx, double dy, double dz, void *workspace, size_t workspace_bytes,
                          vsl_stream_t stream);
+
+/* ---- adjoints (no counterpart in the reference, which has no derivatives) -------------
+ *
+ * Reverse-mode sweeps of the forward operations above, for gradients of a loss L of a
+ * transported and reinitialized field.  Each recomputes what it needs of its forward
+ * pass from the forward input with the same kernels, and differentiates every update as
+ * the forward evaluated it (WENO weights with their epsilon, upwind and Godunov switches,
+ * the interface insertion, the min over the six distances).
+ *
+ * One WENO5 TVD-RK3 advection step F -> F' (vsl_weno5_rk3_advection_* with steps = 1)
+ * with the fixed time step *dt.  lam: on entry dL/dF', on return dL/dF.
+ * gvx, gvy, gvz: dL/dv of this step is ADDED (accumulate over steps; zero them first). */
+int vsl_weno5_rk3_advection_adjoint_f64(const double *F, const double *vx, const double *vy, const double *vz,
+                                        const double *dt, double *lam, double *gvx, double *gvy, double *gvz,
+                                        int rows, int cols, int pges, double dx, double dy, double dz,
+                                        void *workspace, size_t workspace_bytes, vsl_stream_t stream);
+int vsl_weno5_rk3_advection_adjoint_f32(const float *F, const float *vx, const float *vy, const float *vz,
+                                        const double *dt, float *lam, float *gvx, float *gvy, float *gvz, int rows,
+                                        int cols, int pges, double dx, double dy, double dz, void *workspace,
+                                        size_t workspace_bytes, vsl_stream_t stream);
+
+/* The reinitialization F0 -> F' of setDistance (degree-5 roots) followed by
+ * vsl_weno5_rk3_reinitialization_* with `iteration` pseudo-steps.  lam: on entry dL/dF',
+ * on return dL/dF0, including the path through the interface distances (the
+ * implicit-function derivative of each root).  tape: device buffer of
+ * iteration * rows*cols*pges elements, overwritten with the pseudo-step inputs. */
+int vsl_weno5_rk3_reinitialization_adjoint_f64(const double *F0, int iteration, double *lam, double *tape, int rows,
+                                               int cols, int pges, double dx, double dy, double dz, void *workspace,
+                                               size_t workspace_bytes, vsl_stream_t stream);
+int vsl_weno5_rk3_reinitialization_adjoint_f32(const float *F0, int iteration, float *lam, float *tape, int rows,
+                                               int cols, int pges, double dx, double dy, double dz, void *workspace,
+                                               size_t workspace_bytes, vsl_stream_t stream);
 
 #ifdef __cplusplus
 }
