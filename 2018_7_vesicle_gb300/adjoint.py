@@ -207,7 +207,8 @@ def velocity(amplitudes: torch.Tensor, modes: torch.Tensor):
 def smoothed_heaviside(phi: torch.Tensor, eps: float) -> torch.Tensor:
     """H_eps(phi) = 0 below -eps, 1 above eps, 1/2 (1 + phi/eps + sin(pi phi/eps)/pi) between."""
     t = torch.clamp(phi / eps, -1.0, 1.0)
-    return 0.5 * (1.0 + t + torch.sin(math.pi * t) / math.pi)
+    mid = 0.5 * (1.0 + t + torch.sin(math.pi * t) / math.pi)
+    return torch.where(t <= -1.0, torch.zeros_like(t), torch.where(t >= 1.0, torch.ones_like(t), mid))
 
 
 def heaviside_mismatch(phi: torch.Tensor, target: torch.Tensor, eps: float, cell_volume: float) -> torch.Tensor:

@@ -234,6 +234,106 @@ def batched_measure(torch, pkg, S, steps: int, seed: int = 0):
     return out
 
 
+def adjoint_profile_case(torch, pkg, S, n: int = 128):
+    """One forward + backward pass of a shortened differentiation workload at n^3 FP32
+    (4 advection steps, one 2-pseudo-step reinitialization; the ncu capture case)."""
+    import numpy as np
+
+    A = importlib.import_module(PKG + ".adjoint")
+    v = np.linspace(-1.5, 1.5, n)
+    x, y, z = S.meshgrid(v, v, v, device="cuda")
+    phi0 = S.noisy_oblate(x, y, z, axes=(1.0, 1.0, 0.55), seed=0)
+    h = 3.0 / (n - 1)
+    grid = pkg.GD3(x, y, z, spacing=(h, h, h))
+    modes = A.fourier_modes(grid, 8, 3.0, seed=0)
+    a = torch.tensor(np.random.default_rng(1).normal(0.0, 0.1, 8), dtype=torch.float64, device="cuda")
+    a.requires_grad_(True)
+    plan = A.TransportPlan(steps=4, reinit_every=4, reinit_iters=2, checkpoint_every=2)
+    tr = A.Transport(grid, A.time_step(a, modes, grid, CFL), plan, "f32")
+    out = tr(phi0.float(), *[t.float() for t in A.velocity(a, modes)])
+    (out.double() ** 2).sum().backward()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "adjoint", "ok": True}))
+
+
+def differentiation_measure(torch, pkg, S, fd_check: bool = False, n: int = 128):
+    """The differentiation workload at n^3 FP32: 40 WENO5 TVD-RK3 advection steps under
+    u = sum of 8 divergence-free Fourier modes (|k| <= 3, amplitudes N(0, 0.1)), a
+    10-pseudo-step reinitialization after every 10 steps, loss = sum (H_eps(phi_T) -
+    H_eps(phi_target))^2 dx^3 (eps = 1.5 dx, target from the amplitudes of another seed),
+    backpropagated to the 8 amplitudes through the adjoint kernels with a checkpoint every
+    10 steps.  Initial surface: the oblate vesicle (1, 1, 0.55) with l <= 6 harmonic noise
+    on [-1.5, 1.5]^3.  Reports forward and forward+backward times, the gradient, its
+    agreement with the FP64 adjoint and (fd_check) with central differences h = 1e-4 of
+    the FP64 forward map."""
+    import numpy as np
+
+    A = importlib.import_module(PKG + ".adjoint")
+    v = np.linspace(-1.5, 1.5, n)
+    x, y, z = S.meshgrid(v, v, v, device="cuda")
+    phi0 = S.noisy_oblate(x, y, z, axes=(1.0, 1.0, 0.55), seed=0)
+    h = 3.0 / (n - 1)
+    grid = pkg.GD3(x, y, z, spacing=(h, h, h))
+    modes = A.fourier_modes(grid, 8, 3.0, seed=0)
+    a0 = torch.tensor(np.random.default_rng(1).normal(0.0, 0.1, 8), dtype=torch.float64, device="cuda")
+    a_tgt = torch.tensor(np.random.default_rng(2).normal(0.0, 0.1, 8), dtype=torch.float64, device="cuda")
+    dt = A.time_step(a0, modes, grid, CFL)
+    plan = A.TransportPlan(steps=40, reinit_every=10, reinit_iters=10, checkpoint_every=10)
+    eps, dvol = 1.5 * h, h ** 3
+    out = {"workload": f"{n}^3 FP32, 40 WENO5-RK3 advection steps + 10-pseudo-step reinit every 10 steps, "
+                       "8 divergence-free Fourier modes |k|<=3, H_eps mismatch loss, checkpoint every 10",
+           "dt": dt}
+
+    def grad(precision):
+        tr = A.Transport(grid, dt, plan, precision)
+        dtype = tr.dtype
+        p0 = phi0.to(dtype)
+        with torch.no_grad():
+            target = tr(p0, *[t.to(dtype) for t in A.velocity(a_tgt, modes)])
+        # warm-up (workspaces, lazy module loading)
+        a = a0.clone().requires_grad_(True)
+        A.heaviside_mismatch(tr(p0, *[t.to(dtype) for t in A.velocity(a, modes)]), target, eps, dvol).backward()
+        torch.cuda.synchronize()
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        a = a0.clone().requires_grad_(True)
+        e0.record()
+        L = A.heaviside_mismatch(tr(p0, *[t.to(dtype) for t in A.velocity(a, modes)]), target, eps, dvol)
+        e1.record()
+        L.backward()
+        e2.record()
+        torch.cuda.synchronize()
+        return float(L.detach()), a.grad.detach().cpu().numpy(), e0.elapsed_time(e1), e0.elapsed_time(e2), tr, target
+
+    L32, g32, fwd_ms, tot_ms, _, _ = grad("f32")
+    gpt = n ** 3 * (plan.steps + plan.steps // plan.reinit_every * plan.reinit_iters)
+    out.update({"loss": L32, "grad": g32.tolist(), "forward_ms": fwd_ms, "forward_backward_ms": tot_ms,
+                "backward_ms": tot_ms - fwd_ms, "forward_gpt_s": gpt / (fwd_ms / 1e3) / 1e9,
+                "backward_over_forward": (tot_ms - fwd_ms) / fwd_ms})
+    L64, g64, fwd64, tot64, tr64, tgt64 = grad("f64")
+    out["fp64"] = {"loss": L64, "grad": g64.tolist(), "forward_ms": fwd64, "forward_backward_ms": tot64,
+                   "fp32_grad_rel_err": float(np.abs(g32 - g64).max() / np.abs(g64).max())}
+    if fd_check:
+        def loss(a):
+            with torch.no_grad():
+                return float(A.heaviside_mismatch(tr64(phi0, *A.velocity(a, modes)), tgt64, eps, dvol))
+        def central(hh):
+            fd = []
+            for m_ in range(8):
+                e = torch.zeros(8, dtype=torch.float64, device="cuda")
+                e[m_] = hh
+                fd.append((loss(a0 + e) - loss(a0 - e)) / (2 * hh))
+            return np.array(fd)
+
+        fd = central(1e-4)
+        fd6 = central(1e-6)  # a smaller step: FD truncation and switch crossings shrink
+        out["fd_check"] = {"h": 1e-4, "fd_grad": fd.tolist(),
+                           "fp64_adjoint_rel_err": float(np.abs(g64 - fd).max() / np.abs(fd).max()),
+                           "fp32_adjoint_rel_err": float(np.abs(g32 - fd).max() / np.abs(fd).max()),
+                           "h_small": 1e-6, "fd_grad_small": fd6.tolist(),
+                           "fp64_adjoint_rel_err_small": float(np.abs(g64 - fd6).max() / np.abs(fd6).max())}
+    return out
+
+
 def workload_config(ngpus):
     return {"workload": f"vesicle step {N}^3 mixed precision (FP32 stencils, FP64 roots/reductions): "
                         f"{EXT} WENO5-RK3 extension + {ADV} WENO5-RK3 advection + {RE} WENO5-RK3 reinit "
@@ -252,7 +352,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
-    ap.add_argument("--profile", choices=["extend", "reinit", "advect", "step"],
+    ap.add_argument("--no-differentiation", action="store_true")
+    ap.add_argument("--fd-check", action="store_true",
+                    help="also check the 128^3 amplitude gradient against FP64 central differences")
+    ap.add_argument("--profile", choices=["extend", "reinit", "advect", "step", "adjoint"],
                     help="run only a few launches of one operator at 256^3 (the ncu capture case)")
     args = ap.parse_args()
 
@@ -275,6 +378,8 @@ def main():
     pkg = importlib.import_module(PKG)
     pkg.build()
     S = importlib.import_module(PKG + ".shapes")
+    if args.profile == "adjoint":
+        return adjoint_profile_case(torch, pkg, S)
     x, y, z, F0 = S.vesicle_256(N, seed=rank, device="cuda")
     h = 3.0 / (N - 1)
     grid = pkg.GD3(x, y, z, spacing=(h, h, h))
@@ -378,6 +483,11 @@ def main():
         torch.cuda.empty_cache()
         batched = batched_measure(torch, pkg, S, steps=5)
 
+    differentiation = None
+    if not args.no_differentiation and rank == 0:
+        torch.cuda.empty_cache()
+        differentiation = differentiation_measure(torch, pkg, S, fd_check=args.fd_check)
+
     if rank != 0:
         if dist is not None:
             dist.barrier()
@@ -404,6 +514,7 @@ def main():
         "clocks": clk.summary(),
         "fp64_plain": fp64,
         "batched": batched,
+        "differentiation": differentiation,
         "last_info": {"area": info_h[0], "volume": info_h[1], "dt": info_h[2], "max_speed": info_h[3]},
         "cpu_baseline": cpu,
     }
