@@ -7,8 +7,10 @@
 // with J the Jacobian of `step`.  Row c of J touches the 7 values of each axis line
 // through c (clamped at the grid edge), so J^T is applied in two deterministic passes:
 //   1. per node c, the local partials d step_c / d p_ax[o] (o = 0..6 along axis ax) are
-//      evaluated by running the forward per-node code on dual numbers, scaled by
-//      b * lam_c and stored in 21 slots W[ax*7 + o][c] (slot-major, coalesced);
+//      evaluated -- by the closed-form gradient of the uniform WENO5 (weno5_grad), and by
+//      running the forward per-node code on dual numbers where the interface is inserted
+//      -- scaled by b * lam_c and stored in 21 slots W[ax*7 + o][c] (slot-major,
+//      coalesced);
 //   2. per node j, every (c, ax, o) whose clamped stencil position is j is summed in a
 //      fixed order (no atomics), giving (J^T b lam)_j.
 // Partials with respect to the other inputs of a stage (the velocity of advection, the
@@ -53,21 +55,85 @@ __device__ __forceinline__ void adj_node_of(const Grid &g, long long c, int &i, 
     i = (int)(r - (long long)j * g.rows);
 }
 
-// Forward/backward derivative pair of one axis line and its partials with respect to
-// the seven line values (tangents 0..6) and the two interface distances r1, l1 (7, 8):
-// the uniform WENO5 pair, or the nonuniform one with the interface inserted.
+// Jiang-Shu WENO5 of five differences (the weno5_plain formula) and its gradient g[5]:
+// with alpha_k = d_k / (s_k + eps)^2 and w_k = alpha_k / sum alpha,
+//   dD/dv = sum_k w_k dq_k/dv + sum_k c_k ds_k/dv,   c_k = -2 w_k (q_k - D) / (s_k + eps),
+// where the candidates q_k are linear and the smoothness indicators s_k quadratic in v.
 template <typename T>
-__device__ __forceinline__ void axis_pair_jac(const T p[7], T h, bool iface, T r1, T l1, Dual<T, 9> &f,
-                                              Dual<T, 9> &b)
+__device__ __forceinline__ T weno5_grad(T v1, T v2, T v3, T v4, T v5, T g[5])
+{
+    const T q1 = T(1. / 3.) * v1 - T(7. / 6.) * v2 + T(11. / 6.) * v3;
+    const T q2 = T(-1. / 6.) * v2 + T(5. / 6.) * v3 + T(1. / 3.) * v4;
+    const T q3 = T(1. / 3.) * v3 + T(5. / 6.) * v4 - T(1. / 6.) * v5;
+    const T a1 = v1 - 2 * v2 + v3, b1 = v1 - 4 * v2 + 3 * v3;
+    const T a2 = v2 - 2 * v3 + v4, b2 = v2 - v4;
+    const T a3 = v3 - 2 * v4 + v5, b3 = 3 * v3 - 4 * v4 + v5;
+    const T eps = T(1e-6);
+    const T e1 = T(13. / 12.) * a1 * a1 + T(1. / 4.) * b1 * b1 + eps;
+    const T e2 = T(13. / 12.) * a2 * a2 + T(1. / 4.) * b2 * b2 + eps;
+    const T e3 = T(13. / 12.) * a3 * a3 + T(1. / 4.) * b3 * b3 + eps;
+    const T al1 = T(0.1) / (e1 * e1), al2 = T(0.6) / (e2 * e2), al3 = T(0.3) / (e3 * e3);
+    const T inv = T(1) / (al1 + al2 + al3);
+    const T w1 = al1 * inv, w2 = al2 * inv, w3 = al3 * inv;
+    const T D = w1 * q1 + w2 * q2 + w3 * q3;
+    const T c1 = T(-2) * w1 * (q1 - D) / e1;
+    const T c2 = T(-2) * w2 * (q2 - D) / e2;
+    const T c3 = T(-2) * w3 * (q3 - D) / e3;
+    // ds_k/dv: s1 = 13/12 a1^2 + 1/4 b1^2 with a1 = (1,-2,1,0,0).v, b1 = (1,-4,3,0,0).v, etc.
+    const T A1 = T(13. / 6.) * a1 * c1, B1 = T(0.5) * b1 * c1;
+    const T A2 = T(13. / 6.) * a2 * c2, B2 = T(0.5) * b2 * c2;
+    const T A3 = T(13. / 6.) * a3 * c3, B3 = T(0.5) * b3 * c3;
+    g[0] = T(1. / 3.) * w1 + A1 + B1;
+    g[1] = T(-7. / 6.) * w1 - T(1. / 6.) * w2 - 2 * A1 - 4 * B1 + A2 + B2;
+    g[2] = T(11. / 6.) * w1 + T(5. / 6.) * w2 + T(1. / 3.) * w3 + A1 + 3 * B1 - 2 * A2 + A3 + 3 * B3;
+    g[3] = T(1. / 3.) * w2 + T(5. / 6.) * w3 + A2 - B2 - 2 * A3 - 4 * B3;
+    g[4] = T(-1. / 6.) * w3 + A3 + B3;
+    return D;
+}
+
+// Uniform WENO5 pair of one axis line (weno5_pair_plain) with its partials with respect
+// to the seven line values: jf[o] = d D+ / d p[o], jb[o] = d D- / d p[o].
+template <typename T>
+__device__ __forceinline__ void weno5_pair_grad(const T p[7], T h, T &df, T &db, T jf[7], T jb[7])
+{
+    T v[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) v[m] = (p[m + 1] - p[m]) / h;
+    T gb[5], gf[5];
+    db = weno5_grad(v[0], v[1], v[2], v[3], v[4], gb);
+    df = weno5_grad(v[5], v[4], v[3], v[2], v[1], gf);
+    // G*[m] = d D / d v[m], m = 0..5
+    const T Gb[6] = {gb[0], gb[1], gb[2], gb[3], gb[4], T(0)};
+    const T Gf[6] = {T(0), gf[4], gf[3], gf[2], gf[1], gf[0]};
+    const T ih = T(1) / h;
+#pragma unroll
+    for (int o = 0; o < 7; ++o) {
+        const T lb = o >= 1 ? Gb[o - 1] : T(0), rb = o <= 5 ? Gb[o] : T(0);
+        const T lf = o >= 1 ? Gf[o - 1] : T(0), rf = o <= 5 ? Gf[o] : T(0);
+        jb[o] = (lb - rb) * ih;
+        jf[o] = (lf - rf) * ih;
+    }
+}
+
+// Interface-aware pair (nonuniform WENO5 with the interface inserted at r1 / l1, value 0)
+// and its partials with respect to the seven line values (0..6) and r1, l1 (7, 8), by
+// dual numbers; out of line, since only the few band nodes take it.
+template <typename T>
+__device__ __noinline__ void iface_pair_jac(const T p[7], T h, T r1, T l1, T &df, T &db, T jf[9], T jb[9])
 {
     using D = Dual<T, 9>;
     D P[7];
 #pragma unroll
     for (int o = 0; o < 7; ++o) P[o] = D::var(p[o], o);
-    if (iface)
-        interface_pair<D>(P, D::var(r1, 7), D::var(l1, 8), D((double)h), D(0.0), D(0.0), false, f, b);
-    else
-        weno5_pair_plain<D>(P, D((double)h), f, b);
+    D f, b;
+    interface_pair<D>(P, D::var(r1, 7), D::var(l1, 8), D((double)h), D(0.0), D(0.0), false, f, b);
+    df = f.v;
+    db = b.v;
+#pragma unroll
+    for (int o = 0; o < 9; ++o) {
+        jf[o] = f.d[o];
+        jb[o] = b.d[o];
+    }
 }
 
 // ---------------------------------------------------------------------------------------
@@ -85,89 +151,163 @@ __global__ void __launch_bounds__(BX *BY) k_adj_advect_jac(const T *__restrict__
     const T lc = coef * __ldg(lam + c) * (T)__ldg(dt);
 #pragma unroll 1
     for (int ax = 0; ax < 3; ++ax) {
-        using D = Dual<T, 7>;
-        T p[7];
+        T p[7], jf[7], jb[7], df, db;
         load_line7(ps, axis_line(g, i, j, k, ax), p);
-        D P[7];
-#pragma unroll
-        for (int o = 0; o < 7; ++o) P[o] = D::var(p[o], o);
-        D f, b;
-        weno5_pair_plain<D>(P, D(axis_h(g, ax)), f, b);
+        weno5_pair_grad<T>(p, (T)axis_h(g, ax), df, db, jf, jb);
         const T va = __ldg(v.p[ax] + c);
         const T vm = vmin(T(0), va), vp = vmax(T(0), va);
 #pragma unroll
-        for (int o = 0; o < 7; ++o) W[(long long)(ax * 7 + o) * g.num + c] = lc * (vm * f.d[o] + vp * b.d[o]);
+        for (int o = 0; o < 7; ++o) W[(long long)(ax * 7 + o) * g.num + c] = lc * (vm * jf[o] + vp * jb[o]);
         // d step / d v: D- where v > 0, D+ otherwise (the branches of max/min above)
-        gv.p[ax][c] -= lc * (va > T(0) ? b.v : f.v);
+        gv.p[ax][c] -= lc * (va > T(0) ? db : df);
     }
 }
 
 // ---------------------------------------------------------------------------------------
 // reinitialization stage: step = (|grad|_Godunov - 1) * 0.3 min(dist) * (mask ? -1 : 1)
 // ---------------------------------------------------------------------------------------
+// One node of the reinitialization-stage Jacobian.  GENERIC = false handles only nodes
+// whose three axis lines are all uniform (no sign change next to the node); GENERIC =
+// true also differentiates the interface-aware pairs (dual numbers) and is run over the
+// compact list of the remaining nodes, so the register cost of the dual code does not
+// limit the occupancy of the dense pass.
+template <typename T, bool GENERIC>
+__device__ __forceinline__ void reinit_jac_node(const T *__restrict__ ps, const uint8_t fl, Ptr6<const T> d,
+                                                const T lc, T *__restrict__ W, Ptr6<T> mu, const Grid &g, int i,
+                                                int j, int k, long long c)
+{
+    const T h[3] = {(T)g.dx, (T)g.dy, (T)g.dz};
+    // the six distances (stored where flagged, the spacing elsewhere); the pseudo-time
+    // step is 0.3 * their minimum, taken in the order of the forward kernel's vmin tree
+    T dist[6];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) dist[q] = (fl & (1u << q)) ? __ldg(d.p[q] + c) : h[q / 2];
+    const int i01 = dist[0] < dist[1] ? 0 : 1, i23 = dist[2] < dist[3] ? 2 : 3, i45 = dist[4] < dist[5] ? 4 : 5;
+    const int i25 = dist[i23] < dist[i45] ? i23 : i45;
+    const int qmin = dist[i01] < dist[i25] ? i01 : i25;
+    const T dtv = T(0.3) * dist[qmin];
+    const bool neg = fl & CLS_MASK;
+    const T sgn = neg ? T(-1) : T(1);
+
+    // pass 1: the derivative pairs and the partials of the Godunov norm
+    //   G = sqrt(sum_ax max(A_ax, B_ax)) with the branch of each max as the forward took it
+    bool iface[3];
+    T gq[6], S = T(0);
+    const T z = T(0);
+#pragma unroll 1
+    for (int ax = 0; ax < 3; ++ax) {
+        T p[7], df, db;
+        load_line7(ps, axis_line(g, i, j, k, ax), p);
+        iface[ax] = GENERIC && (p[2] * p[3] < T(0) || p[3] * p[4] < T(0));
+        if (GENERIC && iface[ax])
+            interface_pair<T>(p, dist[2 * ax], dist[2 * ax + 1], h[ax], T(0), T(0), false, df, db);
+        else
+            weno5_pair_plain<T>(p, h[ax], df, db);
+        const T A = neg ? sqr(vmin(z, db)) : sqr(vmax(z, db));
+        const T B = neg ? sqr(vmax(z, df)) : sqr(vmin(z, df));
+        if (A < B) {  // vmax(A, B) took B (the forward derivative)
+            S += B;
+            gq[2 * ax] = T(2) * (neg ? vmax(z, df) : vmin(z, df));
+            gq[2 * ax + 1] = T(0);
+        } else {
+            S += A;
+            gq[2 * ax] = T(0);
+            gq[2 * ax + 1] = T(2) * (neg ? vmin(z, db) : vmax(z, db));
+        }
+    }
+    const T G = sqrt(S);
+    const T dG = G > T(0) ? T(0.5) / G : T(0);  // zero derivative of sqrt at 0
+    const T s_dt = dtv * sgn;
+
+    // pass 2: per axis, partials of the pair, scaled into the slots and distance adjoints
+    T md[6];
+#pragma unroll 1
+    for (int ax = 0; ax < 3; ++ax) {
+        T p[7], jf[9], jb[9], df, db;
+        load_line7(ps, axis_line(g, i, j, k, ax), p);
+        if constexpr (GENERIC) {
+            if (iface[ax]) {
+                iface_pair_jac<T>(p, h[ax], dist[2 * ax], dist[2 * ax + 1], df, db, jf, jb);
+            } else {
+                weno5_pair_grad<T>(p, h[ax], df, db, jf, jb);
+                jf[7] = jf[8] = jb[7] = jb[8] = T(0);
+            }
+        } else {
+            weno5_pair_grad<T>(p, h[ax], df, db, jf, jb);
+            jf[7] = jf[8] = jb[7] = jb[8] = T(0);
+        }
+        const T gf = gq[2 * ax] * dG * s_dt, gb = gq[2 * ax + 1] * dG * s_dt;
+#pragma unroll
+        for (int o = 0; o < 7; ++o) W[(long long)(ax * 7 + o) * g.num + c] = lc * (gf * jf[o] + gb * jb[o]);
+        md[2 * ax] = gf * jf[7] + gb * jb[7];
+        md[2 * ax + 1] = gf * jf[8] + gb * jb[8];
+    }
+    // d step / d dist_q: through the interface insertion, and through dt for the minimum
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        if (!(fl & (1u << q))) continue;
+        const T ds = md[q] + (q == qmin ? (G - T(1)) * sgn * T(0.3) : T(0));
+        mu.p[q][c] -= lc * ds;
+    }
+}
+
+// warp-aggregated append of `value` where `pred` holds (all 32 lanes of the warp call it)
+__device__ __forceinline__ void adj_append(bool pred, unsigned value, unsigned *list, unsigned *count)
+{
+    const unsigned m = __ballot_sync(0xffffffffu, pred);
+    if (!m) return;
+    const unsigned lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31u;
+    const int leader = __ffs(m) - 1;
+    unsigned base = 0;
+    if ((int)lane == leader) base = atomicAdd(count, (unsigned)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (pred) list[base + __popc(m & ((1u << lane) - 1u))] = value;
+}
+
+// dense pass: fixed nodes get zero slots; nodes with a sign change next to them on any
+// axis are listed for k_adj_reinit_jac_band; the rest are done here
 template <typename T>
 __global__ void __launch_bounds__(BX *BY) k_adj_reinit_jac(const T *__restrict__ ps, const uint8_t *__restrict__ flags,
                                                              Ptr6<const T> d, const T *__restrict__ lam, T coef,
-                                                             T *__restrict__ W, Ptr6<T> mu, Grid g)
+                                                             T *__restrict__ W, Ptr6<T> mu, NodeList band, Grid g)
 {
-    int i, j, k;
-    long long c;
-    if (!adj_node(g, i, j, k, c)) return;
-    const uint8_t fl = __ldg(flags + c);
+    const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y, k = blockIdx.z;
+    const bool in = i < g.rows && j < g.cols;
+    const long long c = in ? node_index(g, i, j, k) : 0;
+    const uint8_t fl = in ? __ldg(flags + c) : uint8_t(0);
+    bool near = false;
+    if (in && !(fl & CLS_FIXED)) {
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            const AxisLine L = axis_line(g, i, j, k, ax);
+            const T pm = __ldg(ps + L.base + (long long)clampi(L.c - 1, L.n) * L.stride);
+            const T p0 = __ldg(ps + c);
+            const T pp = __ldg(ps + L.base + (long long)clampi(L.c + 1, L.n) * L.stride);
+            near |= pm * p0 < T(0) || p0 * pp < T(0);
+        }
+    }
+    adj_append(near, (unsigned)c, band.idx, band.count);
+    if (!in || near) return;
     if (fl & CLS_FIXED) {
 #pragma unroll
         for (int s = 0; s < SLOTS; ++s) W[(long long)s * g.num + c] = T(0);
         return;
     }
-    const T lc = coef * __ldg(lam + c);
-    const T h[3] = {(T)g.dx, (T)g.dy, (T)g.dz};
-    // the six distances (stored where flagged, the spacing elsewhere) and the pseudo-time
-    // step 0.3 * min, with tangents over the flagged ones
-    using D6 = Dual<T, 6>;
-    T dist[6];
-    D6 dv[6];
-#pragma unroll
-    for (int q = 0; q < 6; ++q) {
-        const bool f = fl & (1u << q);
-        dist[q] = f ? __ldg(d.p[q] + c) : h[q / 2];
-        dv[q] = f ? D6::var(dist[q], q) : D6((double)dist[q]);
-    }
-    const D6 dtd = T(0.3) * vmin(vmin(dv[0], dv[1]), vmin(vmin(dv[2], dv[3]), vmin(dv[4], dv[5])));
-    const bool neg = fl & CLS_MASK;
-    const T sgn = neg ? T(-1) : T(1);
+    reinit_jac_node<T, false>(ps, fl, d, coef * __ldg(lam + c), W, mu, g, i, j, k, c);
+}
 
-    T jf[3][9], jb[3][9];
-    D6 x[6];
-#pragma unroll 1
-    for (int ax = 0; ax < 3; ++ax) {
-        T p[7];
-        load_line7(ps, axis_line(g, i, j, k, ax), p);
-        const bool iface = p[2] * p[3] < T(0) || p[3] * p[4] < T(0);
-        Dual<T, 9> f, b;
-        axis_pair_jac<T>(p, h[ax], iface, dist[2 * ax], dist[2 * ax + 1], f, b);
-#pragma unroll
-        for (int o = 0; o < 9; ++o) {
-            jf[ax][o] = f.d[o];
-            jb[ax][o] = b.d[o];
-        }
-        x[2 * ax] = D6::var(f.v, 2 * ax);
-        x[2 * ax + 1] = D6::var(b.v, 2 * ax + 1);
-    }
-    const D6 G = godunov_norm<D6>(neg, x[0], x[1], x[2], x[3], x[4], x[5]);
-    const T s_dt = dtd.v * sgn;
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax) {
-        const T gf = G.d[2 * ax] * s_dt, gb = G.d[2 * ax + 1] * s_dt;
-#pragma unroll
-        for (int o = 0; o < 7; ++o) W[(long long)(ax * 7 + o) * g.num + c] = lc * (gf * jf[ax][o] + gb * jb[ax][o]);
-    }
-#pragma unroll
-    for (int q = 0; q < 6; ++q) {
-        if (!(fl & (1u << q))) continue;
-        const int ax = q / 2, slot = 7 + (q & 1);
-        const T ds = G.d[2 * ax] * s_dt * jf[ax][slot] + G.d[2 * ax + 1] * s_dt * jb[ax][slot] +
-                     (G.v - T(1)) * sgn * dtd.d[q];
-        mu.p[q][c] -= lc * ds;
+template <typename T>
+__global__ void __launch_bounds__(128) k_adj_reinit_jac_band(const T *__restrict__ ps,
+                                                               const uint8_t *__restrict__ flags, Ptr6<const T> d,
+                                                               const T *__restrict__ lam, T coef, T *__restrict__ W,
+                                                               Ptr6<T> mu, NodeList band, Grid g)
+{
+    const unsigned n = *band.count;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const long long c = band.idx[t];
+        int i, j, k;
+        adj_node_of(g, c, i, j, k);
+        reinit_jac_node<T, true>(ps, __ldg(flags + c), d, coef * __ldg(lam + c), W, mu, g, i, j, k, c);
     }
 }
 
@@ -320,9 +460,12 @@ cudaError_t launch_adj_advect_jac(const T *ps, Ptr3<const T> v, const double *dt
 
 template <typename T>
 cudaError_t launch_adj_reinit_jac(const T *ps, const uint8_t *flags, Ptr6<const T> d, const T *lam, double coef, T *W,
-                                  Ptr6<T> mu, const Grid &g, cudaStream_t s)
+                                  Ptr6<T> mu, NodeList band, const Grid &g, cudaStream_t s)
 {
-    k_adj_reinit_jac<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(ps, flags, d, lam, (T)coef, W, mu, g);
+    cudaError_t err = cudaMemsetAsync(band.count, 0, sizeof(unsigned), s);
+    if (err != cudaSuccess) return err;
+    k_adj_reinit_jac<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(ps, flags, d, lam, (T)coef, W, mu, band, g);
+    k_adj_reinit_jac_band<T><<<adj_list_blocks(), 128, 0, s>>>(ps, flags, d, lam, (T)coef, W, mu, band, g);
     return cudaGetLastError();
 }
 
@@ -354,7 +497,7 @@ cudaError_t launch_adj_dist_edges(const T *f, EdgeLists e, Ptr6<const T> mu, T *
     template cudaError_t launch_adj_advect_jac<T>(const T *, Ptr3<const T>, const double *, const T *, double, T *, \
                                                   Ptr3<T>, const Grid &, cudaStream_t);                             \
     template cudaError_t launch_adj_reinit_jac<T>(const T *, const uint8_t *, Ptr6<const T>, const T *, double, T *, \
-                                                  Ptr6<T>, const Grid &, cudaStream_t);                             \
+                                                  Ptr6<T>, NodeList, const Grid &, cudaStream_t);                   \
     template cudaError_t launch_adj_gather<T>(const T *, const T *, double, const T *, T *, const Grid &,            \
                                               cudaStream_t);                                                        \
     template cudaError_t launch_adj_axpy<T>(T *, const T *, double, bool, const Grid &, cudaStream_t);              \

@@ -157,6 +157,7 @@ template <typename T> struct AdjWork {
     ReinitWork<T> re;
     T *W, *x, *acc;
     Ptr6<T> mu;
+    NodeList band;  // reinitialization: nodes next to a sign change
 };
 template <typename T> AdjWork<T> carve_adj(Bump &w, const Grid &g, bool reinit)
 {
@@ -166,6 +167,7 @@ template <typename T> AdjWork<T> carve_adj(Bump &w, const Grid &g, bool reinit)
     a.x = w.take<T>(g.num);
     a.acc = w.take<T>(g.num);
     for (int q = 0; q < 6; ++q) a.mu.p[q] = reinit ? w.take<T>(g.num) : nullptr;
+    a.band = reinit ? carve_list(w, g) : NodeList{nullptr, nullptr};
     return a;
 }
 
@@ -638,7 +640,7 @@ int op_reinit_adjoint(const T *F0, int iteration, T *lam, T *tape, int rows, int
     }
     for (int q = 0; q < 6; ++q) VSL_TRY(cudaMemsetAsync(w.mu.p[q], 0, field, s));
     auto jac = [&](const T *ps, const T *l, double coef) {
-        return launch_adj_reinit_jac<T>(ps, re.flags, d, l, coef, w.W, w.mu, g, s);
+        return launch_adj_reinit_jac<T>(ps, re.flags, d, l, coef, w.W, w.mu, w.band, g, s);
     };
     for (int k = iteration - 1; k >= 0; --k) {
         const T *phik = tape + (size_t)k * g.num;

@@ -120,9 +120,10 @@ int toolbox_partial_blocks(const Grid &g);
 template <typename T>
 cudaError_t launch_adj_advect_jac(const T *ps, Ptr3<const T> v, const double *dt, const T *lam, double coef, T *W,
                                   Ptr3<T> gv, const Grid &g, cudaStream_t s);
+// band: scratch list (g.num entries + a counter) of the nodes next to a sign change
 template <typename T>
 cudaError_t launch_adj_reinit_jac(const T *ps, const uint8_t *flags, Ptr6<const T> d, const T *lam, double coef, T *W,
-                                  Ptr6<T> mu, const Grid &g, cudaStream_t s);
+                                  Ptr6<T> mu, NodeList band, const Grid &g, cudaStream_t s);
 template <typename T>
 cudaError_t launch_adj_gather(const T *W, const T *lam, double alpha, const T *acc, T *out, const Grid &g,
                               cudaStream_t s);
