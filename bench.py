@@ -234,6 +234,69 @@ def batched_measure(torch, pkg, S, steps: int, seed: int = 0):
     return out
 
 
+def precision_measure(torch, pkg, S, n: int = N):
+    """Max and L2 (rms) error of every output field of the mixed-precision form against the
+    plain FP64 form, both on the GPU from the same n^3 vesicle: reinitialization (20
+    pseudo-steps), extension of the mean curvature (30), one advection step, one whole
+    vesicle step (field, area, volume, dt) and the surface redistance of
+    f = sin(3x) cos(2y) + 0.5 z^2 (10 RK3 steps, 5 extension steps per stage).  Field errors
+    are taken over the band |phi| < 3 dx, in units of dx for level-set fields and of the
+    band's max |value| for the extended and redistanced fields."""
+    x, y, z, F0 = S.vesicle_256(n, seed=0, device="cuda")
+    h = 3.0 / (n - 1)
+    grid = pkg.GD3(x, y, z, spacing=(h, h, h))
+    A0 = torch.sin(3 * x) * torch.cos(2 * y) + 0.5 * z * z
+    del y
+    m64 = pkg.SDF3(grid, Val=F0, precision="f64")
+    m32 = pkg.SDF3(grid, Val=F0, precision="f32")
+    del F0
+    grid.X = grid.Y = grid.Z = None
+    for m in (m64, m32):
+        m.setDistance()
+    band = m64.F.abs() < 3 * h
+
+    def err(a32, a64, scale):
+        d = (a32.double() - a64)[band]
+        return {"max": float(d.abs().max()) / scale, "l2": float(d.pow(2).mean().sqrt()) / scale}
+
+    out = {"band": "|phi| < 3 dx", "grid": [n, n, n]}
+    out["reinitialization_20"] = err(m32.WENO5RK3Reinitialization(m32.F, 20),
+                                     m64.WENO5RK3Reinitialization(m64.F, 20), h)
+    out["reinitialization_20"]["unit"] = "dx"
+    m64.GPUsetCalculusToolBox()
+    C = m64.MeanCurvature
+    cs = float(C[band].abs().max())
+    E64 = m64.WENO5RK3Extend(C, 30)
+    E32 = m32.WENO5RK3Extend(C.float(), 30)
+    out["extension_30"] = err(E32, E64, cs)
+    out["extension_30"]["unit"] = "max |H| in band"
+    vel = [E64 * m64.Nx, E64 * m64.Ny, E64 * m64.Nz]
+    for name in ("Nx", "Ny", "Nz", "Fx", "Fy", "Fz", "FGradMag", "Fxx", "Fyy", "Fzz", "Fxy", "Fyz", "Fzx", "FLaplacian",
+                 "GaussianCurvature", "Heaviside", "DiracDelta", "MeanCurvature", "HPrimal"):
+        setattr(m64, name, None)
+    del E32, E64, C
+    dt = 0.5 * h / float(max(v.abs().max() for v in vel))
+    out["advection_1"] = err(m32.WENO5RK3Advection(m32.F, *[v.float() for v in vel], dt, 1),
+                             m64.WENO5RK3Advection(m64.F, *vel, dt, 1), h)
+    out["advection_1"]["unit"] = "dx"
+    del vel
+    torch.cuda.empty_cache()
+    ref = A0.double()
+    as_ = float(ref[band].abs().max())
+    R64 = m64.WENO5RK3ClosetPointSurfaceRedistance(ref, 10, 5)
+    R32 = m32.WENO5RK3ClosetPointSurfaceRedistance(A0.float(), 10, 5)
+    out["surface_redistance_10x5"] = err(R32, R64, as_)
+    out["surface_redistance_10x5"]["unit"] = "max |f| in band"
+    del R64, R32, ref, A0
+    torch.cuda.empty_cache()
+    i64 = m64.vesicle_step(EXT, RE, CFL).cpu().tolist()
+    i32 = m32.vesicle_step(EXT, RE, CFL).cpu().tolist()
+    out["vesicle_step"] = err(m32.F, m64.F, h)
+    out["vesicle_step"].update({"unit": "dx", "area_rel": abs(i32[0] - i64[0]) / i64[0],
+                                "volume_rel": abs(i32[1] - i64[1]) / i64[1], "dt_rel": abs(i32[2] - i64[2]) / i64[2]})
+    return out
+
+
 def adjoint_profile_case(torch, pkg, S, n: int = 128):
     """One forward + backward pass of a shortened differentiation workload at n^3 FP32
     (4 advection steps, one 2-pseudo-step reinitialization; the ncu capture case)."""
@@ -353,6 +416,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-differentiation", action="store_true")
+    ap.add_argument("--no-precision", action="store_true")
     ap.add_argument("--fd-check", action="store_true",
                     help="also check the 128^3 amplitude gradient against FP64 central differences")
     ap.add_argument("--profile", choices=["extend", "reinit", "advect", "step", "adjoint"],
@@ -483,6 +547,11 @@ def main():
         torch.cuda.empty_cache()
         batched = batched_measure(torch, pkg, S, steps=5)
 
+    precision = None
+    if not args.no_precision and rank == 0:
+        torch.cuda.empty_cache()
+        precision = precision_measure(torch, pkg, S)
+
     differentiation = None
     if not args.no_differentiation and rank == 0:
         torch.cuda.empty_cache()
@@ -514,6 +583,7 @@ def main():
         "clocks": clk.summary(),
         "fp64_plain": fp64,
         "batched": batched,
+        "precision": precision,
         "differentiation": differentiation,
         "last_info": {"area": info_h[0], "volume": info_h[1], "dt": info_h[2], "max_speed": info_h[3]},
         "cpu_baseline": cpu,
