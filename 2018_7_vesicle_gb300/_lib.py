@@ -30,6 +30,9 @@ SIGNATURES = {
     "vsl_set_calculus_toolbox": "p" * 18 + "pp" + _G + "d" + "i" + "s",
     "vsl_advection_step": "ppppp" + _G + "s",
     "vsl_weno_derivative": "ppppppp" + _G + "s",
+    # tuning table of the tiled kernels (pages per block)
+    "vsl_set_tile_pages": "iiiii",
+    "vsl_tile_pages": "iiii",
     # no-allocation variant (static device scratch, no workspace argument)
     "vsl_area_volume_noalloc_f64": "pp" + _G + "s",
 }

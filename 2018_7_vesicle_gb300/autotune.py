@@ -1,0 +1,83 @@
+"""Autotuner of the FP32 tiled stage kernels.
+
+Each tiled kernel block marches `pages` pages of the grid (a launch parameter): fewer
+pages mean more blocks and more parallelism on small grids, more pages mean fewer halo
+reloads per node on large ones.  The library keeps a table of pages per (grid shape,
+stage kind) (vsl_set_tile_pages / vsl_tile_pages of the C ABI); `tune_shape` fills it for
+one level-set object by timing each kind's own operation (extension, reinitialization,
+advection) on that object's field for every candidate, with CUDA events, and keeping
+the fastest.  Tune before recording CUDA graphs: a graph keeps the launch shapes it was
+recorded with.
+"""
+from __future__ import annotations
+
+import torch
+
+from ._lib import lib
+from .sdf3 import SDF3, colmajor_full
+
+KINDS = {"reinit": 0, "extend": 1, "advect": 2}
+CANDIDATES = (4, 8, 16, 32, 64)
+
+
+def get_pages(size, kind: str) -> int:
+    return int(lib().raw("vsl_tile_pages", *size, KINDS[kind]))
+
+
+def set_pages(size, kind: str, pages: int) -> None:
+    """pages = 0 restores the default."""
+    lib().call("vsl_set_tile_pages", *size, KINDS[kind], int(pages))
+
+
+def _elapsed_ms(fn, reps: int) -> float:
+    fn()  # warm-up (workspace, first launch of the shape)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def _candidates(pges: int, candidates):
+    """Candidates that give distinct launch shapes (pages beyond pges all mean one block)."""
+    out, seen = [], set()
+    for c in sorted(candidates):
+        blocks = -(-pges // c)
+        if blocks not in seen:
+            seen.add(blocks)
+            out.append(c)
+    return out
+
+
+def tune_shape(sdf: SDF3, candidates=CANDIDATES, iters: int = 2, reps: int = 3) -> dict:
+    """Pick pages per block for each stage kind on sdf's grid shape; returns
+    {kind: {"pages": best, "ms": {candidate: time}}}.  sdf must be FP32 with its
+    distances set (setDistance)."""
+    if sdf.precision != "f32":
+        raise ValueError("the tiled kernels are the FP32 form's")
+    size = sdf.GD3.Size
+    v = colmajor_full(size, 0.5, torch.float32)
+    dt = 0.1 * min(sdf.GD3.Dx, sdf.GD3.Dy, sdf.GD3.Dz)
+    ops = {
+        "extend": lambda: sdf.WENO5RK3Extend(sdf.F, iters),
+        "reinit": lambda: sdf.WENO5RK3Reinitialization(sdf.F, iters),
+        "advect": lambda: sdf.WENO5RK3Advection(sdf.F, v, v, v, dt, iters),
+    }
+    report = {}
+    for kind, fn in ops.items():
+        times = {}
+        for c in _candidates(size[2], candidates):
+            set_pages(size, kind, c)
+            times[c] = _elapsed_ms(fn, reps)
+        best = min(times, key=times.get)
+        set_pages(size, kind, best)
+        report[kind] = {"pages": best, "ms": times}
+    return report
+
+
+def clear_shape(size) -> None:
+    for kind in KINDS:
+        set_pages(size, kind, 0)

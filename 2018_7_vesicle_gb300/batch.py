@@ -24,6 +24,7 @@ class VesicleBatch:
         self._graph = None
         self._key = None
         self.infos = [torch.zeros(4, dtype=torch.float64, device="cuda") for _ in self.maps]
+        self._tuning = {}
 
     def nodes(self) -> int:
         return sum(m.GD3.NumElt for m in self.maps)
@@ -34,6 +35,65 @@ class VesicleBatch:
         for m, info in zip(self.maps, self.infos):
             m.vesicle_step(ext_iters, reinit_iters, cfl, info=info)
         return self.infos
+
+    def autotune(self, candidates=None, steps: int = 2, ext_iters: int = 30, reinit_iters: int = 20,
+                 cfl: float = 0.5) -> dict:
+        """Pick pages per block of the tiled kernels for the batch's grid shapes by the
+        batch step's own time (graph replay).  Configurations compared: the per-shape
+        choices (each shape timed alone on one of its vesicles), every candidate applied
+        to all shapes, and the default.  Concurrent branches favour other choices than a
+        vesicle timed alone, which is why the whole step decides.  Returns the timings and
+        the configuration kept."""
+        from . import autotune as T
+
+        cand = T.CANDIDATES if candidates is None else candidates
+        shapes = {}
+        for m in self.maps:
+            shapes.setdefault(tuple(m.GD3.Size), m)
+        per_shape = {s: T.tune_shape(m, cand) for s, m in shapes.items()}
+        configs = {"tuned": {s: {k: r["pages"] for k, r in c.items()} for s, c in per_shape.items()},
+                   "default": {s: {k: 0 for k in T.KINDS} for s in shapes}}
+        for c in cand:
+            configs[f"uniform_{c}"] = {s: {k: c for k in T.KINDS} for s in shapes}
+
+        def apply(cfg):
+            for s, kinds in cfg.items():
+                for k, p in kinds.items():
+                    T.set_pages(s, k, p)
+
+        def batch_ms():
+            self._graph, self._key = None, None  # re-record with the current table
+            self.step(ext_iters, reinit_iters, cfl)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            for _ in range(steps):
+                self.step(ext_iters, reinit_iters, cfl)
+            b.record()
+            torch.cuda.synchronize()
+            return a.elapsed_time(b) / steps
+
+        times = {}
+        for name, cfg in configs.items():
+            apply(cfg)
+            times[name] = batch_ms()
+        best = min(times, key=times.get)
+        apply(configs[best])
+        self._graph, self._key = None, None
+        self._tuning = configs
+        return {"shapes": len(shapes), "ms": times, "kept": best.split("_")[0] if best.startswith("uniform") else best,
+                "config": best,
+                "pages": {"x".join(map(str, s)): v for s, v in configs[best].items()}}
+
+    def apply_tuning(self, name: str) -> None:
+        """Put one of the configurations `autotune` compared ("tuned": per-shape choices,
+        "default", "uniform_<pages>") back into the library's table."""
+        from . import autotune as T
+
+        for s, kinds in self._tuning[name].items():
+            for k, p in kinds.items():
+                T.set_pages(s, k, p)
+        self._graph, self._key = None, None
 
     def step(self, ext_iters: int = 30, reinit_iters: int = 20, cfl: float = 0.5):
         """One batch step by graph replay (recorded on first use or when arguments change)."""

@@ -677,6 +677,17 @@ const char *vsl_status_string(int status)
 
 int vsl_version(void) { return 1; }
 
+int vsl_set_tile_pages(int rows, int cols, int pges, int kind, int pages)
+{
+    return set_tile_pages(rows, cols, pges, kind, pages);
+}
+
+int vsl_tile_pages(int rows, int cols, int pges, int kind)
+{
+    if (rows <= 0 || cols <= 0 || pges <= 0 || kind < 0 || kind > 2) return 0;
+    return tile_pages(make_grid(rows, cols, pges, 1.0, 1.0, 1.0), kind);
+}
+
 size_t vsl_workspace_bytes(int op, int rows, int cols, int pges, int elem_bytes)
 {
     if (rows <= 0 || cols <= 0 || pges <= 0) return 0;

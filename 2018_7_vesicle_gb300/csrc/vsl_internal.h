@@ -97,6 +97,10 @@ struct TiledStage {
 };
 // kind: 0 reinitialization, 1 extension, 2 advection
 cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const Grid &g, cudaStream_t s);
+// pages per block of the tiled kernels for a grid shape and kind (the tuning table, or the
+// default); set_tile_pages(..., 0) restores the default
+int tile_pages(const Grid &g, int kind);
+int set_tile_pages(int rows, int cols, int pges, int kind, int pages);
 
 // ---- toolbox and reductions (vsl_toolbox.cu) ------------------------------------------
 // Fields of the calculus toolbox a caller may ask for (null pointers are skipped).

@@ -18,24 +18,26 @@
 // reference's trigger r1 < h || l1 < h; the band kernel applies the exact test).
 #pragma once
 
+#include <mutex>
+
 #include "vsl_fused.cuh"
 
 namespace vsl {
 namespace {
 
-// Pages per block and occupancy target (compile-time tuning constants).  Measured on
-// GB300 at 256^3 (vesicle step with graph replay): KZ 16/32/64 x 4/5 blocks per SM gave
-// 46.6/47.5/47.9 ms at 4 blocks (64 registers, no spills) and 49.5/51.4/53.0 ms at 5
-// blocks (48 registers with spills); 16 pages and 4 blocks is the default.
+// Pages per block (a launch parameter: the default below, or the value the tuning table
+// holds for the grid shape and stage kind) and the occupancy target (compile time).
+// Measured on GB300 at 256^3 (vesicle step with graph replay): 16/32/64 pages x 4/5
+// blocks per SM gave 46.6/47.5/47.9 ms at 4 blocks (64 registers, no spills) and
+// 49.5/51.4/53.0 ms at 5 blocks (48 registers with spills).
 #ifndef VSL_TILED_KZ
 #define VSL_TILED_KZ 16
 #endif
 #ifndef VSL_TILED_MIN_BLOCKS
 #define VSL_TILED_MIN_BLOCKS 4
 #endif
-constexpr int TY = 32;            // rows per tile (threadIdx.x)
-constexpr int TX = 8;             // columns per tile (threadIdx.y)
-constexpr int KZ = VSL_TILED_KZ;  // pages per block
+constexpr int TY = 32;  // rows per tile (threadIdx.x)
+constexpr int TX = 8;   // columns per tile (threadIdx.y)
 constexpr int HALO = 3;
 constexpr int SW = TY + 2 * HALO;  // smem row extent (fastest)
 constexpr int SH = TX + 2 * HALO;
@@ -59,6 +61,7 @@ struct TiledArgs {
     int stage;
     float h[3], inv_h[3], eps2[3];
     float dt_uniform;  // 0.3 * min spacing: the pseudo time step of a node with no crossing
+    int kz;            // pages per block
 };
 
 constexpr int PER_THREAD = (PLANE + TY * TX - 1) / (TY * TX);  // halo elements per thread
@@ -72,8 +75,8 @@ __global__ void __launch_bounds__(TY *TX, VSL_TILED_MIN_BLOCKS) k_stage_tiled(Ti
     const int tid = ty * TY + tx;
     const int i0 = blockIdx.x * TY, j0 = blockIdx.y * TX;
     const int i = i0 + tx, j = j0 + ty;
-    const int k0 = blockIdx.z * KZ;
-    const int k1 = min(k0 + KZ, g.pges);
+    const int k0 = blockIdx.z * a.kz;
+    const int k1 = min(k0 + a.kz, g.pges);
     const bool active = i < g.rows && j < g.cols;
     auto slot = [](int p) { return ((p % RING) + RING) % RING; };
 
@@ -266,7 +269,55 @@ inline TiledArgs tiled_args(const Grid &g)
 
 inline int band_blocks() { return list_blocks(); }
 
-inline dim3 tiled_grid(const Grid &g) { return dim3((g.rows + TY - 1) / TY, (g.cols + TX - 1) / TX, (g.pges + KZ - 1) / KZ); }
+inline dim3 tiled_grid(const Grid &g, int kz)
+{
+    return dim3((g.rows + TY - 1) / TY, (g.cols + TX - 1) / TX, (g.pges + kz - 1) / kz);
+}
+
+// ---------------------------------------------------------------------------------------
+// tuning table: pages per block by grid shape and stage kind (set by an autotuner)
+// ---------------------------------------------------------------------------------------
+namespace {
+struct TileEntry {
+    int rows, cols, pges, kind, pages;
+};
+constexpr int TILE_TABLE = 512;
+std::mutex tile_mutex;
+TileEntry tile_table[TILE_TABLE];
+int tile_count = 0;
+}  // namespace
+
+int tile_pages(const Grid &g, int kind)
+{
+    std::lock_guard<std::mutex> lock(tile_mutex);
+    for (int e = 0; e < tile_count; ++e) {
+        const TileEntry &t = tile_table[e];
+        if (t.rows == g.rows && t.cols == g.cols && t.pges == g.pges && t.kind == kind) return t.pages;
+    }
+    return VSL_TILED_KZ;
+}
+
+int set_tile_pages(int rows, int cols, int pges, int kind, int pages)
+{
+    if (rows <= 0 || cols <= 0 || pges <= 0) return VSL_ERR_SHAPE;
+    if (kind < 0 || kind > 2 || pages < 0 || pages > 65535) return VSL_ERR_VALUE;
+    std::lock_guard<std::mutex> lock(tile_mutex);
+    for (int e = 0; e < tile_count; ++e) {
+        TileEntry &t = tile_table[e];
+        if (t.rows == rows && t.cols == cols && t.pges == pges && t.kind == kind) {
+            if (pages == 0) {  // back to the default: drop the entry
+                t = tile_table[--tile_count];
+            } else {
+                t.pages = pages;
+            }
+            return VSL_OK;
+        }
+    }
+    if (pages == 0) return VSL_OK;
+    if (tile_count == TILE_TABLE) return VSL_ERR_VALUE;
+    tile_table[tile_count++] = TileEntry{rows, cols, pges, kind, pages};
+    return VSL_OK;
+}
 
 cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const Grid &g, cudaStream_t s)
 {
@@ -289,7 +340,8 @@ cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const 
         next = st.band.counter + ((st.seq + 1) & 1);
     }
     a.stage = st.stage;
-    dim3 gr = tiled_grid(g), bl(TY, TX);
+    a.kz = tile_pages(g, kind);
+    dim3 gr = tiled_grid(g, a.kz), bl(TY, TX);
     if (kind == SK_REINIT)
         k_stage_tiled<SK_REINIT><<<gr, bl, 0, s>>>(a);
     else if (kind == SK_EXTEND)

@@ -198,11 +198,12 @@ def profile_case(which, m, torch):
     print(json.dumps({"profile_case": which, "ok": True}))
 
 
-def batched_measure(torch, pkg, S, steps: int, seed: int = 0):
+def batched_measure(torch, pkg, S, steps: int, seed: int = 0, tune: bool = True):
     """The batched workload: 64 vesicles with node counts per axis drawn from
     {48, 64, 96, 128, 160} and half axes U[0.4, 1.0], FP32, advanced `steps` vesicle steps
     as one CUDA graph per batch step (parallel branches) and, for comparison, by the
-    per-vesicle launch loop."""
+    per-vesicle launch loop; with `tune`, pages per block of the tiled kernels are first
+    autotuned per grid shape (kept only if the batch step is faster with them)."""
     B = importlib.import_module(PKG + ".batch")
     maps = []
     for xv, yv, zv, axes in S.random_vesicles(64, seed=seed):
@@ -217,7 +218,14 @@ def batched_measure(torch, pkg, S, steps: int, seed: int = 0):
     batch = B.VesicleBatch(maps, streams=16)
     nodes = batch.nodes()
     out = {"vesicles": len(maps), "nodes": nodes, "steps": steps}
+    if tune:
+        out["autotune"] = batch.autotune()
     for name, fn in (("graph", batch.step), ("loop", batch.step_loop)):
+        if tune and name == "loop":
+            # the launch loop runs one vesicle at a time: the per-shape choices (each shape
+            # timed alone) are its tuning
+            batch.apply_tuning("tuned")
+            out["loop_pages"] = "per-shape choices (each shape timed alone)"
         fn(EXT, RE, CFL)  # warm-up (records the graph)
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -229,6 +237,9 @@ def batched_measure(torch, pkg, S, steps: int, seed: int = 0):
         ms = a.elapsed_time(b) / steps
         out[name] = {"ms_per_step": ms, "value": GPT_PER_NODE * nodes / (ms / 1e3) / 1e9, "unit": UNIT}
     out["speedup_graph_over_loop"] = out["loop"]["ms_per_step"] / out["graph"]["ms_per_step"]
+    # the flow is explicit: vesicles whose time step fell below the parabolic limit can
+    # blow up (FP32 overflow gives NaN); count the ones still finite
+    out["finite_vesicles"] = sum(int(bool(torch.all(torch.isfinite(m.F)))) for m in maps)
     del batch, maps
     torch.cuda.empty_cache()
     return out
@@ -417,6 +428,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-differentiation", action="store_true")
     ap.add_argument("--no-precision", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--fd-check", action="store_true",
                     help="also check the 128^3 amplitude gradient against FP64 central differences")
     ap.add_argument("--profile", choices=["extend", "reinit", "advect", "step", "adjoint"],
@@ -462,6 +474,10 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
+    # pages per block of the tiled kernels for this grid, tuned before the graph is recorded
+    tuning = None
+    if not args.no_autotune:
+        tuning = importlib.import_module(PKG + ".autotune").tune_shape(m, candidates=(8, 16, 32, 64))
     # each step replays one CUDA graph holding the step's whole launch sequence
     for _ in range(args.warmup):
         m.vesicle_step(EXT, RE, CFL, graph=True)
@@ -545,7 +561,7 @@ def main():
     if not args.no_batched and rank == 0:
         del m
         torch.cuda.empty_cache()
-        batched = batched_measure(torch, pkg, S, steps=5)
+        batched = batched_measure(torch, pkg, S, steps=20, tune=not args.no_autotune)
 
     precision = None
     if not args.no_precision and rank == 0:
@@ -581,6 +597,7 @@ def main():
                 "d2h_bytes_per_step": 4 * N**3 + 32, "ms_per_step": e2e_s * 1e3},
         "gpu_launches": LAUNCHES_PER_STEP * args.steps,
         "clocks": clk.summary(),
+        "autotune": tuning,
         "fp64_plain": fp64,
         "batched": batched,
         "precision": precision,

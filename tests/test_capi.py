@@ -105,3 +105,21 @@ def test_workspace_sizes(vsl):
     assert vsl.lib.vsl_workspace_bytes(99, 8, 8, 8, 8) == 0
     assert vsl.lib.vsl_workspace_bytes(1, 8, 8, 8, 2) == 0
     assert vsl.lib.vsl_workspace_bytes(1, 0, 8, 8, 8) == 0
+
+
+def test_tile_pages_table(vsl):
+    """The pages-per-block table of the tiled kernels: default 16, set / replace / remove,
+    argument checks (host only, no launch)."""
+    call = vsl.raw
+    assert call("vsl_tile_pages", 40, 36, 52, 1) == 16
+    assert call("vsl_set_tile_pages", 40, 36, 52, 1, 8) == 0
+    assert call("vsl_tile_pages", 40, 36, 52, 1) == 8
+    assert call("vsl_tile_pages", 40, 36, 52, 0) == 16  # other kind untouched
+    assert call("vsl_set_tile_pages", 40, 36, 52, 1, 4) == 0
+    assert call("vsl_tile_pages", 40, 36, 52, 1) == 4
+    assert call("vsl_set_tile_pages", 40, 36, 52, 1, 0) == 0  # back to the default
+    assert call("vsl_tile_pages", 40, 36, 52, 1) == 16
+    assert call("vsl_set_tile_pages", 0, 36, 52, 1, 8) == 2
+    assert call("vsl_set_tile_pages", 40, 36, 52, 3, 8) == 3
+    assert call("vsl_set_tile_pages", 40, 36, 52, 1, -1) == 3
+    assert call("vsl_tile_pages", 40, 36, 52, 7) == 0
