@@ -171,7 +171,9 @@ def run_reference(args, rank, world):
     v = statistics.median(per)
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": GPT_PER_NODE * N**3 / (v * 1e9) * 1e3,
+        "ms_per_step_basis": "one full 256^3 step at the sampled throughput (each step samples a slab)",
+        "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(args.gpus),
         "cpu_baseline": {**base, "value": v},
@@ -203,7 +205,8 @@ def batched_measure(torch, pkg, S, steps: int, seed: int = 0, tune: bool = True)
     {48, 64, 96, 128, 160} and half axes U[0.4, 1.0], FP32, advanced `steps` vesicle steps
     as one CUDA graph per batch step (parallel branches) and, for comparison, by the
     per-vesicle launch loop; with `tune`, pages per block of the tiled kernels are first
-    autotuned per grid shape (kept only if the batch step is faster with them)."""
+    autotuned (VesicleBatch.autotune: the configuration with the fastest graph step), and
+    the loop runs with the per-shape choices, its own best."""
     B = importlib.import_module(PKG + ".batch")
     maps = []
     for xv, yv, zv, axes in S.random_vesicles(64, seed=seed):
