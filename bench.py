@@ -311,6 +311,19 @@ def precision_measure(torch, pkg, S, n: int = N):
     return out
 
 
+def step128_profile_case(torch, pkg, S, n: int = 128):
+    """Two FP32 vesicle steps of the 128^3 vesicle (the capture case for per-kernel DRAM
+    bytes: ~200 MB of fields, larger than L2, small enough for a multi-metric capture)."""
+    x, y, z, F0 = S.vesicle_256(n, seed=0, device="cuda")
+    h = 3.0 / (n - 1)
+    m = pkg.SDF3(pkg.GD3(x, y, z, spacing=(h, h, h)), Val=F0, precision="f32")
+    m.setDistance()
+    for _ in range(2):
+        m.vesicle_step(EXT, RE, CFL)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "step128", "ok": True}))
+
+
 def adjoint_profile_case(torch, pkg, S, n: int = 128):
     """One forward + backward pass of a shortened differentiation workload at n^3 FP32
     (4 advection steps, one 2-pseudo-step reinitialization; the ncu capture case)."""
@@ -434,7 +447,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--fd-check", action="store_true",
                     help="also check the 128^3 amplitude gradient against FP64 central differences")
-    ap.add_argument("--profile", choices=["extend", "reinit", "advect", "step", "adjoint"],
+    ap.add_argument("--profile", choices=["extend", "reinit", "advect", "step", "step128", "adjoint"],
                     help="run only a few launches of one operator at 256^3 (the ncu capture case)")
     args = ap.parse_args()
 
@@ -459,6 +472,8 @@ def main():
     S = importlib.import_module(PKG + ".shapes")
     if args.profile == "adjoint":
         return adjoint_profile_case(torch, pkg, S)
+    if args.profile == "step128":
+        return step128_profile_case(torch, pkg, S)
     x, y, z, F0 = S.vesicle_256(N, seed=rank, device="cuda")
     h = 3.0 / (N - 1)
     grid = pkg.GD3(x, y, z, spacing=(h, h, h))

@@ -50,6 +50,11 @@ SIGNATURES = {
     "advection_step": "pppppiiiddd",
     "weno_derivative": "pppppppiiiddd",
     "set_calculus_toolbox": "ppppppppppppppppppppiiiddddi",
+    "enork2_boundary_correction": "pppppppiiiiddd",
+    "enork2_re_step": "ppppppppppiiidddi",
+    "enork2_upwind_normal": "ppppppppppiiidddi",
+    "enork2_boundary_interpolate": "pppppppppppppiiidddi",
+    "enork2_extend_step": "ppppppppppppppppppiiidddi",
 }
 _KIND = {"p": _P, "i": _I, "d": _D}
 
@@ -251,14 +256,52 @@ def reinit_eno3(K, g: Grid, F, iteration: int):
 
 
 # ---------------------------------------------------------------------------------------
+# ENORK2 reinitialization: V/+SD/@SDF3/ENORK2Reinitialization.m:3-45
+# ---------------------------------------------------------------------------------------
+
+
+def _rk2(F, stage):
+    """Heun RK2 as the ENORK2 MATLAB loops combine the stages: (F + Ftmp - step) / 2."""
+    step = stage(F)
+    Ftmp = F - step
+    step = stage(Ftmp)
+    return (F + Ftmp - step) / 2
+
+
+def set_distance_enork2(K: KernelSet, g: Grid, F) -> Distances:
+    """Quadratic-ENO distances (ENORK2_boundary_correction on spacing-filled arrays)."""
+    F = F64(F)
+    d = Distances(full(g, g.dx), full(g, g.dx), full(g, g.dy), full(g, g.dy), full(g, g.dz), full(g, g.dz))
+    K.enork2_boundary_correction(*d.six(), F, g.num_ele, *g.args())
+    return d
+
+
+def reinit_enork2(K, g: Grid, F, iteration: int):
+    """ENORK2Reinitialization(F, iteration): distances recomputed from F, Heun RK2."""
+    F = F64(F).copy(order="F")
+    mask = np.asfortranarray(F < 0)
+    dist = set_distance_enork2(K, g, F)
+    deltat = F64(0.3 * dist.min_dist)
+    step = zeros(g)
+
+    def stage(Fs):
+        K.enork2_re_step(step, F64(Fs), mask, deltat, *dist.six(), *g.args(), g.num_ele)
+        return step.copy(order="F")
+
+    for _ in range(iteration):
+        F = F64(_rk2(F, stage))
+    return F
+
+
+# ---------------------------------------------------------------------------------------
 # extension: V/+SD/@SDF3/WENO5RK3Extend.m:9-76 and V/+SD/@SDF3/WENORK3Extend.m:9-98
 # ---------------------------------------------------------------------------------------
 
 
-def extension_velocity(K, g: Grid, F, dist: Distances, eno3: bool = False, floor: float = 1e-6):
+def extension_velocity(K, g: Grid, F, dist: Distances, eno3: bool = False, floor: float = 1e-6, enork2: bool = False):
     """v = sign(F) * n, n = upwind gradient / max(|gradient|, floor)."""
     fx, fy, fz = zeros(g), zeros(g), zeros(g)
-    fn = K.upwind_normal_eno3 if eno3 else K.upwind_normal
+    fn = K.enork2_upwind_normal if enork2 else (K.upwind_normal_eno3 if eno3 else K.upwind_normal)
     fn(fx, fy, fz, F64(F), *dist.six(), *g.args(), g.num_ele)
     grad = np.maximum(np.sqrt(fx ** 2 + fy ** 2 + fz ** 2), floor)
     s = np.sign(F)
@@ -283,6 +326,26 @@ def extend_loop(K, g: Grid, C, iteration, dist: Distances, v, deltat, cp, eno3: 
     C = F64(C).copy(order="F")
     for _ in range(iteration):
         C = F64(_rk3(C, stage))
+    return C
+
+
+def extend_enork2(K, g: Grid, F, C, iteration: int):
+    """ENORK2Extend(C, iteration) (V/+SD/@SDF3/ENORK2Extend.m:9-81): quadratic-ENO
+    distances of F, ENO upwind normals, quadratic crossing values of C, Heun RK2."""
+    dist = set_distance_enork2(K, g, F)
+    v = extension_velocity(K, g, F, dist, enork2=True)
+    cp = [zeros(g) for _ in range(6)]
+    K.enork2_boundary_interpolate(*cp, *dist.six(), F64(C), *g.args(), g.num_ele)
+    deltat = F64(0.3 * dist.min_dist)
+    step = zeros(g)
+
+    def stage(Cs):
+        K.enork2_extend_step(step, deltat, F64(Cs), *v, *dist.six(), *cp, *g.args(), g.num_ele)
+        return step.copy(order="F")
+
+    C = F64(C).copy(order="F")
+    for _ in range(iteration):
+        C = F64(_rk2(C, stage))
     return C
 
 

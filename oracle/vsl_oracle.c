@@ -13,6 +13,7 @@
  *   2_2_WENO5RK3_Extend/{shared_utilities.cuh,shared_utilities.cup,upwind_normal.cu,
  *                        boundary_interpolant.cu,extend_step.cu}
  *   2_1_WENORK3_Extend/wenork3_extend.cu
+ *   1_0_ENORK2_Reinitialization/boundary_correction.cu, 2_0_ENORK2_Extend/enork2_extend.cu
  *   4_0_Calculus_ToolBox/{set_calculus_toolbox.cu,advection_step.cu}
  *   5_0_Nonoscillating_Reconstruction/nonoscillating_interpolant.cu
  *
@@ -876,6 +877,201 @@ void orc_set_calculus_toolbox(double *Fx, double *Fy, double *Fz, double *FGradM
         double pzz = (HPrimal[zp] - 2 * HPrimal[c] + HPrimal[zm]) / (dz * dz);
         double plap = pxx + pyy + pzz;
         DiracDelta[c] = plap / POW(gm, 2) - dot * lap / POW(gm, 4);
+    }
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* ENORK2: second-order ENO with the sub-cell fix and Heun RK2 (Min 2010)                */
+/*   1_0_ENORK2_Reinitialization/boundary_correction.cu                                  */
+/*   2_0_ENORK2_Extend/enork2_extend.cu                                                  */
+/* ------------------------------------------------------------------------------------ */
+
+/* line values v4, v1, v0, v2, v3 = f[-2..+2] along an axis */
+static inline void line5(const double *f, const grid3 *g, int i, int j, int k, int axis, double v[5])
+{
+    for (int s = -2; s <= 2; ++s) v[s + 2] = f[step_node(g, i, j, k, axis, s)];
+}
+
+/* Second-order ENO one-sided derivatives at v0 with the interface at pr / pl where they
+ * differ from ds; the value at the interface is vf / vb (0 for reinitialization).
+ * eno_derivative, boundary_correction.cu:81-101; eno_derivative_field,
+ * enork2_extend.cu:56-75. */
+static void eno2_derivative(const double v[5], double pr, double pl, double ds, double vf, double vb, double *sR,
+                            double *sL)
+{
+    double v4 = v[0], v1 = v[1], v0 = v[2], v2 = v[3], v3 = v[4];
+    double p2m;
+    double p2 = v1 - 2.0 * v0 + v2;
+    double p2r = v0 - 2.0 * v2 + v3;
+    p2m = 0.5 * minmod(p2, p2r) / POW(ds, 2);
+    double vr = (pr == ds) ? v2 : vf;
+    *sR = (vr - v0) / pr - pr * p2m;
+    double p2l = v0 - 2.0 * v1 + v4;
+    p2m = 0.5 * minmod(p2, p2l) / POW(ds, 2);
+    double vl = (pl == ds) ? v1 : vb;
+    *sL = (v0 - vl) / pl + pl * p2m;
+}
+
+/* boundary_correction (ENORK2), boundary_correction.cu:104-146: quadratic-ENO distance at
+ * every crossed edge, scatter form (entries without a crossing keep the caller's value). */
+void orc_enork2_boundary_correction(double *xpr, double *xpl, double *ypf, double *ypb, double *zpu, double *zpd,
+                                    const double *lsf, int num_ele, int rows, int cols, int pges, double dx,
+                                    double dy, double dz)
+{
+    (void)num_ele;
+    grid3 g = {rows, cols, pges};
+    double *fore[3] = {xpr, ypf, zpu}, *back[3] = {xpl, ypb, zpd};
+    double h[3] = {dx, dy, dz};
+    FOR_EACH_NODE(g)
+    {
+        int64_t c = node(&g, i, j, k);
+        double f0 = lsf[c];
+        for (int ax = 0; ax < 3; ++ax) {
+            int64_t nb = step_node(&g, i, j, k, ax, 1);
+            double f2 = lsf[nb];
+            if (f0 * f2 < 0) {
+                fore[ax][c] = eno2_distance(lsf[step_node(&g, i, j, k, ax, -1)], f0, f2,
+                                            lsf[step_node(&g, i, j, k, ax, 2)], h[ax]);
+                back[ax][nb] = h[ax] - fore[ax][c];
+            }
+        }
+    }
+}
+
+/* re_step (ENORK2), boundary_correction.cu:148-200: Godunov Hamiltonian with the
+ * second-order ENO derivatives; no fixed-node test. */
+void orc_enork2_re_step(double *step, const double *lsf, const bool *mask, const double *deltat, const double *xpr,
+                        const double *xpl, const double *ypf, const double *ypb, const double *zpu,
+                        const double *zpd, int rows, int cols, int pges, double dx, double dy, double dz,
+                        int num_ele)
+{
+    (void)num_ele;
+    grid3 g = {rows, cols, pges};
+    const double *fore[3] = {xpr, ypf, zpu}, *back[3] = {xpl, ypb, zpd};
+    double h[3] = {dx, dy, dz};
+    FOR_EACH_NODE(g)
+    {
+        int64_t c = node(&g, i, j, k);
+        double df[3], db[3];
+        for (int ax = 0; ax < 3; ++ax) {
+            double v[5];
+            line5(lsf, &g, i, j, k, ax, v);
+            eno2_derivative(v, fore[ax][c], back[ax][c], h[ax], 0, 0, &df[ax], &db[ax]);
+        }
+        double xR = df[0], xL = db[0], yF = df[1], yB = db[1], zU = df[2], zD = db[2];
+        if (mask[c]) {
+            step[c] = (sqrt(dmax(POW(dmin(0, xL), 2), POW(dmax(0, xR), 2)) + dmax(POW(dmin(0, yB), 2), POW(dmax(0, yF), 2)) +
+                            dmax(POW(dmin(0, zD), 2), POW(dmax(0, zU), 2))) - 1) * deltat[c] * (-1.);
+        } else {
+            step[c] = (sqrt(dmax(POW(dmax(0, xL), 2), POW(dmin(0, xR), 2)) + dmax(POW(dmax(0, yB), 2), POW(dmin(0, yF), 2)) +
+                            dmax(POW(dmax(0, zD), 2), POW(dmin(0, zU), 2))) - 1) * deltat[c] * (1.);
+        }
+    }
+}
+
+/* upwind_normal (ENORK2), enork2_extend.cu:82-141: per axis the ENO derivative toward the
+ * side whose neighbour value (0 across the interface) is smaller in magnitude. */
+void orc_enork2_upwind_normal(double *nx, double *ny, double *nz, const double *lsf, const double *xpr,
+                              const double *xpl, const double *ypf, const double *ypb, const double *zpu,
+                              const double *zpd, int rows, int cols, int pges, double dx, double dy, double dz,
+                              int num_ele)
+{
+    (void)num_ele;
+    grid3 g = {rows, cols, pges};
+    double *n[3] = {nx, ny, nz};
+    const double *fore[3] = {xpr, ypf, zpu}, *back[3] = {xpl, ypb, zpd};
+    double h[3] = {dx, dy, dz};
+    FOR_EACH_NODE(g)
+    {
+        int64_t c = node(&g, i, j, k);
+        for (int ax = 0; ax < 3; ++ax) {
+            double v[5], sR, sL;
+            line5(lsf, &g, i, j, k, ax, v);
+            double pr = fore[ax][c], pl = back[ax][c];
+            eno2_derivative(v, pr, pl, h[ax], 0, 0, &sR, &sL);
+            double vr = (pr == h[ax]) ? v[3] : 0;
+            double vl = (pl == h[ax]) ? v[1] : 0;
+            n[ax][c] = (fabs(vr) < fabs(vl)) ? sR : sL;
+        }
+    }
+}
+
+/* cubic_eno_interp, enork2_extend.cu:144-172: the quadratic ENO interpolant of the cell
+ * cut by the interface, evaluated at the crossing (0 where there is none). */
+static void eno2_crossing(const double v[5], double dis_f, double dis_b, double ds, double *cf, double *cb)
+{
+    double v4 = v[0], v1 = v[1], v0 = v[2], v2 = v[3], v3 = v[4];
+    *cf = 0;
+    *cb = 0;
+    if (dis_f != ds) {
+        double p2 = v2 - 2.0 * v0 + v1;
+        double p2r = v3 - 2.0 * v2 + v0;
+        double c2 = 0.5 * minmod(p2, p2r) / POW(ds, 2);
+        double c1 = (v2 - v0) / ds;
+        double c0 = (v2 + v0) / 2 - c2 * POW(ds, 2) / 4;
+        double x = dis_f - ds / 2;
+        *cf = c2 * x * x + c1 * x + c0;
+    }
+    if (dis_b != ds) {
+        double p2 = v2 - 2.0 * v0 + v1;
+        double p2l = v0 - 2.0 * v1 + v4;
+        double c2 = 0.5 * minmod(p2, p2l) / POW(ds, 2);
+        double c1 = (v0 - v1) / ds;
+        double c0 = (v1 + v0) / 2 - c2 * POW(ds, 2) / 4;
+        double x = ds / 2 - dis_b;
+        *cb = c2 * x * x + c1 * x + c0;
+    }
+}
+
+/* boundary_interpolate (ENORK2), enork2_extend.cu:175-211: every entry is written. */
+void orc_enork2_boundary_interpolate(double *cpr, double *cpl, double *cpf, double *cpb, double *cpu, double *cpd,
+                                     const double *xpr, const double *xpl, const double *ypf, const double *ypb,
+                                     const double *zpu, const double *zpd, const double *lsf, int rows, int cols,
+                                     int pges, double dx, double dy, double dz, int num_ele)
+{
+    (void)num_ele;
+    grid3 g = {rows, cols, pges};
+    double *cf[3] = {cpr, cpf, cpu}, *cb[3] = {cpl, cpb, cpd};
+    const double *fore[3] = {xpr, ypf, zpu}, *back[3] = {xpl, ypb, zpd};
+    double h[3] = {dx, dy, dz};
+    FOR_EACH_NODE(g)
+    {
+        int64_t c = node(&g, i, j, k);
+        for (int ax = 0; ax < 3; ++ax) {
+            double v[5];
+            line5(lsf, &g, i, j, k, ax, v);
+            eno2_crossing(v, fore[ax][c], back[ax][c], h[ax], &cf[ax][c], &cb[ax][c]);
+        }
+    }
+}
+
+/* extend_step (ENORK2), enork2_extend.cu:214-267: upwind transport with the ENO
+ * derivatives whose interface values are the crossing values; no fixed-node test. */
+void orc_enork2_extend_step(double *step, const double *deltat, const double *lsf, const double *vx,
+                            const double *vy, const double *vz, const double *xpr, const double *xpl,
+                            const double *ypf, const double *ypb, const double *zpu, const double *zpd,
+                            const double *cpr, const double *cpl, const double *cpf, const double *cpb,
+                            const double *cpu, const double *cpd, int rows, int cols, int pges, double dx, double dy,
+                            double dz, int num_ele)
+{
+    (void)num_ele;
+    grid3 g = {rows, cols, pges};
+    const double *v[3] = {vx, vy, vz};
+    const double *fore[3] = {xpr, ypf, zpu}, *back[3] = {xpl, ypb, zpd};
+    const double *cf[3] = {cpr, cpf, cpu}, *cb[3] = {cpl, cpb, cpd};
+    double h[3] = {dx, dy, dz};
+    FOR_EACH_NODE(g)
+    {
+        int64_t c = node(&g, i, j, k);
+        double df[3], db[3];
+        for (int ax = 0; ax < 3; ++ax) {
+            double w[5];
+            line5(lsf, &g, i, j, k, ax, w);
+            eno2_derivative(w, fore[ax][c], back[ax][c], h[ax], cf[ax][c], cb[ax][c], &df[ax], &db[ax]);
+        }
+        step[c] = (dmin(0, v[0][c]) * df[0] + dmax(0, v[0][c]) * db[0] + dmin(0, v[1][c]) * df[1] +
+                   dmax(0, v[1][c]) * db[1] + dmin(0, v[2][c]) * df[2] + dmax(0, v[2][c]) * db[2]) *
+                  deltat[c];
     }
 }
 

@@ -63,6 +63,27 @@ void orc_set_calculus_toolbox(double *Fx, double *Fy, double *Fz, double *FGradM
                               double *Fzx, double *FLaplacian, double *MeanCurvature, double *GaussianCurvature,
                               double *Heaviside, double *DiracDelta, const double *lsf, const double *HPrimal,
                               int rows, int cols, int pges, double dx, double dy, double dz, double ds, int num_ele);
+void orc_enork2_boundary_correction(double *xpr, double *xpl, double *ypf, double *ypb, double *zpu, double *zpd,
+                                    const double *lsf, int num_ele, int rows, int cols, int pges, double dx,
+                                    double dy, double dz);
+void orc_enork2_re_step(double *step, const double *lsf, const bool *mask, const double *deltat, const double *xpr,
+                        const double *xpl, const double *ypf, const double *ypb, const double *zpu,
+                        const double *zpd, int rows, int cols, int pges, double dx, double dy, double dz,
+                        int num_ele);
+void orc_enork2_upwind_normal(double *nx, double *ny, double *nz, const double *lsf, const double *xpr,
+                              const double *xpl, const double *ypf, const double *ypb, const double *zpu,
+                              const double *zpd, int rows, int cols, int pges, double dx, double dy, double dz,
+                              int num_ele);
+void orc_enork2_boundary_interpolate(double *cpr, double *cpl, double *cpf, double *cpb, double *cpu, double *cpd,
+                                     const double *xpr, const double *xpl, const double *ypf, const double *ypb,
+                                     const double *zpu, const double *zpd, const double *lsf, int rows, int cols,
+                                     int pges, double dx, double dy, double dz, int num_ele);
+void orc_enork2_extend_step(double *step, const double *deltat, const double *lsf, const double *vx,
+                            const double *vy, const double *vz, const double *xpr, const double *xpl,
+                            const double *ypf, const double *ypb, const double *zpu, const double *zpd,
+                            const double *cpr, const double *cpl, const double *cpf, const double *cpb,
+                            const double *cpu, const double *cpd, int rows, int cols, int pges, double dx, double dy,
+                            double dz, int num_ele);
 int orc_version(void);
 
 #ifdef __cplusplus

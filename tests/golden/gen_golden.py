@@ -129,6 +129,22 @@ def run_case(K, name, x, y, z, F, C):
     for nm, a in zip(("back_x", "fore_x", "back_y", "fore_y", "back_z", "fore_z"), wd):
         rec["wd_" + nm] = a
     rec["redistance_2_2"] = O.surface_redistance(K, g, F, C, 2, 2)
+    # ENORK2: quadratic-ENO distances, re_step, Heun RK2 reinitialization and extension
+    d2 = O.set_distance_enork2(K, g, F)
+    for nm, a in zip(("xpr", "xpl", "ypf", "ypb", "zpu", "zpd"), d2.six()):
+        rec["dist2_" + nm] = a
+    K.enork2_re_step(step, F, mask, O.F64(0.3 * d2.min_dist), *d2.six(), *g.args(), g.num_ele)
+    rec["re_step2"] = step.copy(order="F")
+    n3 = [O.zeros(g) for _ in range(3)]
+    K.enork2_upwind_normal(*n3, F, *d2.six(), *g.args(), g.num_ele)
+    for ax, a in zip("xyz", n3):
+        rec[f"normal2_{ax}"] = a
+    cp = [O.zeros(g) for _ in range(6)]
+    K.enork2_boundary_interpolate(*cp, *d2.six(), C, *g.args(), g.num_ele)
+    for nm, a in zip(("cpr", "cpl", "cpf", "cpb", "cpu", "cpd"), cp):
+        rec[f"cross2_{nm}"] = a
+    rec["reinit2_it4"] = O.reinit_enork2(K, g, F, 4)
+    rec["extend2_it3"] = O.extend_enork2(K, g, F, C, 3)
     rec["area"] = np.array(O.cal_area(g, F, tb["DiracDelta"]))
     rec["volume"] = np.array(O.cal_volume(g, F, tb["Heaviside"]))
     return rec

@@ -105,3 +105,27 @@ def test_surface_redistance(case):
     K = O.kernels("port")
     g, F, C = setup(O, G)
     close(O.surface_redistance(K, g, F, C, 2, 2), G["redistance_2_2"])
+
+
+def test_enork2(case):
+    """ENORK2 (second-order ENO with the sub-cell fix, Heun RK2): distances, one re_step,
+    upwind normals, crossing values, and the reinitialization and extension loops."""
+    name, G, O = case
+    K = O.kernels("port")
+    g, F, C = setup(O, G)
+    d2 = O.set_distance_enork2(K, g, F)
+    for nm, a in zip(DIRS, d2.six()):
+        close(a, G["dist2_" + nm])
+    step = O.zeros(g)
+    K.enork2_re_step(step, F, np.asfortranarray(F < 0), O.F64(0.3 * d2.min_dist), *d2.six(), *g.args(), g.num_ele)
+    close(step, G["re_step2"])
+    n = [O.zeros(g) for _ in range(3)]
+    K.enork2_upwind_normal(*n, F, *d2.six(), *g.args(), g.num_ele)
+    for ax, a in zip("xyz", n):
+        close(a, G[f"normal2_{ax}"])
+    cp = [O.zeros(g) for _ in range(6)]
+    K.enork2_boundary_interpolate(*cp, *d2.six(), C, *g.args(), g.num_ele)
+    for nm, a in zip(CROSS, cp):
+        close(a, G[f"cross2_{nm}"])
+    close(O.reinit_enork2(K, g, F, 4), G["reinit2_it4"])
+    close(O.extend_enork2(K, g, F, C, 3), G["extend2_it3"])
