@@ -30,6 +30,12 @@ SIGNATURES = {
     "vsl_set_calculus_toolbox": "p" * 18 + "pp" + _G + "d" + "i" + "s",
     "vsl_advection_step": "ppppp" + _G + "s",
     "vsl_weno_derivative": "ppppppp" + _G + "s",
+    # ENORK2 drop-ins (FP64, reference argument order)
+    "vsl_enork2_boundary_correction": "ppppppp" + "i" + _G + "s",
+    "vsl_enork2_re_step": "pppp" + "pppppp" + _G + "i" + "s",
+    "vsl_enork2_upwind_normal": "pppp" + "pppppp" + _G + "i" + "s",
+    "vsl_enork2_boundary_interpolate": "pppppp" + "pppppp" + "p" + _G + "i" + "s",
+    "vsl_enork2_extend_step": "pppppp" + "pppppp" + "pppppp" + _G + "i" + "s",
     # tuning table of the tiled kernels (pages per block)
     "vsl_set_tile_pages": "iiiii",
     "vsl_tile_pages": "iiii",
@@ -48,6 +54,8 @@ for _suf in ("f64", "f32"):
             f"vsl_area_volume_{_suf}": "pp" + _G + "pz" + "s",
             f"vsl_weno5_rk3_advection_{_suf}": "pppppi" + _G + "pz" + "s",
             f"vsl_vesicle_step_{_suf}": "p" + "pppppp" + "iid" + "p" + _G + "pz" + "s",
+            f"vsl_enork2_reinitialization_{_suf}": "pi" + _G + "pz" + "s",
+            f"vsl_enork2_extend_{_suf}": "pip" + _G + "pz" + "s",
             f"vsl_weno5_rk3_advection_adjoint_{_suf}": "ppppp" + "pppp" + _G + "pz" + "s",
             f"vsl_weno5_rk3_reinitialization_adjoint_{_suf}": "pipp" + _G + "pz" + "s",
         }
@@ -65,6 +73,8 @@ OP = {
     "set_distance": 9,
     "advection_adjoint": 10,
     "reinit_adjoint": 11,
+    "reinit_enork2": 12,
+    "extend_enork2": 13,
 }
 
 

@@ -188,6 +188,8 @@ size_t measure(int op, const Grid &g, int elem)
         case VSL_OP_SET_DISTANCE: carve_edges(w, g); break;
         case VSL_OP_ADVECTION_ADJOINT: carve_adj<T>(w, g, false); break;
         case VSL_OP_REINIT_ADJOINT: carve_adj<T>(w, g, true); break;
+        case VSL_OP_REINIT_ENORK2: carve_reinit<T>(w, g, true); break;
+        case VSL_OP_EXTEND_ENORK2: carve_extend<T>(w, g, true); break;
         default: return false;
         }
         return true;
@@ -537,6 +539,56 @@ int op_vesicle_step(T *F, T *xpr, T *xpl, T *ypf, T *ypb, T *zpu, T *zpd, int ex
 }
 
 // ---------------------------------------------------------------------------------------
+// ENORK2 (ENORK2Reinitialization.m:3-45, ENORK2Extend.m:9-81)
+// ---------------------------------------------------------------------------------------
+
+template <typename T>
+int op_reinit_enork2(T *F, int iteration, int rows, int cols, int pges, double dx, double dy, double dz, void *ws,
+                     size_t bytes, cudaStream_t s)
+{
+    if (any_null(F)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    if (iteration < 0) return VSL_ERR_VALUE;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    if (int st = check_ws(VSL_OP_REINIT_ENORK2, g, sizeof(T), ws, bytes)) return st;
+    Bump b(ws);
+    ReinitWork<T> w = carve_reinit<T>(b, g, true);
+    VSL_TRY(launch_set_distance_eno2<T>(F, w.dist, g, w.edges, s));
+    const Ptr6<const T> d = cview(w.dist);
+    VSL_TRY(launch_classify<T>(F, d, w.flags, NodeList{nullptr, nullptr}, g, s));
+    for (int it = 0; it < iteration; ++it) {
+        VSL_TRY(launch_enork2_reinit_stage<T>(F, F, w.b, w.flags, d, g, 0, s));
+        VSL_TRY(launch_enork2_reinit_stage<T>(w.b, F, F, w.flags, d, g, 1, s));
+    }
+    return VSL_OK;
+}
+
+template <typename T>
+int op_extend_enork2(T *C, int iteration, const T *F, int rows, int cols, int pges, double dx, double dy, double dz,
+                     void *ws, size_t bytes, cudaStream_t s)
+{
+    if (any_null(C, F)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    if (iteration < 0) return VSL_ERR_VALUE;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    if (int st = check_ws(VSL_OP_EXTEND_ENORK2, g, sizeof(T), ws, bytes)) return st;
+    Bump b(ws);
+    ExtendWork<T> w = carve_extend<T>(b, g, true);
+    VSL_TRY(launch_set_distance_eno2<T>(F, w.dist, g, w.edges, s));
+    const Ptr6<const T> d = cview(w.dist);
+    VSL_TRY(launch_enork2_velocity<T>(F, d, w.v, g, 1e-6, s));
+    VSL_TRY(launch_classify<T>(F, d, w.flags, w.flagged, g, s));
+    VSL_TRY(launch_enork2_crossing<T>(C, d, w.cp, w.flagged, g, s));
+    const Ptr6<const T> cp = cview(w.cp);
+    const Ptr3<const T> v = cview3(w.v);
+    for (int it = 0; it < iteration; ++it) {
+        VSL_TRY(launch_enork2_extend_stage<T>(C, C, w.b, w.flags, d, cp, v, g, 0, s));
+        VSL_TRY(launch_enork2_extend_stage<T>(w.b, C, C, w.flags, d, cp, v, g, 1, s));
+    }
+    return VSL_OK;
+}
+
+// ---------------------------------------------------------------------------------------
 // adjoints (no counterpart in the reference)
 // ---------------------------------------------------------------------------------------
 
@@ -751,6 +803,16 @@ size_t vsl_workspace_bytes(int op, int rows, int cols, int pges, int elem_bytes)
     {                                                                                                              \
         return op_vesicle_step<T>(F, xpr, xpl, ypf, ypb, zpu, zpd, ext_iters, reinit_iters, cfl, info, rows, cols, \
                                   pges, dx, dy, dz, ws, bytes, stream);                                            \
+    }                                                                                                              \
+    int vsl_enork2_reinitialization_##SUF(T *F, int iteration, int rows, int cols, int pges, double dx, double dy,  \
+                                          double dz, void *ws, size_t bytes, vsl_stream_t stream)                   \
+    {                                                                                                              \
+        return op_reinit_enork2<T>(F, iteration, rows, cols, pges, dx, dy, dz, ws, bytes, stream);                 \
+    }                                                                                                              \
+    int vsl_enork2_extend_##SUF(T *C, int iteration, const T *F, int rows, int cols, int pges, double dx,          \
+                                double dy, double dz, void *ws, size_t bytes, vsl_stream_t stream)                 \
+    {                                                                                                              \
+        return op_extend_enork2<T>(C, iteration, F, rows, cols, pges, dx, dy, dz, ws, bytes, stream);              \
     }                                                                                                              \
     int vsl_weno5_rk3_advection_adjoint_##SUF(const T *F, const T *vx, const T *vy, const T *vz, const double *dt, \
                                               T *lam, T *gvx, T *gvy, T *gvz, int rows, int cols, int pges,        \

@@ -743,4 +743,82 @@ __device__ __forceinline__ void crossing_cubic_fast(const float p[7], float dis_
     if (dis_b < h) cb = lagrange_equispaced<4>(p + 1, 2.f - dis_b / h);  // nodes p[1..4] at 0..3
 }
 
+// ---------------------------------------------------------------------------------------
+// ENORK2: second-order ENO derivatives with the sub-cell fix (Min 2010), on the five
+// values p[1..5] of a 7-point line centred at p[3]
+// ---------------------------------------------------------------------------------------
+
+// Forward (sR) and backward (sL) derivatives at p[3]; where the interface cuts the cell
+// (r1 / l1 differs from h) the one-sided difference runs to the interface, whose value is
+// hf / hb (0 for reinitialization, the crossing value for extension).  eno_derivative,
+// boundary_correction.cu:81-101; eno_derivative_field, enork2_extend.cu:56-75.
+template <typename T>
+__device__ __forceinline__ void eno2_pair(const T p[7], T r1, T l1, T h, T hf, T hb, T &sR, T &sL)
+{
+    const T v4 = p[1], v1 = p[2], v0 = p[3], v2 = p[4], v3 = p[5];
+    const T h2 = sqr(h);
+    const T p2 = v1 - T(2.0) * v0 + v2;
+    const T p2r = v0 - T(2.0) * v2 + v3;
+    T p2m = T(0.5) * minmod(p2, p2r) / h2;
+    const T vr = (r1 == h) ? v2 : hf;
+    sR = (vr - v0) / r1 - r1 * p2m;
+    const T p2l = v0 - T(2.0) * v1 + v4;
+    p2m = T(0.5) * minmod(p2, p2l) / h2;
+    const T vl = (l1 == h) ? v1 : hb;
+    sL = (v0 - vl) / l1 + l1 * p2m;
+}
+
+// The ENO derivative toward the side whose neighbour value (0 across the interface) is
+// smaller in magnitude (upwind_normal_point, enork2_extend.cu:82-100).
+template <typename T> __device__ __forceinline__ T eno2_upwind(const T p[7], T r1, T l1, T h)
+{
+    T sR, sL;
+    eno2_pair(p, r1, l1, h, T(0), T(0), sR, sL);
+    const T vr = (r1 == h) ? p[4] : T(0);
+    const T vl = (l1 == h) ? p[2] : T(0);
+    return (fabs(vr) < fabs(vl)) ? sR : sL;
+}
+
+// Value at the crossing of the quadratic ENO interpolant of the cut cell, 0 where the
+// cell is not cut (cubic_eno_interp, enork2_extend.cu:144-172).
+template <typename T>
+__device__ __forceinline__ void eno2_crossing(const T p[7], T dis_f, T dis_b, T h, T &cf, T &cb)
+{
+    const T v4 = p[1], v1 = p[2], v0 = p[3], v2 = p[4], v3 = p[5];
+    const T h2 = sqr(h);
+    cf = T(0);
+    cb = T(0);
+    if (dis_f != h) {
+        const T p2 = v2 - T(2.0) * v0 + v1;
+        const T p2r = v3 - T(2.0) * v2 + v0;
+        const T c2 = T(0.5) * minmod(p2, p2r) / h2;
+        const T c1 = (v2 - v0) / h;
+        const T c0 = (v2 + v0) / T(2) - c2 * h2 / T(4);
+        const T x = dis_f - h / T(2);
+        cf = c2 * x * x + c1 * x + c0;
+    }
+    if (dis_b != h) {
+        const T p2 = v2 - T(2.0) * v0 + v1;
+        const T p2l = v0 - T(2.0) * v1 + v4;
+        const T c2 = T(0.5) * minmod(p2, p2l) / h2;
+        const T c1 = (v0 - v1) / h;
+        const T c0 = (v1 + v0) / T(2) - c2 * h2 / T(4);
+        const T x = h / T(2) - dis_b;
+        cb = c2 * x * x + c1 * x + c0;
+    }
+}
+
+// Distance from the node at L.c to the interface between it and its +1 neighbour along
+// L by the quadratic ENO fit alone (the ENORK2 boundary_correction,
+// boundary_correction.cu:104-146), double arithmetic on the promoted samples.
+template <typename T>
+__device__ __forceinline__ double eno2_fore_distance(const T *__restrict__ f, const AxisLine &L, double h)
+{
+    const double a = (double)__ldg(f + L.base + (long long)clampi(L.c - 1, L.n) * L.stride);
+    const double b = (double)__ldg(f + L.base + (long long)L.c * L.stride);
+    const double c = (double)__ldg(f + L.base + (long long)clampi(L.c + 1, L.n) * L.stride);
+    const double d = (double)__ldg(f + L.base + (long long)clampi(L.c + 2, L.n) * L.stride);
+    return eno2_distance(a, b, c, d, h);
+}
+
 }  // namespace vsl

@@ -378,6 +378,135 @@ __global__ void __launch_bounds__(BX *BY) k_advect_stage(const T *__restrict__ p
     out[c] = rk3_combine(stage, pn, __ldg(phi_s + c) - step);
 }
 
+// ---------------------------------------------------------------------------------------
+// ENORK2 (second-order ENO with the sub-cell fix, Heun RK2): ENORK2Reinitialization.m:3-45
+// and ENORK2Extend.m:9-81 over the kernels of boundary_correction.cu and enork2_extend.cu.
+// The fused stage writes
+//   stage 0: out = phi_s - step(phi_s)
+//   stage 1: out = (phi_n + phi_s - step(phi_s)) / 2
+// the elementwise updates of the MATLAB loops.  There is no fixed-node test.
+// ---------------------------------------------------------------------------------------
+template <typename T> __device__ __forceinline__ T rk2_combine(int stage, T phi_n, T phi_s, T step)
+{
+    return stage == 0 ? phi_s - step : (phi_n + phi_s - step) / T(2);
+}
+
+// one quadratic-ENO root per listed crossed edge (k_dist_roots with the ENORK2 distance)
+template <typename T>
+__global__ void __launch_bounds__(128) k_dist_roots_eno2(const T *__restrict__ f, Ptr6<T> d, EdgeLists e, Grid g)
+{
+    for (int ax = 0; ax < 3; ++ax) {
+        const unsigned n = *(e.count + ax);
+        const double h = axis_h(g, ax);
+        for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+            const long long c = e.idx[ax][t];
+            int i, j, k;
+            node_of(g, c, i, j, k);
+            const AxisLine L = axis_line(g, i, j, k, ax);
+            const double dist = eno2_fore_distance(f, L, h);
+            d.p[2 * ax][c] = (T)dist;
+            d.p[2 * ax + 1][c + L.stride] = (T)(h - dist);
+        }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BX *BY) k_enork2_reinit_stage(const T *__restrict__ phi_s,
+                                                                  const T *__restrict__ phi_n, T *__restrict__ out,
+                                                                  const uint8_t *__restrict__ flags, Ptr6<const T> d,
+                                                                  Grid g, int stage)
+{
+    int i, j, k;
+    if (!fused_node(g, i, j, k)) return;
+    const long long c = node_index(g, i, j, k);
+    const uint8_t fl = __ldg(flags + c);
+    const T hs[3] = {(T)g.dx, (T)g.dy, (T)g.dz};
+    T df[3], db[3];
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        T p[7];
+        load_line7(phi_s, axis_line(g, i, j, k, ax), p);
+        eno2_pair(p, flagged_distance(fl, 2 * ax, d, c, hs[ax]), flagged_distance(fl, 2 * ax + 1, d, c, hs[ax]),
+                  hs[ax], T(0), T(0), df[ax], db[ax]);
+    }
+    const bool neg = fl & MASK_BIT;
+    const T gn = godunov_norm(neg, df[0], db[0], df[1], db[1], df[2], db[2]);
+    const T step = (gn - T(1)) * pseudo_dt(fl, d, c, hs[0], hs[1], hs[2]) * (neg ? T(-1) : T(1));
+    const T pn = stage == 0 ? T(0) : __ldg(phi_n + c);
+    out[c] = rk2_combine(stage, pn, __ldg(phi_s + c), step);
+}
+
+// v = sign(F) * n / max(|n|, floor) with the ENO upwind normal (enork2_extend.cu:103-141,
+// ENORK2Extend.m:26-42)
+template <typename T>
+__global__ void __launch_bounds__(BX *BY) k_enork2_velocity(const T *__restrict__ phi, Ptr6<const T> d, Ptr3<T> v,
+                                                              Grid g, T floor)
+{
+    int i, j, k;
+    if (!fused_node(g, i, j, k)) return;
+    const long long c = node_index(g, i, j, k);
+    T n[3];
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        T p[7];
+        load_line7(phi, axis_line(g, i, j, k, ax), p);
+        n[ax] = eno2_upwind(p, __ldg(d.p[2 * ax] + c), __ldg(d.p[2 * ax + 1] + c), (T)axis_h(g, ax));
+    }
+    const T grad = vmax(sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]), floor);
+    const T f0 = __ldg(phi + c);
+    const T s = f0 > T(0) ? T(1) : (f0 < T(0) ? T(-1) : T(0));
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) v.p[ax][c] = s * (n[ax] / grad);
+}
+
+// quadratic crossing values (enork2_extend.cu:144-211) at the listed nodes
+template <typename T>
+__global__ void __launch_bounds__(128) k_enork2_crossing(const T *__restrict__ cfield, Ptr6<const T> d, Ptr6<T> cp,
+                                                           NodeList list, Grid g)
+{
+    const unsigned n = *list.count;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const long long c = list.idx[t];
+        int i, j, k;
+        node_of(g, c, i, j, k);
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            T p[7], cf, cb;
+            load_line7(cfield, axis_line(g, i, j, k, ax), p);
+            eno2_crossing(p, __ldg(d.p[2 * ax] + c), __ldg(d.p[2 * ax + 1] + c), (T)axis_h(g, ax), cf, cb);
+            cp.p[2 * ax][c] = cf;
+            cp.p[2 * ax + 1][c] = cb;
+        }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BX *BY) k_enork2_extend_stage(const T *__restrict__ c_s, const T *__restrict__ c_n,
+                                                                  T *__restrict__ out, const uint8_t *__restrict__ flags,
+                                                                  Ptr6<const T> d, Ptr6<const T> cp, Ptr3<const T> v,
+                                                                  Grid g, int stage)
+{
+    int i, j, k;
+    if (!fused_node(g, i, j, k)) return;
+    const long long c = node_index(g, i, j, k);
+    const uint8_t fl = __ldg(flags + c);
+    const T hs[3] = {(T)g.dx, (T)g.dy, (T)g.dz};
+    T df[3], db[3];
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        T p[7];
+        load_line7(c_s, axis_line(g, i, j, k, ax), p);
+        const bool ff = fl & (1u << (2 * ax)), fb = fl & (1u << (2 * ax + 1));
+        eno2_pair(p, ff ? __ldg(d.p[2 * ax] + c) : hs[ax], fb ? __ldg(d.p[2 * ax + 1] + c) : hs[ax], hs[ax],
+                  ff ? __ldg(cp.p[2 * ax] + c) : T(0), fb ? __ldg(cp.p[2 * ax + 1] + c) : T(0), df[ax], db[ax]);
+    }
+    const T step = upwind_dot(__ldg(v.p[0] + c), __ldg(v.p[1] + c), __ldg(v.p[2] + c), df[0], db[0], df[1], db[1],
+                              df[2], db[2]) *
+                   pseudo_dt(fl, d, c, hs[0], hs[1], hs[2]);
+    const T pn = stage == 0 ? T(0) : __ldg(c_n + c);
+    out[c] = rk2_combine(stage, pn, __ldg(c_s + c), step);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------------------
@@ -493,6 +622,48 @@ cudaError_t launch_advect_stage(const T *phi_s, const T *phi_n, T *out, Ptr3<con
     return cudaGetLastError();
 }
 
+template <typename T>
+cudaError_t launch_set_distance_eno2(const T *phi, Ptr6<T> dist, const Grid &g, EdgeLists e, cudaStream_t s)
+{
+    cudaError_t err = cudaMemsetAsync(e.count, 0, 3 * sizeof(unsigned), s);
+    if (err != cudaSuccess) return err;
+    k_dist_scan<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, dist, e, g);
+    k_dist_roots_eno2<T><<<list_blocks(), 128, 0, s>>>(phi, dist, e, g);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_enork2_reinit_stage(const T *phi_s, const T *phi_n, T *out, const uint8_t *flags,
+                                       Ptr6<const T> dist, const Grid &g, int stage, cudaStream_t s)
+{
+    k_enork2_reinit_stage<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi_s, phi_n, out, flags, dist, g, stage);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_enork2_velocity(const T *phi, Ptr6<const T> dist, Ptr3<T> v, const Grid &g, double floor,
+                                   cudaStream_t s)
+{
+    k_enork2_velocity<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, dist, v, g, (T)floor);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_enork2_crossing(const T *c, Ptr6<const T> dist, Ptr6<T> cp, NodeList list, const Grid &g,
+                                   cudaStream_t s)
+{
+    k_enork2_crossing<T><<<list_blocks(), 128, 0, s>>>(c, dist, cp, list, g);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_enork2_extend_stage(const T *c_s, const T *c_n, T *out, const uint8_t *flags, Ptr6<const T> dist,
+                                       Ptr6<const T> cp, Ptr3<const T> v, const Grid &g, int stage, cudaStream_t s)
+{
+    k_enork2_extend_stage<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(c_s, c_n, out, flags, dist, cp, v, g, stage);
+    return cudaGetLastError();
+}
+
 #define VSL_INSTANTIATE_FUSED(T)                                                                                   \
     template cudaError_t launch_set_distance<T>(const T *, Ptr6<T>, const Grid &, bool, EdgeLists, cudaStream_t);   \
     template cudaError_t launch_classify<T>(const T *, Ptr6<const T>, uint8_t *, NodeList, const Grid &,            \
@@ -507,6 +678,15 @@ cudaError_t launch_advect_stage(const T *phi_s, const T *phi_n, T *out, Ptr3<con
                                                 Ptr6<const T>, Ptr3<const T>, const Grid &, int, bool, bool,        \
                                                 cudaStream_t);                                                      \
     template cudaError_t launch_advect_stage<T>(const T *, const T *, T *, Ptr3<const T>, const T *,                \
-                                                const double *, const Grid &, int, bool, cudaStream_t);
+                                                const double *, const Grid &, int, bool, cudaStream_t);             \
+    template cudaError_t launch_set_distance_eno2<T>(const T *, Ptr6<T>, const Grid &, EdgeLists, cudaStream_t);    \
+    template cudaError_t launch_enork2_reinit_stage<T>(const T *, const T *, T *, const uint8_t *, Ptr6<const T>,   \
+                                                       const Grid &, int, cudaStream_t);                            \
+    template cudaError_t launch_enork2_velocity<T>(const T *, Ptr6<const T>, Ptr3<T>, const Grid &, double,         \
+                                                   cudaStream_t);                                                   \
+    template cudaError_t launch_enork2_crossing<T>(const T *, Ptr6<const T>, Ptr6<T>, NodeList, const Grid &,       \
+                                                   cudaStream_t);                                                   \
+    template cudaError_t launch_enork2_extend_stage<T>(const T *, const T *, T *, const uint8_t *, Ptr6<const T>,   \
+                                                       Ptr6<const T>, Ptr3<const T>, const Grid &, int, cudaStream_t);
 
 }  // namespace vsl

@@ -73,6 +73,23 @@ template <typename T>
 cudaError_t launch_advect_stage(const T *phi_s, const T *phi_n, T *out, Ptr3<const T> v, const T *speed,
                                 const double *dt, const Grid &g, int stage, bool fast, cudaStream_t s);
 
+// ENORK2 (second-order ENO, Heun RK2 stages 0 and 1): quadratic-ENO distances, the
+// reinitialization and extension stages, the extension velocity and crossing values
+template <typename T>
+cudaError_t launch_set_distance_eno2(const T *phi, Ptr6<T> dist, const Grid &g, EdgeLists e, cudaStream_t s);
+template <typename T>
+cudaError_t launch_enork2_reinit_stage(const T *phi_s, const T *phi_n, T *out, const uint8_t *flags,
+                                       Ptr6<const T> dist, const Grid &g, int stage, cudaStream_t s);
+template <typename T>
+cudaError_t launch_enork2_velocity(const T *phi, Ptr6<const T> dist, Ptr3<T> v, const Grid &g, double floor,
+                                   cudaStream_t s);
+template <typename T>
+cudaError_t launch_enork2_crossing(const T *c, Ptr6<const T> dist, Ptr6<T> cp, NodeList list, const Grid &g,
+                                   cudaStream_t s);
+template <typename T>
+cudaError_t launch_enork2_extend_stage(const T *c_s, const T *c_n, T *out, const uint8_t *flags, Ptr6<const T> dist,
+                                       Ptr6<const T> cp, Ptr3<const T> v, const Grid &g, int stage, cudaStream_t s);
+
 // ---- tiled FP32 stage kernels (vsl_tiled.cuh, built into vsl_fused_f32.cu) ----------
 // compact queue of the nodes that need the interface-aware stencil, two counters used
 // alternately by consecutive stages (zeroed at the start of an operation)

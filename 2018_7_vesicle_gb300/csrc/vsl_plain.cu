@@ -261,6 +261,108 @@ __global__ void __launch_bounds__(BX *BY) k_set_calculus_toolbox(Fields18 o, con
     for (int q = 0; q < 18; ++q) o.p[q][c] = vals[q];
 }
 
+// ---- ENORK2 (1_0_ENORK2_Reinitialization/boundary_correction.cu,
+//      2_0_ENORK2_Extend/enork2_extend.cu) ---------------------------------------------
+
+// boundary_correction (ENORK2, boundary_correction.cu:104-146) in the gather form of
+// k_boundary_location: quadratic-ENO distances only.
+__global__ void __launch_bounds__(BX *BY) k_enork2_boundary_correction(Fields6 d, const double *__restrict__ f, Grid g)
+{
+    int i, j, k;
+    if (!node_of_thread(g, i, j, k)) return;
+    const long long c = node_index(g, i, j, k);
+    const double f0 = __ldg(f + c);
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        AxisLine L = axis_line(g, i, j, k, ax);
+        const double h = axis_h(g, ax);
+        const double fn = __ldg(f + L.base + (long long)clampi(L.c + 1, L.n) * L.stride);
+        if (f0 * fn < 0) d.p[2 * ax][c] = eno2_fore_distance(f, L, h);
+        if (L.c > 0) {
+            const double fp = __ldg(f + L.base + (long long)(L.c - 1) * L.stride);
+            if (fp * f0 < 0) {
+                AxisLine Lp = L;
+                Lp.c = L.c - 1;
+                d.p[2 * ax + 1][c] = h - eno2_fore_distance(f, Lp, h);
+            }
+        }
+    }
+}
+
+// re_step (ENORK2, boundary_correction.cu:148-200): no fixed-node test.
+__global__ void __launch_bounds__(BX *BY) k_enork2_re_step(double *__restrict__ step, const double *__restrict__ lsf,
+                                                             const bool *__restrict__ mask,
+                                                             const double *__restrict__ deltat, CFields6 d, Grid g)
+{
+    int i, j, k;
+    if (!node_of_thread(g, i, j, k)) return;
+    const long long c = node_index(g, i, j, k);
+    double df[3], db[3];
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        double p[7];
+        load_line7(lsf, axis_line(g, i, j, k, ax), p);
+        eno2_pair(p, __ldg(d.p[2 * ax] + c), __ldg(d.p[2 * ax + 1] + c), axis_h(g, ax), 0.0, 0.0, df[ax], db[ax]);
+    }
+    const bool neg = mask[c];
+    const double gn = godunov_norm(neg, df[0], db[0], df[1], db[1], df[2], db[2]);
+    step[c] = (gn - 1) * __ldg(deltat + c) * (neg ? -1. : 1.);
+}
+
+// upwind_normal (ENORK2, enork2_extend.cu:103-141).
+__global__ void __launch_bounds__(BX *BY) k_enork2_upwind_normal(Fields6 n, const double *__restrict__ lsf, CFields6 d,
+                                                                   Grid g)
+{
+    int i, j, k;
+    if (!node_of_thread(g, i, j, k)) return;
+    const long long c = node_index(g, i, j, k);
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        double p[7];
+        load_line7(lsf, axis_line(g, i, j, k, ax), p);
+        n.p[ax][c] = eno2_upwind(p, __ldg(d.p[2 * ax] + c), __ldg(d.p[2 * ax + 1] + c), axis_h(g, ax));
+    }
+}
+
+// boundary_interpolate (ENORK2, enork2_extend.cu:175-211): every entry is written.
+__global__ void __launch_bounds__(BX *BY) k_enork2_boundary_interpolate(Fields6 cp, CFields6 d,
+                                                                          const double *__restrict__ lsf, Grid g)
+{
+    int i, j, k;
+    if (!node_of_thread(g, i, j, k)) return;
+    const long long c = node_index(g, i, j, k);
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        double p[7], cf, cb;
+        load_line7(lsf, axis_line(g, i, j, k, ax), p);
+        eno2_crossing(p, __ldg(d.p[2 * ax] + c), __ldg(d.p[2 * ax + 1] + c), axis_h(g, ax), cf, cb);
+        cp.p[2 * ax][c] = cf;
+        cp.p[2 * ax + 1][c] = cb;
+    }
+}
+
+// extend_step (ENORK2, enork2_extend.cu:214-267): no fixed-node test.
+__global__ void __launch_bounds__(BX *BY) k_enork2_extend_step(double *__restrict__ step,
+                                                                 const double *__restrict__ deltat,
+                                                                 const double *__restrict__ lsf, CFields6 v3,
+                                                                 CFields6 d, CFields6 cp, Grid g)
+{
+    int i, j, k;
+    if (!node_of_thread(g, i, j, k)) return;
+    const long long c = node_index(g, i, j, k);
+    double df[3], db[3];
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        double p[7];
+        load_line7(lsf, axis_line(g, i, j, k, ax), p);
+        eno2_pair(p, __ldg(d.p[2 * ax] + c), __ldg(d.p[2 * ax + 1] + c), axis_h(g, ax), __ldg(cp.p[2 * ax] + c),
+                  __ldg(cp.p[2 * ax + 1] + c), df[ax], db[ax]);
+    }
+    step[c] = upwind_dot(__ldg(v3.p[0] + c), __ldg(v3.p[1] + c), __ldg(v3.p[2] + c), df[0], db[0], df[1], db[1],
+                         df[2], db[2]) *
+              __ldg(deltat + c);
+}
+
 // ---- argument checks ---------------------------------------------------------------
 
 template <typename... P> bool any_null(P... p) { return ((p == nullptr) || ...); }
@@ -446,6 +548,77 @@ int vsl_extend_step_eno3(double *step, const double *deltat, const double *lsf, 
 {
     return extend_step_common(true, step, deltat, lsf, vx, vy, vz, xpr, xpl, ypf, ypb, zpu, zpd, cpr, cpl, cpf,
                               cpb, cpu, cpd, rows, cols, pges, dx, dy, dz, num_ele, stream);
+}
+
+int vsl_enork2_boundary_correction(double *xpr, double *xpl, double *ypf, double *ypb, double *zpu, double *zpd,
+                                   const double *lsf, int num_ele, int rows, int cols, int pges, double dx,
+                                   double dy, double dz, vsl_stream_t stream)
+{
+    if (any_null(xpr, xpl, ypf, ypb, zpu, zpd, lsf)) return VSL_ERR_NULL;
+    if (int st = prologue(rows, cols, pges, dx, dy, dz, num_ele, true)) return st;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    Fields6 d = {{xpr, xpl, ypf, ypb, zpu, zpd}};
+    k_enork2_boundary_correction<<<node_grid(g), dim3(BX, BY), 0, stream>>>(d, lsf, g);
+    return launch_status(cudaGetLastError());
+}
+
+int vsl_enork2_re_step(double *step, const double *lsf, const bool *mask, const double *deltat, const double *xpr,
+                       const double *xpl, const double *ypf, const double *ypb, const double *zpu, const double *zpd,
+                       int rows, int cols, int pges, double dx, double dy, double dz, int num_ele,
+                       vsl_stream_t stream)
+{
+    if (any_null(step, lsf, mask, deltat, xpr, xpl, ypf, ypb, zpu, zpd)) return VSL_ERR_NULL;
+    if (int st = prologue(rows, cols, pges, dx, dy, dz, num_ele, true)) return st;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    CFields6 d = {{xpr, xpl, ypf, ypb, zpu, zpd}};
+    k_enork2_re_step<<<node_grid(g), dim3(BX, BY), 0, stream>>>(step, lsf, mask, deltat, d, g);
+    return launch_status(cudaGetLastError());
+}
+
+int vsl_enork2_upwind_normal(double *nx, double *ny, double *nz, const double *lsf, const double *xpr,
+                             const double *xpl, const double *ypf, const double *ypb, const double *zpu,
+                             const double *zpd, int rows, int cols, int pges, double dx, double dy, double dz,
+                             int num_ele, vsl_stream_t stream)
+{
+    if (any_null(nx, ny, nz, lsf, xpr, xpl, ypf, ypb, zpu, zpd)) return VSL_ERR_NULL;
+    if (int st = prologue(rows, cols, pges, dx, dy, dz, num_ele, true)) return st;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    Fields6 n = {{nx, ny, nz, nullptr, nullptr, nullptr}};
+    CFields6 d = {{xpr, xpl, ypf, ypb, zpu, zpd}};
+    k_enork2_upwind_normal<<<node_grid(g), dim3(BX, BY), 0, stream>>>(n, lsf, d, g);
+    return launch_status(cudaGetLastError());
+}
+
+int vsl_enork2_boundary_interpolate(double *cpr, double *cpl, double *cpf, double *cpb, double *cpu, double *cpd,
+                                    const double *xpr, const double *xpl, const double *ypf, const double *ypb,
+                                    const double *zpu, const double *zpd, const double *lsf, int rows, int cols,
+                                    int pges, double dx, double dy, double dz, int num_ele, vsl_stream_t stream)
+{
+    if (any_null(cpr, cpl, cpf, cpb, cpu, cpd, xpr, xpl, ypf, ypb, zpu, zpd, lsf)) return VSL_ERR_NULL;
+    if (int st = prologue(rows, cols, pges, dx, dy, dz, num_ele, true)) return st;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    Fields6 cp = {{cpr, cpl, cpf, cpb, cpu, cpd}};
+    CFields6 d = {{xpr, xpl, ypf, ypb, zpu, zpd}};
+    k_enork2_boundary_interpolate<<<node_grid(g), dim3(BX, BY), 0, stream>>>(cp, d, lsf, g);
+    return launch_status(cudaGetLastError());
+}
+
+int vsl_enork2_extend_step(double *step, const double *deltat, const double *lsf, const double *vx, const double *vy,
+                           const double *vz, const double *xpr, const double *xpl, const double *ypf,
+                           const double *ypb, const double *zpu, const double *zpd, const double *cpr,
+                           const double *cpl, const double *cpf, const double *cpb, const double *cpu,
+                           const double *cpd, int rows, int cols, int pges, double dx, double dy, double dz,
+                           int num_ele, vsl_stream_t stream)
+{
+    if (any_null(step, deltat, lsf, vx, vy, vz, xpr, xpl, ypf, ypb, zpu, zpd, cpr, cpl, cpf, cpb, cpu, cpd))
+        return VSL_ERR_NULL;
+    if (int st = prologue(rows, cols, pges, dx, dy, dz, num_ele, true)) return st;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    CFields6 v = {{vx, vy, vz, nullptr, nullptr, nullptr}};
+    CFields6 d = {{xpr, xpl, ypf, ypb, zpu, zpd}};
+    CFields6 cp = {{cpr, cpl, cpf, cpb, cpu, cpd}};
+    k_enork2_extend_step<<<node_grid(g), dim3(BX, BY), 0, stream>>>(step, deltat, lsf, v, d, cp, g);
+    return launch_status(cudaGetLastError());
 }
 
 int vsl_set_calculus_toolbox(double *Fx, double *Fy, double *Fz, double *FGradMag, double *Nx, double *Ny,

@@ -192,6 +192,15 @@ class SDF3:
                    ws.numel(), _stream())
         return out
 
+    def ENORK2Reinitialization(self, F, iteration: int):
+        """ENORK2Reinitialization.m:3-45: quadratic-ENO distances recomputed from F, Heun RK2
+        pseudo-steps with the second-order ENO Godunov Hamiltonian."""
+        out = self._field(F).clone()
+        ws = self.workspace("reinit_enork2")
+        lib().call(self._fn("vsl_enork2_reinitialization"), _ptr(out), int(iteration), *self.GD3.args(), _ptr(ws),
+                   ws.numel(), _stream())
+        return out
+
     # -- extension ---------------------------------------------------------------------------
     def WENO5RK3Extend(self, C, iteration: int):
         """WENO5RK3Extend.m:9-76."""
@@ -207,6 +216,15 @@ class SDF3:
         ws = self.workspace("extend_eno3")
         lib().call(self._fn("vsl_wenork3_extend"), _ptr(out), int(iteration), _ptr(self.F), *self.GD3.args(), _ptr(ws),
                    ws.numel(), _stream())
+        return out
+
+    def ENORK2Extend(self, C, iteration: int):
+        """ENORK2Extend.m:9-81: C extended off the zero set of self.F (quadratic-ENO distances
+        and ENO upwind normals of F, quadratic crossing values of C, Heun RK2)."""
+        out = self._field(C).clone()
+        ws = self.workspace("extend_enork2")
+        lib().call(self._fn("vsl_enork2_extend"), _ptr(out), int(iteration), _ptr(self.F), *self.GD3.args(),
+                   _ptr(ws), ws.numel(), _stream())
         return out
 
     # -- surface redistance -------------------------------------------------------------------

@@ -109,6 +109,40 @@ int vsl_extend_step_eno3(double *step, const double *deltat, const double *lsf, 
                          const double *cpd, int rows, int cols, int pges, double dx, double dy, double dz,
                          int num_ele, vsl_stream_t stream);
 
+/* ---- ENORK2: second-order ENO with the sub-cell fix (Min 2010), Heun RK2 -----------
+ * The kernels of CUDA_Code/1_0_ENORK2_Reinitialization/boundary_correction.cu and
+ * CUDA_Code/2_0_ENORK2_Extend/enork2_extend.cu (the MATLAB objects ENORK2_*), FP64. */
+
+/* ref: boundary_correction.cu:104 (boundary_correction).  Quadratic-ENO distance at every
+ * crossed edge; entries without a crossing keep the caller's value (pre-fill with the
+ * spacing, as ENORK2Reinitialization.m:10-15 does). */
+int vsl_enork2_boundary_correction(double *xpr, double *xpl, double *ypf, double *ypb, double *zpu, double *zpd,
+                                   const double *lsf, int num_ele, int rows, int cols, int pges, double dx,
+                                   double dy, double dz, vsl_stream_t stream);
+/* ref: boundary_correction.cu:148 (re_step).  No fixed-node test. */
+int vsl_enork2_re_step(double *step, const double *lsf, const bool *mask, const double *deltat, const double *xpr,
+                       const double *xpl, const double *ypf, const double *ypb, const double *zpu, const double *zpd,
+                       int rows, int cols, int pges, double dx, double dy, double dz, int num_ele,
+                       vsl_stream_t stream);
+/* ref: enork2_extend.cu:103 (upwind_normal). */
+int vsl_enork2_upwind_normal(double *nx, double *ny, double *nz, const double *lsf, const double *xpr,
+                             const double *xpl, const double *ypf, const double *ypb, const double *zpu,
+                             const double *zpd, int rows, int cols, int pges, double dx, double dy, double dz,
+                             int num_ele, vsl_stream_t stream);
+/* ref: enork2_extend.cu:175 (boundary_interpolate).  Every entry is written (0 where the
+ * cell is not cut). */
+int vsl_enork2_boundary_interpolate(double *cpr, double *cpl, double *cpf, double *cpb, double *cpu, double *cpd,
+                                    const double *xpr, const double *xpl, const double *ypf, const double *ypb,
+                                    const double *zpu, const double *zpd, const double *lsf, int rows, int cols,
+                                    int pges, double dx, double dy, double dz, int num_ele, vsl_stream_t stream);
+/* ref: enork2_extend.cu:214 (extend_step).  No fixed-node test. */
+int vsl_enork2_extend_step(double *step, const double *deltat, const double *lsf, const double *vx, const double *vy,
+                           const double *vz, const double *xpr, const double *xpl, const double *ypf,
+                           const double *ypb, const double *zpu, const double *zpd, const double *cpr,
+                           const double *cpl, const double *cpf, const double *cpb, const double *cpu,
+                           const double *cpd, int rows, int cols, int pges, double dx, double dy, double dz,
+                           int num_ele, vsl_stream_t stream);
+
 /* ref: CUDA_Code/4_0_Calculus_ToolBox/set_calculus_toolbox.cu:9-107 (set_calculus_toolbox) */
 int vsl_set_calculus_toolbox(double *Fx, double *Fy, double *Fz, double *FGradMag, double *Nx, double *Ny,
                              double *Nz, double *Fxx, double *Fyy, double *Fzz, double *Fxy, double *Fyz,
@@ -144,7 +178,9 @@ enum {
     VSL_OP_VESICLE_STEP = 8,
     VSL_OP_SET_DISTANCE = 9,
     VSL_OP_ADVECTION_ADJOINT = 10,
-    VSL_OP_REINIT_ADJOINT = 11
+    VSL_OP_REINIT_ADJOINT = 11,
+    VSL_OP_REINIT_ENORK2 = 12,
+    VSL_OP_EXTEND_ENORK2 = 13
 };
 
 /* Tuning of the FP32 tiled stage kernels (no counterpart in the reference).  Each block
@@ -266,6 +302,21 @@ int vsl_vesicle_step_f32(float *F, float *xpr, float *xpl, float *ypf, float *yp
                          int ext_iters, int reinit_iters, double cfl, double *info, int rows, int cols, int pges,
                          double dx, double dy, double dz, void *workspace, size_t workspace_bytes,
                          vsl_stream_t stream);
+
+/* ref: +SD/@SDF3/ENORK2Reinitialization.m:3-45.  Quadratic-ENO distances recomputed from
+ * F, then `iteration` Heun RK2 pseudo-steps F1 = F - step(F), F = (F + F1 - step(F1)) / 2
+ * with the mask and dt = 0.3 min(distances) of F at the start. */
+int vsl_enork2_reinitialization_f64(double *F, int iteration, int rows, int cols, int pges, double dx, double dy,
+                                    double dz, void *workspace, size_t workspace_bytes, vsl_stream_t stream);
+int vsl_enork2_reinitialization_f32(float *F, int iteration, int rows, int cols, int pges, double dx, double dy,
+                                    double dz, void *workspace, size_t workspace_bytes, vsl_stream_t stream);
+/* ref: +SD/@SDF3/ENORK2Extend.m:9-81.  C extended off the zero set of F: quadratic-ENO
+ * distances of F, ENO upwind normals v = sign(F) n / max(|n|, 1e-6), quadratic crossing
+ * values of C, `iteration` Heun RK2 pseudo-steps. */
+int vsl_enork2_extend_f64(double *C, int iteration, const double *F, int rows, int cols, int pges, double dx,
+                          double dy, double dz, void *workspace, size_t workspace_bytes, vsl_stream_t stream);
+int vsl_enork2_extend_f32(float *C, int iteration, const float *F, int rows, int cols, int pges, double dx, double dy,
+                          double dz, void *workspace, size_t workspace_bytes, vsl_stream_t stream);
 
 /* ---- adjoints (no counterpart in the reference, which has no derivatives) -------------
  *
