@@ -56,6 +56,7 @@ for _suf in ("f64", "f32"):
             f"vsl_vesicle_step_{_suf}": "p" + "pppppp" + "iid" + "p" + _G + "pz" + "s",
             f"vsl_enork2_reinitialization_{_suf}": "pi" + _G + "pz" + "s",
             f"vsl_enork2_extend_{_suf}": "pip" + _G + "pz" + "s",
+            f"vsl_enork2_surface_redistance_{_suf}": "piip" + _G + "pz" + "s",
             f"vsl_weno5_rk3_advection_adjoint_{_suf}": "ppppp" + "pppp" + _G + "pz" + "s",
             f"vsl_weno5_rk3_reinitialization_adjoint_{_suf}": "pipp" + _G + "pz" + "s",
         }
@@ -75,6 +76,7 @@ OP = {
     "reinit_adjoint": 11,
     "reinit_enork2": 12,
     "extend_enork2": 13,
+    "surface_redistance_enork2": 14,
 }
 
 

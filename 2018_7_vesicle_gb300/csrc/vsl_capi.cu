@@ -190,6 +190,7 @@ size_t measure(int op, const Grid &g, int elem)
         case VSL_OP_REINIT_ADJOINT: carve_adj<T>(w, g, true); break;
         case VSL_OP_REINIT_ENORK2: carve_reinit<T>(w, g, true); break;
         case VSL_OP_EXTEND_ENORK2: carve_extend<T>(w, g, true); break;
+        case VSL_OP_SURFACE_REDISTANCE_ENORK2: carve_redist<T>(w, g); break;
         default: return false;
         }
         return true;
@@ -588,6 +589,51 @@ int op_extend_enork2(T *C, int iteration, const T *F, int rows, int cols, int pg
     return VSL_OK;
 }
 
+// crossing values of C, then `iters` Heun RK2 extension steps of C in place
+template <typename T>
+int enork2_extend_loop(T *C, int iters, Ptr6<const T> d, ExtendWork<T> &w, const Grid &g, cudaStream_t s)
+{
+    VSL_TRY(launch_enork2_crossing<T>(C, d, w.cp, w.flagged, g, s));
+    const Ptr6<const T> cp = cview(w.cp);
+    const Ptr3<const T> v = cview3(w.v);
+    for (int it = 0; it < iters; ++it) {
+        VSL_TRY(launch_enork2_extend_stage<T>(C, C, w.b, w.flags, d, cp, v, g, 0, s));
+        VSL_TRY(launch_enork2_extend_stage<T>(w.b, C, C, w.flags, d, cp, v, g, 1, s));
+    }
+    return VSL_OK;
+}
+
+// ENORK2ClosetPointSurfaceRedistance.m:4-128
+template <typename T>
+int op_redistance_enork2(T *A, int iter1, int iter2, const T *F, int rows, int cols, int pges, double dx, double dy,
+                         double dz, void *ws, size_t bytes, cudaStream_t s)
+{
+    if (any_null(A, F)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    if (iter1 < 0 || iter2 < 0) return VSL_ERR_VALUE;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    if (int st = check_ws(VSL_OP_SURFACE_REDISTANCE_ENORK2, g, sizeof(T), ws, bytes)) return st;
+    Bump b(ws);
+    RedistWork<T> w = carve_redist<T>(b, g);
+    // A's distances, mask and pseudo time step (reinitialization)
+    VSL_TRY(launch_set_distance_eno2<T>(A, w.re.dist, g, w.re.edges, s));
+    const Ptr6<const T> dA = cview(w.re.dist);
+    VSL_TRY(launch_classify<T>(A, dA, w.re.flags, NodeList{nullptr, nullptr}, g, s));
+    // F's distances, normals (floor 1e-14) and pseudo time step (extensions)
+    VSL_TRY(launch_set_distance_eno2<T>(F, w.ext.dist, g, w.ext.edges, s));
+    const Ptr6<const T> dF = cview(w.ext.dist);
+    VSL_TRY(launch_enork2_velocity<T>(F, dF, w.ext.v, g, 1e-14, s));
+    VSL_TRY(launch_classify<T>(F, dF, w.ext.flags, w.ext.flagged, g, s));
+    T *t = w.re.b;
+    for (int it = 0; it < iter1; ++it) {
+        if (int st = enork2_extend_loop<T>(A, iter2, dF, w.ext, g, s)) return st;
+        VSL_TRY(launch_enork2_reinit_stage<T>(A, A, t, w.re.flags, dA, g, 0, s));
+        if (int st = enork2_extend_loop<T>(t, iter2, dF, w.ext, g, s)) return st;
+        VSL_TRY(launch_enork2_reinit_stage<T>(t, A, A, w.re.flags, dA, g, 2, s));
+    }
+    return enork2_extend_loop<T>(A, iter2, dF, w.ext, g, s);
+}
+
 // ---------------------------------------------------------------------------------------
 // adjoints (no counterpart in the reference)
 // ---------------------------------------------------------------------------------------
@@ -813,6 +859,12 @@ size_t vsl_workspace_bytes(int op, int rows, int cols, int pges, int elem_bytes)
                                 double dy, double dz, void *ws, size_t bytes, vsl_stream_t stream)                 \
     {                                                                                                              \
         return op_extend_enork2<T>(C, iteration, F, rows, cols, pges, dx, dy, dz, ws, bytes, stream);              \
+    }                                                                                                              \
+    int vsl_enork2_surface_redistance_##SUF(T *A, int iter1, int iter2, const T *F, int rows, int cols, int pges,   \
+                                            double dx, double dy, double dz, void *ws, size_t bytes,                \
+                                            vsl_stream_t stream)                                                    \
+    {                                                                                                              \
+        return op_redistance_enork2<T>(A, iter1, iter2, F, rows, cols, pges, dx, dy, dz, ws, bytes, stream);        \
     }                                                                                                              \
     int vsl_weno5_rk3_advection_adjoint_##SUF(const T *F, const T *vx, const T *vy, const T *vz, const double *dt, \
                                               T *lam, T *gvx, T *gvy, T *gvz, int rows, int cols, int pges,        \

@@ -383,12 +383,18 @@ __global__ void __launch_bounds__(BX *BY) k_advect_stage(const T *__restrict__ p
 // and ENORK2Extend.m:9-81 over the kernels of boundary_correction.cu and enork2_extend.cu.
 // The fused stage writes
 //   stage 0: out = phi_s - step(phi_s)
-//   stage 1: out = (phi_n + phi_s - step(phi_s)) / 2
-// the elementwise updates of the MATLAB loops.  There is no fixed-node test.
+//   stage 1: out = (phi_n + phi_s - step(phi_s)) / 2      (the reinitialization and
+//            extension loops)
+//   stage 2: out = (phi_n + (phi_s - step(phi_s))) / 2    (the closest-point surface
+//            redistance, ENORK2ClosetPointSurfaceRedistance.m:96-100)
+// the elementwise updates of the MATLAB loops in their rounding order.  There is no
+// fixed-node test.
 // ---------------------------------------------------------------------------------------
 template <typename T> __device__ __forceinline__ T rk2_combine(int stage, T phi_n, T phi_s, T step)
 {
-    return stage == 0 ? phi_s - step : (phi_n + phi_s - step) / T(2);
+    if (stage == 0) return phi_s - step;
+    if (stage == 1) return (phi_n + phi_s - step) / T(2);
+    return (phi_n + (phi_s - step)) / T(2);
 }
 
 // one quadratic-ENO root per listed crossed edge (k_dist_roots with the ENORK2 distance)

@@ -236,6 +236,14 @@ class SDF3:
                    *self.GD3.args(), _ptr(ws), ws.numel(), _stream())
         return out
 
+    def ENORK2ClosetPointSurfaceRedistance(self, A, iter1: int, iter2: int):
+        """ENORK2ClosetPointSurfaceRedistance.m:4-128 (second-order ENO, Heun RK2)."""
+        out = self._field(A).clone()
+        ws = self.workspace("surface_redistance_enork2")
+        lib().call(self._fn("vsl_enork2_surface_redistance"), _ptr(out), int(iter1), int(iter2), _ptr(self.F),
+                   *self.GD3.args(), _ptr(ws), ws.numel(), _stream())
+        return out
+
     # -- calculus toolbox and integrals ----------------------------------------------------
     def GPUsetCalculusToolBox(self):
         """GPUsetCalculusToolBox.m:2-42: the 18 toolbox fields (computed in FP64)."""

@@ -180,7 +180,8 @@ enum {
     VSL_OP_ADVECTION_ADJOINT = 10,
     VSL_OP_REINIT_ADJOINT = 11,
     VSL_OP_REINIT_ENORK2 = 12,
-    VSL_OP_EXTEND_ENORK2 = 13
+    VSL_OP_EXTEND_ENORK2 = 13,
+    VSL_OP_SURFACE_REDISTANCE_ENORK2 = 14
 };
 
 /* Tuning of the FP32 tiled stage kernels (no counterpart in the reference).  Each block
@@ -317,6 +318,16 @@ int vsl_enork2_extend_f64(double *C, int iteration, const double *F, int rows, i
                           double dy, double dz, void *workspace, size_t workspace_bytes, vsl_stream_t stream);
 int vsl_enork2_extend_f32(float *C, int iteration, const float *F, int rows, int cols, int pges, double dx, double dy,
                           double dz, void *workspace, size_t workspace_bytes, vsl_stream_t stream);
+/* ref: +SD/@SDF3/ENORK2ClosetPointSurfaceRedistance.m:4-128.  A is redistanced in place
+ * on the zero set of F: iter1 Heun RK2 steps with A's quadratic-ENO distances, each
+ * stage preceded by iter2 ENORK2 extension steps of its input off F (normals with a
+ * 1e-14 floor), and a final extension. */
+int vsl_enork2_surface_redistance_f64(double *A, int iter1, int iter2, const double *F, int rows, int cols, int pges,
+                                      double dx, double dy, double dz, void *workspace, size_t workspace_bytes,
+                                      vsl_stream_t stream);
+int vsl_enork2_surface_redistance_f32(float *A, int iter1, int iter2, const float *F, int rows, int cols, int pges,
+                                      double dx, double dy, double dz, void *workspace, size_t workspace_bytes,
+                                      vsl_stream_t stream);
 
 /* ---- adjoints (no counterpart in the reference, which has no derivatives) -------------
  *

@@ -402,6 +402,48 @@ def surface_redistance(K, g: Grid, F, A, iter1: int, iter2: int):
     return ext(new)
 
 
+def surface_redistance_enork2(K, g: Grid, F, A, iter1: int, iter2: int):
+    """ENORK2ClosetPointSurfaceRedistance(A, iter1, iter2)
+    (V/+SD/@SDF3/ENORK2ClosetPointSurfaceRedistance.m:4-128): A's quadratic-ENO distances,
+    mask and dt for the reinitialization; F's distances, ENO upwind normals (floor 1e-14)
+    and dt for the extensions, whose crossing values are taken from each input."""
+    A = F64(A).copy(order="F")
+    dA = set_distance_enork2(K, g, A)
+    deltat = F64(0.3 * dA.min_dist)
+    mask = np.asfortranarray(A < 0)
+    dF = set_distance_enork2(K, g, F)
+    fdeltat = F64(0.3 * dF.min_dist)
+    v = extension_velocity(K, g, F, dF, floor=1e-14, enork2=True)
+    step = zeros(g)
+
+    def ext(C):
+        cp = [zeros(g) for _ in range(6)]
+        K.enork2_boundary_interpolate(*cp, *dF.six(), F64(C), *g.args(), g.num_ele)
+        st = zeros(g)
+
+        def stage(Cs):
+            K.enork2_extend_step(st, fdeltat, F64(Cs), *v, *dF.six(), *cp, *g.args(), g.num_ele)
+            return st.copy(order="F")
+
+        C = F64(C).copy(order="F")
+        for _ in range(iter2):
+            C = F64(_rk2(C, stage))
+        return C
+
+    def re(Cs):
+        K.enork2_re_step(step, F64(Cs), mask, deltat, *dA.six(), *g.args(), g.num_ele)
+        return step.copy(order="F")
+
+    new = A
+    for _ in range(iter1):
+        new = ext(new)
+        t = new - re(new)
+        t = ext(t)
+        t2 = t - re(t)
+        new = F64((new + t2) / 2)
+    return ext(new)
+
+
 # ---------------------------------------------------------------------------------------
 # calculus toolbox and reductions: V/+SD/@SDF3/GPUsetCalculusToolBox.m:2-42, SDF3.m:73-85
 # ---------------------------------------------------------------------------------------

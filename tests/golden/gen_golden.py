@@ -145,6 +145,7 @@ def run_case(K, name, x, y, z, F, C):
         rec[f"cross2_{nm}"] = a
     rec["reinit2_it4"] = O.reinit_enork2(K, g, F, 4)
     rec["extend2_it3"] = O.extend_enork2(K, g, F, C, 3)
+    rec["redistance2_2_2"] = O.surface_redistance_enork2(K, g, F, C, 2, 2)
     rec["area"] = np.array(O.cal_area(g, F, tb["DiracDelta"]))
     rec["volume"] = np.array(O.cal_volume(g, F, tb["Heaviside"]))
     return rec

@@ -4,8 +4,10 @@ ENORK2Reinitialization.m / ENORK2Extend.m) on the GPU.
 
 * FP64 drop-in kernels against the golden fixtures of the reference's own kernels
   (1e-12 relative per grid value);
-* the fused FP64 methods bit-identical to the oracle built with integer powers rounded
-  once, and within 1e-12 of the golden loop outputs and of the oracle with libm's pow;
+* the fused FP64 methods (reinitialization, extension, closest-point surface
+  redistance) bit-identical to the oracle built with integer powers rounded once, and
+  within 1e-12 of the golden loop outputs and of the oracle with libm's pow (1e-10 for
+  the redistance, whose 1e-14 normal floor amplifies one-ulp pow differences);
 * the FP32 form against the FP64 oracle: reinitialization within 1e-5 dx over the band
   |phi| < 3 dx, extension within 5e-5 relative to the field's scale.
 GPU only; calls go through the C ABI."""
@@ -91,6 +93,10 @@ def test_golden_loops(golden, pkg, oracle_mod):
     got = host(m.ENORK2Extend(dev(Cn), 3))
     assert same(got, O.extend_enork2(KC, g, F, Cn, 3))
     assert max_rel(got, G["extend2_it3"]) <= TOL and max_rel(got, O.extend_enork2(K, g, F, Cn, 3)) <= TOL
+    got = host(m.ENORK2ClosetPointSurfaceRedistance(dev(Cn), 2, 2))
+    assert same(got, O.surface_redistance_enork2(KC, g, F, Cn, 2, 2))
+    # the 1e-14 normal floor amplifies one-ulp differences of libm's pow (see test_gpu_methods)
+    assert max_rel(got, G["redistance2_2_2"]) <= 1e-10
 
 
 @pytest.fixture(scope="module")

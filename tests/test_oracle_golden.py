@@ -129,3 +129,4 @@ def test_enork2(case):
         close(a, G[f"cross2_{nm}"])
     close(O.reinit_enork2(K, g, F, 4), G["reinit2_it4"])
     close(O.extend_enork2(K, g, F, C, 3), G["extend2_it3"])
+    close(O.surface_redistance_enork2(K, g, F, C, 2, 2), G["redistance2_2_2"])

@@ -43,3 +43,5 @@ def test_bit_identical_on_seeded_inputs(both, seed):
                                                      O.set_distance_enork2(R, g, F).six()))
     assert np.array_equal(O.reinit_enork2(P, g, F, 3), O.reinit_enork2(R, g, F, 3))
     assert np.array_equal(O.extend_enork2(P, g, F, C, 3), O.extend_enork2(R, g, F, C, 3))
+    assert np.array_equal(O.surface_redistance_enork2(P, g, F, C, 2, 2),
+                          O.surface_redistance_enork2(R, g, F, C, 2, 2))
