@@ -27,6 +27,7 @@ FILE_FLAGS = {
     # The mixed form's FP32 stencils use the hardware-approximate quotient and square root
     # (FP64 code in the same file keeps IEEE division and square root).
     "vsl_fused_f32.cu": ["-prec-div=false", "-prec-sqrt=false"],
+    "vsl_toolbox_f32.cu": ["-prec-div=false", "-prec-sqrt=false"],
 }
 
 

@@ -276,8 +276,8 @@ template <typename T>
 int extend_setup(const T *F, Ptr6<const T> d, const ExtendWork<T> &w, const Grid &g, bool eno3, double floor,
                  cudaStream_t s)
 {
-    VSL_TRY(launch_extension_velocity<T>(F, d, w.v, g, eno3, floor, s));
     VSL_TRY(launch_classify<T>(F, d, w.flags, w.flagged, g, s));
+    VSL_TRY(launch_extension_velocity<T>(F, w.flags, d, w.v, g, eno3, floor, s));
     return VSL_OK;
 }
 

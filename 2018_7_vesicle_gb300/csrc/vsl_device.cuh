@@ -694,6 +694,30 @@ __device__ __forceinline__ void weno5_pair_fast2(const float p[7], float inv_h, 
     d_fore = d.y;
 }
 
+// Upwind WENO5 derivatives of two lines as the two lanes of one packed evaluation: lane
+// .x takes the backward derivative of line a where back_a holds and its forward derivative
+// (the mirrored window) otherwise, lane .y the same for line b.  For a transport term
+// min(0,v) D+ + max(0,v) D- only the derivative on the upwind side is ever multiplied by
+// a nonzero speed, so one lane per axis replaces the pair.
+__device__ __forceinline__ float2 weno5_upwind2(const float pa[7], bool back_a, const float pb[7], bool back_b,
+                                                float2 inv_h, float2 eps2)
+{
+    float ua[6], ub[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) {
+        ua[m] = pa[m + 1] - pa[m];
+        ub[m] = pb[m + 1] - pb[m];
+    }
+    // backward window u0..u4, forward window u5..u1
+    float2 U[5];
+#pragma unroll
+    for (int m = 0; m < 5; ++m) U[m] = f2(back_a ? ua[m] : ua[5 - m], back_b ? ub[m] : ub[5 - m]);
+    float2 q1, q2, q3, r1, r2, r3;
+    weno5_candidates2(U[0], U[1], U[2], U[3], U[4], q1, q2, q3);
+    weno5_weights2(U[0], U[1], U[2], U[3], U[4], eps2, r1, r2, r3);
+    return mul2(weno5_combine2(q1, q2, q3, r1, r2, r3), inv_h);
+}
+
 // Crossing values for the mixed-precision form: the same interpolating polynomials
 // (degree 5 through six nodes, or the cubic through four) evaluated in FP32 in Lagrange
 // product form with the equispaced denominators folded into constants, at the normalised

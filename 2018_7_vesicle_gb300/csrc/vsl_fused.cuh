@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(BX *BY) k_dist_scan(const T *__restrict__ f, P
     const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y, k = blockIdx.z;
     const bool in = i < g.rows && j < g.cols;
     const long long c = in ? node_index(g, i, j, k) : 0;
-    const double f0 = in ? (double)__ldg(f + c) : 0.0;
+    const T f0 = in ? __ldg(f + c) : T(0);
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax) {
         bool cross = false;
@@ -118,8 +118,13 @@ __global__ void __launch_bounds__(BX *BY) k_dist_scan(const T *__restrict__ f, P
             const T h = (T)axis_h(g, ax);
             d.p[2 * ax][c] = h;
             d.p[2 * ax + 1][c] = h;
-            const double fn = (double)__ldg(f + L.base + (long long)clampi(L.c + 1, L.n) * L.stride);
-            cross = f0 * fn < 0;
+            const T fn = __ldg(f + L.base + (long long)clampi(L.c + 1, L.n) * L.stride);
+            // the reference's test f0 * fn < 0 in FP64; for FP32 inputs the FP64 product of
+            // two nonzero values never underflows, so it is exactly the sign test below
+            if constexpr (std::is_same<T, float>::value)
+                cross = (f0 > T(0) && fn < T(0)) || (f0 < T(0) && fn > T(0));
+            else
+                cross = f0 * fn < 0;
         }
         warp_append(cross, (unsigned)c, e.idx[ax], e.count + ax);
     }
@@ -220,24 +225,32 @@ __global__ void __launch_bounds__(BX *BY) k_reinit_stage(const T *__restrict__ p
 // upwind_normal.cu:4-104 (WENORK3: wenork3_extend.cu:192-292) and the normalisation of
 // WENO5RK3Extend.m:23-31
 // ---------------------------------------------------------------------------------------
+// The classification byte says which distances differ from the spacing (only those are
+// read); away from the interface the mixed form takes the packed fast WENO5 pair.
 template <typename T, bool ENO3>
-__global__ void __launch_bounds__(BX *BY) k_extension_velocity(const T *__restrict__ phi, Ptr6<const T> d, Ptr3<T> v,
-                                                                 Grid g, T floor)
+__global__ void __launch_bounds__(BX *BY) k_extension_velocity(const T *__restrict__ phi,
+                                                                 const uint8_t *__restrict__ flags, Ptr6<const T> d,
+                                                                 Ptr3<T> v, Grid g, T floor)
 {
     int i, j, k;
     if (!fused_node(g, i, j, k)) return;
     const long long c = node_index(g, i, j, k);
+    const uint8_t fl = __ldg(flags + c);
     T n[3];
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax) {
         T p[7], df, db;
         load_line7(phi, axis_line(g, i, j, k, ax), p);
         const T h = (T)axis_h(g, ax);
-        const T r1 = __ldg(d.p[2 * ax] + c), l1 = __ldg(d.p[2 * ax + 1] + c);
-        if (r1 < h || l1 < h)
+        const T r1 = flagged_distance(fl, 2 * ax, d, c, h), l1 = flagged_distance(fl, 2 * ax + 1, d, c, h);
+        if (r1 < h || l1 < h) {
             interface_pair(p, r1, l1, h, T(0), T(0), ENO3, df, db);
-        else
-            weno5_pair_plain(p, h, df, db);
+        } else {
+            if constexpr (std::is_same<T, float>::value)
+                weno5_pair_fast2(p, 1.0f / h, 1e-6f * h * h, df, db);
+            else
+                weno5_pair_plain(p, h, df, db);
+        }
         n[ax] = (fabs(p[4]) < fabs(p[2])) ? df : db;
     }
     const T grad = vmax(sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]), floor);
@@ -576,13 +589,13 @@ cudaError_t launch_reinit_stage(const T *phi_s, const T *phi_n, T *out, const ui
 }
 
 template <typename T>
-cudaError_t launch_extension_velocity(const T *phi, Ptr6<const T> dist, Ptr3<T> v, const Grid &g, bool eno3,
-                                      double floor, cudaStream_t s)
+cudaError_t launch_extension_velocity(const T *phi, const uint8_t *flags, Ptr6<const T> dist, Ptr3<T> v, const Grid &g,
+                                      bool eno3, double floor, cudaStream_t s)
 {
     if (eno3)
-        k_extension_velocity<T, true><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, dist, v, g, (T)floor);
+        k_extension_velocity<T, true><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, flags, dist, v, g, (T)floor);
     else
-        k_extension_velocity<T, false><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, dist, v, g, (T)floor);
+        k_extension_velocity<T, false><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, flags, dist, v, g, (T)floor);
     return cudaGetLastError();
 }
 
@@ -676,8 +689,8 @@ cudaError_t launch_enork2_extend_stage(const T *c_s, const T *c_n, T *out, const
                                             cudaStream_t);                                                          \
     template cudaError_t launch_reinit_stage<T>(const T *, const T *, T *, const uint8_t *, Ptr6<const T>,          \
                                                 const Grid &, int, bool, bool, cudaStream_t);                       \
-    template cudaError_t launch_extension_velocity<T>(const T *, Ptr6<const T>, Ptr3<T>, const Grid &, bool,        \
-                                                      double, cudaStream_t);                                        \
+    template cudaError_t launch_extension_velocity<T>(const T *, const uint8_t *, Ptr6<const T>, Ptr3<T>,           \
+                                                      const Grid &, bool, double, cudaStream_t);                    \
     template cudaError_t launch_crossing<T>(const T *, Ptr6<const T>, Ptr6<T>, NodeList, const Grid &, bool,        \
                                             cudaStream_t);                                                          \
     template cudaError_t launch_extend_stage<T>(const T *, const T *, T *, const uint8_t *, Ptr6<const T>,          \

@@ -178,7 +178,8 @@ __global__ void __launch_bounds__(TY *TX, VSL_TILED_MIN_BLOCKS) k_stage_tiled(Ti
             } else if (compute && KIND == SK_EXTEND) {
                 band = (fl & 0x3F) != 0;
             }
-            if (compute && !band) {
+            if (compute && !band && KIND == SK_REINIT) {
+                // the Godunov norm needs both one-sided derivatives of every axis
                 float dxf, dxb, dyf, dyb;
                 weno5_pair_fast2(px, a.inv_h[0], a.eps2[0], dxf, dxb);
                 weno5_pair_fast2(py, a.inv_h[1], a.eps2[1], dyf, dyb);
@@ -187,18 +188,25 @@ __global__ void __launch_bounds__(TY *TX, VSL_TILED_MIN_BLOCKS) k_stage_tiled(Ti
                 weno5_candidates2(f2(v1, v6), f2(v2, v5), f2(v3, v4), f2(v4, v3), f2(v5, v2), q1, q2, q3);
                 const float2 dz = mul2(weno5_combine2(q1, q2, q3, f2(zr1, nr3), f2(zr2, nr2), f2(zr3, nr1)),
                                        f2s(a.inv_h[2]));
-                const float dzb = dz.x, dzf = dz.y;
-                if (KIND == SK_REINIT) {
-                    const bool neg = fl & MASK_BIT;
-                    const float dtn = (fl & 0x3F) ? pseudo_dt(fl, a.d, c, a.h[0], a.h[1], a.h[2]) : a.dt_uniform;
-                    const float gn = godunov_norm(neg, dxf, dxb, dyf, dyb, dzf, dzb);
-                    step = (gn - 1.f) * dtn * (neg ? -1.f : 1.f);
-                } else if (KIND == SK_EXTEND) {
-                    step = upwind_dot(vx0, vy0, vz0, dxf, dxb, dyf, dyb, dzf, dzb) * a.dt_uniform;
-                } else {
-                    step = (float)__ldg(a.dt) *
-                           upwind_dot(vx0 * sp, vy0 * sp, vz0 * sp, dxf, dxb, dyf, dyb, dzf, dzb);
-                }
+                const bool neg = fl & MASK_BIT;
+                const float dtn = (fl & 0x3F) ? pseudo_dt(fl, a.d, c, a.h[0], a.h[1], a.h[2]) : a.dt_uniform;
+                const float gn = godunov_norm(neg, dxf, dxb, dyf, dyb, dz.y, dz.x);
+                step = (gn - 1.f) * dtn * (neg ? -1.f : 1.f);
+            } else if (compute && !band) {
+                // transport sum_ax min(0,v) D+ + max(0,v) D-: the velocity is fixed, so each
+                // axis needs only its upwind derivative (D- where v > 0); x and y share one
+                // packed evaluation, z reuses the carried window weights
+                const float ux = KIND == SK_ADVECT ? vx0 * sp : vx0;
+                const float uy = KIND == SK_ADVECT ? vy0 * sp : vy0;
+                const float uz = KIND == SK_ADVECT ? vz0 * sp : vz0;
+                const float2 dxy = weno5_upwind2(px, ux > 0.f, py, uy > 0.f, f2(a.inv_h[0], a.inv_h[1]),
+                                                 f2(a.eps2[0], a.eps2[1]));
+                const bool zb = uz > 0.f;
+                const float dz = weno5_with_weights(zb ? v1 : v6, zb ? v2 : v5, zb ? v3 : v4, zb ? v4 : v3,
+                                                    zb ? v5 : v2, zb ? zr1 : nr3, zb ? zr2 : nr2, zb ? zr3 : nr1) *
+                                 a.inv_h[2];
+                const float tr = ux * dxy.x + uy * dxy.y + uz * dz;
+                step = KIND == SK_EXTEND ? tr * a.dt_uniform : (float)__ldg(a.dt) * tr;
             }
             if (!band) a.out[c] = rk3_combine(a.stage, pn, ps - step);
         }
@@ -267,7 +275,8 @@ inline TiledArgs tiled_args(const Grid &g)
     return a;
 }
 
-inline int band_blocks() { return list_blocks(); }
+// the band kernels run latency-bound per-node code: 16 blocks of 128 threads per SM
+inline int band_blocks() { return list_blocks() * 4; }
 
 inline dim3 tiled_grid(const Grid &g, int kz)
 {

@@ -1,0 +1,219 @@
+// vsl_toolbox.cuh -- calculus toolbox fused with the FP64 area/volume reductions and the
+// band maximum of the normal speed, templated on the field type.  Included by
+// vsl_toolbox.cu (the FP64 plain form, compiled without multiply-add contraction so that
+// it rounds like the reference) and vsl_toolbox_f32.cu (the FP32 mixed form, fast
+// division); all reductions in a fixed order (per-block warp-shuffle trees, then one
+// block summing the block partials in index order), so a result is bitwise reproducible
+// for a given grid.
+#pragma once
+
+#include <cmath>
+#include <limits>
+
+#include "vsl_internal.h"
+
+namespace vsl {
+namespace {
+
+constexpr int NT = BX * BY;  // threads per node block
+constexpr int NW = NT / 32;
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__device__ __forceinline__ long long block_linear() { return blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z); }
+
+// set_calculus_toolbox (set_calculus_toolbox.cu:9-107) in the field's precision T (the
+// plain form is FP64 throughout; the mixed form computes these stencils in FP32), with
+// HPrimal = max(F, 0) formed on the fly (GPUsetCalculusToolBox.m:4); per block the FP64
+// sums of DiracDelta over |F| < 2Ds and of 1 - Heaviside over F < 2Ds (SDF3.m:73-80).
+template <typename T> __device__ __forceinline__ T cube(T x);
+template <> __device__ __forceinline__ double cube<double>(double x) { return pow_cr<3>(x); }
+template <> __device__ __forceinline__ float cube<float>(float x) { return x * x * x; }
+template <typename T> __device__ __forceinline__ T fourth(T x);
+template <> __device__ __forceinline__ double fourth<double>(double x) { return pow_cr<4>(x); }
+template <> __device__ __forceinline__ float fourth<float>(float x) { return (x * x) * (x * x); }
+
+// thr2ds: 2 Ds as the smallest T not below it, so that x < thr2ds in T is exactly
+// (double)x < 2 Ds for every x of type T (the reference's FP64 band tests)
+template <typename T>
+__global__ void __launch_bounds__(NT) k_toolbox(const T *__restrict__ f, ToolboxOut<T> o, Grid g, double ds_,
+                                                T thr2ds, double *__restrict__ partials)
+{
+    const int i = blockIdx.x * BX + threadIdx.x;
+    const int j = blockIdx.y * BY + threadIdx.y;
+    const int k = blockIdx.z;
+    double area = 0.0, vol = 0.0;
+    bool unit = false;  // a volume term equal to exactly 1
+    if (i < g.rows && j < g.cols) {
+        const long long c = node_index(g, i, j, k);
+        auto F = [&](int a, int b, int e) { return __ldg(f + clamped_index(g, a, b, e)); };
+        auto H = [&](int a, int b, int e) { return vmax(__ldg(f + clamped_index(g, a, b, e)), T(0)); };
+        const T dx = (T)g.dx, dy = (T)g.dy, dz = (T)g.dz, ds = (T)ds_;
+        const T fc = __ldg(f + c);
+        const T fxp = F(i, j + 1, k), fxm = F(i, j - 1, k), fyp = F(i + 1, j, k), fym = F(i - 1, j, k);
+        const T fzp = F(i, j, k + 1), fzm = F(i, j, k - 1);
+        T fx = (fxp - fxm) / (2 * dx);
+        T fy = (fyp - fym) / (2 * dy);
+        T fz = (fzp - fzm) / (2 * dz);
+        T gm = vmax(sqrt(fx * fx + fy * fy + fz * fz), T(1e-14));
+        T fxx = (fxp - 2 * fc + fxm) / (dx * dx);
+        T fyy = (fyp - 2 * fc + fym) / (dy * dy);
+        T fzz = (fzp - 2 * fc + fzm) / (dz * dz);
+        T fxy = (F(i + 1, j + 1, k) + F(i - 1, j - 1, k) - F(i + 1, j - 1, k) - F(i - 1, j + 1, k)) / (4 * ds * ds);
+        T fyz = (F(i + 1, j, k + 1) + F(i - 1, j, k - 1) - F(i + 1, j, k - 1) - F(i - 1, j, k + 1)) / (4 * ds * ds);
+        T fzx = (F(i, j + 1, k + 1) + F(i, j - 1, k - 1) - F(i, j + 1, k - 1) - F(i, j - 1, k + 1)) / (4 * ds * ds);
+        T lap = fxx + fyy + fzz;
+        T r1 = fxx * fx + fxy * fy + fzx * fz;
+        T r2 = fxy * fx + fyy * fy + fyz * fz;
+        T r3 = fzx * fx + fyz * fy + fzz * fz;
+        T gm2 = gm * gm;
+        T mean = -lap / gm + (fx * r1 + fy * r2 + fz * r3) / cube(gm);
+        const T gm4 = fourth(gm);
+        T hc = vmax(fc, T(0));
+        T hxp = H(i, j + 1, k), hxm = H(i, j - 1, k), hyp = H(i + 1, j, k), hym = H(i - 1, j, k);
+        T hzp = H(i, j, k + 1), hzm = H(i, j, k - 1);
+        T px = (hxp - hxm) / (2 * dx), py = (hyp - hym) / (2 * dy), pz = (hzp - hzm) / (2 * dz);
+        T dot = px * fx + py * fy + pz * fz;
+        T pxx = (hxp - 2 * hc + hxm) / (dx * dx);
+        T pyy = (hyp - 2 * hc + hym) / (dy * dy);
+        T pzz = (hzp - 2 * hc + hzm) / (dz * dz);
+        T plap = pxx + pyy + pzz;
+        T heav = dot / gm2;
+        T delta = plap / gm2 - dot * lap / gm4;
+        if (fabs(fc) < thr2ds) area = (double)delta;
+        if (fc < thr2ds) {
+            // 1 - heav in FP64; heav == 0 (no positive neighbour) gives exactly 1
+            if (heav == T(0)) {
+                unit = true;
+            } else {
+                vol = 1 - (double)heav;
+                if (vol == 1.0) {
+                    unit = true;
+                    vol = 0.0;
+                }
+            }
+        }
+        if (o.f[0]) o.f[0][c] = fx;
+        if (o.f[1]) o.f[1][c] = fy;
+        if (o.f[2]) o.f[2][c] = fz;
+        if (o.f[3]) o.f[3][c] = gm;
+        if (o.f[4]) o.f[4][c] = fx / gm;
+        if (o.f[5]) o.f[5][c] = fy / gm;
+        if (o.f[6]) o.f[6][c] = fz / gm;
+        if (o.f[7]) o.f[7][c] = fxx;
+        if (o.f[8]) o.f[8][c] = fyy;
+        if (o.f[9]) o.f[9][c] = fzz;
+        if (o.f[10]) o.f[10][c] = fxy;
+        if (o.f[11]) o.f[11][c] = fyz;
+        if (o.f[12]) o.f[12][c] = fzx;
+        if (o.f[13]) o.f[13][c] = lap;
+        if (o.f[14]) o.f[14][c] = mean;
+        if (o.f[15]) {
+            T q1 = (fyy * fzz - fyz * fyz) * fx + (fzx * fyz - fxy * fzz) * fy + (fxy * fyz - fzx * fyy) * fz;
+            T q2 = (fyz * fzx - fxy * fzz) * fx + (fxx * fzz - fzx * fzx) * fy + (fzx * fxy - fxx * fyz) * fz;
+            T q3 = (fxy * fyz - fyy * fzx) * fx + (fzx * fxy - fxx * fyz) * fy + (fxx * fyy - fxy * fxy) * fz;
+            o.f[15][c] = (fx * q1 + fy * q2 + fz * q3) / gm4;
+        }
+        if (o.f[16]) o.f[16][c] = heav;
+        if (o.f[17]) o.f[17][c] = delta;
+    }
+    if (!partials) return;
+    // Volume terms equal to exactly 1 (nodes with no positive neighbour) are counted as
+    // integers; only warps holding other terms run the FP64 shuffle tree.  Per block:
+    // partial = (double)count + FP64 tree sum of the rest, in a fixed order.
+    __shared__ double sa[NW], sv[NW];
+    __shared__ int sc[NW];
+    const int t = threadIdx.y * BX + threadIdx.x;
+    const unsigned ones = __ballot_sync(0xffffffffu, unit);
+    if (__any_sync(0xffffffffu, area != 0.0)) area = warp_sum(area);
+    if (__any_sync(0xffffffffu, vol != 0.0)) vol = warp_sum(vol);
+    if ((t & 31) == 0) {
+        sa[t >> 5] = area;
+        sv[t >> 5] = vol;
+        sc[t >> 5] = __popc(ones);
+    }
+    __syncthreads();
+    if (t == 0) {
+        double a = 0.0, v = 0.0;
+        int n = 0;
+        for (int w = 0; w < NW; ++w) {
+            a += sa[w];
+            v += sv[w];
+            n += sc[w];
+        }
+        const long long b = block_linear();
+        partials[2 * b] = a;
+        partials[2 * b + 1] = (double)n + v;
+    }
+}
+
+// per-block max |f| over the band |phi| < band (p00_test_singlephase_relax.m:86-89)
+// In T: the band test against `band` rounded up to T (exactly the FP64 test) and the
+// maximum of |f| (exact: conversion to double is monotonic), converted once per block.
+template <typename T>
+__global__ void __launch_bounds__(NT) k_band_maxabs(const T *__restrict__ f, const T *__restrict__ phi, T band,
+                                                    Grid g, double *__restrict__ partials)
+{
+    const int i = blockIdx.x * BX + threadIdx.x;
+    const int j = blockIdx.y * BY + threadIdx.y;
+    const int k = blockIdx.z;
+    T m = T(0);
+    if (i < g.rows && j < g.cols) {
+        const long long c = node_index(g, i, j, k);
+        if (fabs(__ldg(phi + c)) < band) m = fabs(__ldg(f + c));
+    }
+    __shared__ T s[NW];
+    const int t = threadIdx.y * BX + threadIdx.x;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((t & 31) == 0) s[t >> 5] = m;
+    __syncthreads();
+    if (t == 0) {
+        T r = T(0);
+        for (int w = 0; w < NW; ++w) r = fmax(r, s[w]);
+        partials[block_linear()] = (double)r;
+    }
+}
+
+// the smallest T not below x: x < round_up<T>(x') in T  <=>  (double)x < x'
+template <typename T> T round_up(double x);
+template <> double round_up<double>(double x) { return x; }
+template <> float round_up<float>(double x)
+{
+    float r = (float)x;
+    if ((double)r < x) r = std::nextafter(r, std::numeric_limits<float>::infinity());
+    return r;
+}
+
+}  // namespace
+
+template <typename T>
+cudaError_t launch_toolbox(const T *phi, ToolboxOut<T> out, const Grid &g, double ds, double *partials,
+                           int *nblocks, cudaStream_t s)
+{
+    if (nblocks) *nblocks = toolbox_partial_blocks(g);
+    k_toolbox<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, out, g, ds, round_up<T>(2 * ds), partials);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_band_maxabs(const T *f, const T *phi, double band, const Grid &g, double *partials,
+                               int *nblocks, cudaStream_t s)
+{
+    if (nblocks) *nblocks = toolbox_partial_blocks(g);
+    k_band_maxabs<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(f, phi, round_up<T>(band), g, partials);
+    return cudaGetLastError();
+}
+
+}  // namespace vsl
