@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(TY *TX, VSL_TILED_MIN_BLOCKS) k_stage_tiled(Ti
                 const float dtn = (fl & 0x3F) ? pseudo_dt(fl, a.d, c, a.h[0], a.h[1], a.h[2]) : a.dt_uniform;
                 const float gn = godunov_norm(neg, dxf, dxb, dyf, dyb, dz.y, dz.x);
                 step = (gn - 1.f) * dtn * (neg ? -1.f : 1.f);
-            } else if (compute && !band) {
+            } else if (compute && !band && KIND != SK_REINIT) {
                 // transport sum_ax min(0,v) D+ + max(0,v) D-: the velocity is fixed, so each
                 // axis needs only its upwind derivative (D- where v > 0); x and y share one
                 // packed evaluation, z reuses the carried window weights
