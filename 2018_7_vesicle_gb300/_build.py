@@ -28,6 +28,9 @@ FILE_FLAGS = {
     # (FP64 code in the same file keeps IEEE division and square root).
     "vsl_fused_f32.cu": ["-prec-div=false", "-prec-sqrt=false"],
     "vsl_toolbox_f32.cu": ["-prec-div=false", "-prec-sqrt=false"],
+    "vsl_relax_f64.cu": ["-fmad=false"],
+    "vsl_relax_f32.cu": ["-prec-div=false", "-prec-sqrt=false"],
+    "vsl_spectral.cu": ["-fmad=false"],
 }
 
 
@@ -74,7 +77,9 @@ def build(force: bool = False, extra_flags=()) -> str:
         objs = list(ex.map(lambda s: _compile(s, list(extra_flags)), srcs))
     if _stale(LIB, objs):
         tmp = LIB + ".tmp"
-        r = subprocess.run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs], capture_output=True, text=True)
+        cuda_lib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "lib64")
+        r = subprocess.run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcufft", "-Xlinker", "-rpath," + cuda_lib],
+                           capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")
         os.replace(tmp, LIB)

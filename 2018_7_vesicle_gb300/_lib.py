@@ -57,6 +57,9 @@ for _suf in ("f64", "f32"):
             f"vsl_enork2_reinitialization_{_suf}": "pi" + _G + "pz" + "s",
             f"vsl_enork2_extend_{_suf}": "pip" + _G + "pz" + "s",
             f"vsl_enork2_surface_redistance_{_suf}": "piip" + _G + "pz" + "s",
+            f"vsl_laplacian_{_suf}": "pp" + _G + "s",
+            f"vsl_smooth_bilaplacian_{_suf}": "pppdi" + _G + "pz" + "s",
+            f"vsl_relax_step_{_suf}": "p" + "pppppp" + "dddddd" + "ii" + "p" + _G + "pz" + "s",
             f"vsl_weno5_rk3_advection_adjoint_{_suf}": "ppppp" + "pppp" + _G + "pz" + "s",
             f"vsl_weno5_rk3_reinitialization_adjoint_{_suf}": "pipp" + _G + "pz" + "s",
         }
@@ -77,6 +80,8 @@ OP = {
     "reinit_enork2": 12,
     "extend_enork2": 13,
     "surface_redistance_enork2": 14,
+    "smooth": 15,
+    "relax_step": 16,
 }
 
 

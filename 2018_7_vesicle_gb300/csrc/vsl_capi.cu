@@ -171,6 +171,48 @@ template <typename T> AdjWork<T> carve_adj(Bump &w, const Grid &g, bool reinit)
     return a;
 }
 
+// spectral smoothing: the complex spectrum and cuFFT's work area
+template <typename T> struct SpecWork {
+    void *spec = nullptr;
+    void *work = nullptr;
+    size_t work_bytes = 0;
+};
+template <typename T> SpecWork<T> carve_spec(Bump &w, const Grid &g)
+{
+    SpecWork<T> sp;
+    sp.spec = w.take<T>(2 * g.num);
+    sp.work_bytes = spectral_work_bytes<T>(g);
+    sp.work = w.take<char>((long long)sp.work_bytes);
+    return sp;
+}
+
+// relaxation step: toolbox outputs (H extended in place), bending and normal speeds, the
+// extensions, reductions, setDistance's edge lists, the reinitialization and smoothing
+template <typename T> struct RelaxWork {
+    T *H, *K, *G, *D, *nsb, *vn;
+    ExtendWork<T> ext;
+    ReduceWork red;
+    EdgeLists edges;
+    ReinitWork<T> re;
+    SpecWork<T> spec;
+};
+template <typename T> RelaxWork<T> carve_relax(Bump &w, const Grid &g)
+{
+    RelaxWork<T> r;
+    r.H = w.take<T>(g.num);
+    r.K = w.take<T>(g.num);
+    r.G = w.take<T>(g.num);
+    r.D = w.take<T>(g.num);
+    r.nsb = w.take<T>(g.num);
+    r.vn = w.take<T>(g.num);
+    r.ext = carve_extend<T>(w, g, true);
+    r.red = carve_reduce(w, g, 4);
+    r.edges = carve_edges(w, g);
+    r.re = carve_reinit<T>(w, g, false);
+    r.spec = carve_spec<T>(w, g);
+    return r;
+}
+
 size_t measure(int op, const Grid &g, int elem)
 {
     Bump w(nullptr);
@@ -191,6 +233,12 @@ size_t measure(int op, const Grid &g, int elem)
         case VSL_OP_REINIT_ENORK2: carve_reinit<T>(w, g, true); break;
         case VSL_OP_EXTEND_ENORK2: carve_extend<T>(w, g, true); break;
         case VSL_OP_SURFACE_REDISTANCE_ENORK2: carve_redist<T>(w, g); break;
+        case VSL_OP_SMOOTH: {
+            SpecWork<T> sp = carve_spec<T>(w, g);
+            if (sp.work_bytes == 0 && g.num > 0) w.take<char>(1);  // plan creation failed: keep a size
+            break;
+        }
+        case VSL_OP_RELAX_STEP: carve_relax<T>(w, g); break;
         default: return false;
         }
         return true;
@@ -635,6 +683,112 @@ int op_redistance_enork2(T *A, int iter1, int iter2, const T *F, int rows, int c
 }
 
 // ---------------------------------------------------------------------------------------
+// GD3.Laplacian, GD3.smoothGMRES / smoothFFT and the relaxation step of the vesicle driver
+// (p00_test_singlephase_relax.m:60-196)
+// ---------------------------------------------------------------------------------------
+
+template <typename T>
+int op_laplacian(const T *f, T *out, int rows, int cols, int pges, double dx, double dy, double dz, cudaStream_t s)
+{
+    if (any_null(f, out)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    VSL_TRY(launch_laplacian<T>(f, out, make_grid(rows, cols, pges, dx, dy, dz), s));
+    return VSL_OK;
+}
+
+template <typename T>
+int op_smooth(const T *rhs, T *out, const double *dt, double alpha, int exact, int rows, int cols, int pges, double dx,
+              double dy, double dz, void *ws, size_t bytes, cudaStream_t s)
+{
+    if (any_null(rhs, out, dt)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    if (!(alpha >= 0)) return VSL_ERR_VALUE;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    if (int st = check_ws(VSL_OP_SMOOTH, g, sizeof(T), ws, bytes)) return st;
+    Bump b(ws);
+    SpecWork<T> sp = carve_spec<T>(b, g);
+    if (sp.work_bytes == 0 && sp.work == nullptr) return VSL_ERR_CUDA;
+    return launch_smooth_bilaplacian<T>(rhs, out, dt, alpha, exact != 0, g, sp.spec, sp.work, sp.work_bytes, s);
+}
+
+// C extended off the zero set of F by WENORK3Extend (cubic distances of F) or ENORK2Extend
+// (quadratic distances of F), in place
+template <typename T>
+int extend_eno3_inplace(T *C, int iters, const T *F, ExtendWork<T> &w, const Grid &g, cudaStream_t s)
+{
+    VSL_TRY(launch_set_distance<T>(F, w.dist, g, false, w.edges, s));
+    const Ptr6<const T> d = cview(w.dist);
+    if (int st = extend_setup<T>(F, d, w, g, true, 1e-6, s)) return st;
+    return extend_loop<T>(C, iters, d, w, g, true, s);
+}
+
+template <typename T>
+int extend_enork2_inplace(T *C, int iters, const T *F, ExtendWork<T> &w, const Grid &g, cudaStream_t s)
+{
+    VSL_TRY(launch_set_distance_eno2<T>(F, w.dist, g, w.edges, s));
+    const Ptr6<const T> d = cview(w.dist);
+    VSL_TRY(launch_enork2_velocity<T>(F, d, w.v, g, 1e-6, s));
+    VSL_TRY(launch_classify<T>(F, d, w.flags, w.flagged, g, s));
+    return enork2_extend_loop<T>(C, iters, d, w, g, s);
+}
+
+template <typename T>
+int op_relax_step(T *F, T *xpr, T *xpl, T *ypf, T *ypb, T *zpu, T *zpd, double A0, double V0, double kappa,
+                  double spon_c, double cfl, double alpha, int ext_iters, int reinit_iters, double *info, int rows,
+                  int cols, int pges, double dx, double dy, double dz, void *ws, size_t bytes, cudaStream_t s)
+{
+    if (any_null(F, xpr, xpl, ypf, ypb, zpu, zpd, info)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    if (!(cfl > 0) || !(alpha >= 0) || ext_iters < 0 || reinit_iters < 0) return VSL_ERR_VALUE;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    if (int st = check_ws(VSL_OP_RELAX_STEP, g, sizeof(T), ws, bytes)) return st;
+    Bump b(ws);
+    RelaxWork<T> w = carve_relax<T>(b, g);
+    if (w.spec.work_bytes == 0 && w.spec.work == nullptr) return VSL_ERR_CUDA;
+    const double ds = (dx + dy + dz) / 3, ds3 = std::pow(ds, 3);
+    double *area_volume = info, *dt = info + 2, *vmax = info + 3, *mom = info + 4, *tp = info + 8, *ene = info + 10;
+    int nb = 0;
+    // calculus toolbox: mean and Gaussian curvature, |grad F|, DiracDelta; area and volume
+    ToolboxOut<T> tb{};
+    tb.f[3] = w.G;
+    tb.f[14] = w.H;
+    tb.f[15] = w.K;
+    tb.f[17] = w.D;
+    VSL_TRY(launch_toolbox<T>(F, tb, g, ds, w.red.partials, &nb, s));
+    VSL_TRY(launch_sum_partials(w.red.partials, nb, 2, ds3, area_volume, s));
+    // MeanCurvature = WENORK3Extend(MeanCurvature, ext_iters)
+    if (int st = extend_eno3_inplace<T>(w.H, ext_iters, F, w.ext, g, s)) return st;
+    // bending speed, ENORK2-extended
+    VSL_TRY(launch_bending_speed<T>(w.H, w.K, w.nsb, g, kappa, spon_c, s));
+    if (int st = extend_enork2_inplace<T>(w.nsb, ext_iters, F, w.ext, g, s)) return st;
+    // Dt = cfl * Ds / max |NSB| over |F| < 2 Ds
+    VSL_TRY(launch_band_maxabs<T>(w.nsb, F, 2 * ds, g, w.red.partials, &nb, s));
+    VSL_TRY(launch_time_step(w.red.partials, nb, cfl * ds, dt, vmax, s));
+    // tension and pressure
+    VSL_TRY(launch_relax_moments<T>(F, w.H, w.nsb, w.D, w.G, 2 * ds, spon_c, false, g, w.red.partials, &nb, s));
+    VSL_TRY(launch_sum_partials(w.red.partials, nb, 4, ds3, mom, s));
+    VSL_TRY(launch_tension_pressure(mom, area_volume, dt, A0, V0, tp, s));
+    // normal speed, smoothed by (I + alpha Dt L^2)^-1, ENORK2-extended
+    VSL_TRY(launch_normal_speed<T>(w.H, w.nsb, w.G, tp, w.vn, g, s));
+    if (int st = launch_smooth_bilaplacian<T>(w.vn, w.vn, dt, alpha, true, g, w.spec.spec, w.spec.work,
+                                              w.spec.work_bytes, s))
+        return st;
+    if (int st = extend_enork2_inplace<T>(w.vn, ext_iters, F, w.ext, g, s)) return st;
+    // F = F - Dt * v, setDistance
+    VSL_TRY(launch_euler<T>(F, w.vn, dt, g, s));
+    VSL_TRY(launch_set_distance<T>(F, Ptr6<T>{{xpr, xpl, ypf, ypb, zpu, zpd}}, g, true, w.edges, s));
+    // the energy int (H - c0)^2 over the new band (the toolbox's DiracDelta, |grad F|)
+    VSL_TRY(launch_relax_moments<T>(F, w.H, nullptr, w.D, w.G, 2 * ds, spon_c, true, g, w.red.partials, &nb, s));
+    VSL_TRY(launch_sum_partials(w.red.partials, nb, 1, ds3, ene, s));
+    if (reinit_iters > 0) {
+        const Ptr6<const T> d = six<T>(xpr, xpl, ypf, ypb, zpu, zpd);
+        VSL_TRY(launch_classify<T>(F, d, w.re.flags, NodeList{nullptr, nullptr}, g, s));
+        return reinit_loop<T>(F, reinit_iters, d, w.re, g, false, s);
+    }
+    return VSL_OK;
+}
+
+// ---------------------------------------------------------------------------------------
 // adjoints (no counterpart in the reference)
 // ---------------------------------------------------------------------------------------
 
@@ -865,6 +1019,25 @@ size_t vsl_workspace_bytes(int op, int rows, int cols, int pges, int elem_bytes)
                                             vsl_stream_t stream)                                                    \
     {                                                                                                              \
         return op_redistance_enork2<T>(A, iter1, iter2, F, rows, cols, pges, dx, dy, dz, ws, bytes, stream);        \
+    }                                                                                                              \
+    int vsl_laplacian_##SUF(const T *field, T *out, int rows, int cols, int pges, double dx, double dy, double dz, \
+                            vsl_stream_t stream)                                                                   \
+    {                                                                                                              \
+        return op_laplacian<T>(field, out, rows, cols, pges, dx, dy, dz, stream);                                  \
+    }                                                                                                              \
+    int vsl_smooth_bilaplacian_##SUF(const T *rhs, T *out, const double *dt, double alpha, int exact, int rows,    \
+                                     int cols, int pges, double dx, double dy, double dz, void *ws, size_t bytes,  \
+                                     vsl_stream_t stream)                                                          \
+    {                                                                                                              \
+        return op_smooth<T>(rhs, out, dt, alpha, exact, rows, cols, pges, dx, dy, dz, ws, bytes, stream);          \
+    }                                                                                                              \
+    int vsl_relax_step_##SUF(T *F, T *xpr, T *xpl, T *ypf, T *ypb, T *zpu, T *zpd, double A0, double V0,           \
+                             double kappa, double spon_c, double cfl, double alpha, int ext_iters, int reinit_iters, \
+                             double *info, int rows, int cols, int pges, double dx, double dy, double dz, void *ws, \
+                             size_t bytes, vsl_stream_t stream)                                                    \
+    {                                                                                                              \
+        return op_relax_step<T>(F, xpr, xpl, ypf, ypb, zpu, zpd, A0, V0, kappa, spon_c, cfl, alpha, ext_iters,     \
+                                reinit_iters, info, rows, cols, pges, dx, dy, dz, ws, bytes, stream);              \
     }                                                                                                              \
     int vsl_weno5_rk3_advection_adjoint_##SUF(const T *F, const T *vx, const T *vy, const T *vz, const double *dt, \
                                               T *lam, T *gvx, T *gvy, T *gvz, int rows, int cols, int pges,        \

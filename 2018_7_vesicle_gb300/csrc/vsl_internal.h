@@ -91,6 +91,29 @@ template <typename T>
 cudaError_t launch_enork2_extend_stage(const T *c_s, const T *c_n, T *out, const uint8_t *flags, Ptr6<const T> dist,
                                        Ptr6<const T> cp, Ptr3<const T> v, const Grid &g, int stage, cudaStream_t s);
 
+// ---- the relaxation step (vsl_relax.cuh, vsl_spectral.cu), T in {float, double} ------
+template <typename T> cudaError_t launch_laplacian(const T *f, T *out, const Grid &g, cudaStream_t s);
+template <typename T>
+cudaError_t launch_bending_speed(const T *H, const T *K, T *out, const Grid &g, double kappa, double c0,
+                                 cudaStream_t s);
+// per-block partials of the surface integrals over |F| < band: 4 (H^2, H, H NSB, NSB) or,
+// with energy, 1 ((H - c0)^2)
+template <typename T>
+cudaError_t launch_relax_moments(const T *F, const T *H, const T *nsb, const T *delta, const T *gmag, double band,
+                                 double c0, bool energy, const Grid &g, double *partials, int *nblocks, cudaStream_t s);
+cudaError_t launch_tension_pressure(const double *moments, const double *area_volume, const double *dt, double A0,
+                                    double V0, double *tp, cudaStream_t s);
+template <typename T>
+cudaError_t launch_normal_speed(const T *H, const T *nsb, const T *gmag, const double *tp, T *out, const Grid &g,
+                                cudaStream_t s);
+template <typename T> cudaError_t launch_euler(T *F, const T *v, const double *dt, const Grid &g, cudaStream_t s);
+// cuFFT work bytes of a shape (creates the shape's plan on first use; 0 on failure)
+template <typename T> size_t spectral_work_bytes(const Grid &g);
+// out = real(ifftn(fftn(rhs) ./ (1 + alpha dt symbol))); spectrum: num complex elements
+template <typename T>
+int launch_smooth_bilaplacian(const T *rhs, T *out, const double *dt, double alpha, bool exact, const Grid &g,
+                              void *spectrum, void *work, size_t work_bytes, cudaStream_t s);
+
 // ---- tiled FP32 stage kernels (vsl_tiled.cuh, built into vsl_fused_f32.cu) ----------
 // compact queue of the nodes that need the interface-aware stencil, two counters used
 // alternately by consecutive stages (zeroed at the start of an operation)

@@ -108,6 +108,34 @@ class GD3:
         lib().call("vsl_advection_step", _ptr(out), *map(_ptr, v), _ptr(f), *self.args(), _stream())
         return out
 
+    def Laplacian(self, field, precision: str = "f64"):
+        """GD3.Laplacian (GD3.m:344-346): 7-point Laplacian with periodic neighbours."""
+        dtype = _DTYPES[precision]
+        f = as_field(field, dtype)
+        out = colmajor_empty(self.Size, dtype)
+        lib().call(f"vsl_laplacian_{precision}", _ptr(f), _ptr(out), *self.args(), _stream())
+        return out
+
+    def _smooth(self, rhs, Dt, Alpha, exact: int, precision: str):
+        dtype = _DTYPES[precision]
+        f = as_field(rhs, dtype)
+        out = colmajor_empty(self.Size, dtype)
+        dt = Dt if isinstance(Dt, torch.Tensor) else torch.tensor([float(Dt)], dtype=torch.float64, device="cuda")
+        n = lib().workspace_bytes("smooth", *self.Size, 8 if precision == "f64" else 4)
+        ws = torch.empty(max(n, 256), dtype=torch.uint8, device="cuda")
+        lib().call(f"vsl_smooth_bilaplacian_{precision}", _ptr(f), _ptr(out), _ptr(dt), float(Alpha), int(exact),
+                   *self.args(), _ptr(ws), ws.numel(), _stream())
+        return out
+
+    def smoothGMRES(self, rhs, Dt, Alpha, precision: str = "f64"):
+        """GD3.smoothGMRES (GD3.m:436-452): the solution of (I + Alpha Dt L^2) x = rhs, L the
+        periodic 7-point Laplacian, by the exact spectral solve the GMRES iteration approaches."""
+        return self._smooth(rhs, Dt, Alpha, 1, precision)
+
+    def smoothFFT(self, rhs, Dt, Alpha, precision: str = "f64"):
+        """GD3.smoothFFT (GD3.m:455-460): rhs filtered by 1 / (1 + Alpha Dt |k|^4)."""
+        return self._smooth(rhs, Dt, Alpha, 0, precision)
+
     def GPUWENODerivative(self, field):
         """Six one-sided WENO5 derivatives [back_x, fore_x, back_y, fore_y, back_z, fore_z]."""
         f = as_field(field, torch.float64)
@@ -302,6 +330,24 @@ class SDF3:
         ws = self.workspace("vesicle_step")
         lib().call(self._fn("vsl_vesicle_step"), _ptr(self.F), *map(_ptr, self._dist()), int(ext_iters),
                    int(reinit_iters), float(cfl), _ptr(info), *self.GD3.args(), _ptr(ws), ws.numel(), _stream())
+        return info
+
+    def relax_step(self, A0: float, V0: float, kappa: float = 1.0, spon_c: float = 0.0, cfl: float = 0.5,
+                   alpha: float = 0.5, ext_iters: int = 100, reinit_iters: int = 0, info=None) -> torch.Tensor:
+        """One pass of the single-phase relaxation driver's time loop
+        (p00_test_singlephase_relax.m:60-196, without plotting) in place on self.F and its
+        cached distances: bending speed from the extended mean curvature, tension and
+        pressure enforcing the area A0 and volume V0, the smoothed normal speed, the
+        explicit update, setDistance, and `reinit_iters` reinitialization pseudo-steps
+        (0: none).  Returns the device tensor of 11 values {area, volume, Dt, max|NSB|,
+        int H^2, int H, int H NSB, int NSB, tension, pressure, energy}."""
+        info = torch.empty(11, dtype=torch.float64, device="cuda") if info is None else info
+        if self.xpr is None:
+            self.setDistance()
+        ws = self.workspace("relax_step")
+        lib().call(self._fn("vsl_relax_step"), _ptr(self.F), *map(_ptr, self._dist()), float(A0), float(V0),
+                   float(kappa), float(spon_c), float(cfl), float(alpha), int(ext_iters), int(reinit_iters),
+                   _ptr(info), *self.GD3.args(), _ptr(ws), ws.numel(), _stream())
         return info
 
     def _vesicle_step_graph(self, ext_iters: int, reinit_iters: int, cfl: float) -> torch.Tensor:

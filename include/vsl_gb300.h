@@ -181,7 +181,9 @@ enum {
     VSL_OP_REINIT_ADJOINT = 11,
     VSL_OP_REINIT_ENORK2 = 12,
     VSL_OP_EXTEND_ENORK2 = 13,
-    VSL_OP_SURFACE_REDISTANCE_ENORK2 = 14
+    VSL_OP_SURFACE_REDISTANCE_ENORK2 = 14,
+    VSL_OP_SMOOTH = 15,
+    VSL_OP_RELAX_STEP = 16
 };
 
 /* Tuning of the FP32 tiled stage kernels (no counterpart in the reference).  Each block
@@ -328,6 +330,52 @@ int vsl_enork2_surface_redistance_f64(double *A, int iter1, int iter2, const dou
 int vsl_enork2_surface_redistance_f32(float *A, int iter1, int iter2, const float *F, int rows, int cols, int pges,
                                       double dx, double dy, double dz, void *workspace, size_t workspace_bytes,
                                       vsl_stream_t stream);
+
+/* ---- the single-phase relaxation step of the vesicle driver and its SD.GD3 operators -- */
+
+/* ref: +SD/@GD3/GD3.m:344-346 (Laplacian) with the circshift neighbours of GD3.m:110-116:
+ * out = (Fxx + Fyy) + Fzz, Fxx = (F(x+dx) - 2F + F(x-dx)) / Dx^2, periodic in every axis. */
+int vsl_laplacian_f64(const double *field, double *out, int rows, int cols, int pges, double dx, double dy,
+                      double dz, vsl_stream_t stream);
+int vsl_laplacian_f32(const float *field, float *out, int rows, int cols, int pges, double dx, double dy, double dz,
+                      vsl_stream_t stream);
+
+/* ref: +SD/@GD3/GD3.m:434-485 (smoothGMRES, smoothFFT).  out = real(ifftn(fftn(rhs) ./ S))
+ * with S = 1 + alpha * (*dt) * symbol: exact = 1 takes the symbol of the periodic discrete
+ * bi-Laplacian (lambda^2, lambda = sum (2 cos(2 pi m/n) - 2) / h^2), which makes out the
+ * solution of smoothGMRES's system (I + alpha Dt L^2) out = rhs; exact = 0 takes smoothFFT's
+ * (kx^2 + ky^2 + kz^2)^2.  rhs and out may be the same array.  dt: device pointer.  Uses
+ * cuFFT: the first call for a grid shape and precision (or vsl_workspace_bytes for
+ * VSL_OP_SMOOTH / VSL_OP_RELAX_STEP) creates that shape's cuFFT plan; cuFFT allocates the
+ * plan's own tables then, so make that first call before any stream capture.  The
+ * transform's work area and spectrum are in the workspace. */
+int vsl_smooth_bilaplacian_f64(const double *rhs, double *out, const double *dt, double alpha, int exact, int rows,
+                               int cols, int pges, double dx, double dy, double dz, void *workspace,
+                               size_t workspace_bytes, vsl_stream_t stream);
+int vsl_smooth_bilaplacian_f32(const float *rhs, float *out, const double *dt, double alpha, int exact, int rows,
+                               int cols, int pges, double dx, double dy, double dz, void *workspace,
+                               size_t workspace_bytes, vsl_stream_t stream);
+
+/* ref: p00_test_singlephase_relax.m:60-196 (one pass of the time loop, without plotting).
+ * Calculus toolbox of F -> area, volume -> H = WENORK3Extend(MeanCurvature, ext_iters) ->
+ * NSB = kappa (Laplacian(H) + 0.5 H (H^2 - 4K) + 2 c0 K - 0.5 c0^2 H) ->
+ * NSB = ENORK2Extend(NSB, ext_iters) -> Dt = cfl Ds / max|NSB| over |F| < 2Ds ->
+ * [tension; pressure] = [c11 c12; c12 A0] \ [s1; s2] from the surface integrals ->
+ * v = (tension H - NSB + pressure) |grad F| -> (I + alpha Dt L^2)^-1 v (exact spectral
+ * solve of smoothGMRES's system) -> ENORK2Extend(v, ext_iters) -> F = F - Dt v ->
+ * setDistance (F's cached distances xpr..zpd are rewritten) -> energy -> reinit_iters
+ * WENO5 RK3 reinitialization pseudo-steps (0: none; the driver reinitializes every
+ * ReinitializationRate steps).  A0, V0: the initial area and volume; c0 = spon_c.
+ * info: device pointer to 11 doubles {area, volume (at the start), Dt, max|NSB|, c11 =
+ * int H^2, c12 = int H, int H NSB, int NSB, tension, pressure, energy int (H - c0)^2}. */
+int vsl_relax_step_f64(double *F, double *xpr, double *xpl, double *ypf, double *ypb, double *zpu, double *zpd,
+                       double A0, double V0, double kappa, double spon_c, double cfl, double alpha, int ext_iters,
+                       int reinit_iters, double *info, int rows, int cols, int pges, double dx, double dy, double dz,
+                       void *workspace, size_t workspace_bytes, vsl_stream_t stream);
+int vsl_relax_step_f32(float *F, float *xpr, float *xpl, float *ypf, float *ypb, float *zpu, float *zpd, double A0,
+                       double V0, double kappa, double spon_c, double cfl, double alpha, int ext_iters,
+                       int reinit_iters, double *info, int rows, int cols, int pges, double dx, double dy, double dz,
+                       void *workspace, size_t workspace_bytes, vsl_stream_t stream);
 
 /* ---- adjoints (no counterpart in the reference, which has no derivatives) -------------
  *

@@ -521,3 +521,103 @@ def vesicle_step(K, g: Grid, F, dist: Distances, ext_iters=30, reinit_iters=20, 
     dist = set_distance(K, g, F)
     F = reinit_weno5(K, g, F, reinit_iters, dist)
     return F, dist, {"area": area, "volume": volume, "dt": dt, "vmax": vmax}
+
+
+# ---------------------------------------------------------------------------------------
+# SD.GD3 operators with periodic neighbours (V/+SD/@GD3/GD3.m:110-207, 344-346, 434-485)
+# and one pass of the relaxation driver's time loop (V/p00_test_singlephase_relax.m:60-196)
+# ---------------------------------------------------------------------------------------
+
+
+def laplacian(g: Grid, f):
+    """GD3.Laplacian: (Fxx + Fyy) + Fzz, Fxx = (F(oXo) - 2F + F(oxo)) / Dx^2 with circshift
+    neighbours; arrays are (rows = y, cols = x, pges = z)."""
+    f = F64(f)
+    fxx = (np.roll(f, -1, axis=1) - 2 * f + np.roll(f, 1, axis=1)) / (g.dx * g.dx)
+    fyy = (np.roll(f, -1, axis=0) - 2 * f + np.roll(f, 1, axis=0)) / (g.dy * g.dy)
+    fzz = (np.roll(f, -1, axis=2) - 2 * f + np.roll(f, 1, axis=2)) / (g.dz * g.dz)
+    return F64(fxx + fyy + fzz)
+
+
+def wave_numbers(g: Grid):
+    """GD3.m:195-207: kx, ky, kz from fftshift(2 pi (-n/2 : n/2-1) / (n h)) on meshgrid."""
+    def axis(n, h):
+        v = 2 * np.pi * (-n / 2 + np.arange(n)) / (n * h)
+        return np.roll(v, n // 2)  # MATLAB fftshift = circshift by floor(n/2)
+    kx, ky, kz = np.meshgrid(axis(g.cols, g.dx), axis(g.rows, g.dy), axis(g.pges, g.dz))
+    return kx, ky, kz
+
+
+def smooth_fft(g: Grid, rhs, dt: float, alpha: float):
+    """GD3.smoothFFT: real(ifftn(fftn(rhs) ./ (1 + alpha dt (kx^2 + ky^2 + kz^2)^2)))."""
+    kx, ky, kz = wave_numbers(g)
+    s = np.fft.fftn(F64(rhs)) / (1 + alpha * dt * (kx ** 2 + ky ** 2 + kz ** 2) ** 2)
+    return F64(np.real(np.fft.ifftn(s)))
+
+
+def smooth_gmres(g: Grid, rhs, dt: float, alpha: float, tol: float = 1e-12, maxit: int = 300):
+    """GD3.smoothGMRES: (I + alpha dt L^2) x = rhs by GMRES (no restart, at most 300
+    iterations, relative tolerance 1e-12) preconditioned by smoothFFT's inverse symbol."""
+    from scipy.sparse.linalg import LinearOperator, gmres
+
+    n = g.num_ele
+    shape = g.size
+
+    def op(x):
+        u = x.reshape(shape, order="F")
+        return (u + alpha * dt * laplacian(g, laplacian(g, u))).ravel(order="F")
+
+    kx, ky, kz = wave_numbers(g)
+    denom = 1 + alpha * dt * (kx ** 2 + ky ** 2 + kz ** 2) ** 2
+
+    def pre(x):
+        u = x.reshape(shape, order="F")
+        return np.real(np.fft.ifftn(np.fft.fftn(u) / denom)).ravel(order="F")
+
+    A = LinearOperator((n, n), matvec=op, dtype=np.float64)
+    M = LinearOperator((n, n), matvec=pre, dtype=np.float64)
+    x, info = gmres(A, F64(rhs).ravel(order="F"), rtol=tol, atol=0.0, restart=maxit, maxiter=maxit, M=M)
+    return F64(x.reshape(shape, order="F"))
+
+
+def surface_integral_mask(g: Grid, F, field, delta, gradmag) -> float:
+    """SDF3.surfaceIntegral (SDF3.m:82-85): sum((f .* DiracDelta) .* FGradMag) over
+    |F| < 2 Ds, times Ds^3 (exactly rounded sum)."""
+    mask = np.abs(F64(F)) < 2 * g.ds
+    return exact_sum((F64(field)[mask] * F64(delta)[mask]) * F64(gradmag)[mask]) * g.ds ** 3
+
+
+def relax_step(K, g: Grid, F, A0: float, V0: float, kappa: float = 1.0, spon_c: float = 0.0, cfl: float = 0.5,
+               alpha: float = 0.5, ext_iters: int = 100, reinit_iters: int = 0):
+    """One pass of the driver's time loop without plotting: returns (F, dist, info) with
+    info the 11 values of the C ABI's relax step."""
+    F = F64(F).copy(order="F")
+    tb = calculus_toolbox(K, g, F)
+    area = cal_area(g, F, tb["DiracDelta"])
+    volume = cal_volume(g, F, tb["Heaviside"])
+    H = extend_eno3(K, g, F, tb["MeanCurvature"], ext_iters)
+    Kg = tb["GaussianCurvature"]
+    nsb = kappa * (laplacian(g, H) + 0.5 * H * (H * H - 4 * Kg) + 2. * spon_c * Kg - 0.5 * (spon_c * spon_c) * H)
+    nsb = extend_enork2(K, g, F, F64(nsb), ext_iters)
+    band = np.abs(F) < 2 * g.ds
+    vmax = float(np.max(np.abs(nsb[band])))
+    dt = cfl * g.ds / vmax
+    d, G = tb["DiracDelta"], tb["FGradMag"]
+    c11 = surface_integral_mask(g, F, H * H, d, G)
+    c12 = surface_integral_mask(g, F, H, d, G)
+    i_hn = surface_integral_mask(g, F, H * nsb, d, G)
+    i_n = surface_integral_mask(g, F, nsb, d, G)
+    s1 = i_hn - (A0 - area) / dt
+    s2 = i_n + (V0 - volume) / dt
+    tension, pressure = np.linalg.solve(np.array([[c11, c12], [c12, A0]]), np.array([s1, s2]))
+    vn = F64((tension * H - nsb + pressure) * G)
+    vs = smooth_gmres(g, vn, dt, alpha)
+    vs = extend_enork2(K, g, F, vs, ext_iters)
+    F = F64(F - dt * vs)
+    dist = set_distance(K, g, F)
+    ene = surface_integral_mask(g, F, (H - spon_c) ** 2, d, G)
+    if reinit_iters > 0:
+        F = reinit_weno5(K, g, F, reinit_iters, dist)
+    info = np.array([area, volume, dt, vmax, c11, c12, i_hn, i_n, tension, pressure, ene])
+    return F, dist, info
+
