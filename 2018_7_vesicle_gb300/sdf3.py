@@ -333,22 +333,44 @@ class SDF3:
         return info
 
     def relax_step(self, A0: float, V0: float, kappa: float = 1.0, spon_c: float = 0.0, cfl: float = 0.5,
-                   alpha: float = 0.5, ext_iters: int = 100, reinit_iters: int = 0, info=None) -> torch.Tensor:
+                   alpha: float = 0.5, ext_iters: int = 100, reinit_iters: int = 0, info=None,
+                   graph: bool = False) -> torch.Tensor:
         """One pass of the single-phase relaxation driver's time loop
         (p00_test_singlephase_relax.m:60-196, without plotting) in place on self.F and its
         cached distances: bending speed from the extended mean curvature, tension and
         pressure enforcing the area A0 and volume V0, the smoothed normal speed, the
         explicit update, setDistance, and `reinit_iters` reinitialization pseudo-steps
         (0: none).  Returns the device tensor of 11 values {area, volume, Dt, max|NSB|,
-        int H^2, int H, int H NSB, int NSB, tension, pressure, energy}."""
-        info = torch.empty(11, dtype=torch.float64, device="cuda") if info is None else info
+        int H^2, int H, int H NSB, int NSB, tension, pressure, energy}.  graph=True records
+        the step's launches (toolbox, extensions, reductions, FFTs, update, setDistance,
+        reinitialization) as one CUDA graph on first use and replays it; the returned tensor
+        is then the graph's own, overwritten by the next replay."""
         if self.xpr is None:
             self.setDistance()
         ws = self.workspace("relax_step")
-        lib().call(self._fn("vsl_relax_step"), _ptr(self.F), *map(_ptr, self._dist()), float(A0), float(V0),
-                   float(kappa), float(spon_c), float(cfl), float(alpha), int(ext_iters), int(reinit_iters),
-                   _ptr(info), *self.GD3.args(), _ptr(ws), ws.numel(), _stream())
-        return info
+        args = (float(A0), float(V0), float(kappa), float(spon_c), float(cfl), float(alpha), int(ext_iters),
+                int(reinit_iters))
+
+        def launch(out):
+            lib().call(self._fn("vsl_relax_step"), _ptr(self.F), *map(_ptr, self._dist()), *args, _ptr(out),
+                       *self.GD3.args(), _ptr(ws), ws.numel(), _stream())
+
+        if not graph:
+            info = torch.empty(11, dtype=torch.float64, device="cuda") if info is None else info
+            launch(info)
+            return info
+        key = (args, _ptr(self.F), tuple(map(_ptr, self._dist())), _ptr(ws))
+        if getattr(self, "_relax_graph_key", None) != key:
+            out = torch.empty(11, dtype=torch.float64, device="cuda")
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                launch(out)
+            self._relax_graph, self._relax_graph_info, self._relax_graph_key = g, out, key
+        self._relax_graph.replay()
+        if info is not None:
+            info.copy_(self._relax_graph_info)
+            return info
+        return self._relax_graph_info
 
     def _vesicle_step_graph(self, ext_iters: int, reinit_iters: int, cfl: float) -> torch.Tensor:
         key = (ext_iters, reinit_iters, cfl, _ptr(self.F), tuple(map(_ptr, self._dist())))

@@ -144,6 +144,26 @@ def vesicle_256(n: int = 256, seed: int = 0, reduced_volume: float = 0.65, pages
     return x, y, z, noisy_oblate(x, y, z, axes=(1.0, 1.0, c), seed=seed)
 
 
+def oblate_ellipsoid(size=(96, 96, 96), reduced_volume: float = 0.6, ratio: float = 0.35, device=None):
+    """The relaxation driver's initial shape, SD.Shape.Ellipsoid(size, rv, 'O', ratio)
+    (Ellipsoid.m:7-47, p00_test_singlephase_relax.m:24): x = linspace(-1, 1, size[0]),
+    y and z centred on 0 with the same spacing ((1-n)/2 : (n-1)/2 times dx), half axes
+    a = b = 2 ratio and c = a cq, cq interpolated linearly in the table of reduced volumes
+    of (1, 1, c) at c = 0.01 : 0.01 : 0.99.  Returns x, y, z and the field."""
+    nx, ny, nz = size
+    xv = np.linspace(-1.0, 1.0, nx)
+    dx = xv[1] - xv[0]
+    yv = (np.arange(ny) + (1 - ny) / 2.0) * dx
+    zv = (np.arange(nz) + (1 - nz) / 2.0) * dx
+    x, y, z = meshgrid(xv, yv, zv, device=device)
+    cs = np.arange(1, 100) / 100.0
+    rv = np.array([oblate_reduced_volume(c) for c in cs])
+    a = ratio * 2.0
+    c = a * float(np.interp(reduced_volume, rv, cs))
+    xp = _Ops(x)
+    return x, y, z, xp.fortran(xp.sqrt(x**2 / a**2 + y**2 / a**2 + z**2 / c**2) - 1)
+
+
 def surface_field(x, y, z):
     """The scalar field redistanced on the interface: sin(3x) cos(2y) + 0.5 z^2."""
     return np.asfortranarray(np.sin(3 * x) * np.cos(2 * y) + 0.5 * z**2)

@@ -424,6 +424,72 @@ def differentiation_measure(torch, pkg, S, fd_check: bool = False, n: int = 128)
     return out
 
 
+RELAX_EXT, RELAX_RE = 100, 100  # p00_test_singlephase_relax.m:75, 86, 121, 192
+
+
+def relax_measure(torch, pkg, S, n: int = 96, steps: int = 10, fp64_steps: int = 2):
+    """The relaxation driver's time loop at its own configuration
+    (p00_test_singlephase_relax.m:8-28, 60-193): n^3 grid, oblate ellipsoid of reduced
+    volume 0.6 (ratio 0.35), setDistance and 500 reinitialization pseudo-steps, the area and
+    volume as targets; then each step the toolbox, WENORK3Extend(H, 100), the bending speed
+    (kappa 1, SponC 0), ENORK2Extend(100), Dt at CFL 0.5, the tension/pressure solve, the
+    normal speed smoothed by the exact spectral solve of smoothGMRES (alpha 0.5),
+    ENORK2Extend(100), the update, setDistance, the energy and 100 reinitialization
+    pseudo-steps (ReinitializationRate 1).  FP32 as one CUDA graph per step, and the plain
+    FP64 form.  Unit: grid-point pseudo-steps, 300 extension + 100 reinitialization per
+    node and step."""
+    import numpy as np
+
+    gpt = (3 * RELAX_EXT + RELAX_RE) * n ** 3
+    out = {"workload": f"relaxation step {n}^3 (p00 driver configuration): 3 x {RELAX_EXT} extension "
+                       f"+ {RELAX_RE} reinit pseudo-steps, spectral smoothing, tension/pressure solve",
+           "gpt_per_step": gpt}
+    x, y, z, F = S.oblate_ellipsoid((n, n, n), 0.6, 0.35, device="cuda")
+    grid = pkg.GD3(x, y, z)
+
+    def setup(prec):
+        m = pkg.SDF3(grid, Val=F, precision=prec)
+        m.setDistance()
+        m.F = m.WENO5RK3Reinitialization(m.F, 500)
+        m.setDistance()
+        A0, V0 = (float(v) for v in m.area_volume().cpu())
+        return m, A0, V0
+
+    res = {}
+    for prec, k in (("f32", steps), ("f64", fp64_steps)):
+        m, A0, V0 = setup(prec)
+        kw = dict(kappa=1.0, spon_c=0.0, cfl=0.5, alpha=0.5, ext_iters=RELAX_EXT, reinit_iters=RELAX_RE,
+                  graph=prec == "f32")
+        m.relax_step(A0, V0, **kw)  # warm-up: FFT plans, graph recording
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(k):
+            info = m.relax_step(A0, V0, **kw)
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / k
+        inf = info.cpu().numpy()
+        res[prec] = (m, ms, k + 1)
+        out[prec] = {"ms_per_step": ms, "gpt_s": gpt / (ms / 1e3) / 1e9, "steps_taken": k + 1,
+                     "area_rel_dev": float(inf[0] / A0 - 1), "volume_rel_dev": float(inf[1] / V0 - 1),
+                     "dt": float(inf[2]), "tension": float(inf[8]), "pressure": float(inf[9]),
+                     "energy": float(inf[10]), "finite": bool(np.isfinite(inf).all())}
+    out["ratio_fp32_over_fp64"] = res["f64"][1] / res["f32"][1]
+    # FP32 against FP64 after the same number of steps from the same set-up
+    m32, A0, V0 = setup("f32")
+    for _ in range(res["f64"][2]):
+        m32.relax_step(A0, V0, kappa=1.0, spon_c=0.0, cfl=0.5, alpha=0.5, ext_iters=RELAX_EXT,
+                       reinit_iters=RELAX_RE)
+    m64 = res["f64"][0]
+    h = grid.Dx
+    d = (m32.F.double() - m64.F).abs()
+    band = m64.F.abs() < 3 * h
+    out["fp32_vs_fp64"] = {"after_steps": res["f64"][2], "band_max_dx": float(d[band].max()) / h,
+                           "band_rms_dx": float(d[band].pow(2).mean().sqrt()) / h}
+    return out
+
+
 def workload_config(ngpus):
     return {"workload": f"vesicle step {N}^3 mixed precision (FP32 stencils, FP64 roots/reductions): "
                         f"{EXT} WENO5-RK3 extension + {ADV} WENO5-RK3 advection + {RE} WENO5-RK3 reinit "
@@ -444,6 +510,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-differentiation", action="store_true")
     ap.add_argument("--no-precision", action="store_true")
+    ap.add_argument("--no-relax", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--fd-check", action="store_true",
                     help="also check the 128^3 amplitude gradient against FP64 central differences")
@@ -591,6 +658,11 @@ def main():
         torch.cuda.empty_cache()
         differentiation = differentiation_measure(torch, pkg, S, fd_check=args.fd_check)
 
+    relax = None
+    if not args.no_relax and rank == 0:
+        torch.cuda.empty_cache()
+        relax = relax_measure(torch, pkg, S)
+
     if rank != 0:
         if dist is not None:
             dist.barrier()
@@ -620,6 +692,7 @@ def main():
         "batched": batched,
         "precision": precision,
         "differentiation": differentiation,
+        "relax": relax,
         "last_info": {"area": info_h[0], "volume": info_h[1], "dt": info_h[2], "max_speed": info_h[3]},
         "cpu_baseline": cpu,
     }

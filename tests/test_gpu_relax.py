@@ -112,3 +112,21 @@ def test_relax_step_fp32_vs_fp64(pkg, vsl):
               abs(i32[0] / i64[0] - 1), abs(i32[1] / i64[1] - 1))
         assert err <= 1e-3 and rms <= 2e-5
         assert abs(i32[0] / i64[0] - 1) <= 1e-6 and abs(i32[1] / i64[1] - 1) <= 1e-6
+
+
+def test_relax_step_graph_replay_is_bitwise(pkg, vsl):
+    """graph=True records the step once and replays it: same fields and scalars, bit for
+    bit, as the direct launches, over three steps (FP32, the driver's initial shape)."""
+    x, y, z, F = S.oblate_ellipsoid((32, 30, 28), 0.6, 0.35)
+    ms = []
+    for graph in (False, True):
+        m = pkg.SDF3(pkg.GD3(x, y, z), Val=F, precision="f32")
+        m.setDistance()
+        av = m.area_volume().cpu().numpy()
+        infos = []
+        for _ in range(3):
+            infos.append(m.relax_step(av[0], av[1], cfl=0.5, ext_iters=10, reinit_iters=5, graph=graph)
+                         .cpu().numpy())
+        ms.append((host(m.F), np.array(infos)))
+    assert np.array_equal(ms[0][0], ms[1][0])
+    assert np.array_equal(ms[0][1], ms[1][1])
