@@ -10,12 +10,13 @@
 // both the forward derivative at k and the backward derivative at k+1.
 //
 // Nodes whose update needs the interface-aware (nonuniform) stencil -- the "band" -- are
-// not computed here: their indices go to a compact queue (warp-aggregated atomics) and
-// band_stage_kernel processes them with the generic per-node code, so the uniform WENO5
-// path runs without divergence.  A node is band when, for the reinitialization, the sign
-// of phi changes on one of its stencil edges (the reference's trigger), and for the
-// extension when one of its distances differs from the spacing (a superset of the
-// reference's trigger r1 < h || l1 < h; the band kernel applies the exact test).
+// not computed here; k_band_stage processes them with the generic per-node code, so the
+// uniform WENO5 path runs without divergence.  For the reinitialization a node is band
+// when the sign of phi changes on one of its stencil edges (the reference's trigger); the
+// tiled kernel queues those (warp-aggregated atomics) and the band kernel follows it.  For
+// the extension a node is band when one of its distances differs from the spacing (a
+// superset of the reference's trigger r1 < h || l1 < h; the band kernel applies the exact
+// test): a static list, so the band kernel runs beside the tiled kernel on a side stream.
 #pragma once
 
 #include <mutex>
@@ -175,7 +176,9 @@ __global__ void __launch_bounds__(TY *TX, VSL_TILED_MIN_BLOCKS) k_stage_tiled(Ti
             if (compute && KIND == SK_REINIT) {
                 band = px[2] * px[3] < 0.f || px[3] * px[4] < 0.f || py[2] * py[3] < 0.f || py[3] * py[4] < 0.f ||
                        q[2] * q[3] < 0.f || q[3] * q[4] < 0.f;
-            } else if (compute && KIND == SK_EXTEND) {
+            } else if (KIND == SK_EXTEND) {
+                // every node of the static list (fixed ones too) belongs to the band kernel,
+                // which may run at the same time: each node has exactly one writer
                 band = (fl & 0x3F) != 0;
             }
             if (compute && !band && KIND == SK_REINIT) {
@@ -328,6 +331,54 @@ int set_tile_pages(int rows, int cols, int pges, int kind, int pages)
     return VSL_OK;
 }
 
+// ---------------------------------------------------------------------------------------
+// side lanes: the extension's band kernel reads only the stage input and writes only the
+// nodes of the static list, which the tiled kernel leaves alone, so it runs beside the
+// tiled kernel on a second stream (forked from and joined back into the caller's stream
+// by events; under stream capture the two launches become parallel graph branches).
+// One lane per (device, caller stream), created on first use with this thread's capture
+// mode relaxed for the creation calls, so a first use inside a capture sequence is legal.
+// With the pool full, or if creation fails, the band kernel follows the tiled kernel on
+// the caller's stream.
+// ---------------------------------------------------------------------------------------
+namespace {
+struct SideLane {
+    int device;
+    cudaStream_t user;
+    cudaStream_t side;
+    cudaEvent_t fork, join;
+};
+constexpr int MAX_LANES = 256;
+std::mutex lane_mutex;
+SideLane lanes[MAX_LANES];
+int n_lanes = 0;
+
+SideLane *side_lane(cudaStream_t s)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> lock(lane_mutex);
+    for (int e = 0; e < n_lanes; ++e)
+        if (lanes[e].device == dev && lanes[e].user == s) return &lanes[e];
+    if (n_lanes == MAX_LANES) return nullptr;
+    SideLane ln{dev, s, nullptr, nullptr, nullptr};
+    cudaStreamCaptureMode mode = cudaStreamCaptureModeRelaxed;
+    if (cudaThreadExchangeStreamCaptureMode(&mode) != cudaSuccess) return nullptr;
+    bool ok = cudaStreamCreateWithFlags(&ln.side, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && cudaEventCreateWithFlags(&ln.fork, cudaEventDisableTiming) == cudaSuccess;
+    ok = ok && cudaEventCreateWithFlags(&ln.join, cudaEventDisableTiming) == cudaSuccess;
+    cudaThreadExchangeStreamCaptureMode(&mode);
+    if (!ok) {
+        if (ln.join) cudaEventDestroy(ln.join);
+        if (ln.fork) cudaEventDestroy(ln.fork);
+        if (ln.side) cudaStreamDestroy(ln.side);
+        return nullptr;
+    }
+    lanes[n_lanes] = ln;
+    return &lanes[n_lanes++];
+}
+}  // namespace
+
 cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const Grid &g, cudaStream_t s)
 {
     TiledArgs a = tiled_args(g);
@@ -351,25 +402,37 @@ cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const 
     a.stage = st.stage;
     a.kz = tile_pages(g, kind);
     dim3 gr = tiled_grid(g, a.kz), bl(TY, TX);
+    if (kind == SK_EXTEND) {
+        SideLane *ln = side_lane(s);
+        cudaStream_t bs = s;
+        cudaError_t e;
+        if (ln) {
+            if ((e = cudaEventRecord(ln->fork, s)) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(ln->side, ln->fork, 0)) != cudaSuccess) return e;
+            bs = ln->side;
+        }
+        if (eno3)
+            k_band_stage<SK_EXTEND, true><<<band_blocks(), 128, 0, bs>>>(a, st.cp, next);
+        else
+            k_band_stage<SK_EXTEND, false><<<band_blocks(), 128, 0, bs>>>(a, st.cp, next);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if (ln && (e = cudaEventRecord(ln->join, bs)) != cudaSuccess) return e;
+        k_stage_tiled<SK_EXTEND><<<gr, bl, 0, s>>>(a);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if (ln && (e = cudaStreamWaitEvent(s, ln->join, 0)) != cudaSuccess) return e;
+        return cudaSuccess;
+    }
     if (kind == SK_REINIT)
         k_stage_tiled<SK_REINIT><<<gr, bl, 0, s>>>(a);
-    else if (kind == SK_EXTEND)
-        k_stage_tiled<SK_EXTEND><<<gr, bl, 0, s>>>(a);
     else
         k_stage_tiled<SK_ADVECT><<<gr, bl, 0, s>>>(a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || kind == SK_ADVECT) return e;
-    if (kind == SK_REINIT) {
-        if (eno3)
-            k_band_stage<SK_REINIT, true><<<band_blocks(), 128, 0, s>>>(a, st.cp, next);
-        else
-            k_band_stage<SK_REINIT, false><<<band_blocks(), 128, 0, s>>>(a, st.cp, next);
-    } else {
-        if (eno3)
-            k_band_stage<SK_EXTEND, true><<<band_blocks(), 128, 0, s>>>(a, st.cp, next);
-        else
-            k_band_stage<SK_EXTEND, false><<<band_blocks(), 128, 0, s>>>(a, st.cp, next);
-    }
+    // the reinitialization's band is queued by the tiled kernel, so its kernel follows it
+    if (eno3)
+        k_band_stage<SK_REINIT, true><<<band_blocks(), 128, 0, s>>>(a, st.cp, next);
+    else
+        k_band_stage<SK_REINIT, false><<<band_blocks(), 128, 0, s>>>(a, st.cp, next);
     return cudaGetLastError();
 }
 

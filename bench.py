@@ -324,6 +324,20 @@ def step128_profile_case(torch, pkg, S, n: int = 128):
     print(json.dumps({"profile_case": "step128", "ok": True}))
 
 
+def relax_profile_case(torch, pkg, S, n: int = 96):
+    """Two FP32 relaxation steps at the driver's 96^3 configuration without a graph (the
+    launch-list case); the first creates the FFT plans."""
+    x, y, z, F = S.oblate_ellipsoid((n, n, n), 0.6, 0.35, device="cuda")
+    m = pkg.SDF3(pkg.GD3(x, y, z), Val=F, precision="f32")
+    m.setDistance()
+    A0, V0 = (float(v) for v in m.area_volume().cpu())
+    for _ in range(2):
+        m.relax_step(A0, V0, kappa=1.0, spon_c=0.0, cfl=0.5, alpha=0.5, ext_iters=RELAX_EXT,
+                     reinit_iters=RELAX_RE)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "relax", "ok": True}))
+
+
 def adjoint_profile_case(torch, pkg, S, n: int = 128):
     """One forward + backward pass of a shortened differentiation workload at n^3 FP32
     (4 advection steps, one 2-pseudo-step reinitialization; the ncu capture case)."""
@@ -455,8 +469,7 @@ def relax_measure(torch, pkg, S, n: int = 96, steps: int = 10, fp64_steps: int =
         A0, V0 = (float(v) for v in m.area_volume().cpu())
         return m, A0, V0
 
-    res = {}
-    for prec, k in (("f32", steps), ("f64", fp64_steps)):
+    def timed(prec, k):
         m, A0, V0 = setup(prec)
         kw = dict(kappa=1.0, spon_c=0.0, cfl=0.5, alpha=0.5, ext_iters=RELAX_EXT, reinit_iters=RELAX_RE,
                   graph=prec == "f32")
@@ -468,7 +481,17 @@ def relax_measure(torch, pkg, S, n: int = 96, steps: int = 10, fp64_steps: int =
             info = m.relax_step(A0, V0, **kw)
         b.record()
         torch.cuda.synchronize()
-        ms = a.elapsed_time(b) / k
+        return m, A0, V0, a.elapsed_time(b) / k, info
+
+    # FP32 with the default tiles, then with pages per block tuned for this grid (each
+    # with its own graph, recorded after the tiles are set)
+    out["f32_default_tiles_ms"] = timed("f32", steps)[3]
+    m, _, _ = setup("f32")
+    out["autotune"] = importlib.import_module(PKG + ".autotune").tune_shape(m, candidates=(2, 4, 8, 16, 32, 64))
+    del m
+    res = {}
+    for prec, k in (("f32", steps), ("f64", fp64_steps)):
+        m, A0, V0, ms, info = timed(prec, k)
         inf = info.cpu().numpy()
         res[prec] = (m, ms, k + 1)
         out[prec] = {"ms_per_step": ms, "gpt_s": gpt / (ms / 1e3) / 1e9, "steps_taken": k + 1,
@@ -514,7 +537,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--fd-check", action="store_true",
                     help="also check the 128^3 amplitude gradient against FP64 central differences")
-    ap.add_argument("--profile", choices=["extend", "reinit", "advect", "step", "step128", "adjoint"],
+    ap.add_argument("--profile", choices=["extend", "reinit", "advect", "step", "step128", "adjoint", "relax"],
                     help="run only a few launches of one operator at 256^3 (the ncu capture case)")
     args = ap.parse_args()
 
@@ -539,6 +562,8 @@ def main():
     S = importlib.import_module(PKG + ".shapes")
     if args.profile == "adjoint":
         return adjoint_profile_case(torch, pkg, S)
+    if args.profile == "relax":
+        return relax_profile_case(torch, pkg, S)
     if args.profile == "step128":
         return step128_profile_case(torch, pkg, S)
     x, y, z, F0 = S.vesicle_256(N, seed=rank, device="cuda")
