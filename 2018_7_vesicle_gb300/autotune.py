@@ -5,7 +5,7 @@ pages mean more blocks and more parallelism on small grids, more pages mean fewe
 reloads per node on large ones.  The library keeps a table of pages per (grid shape,
 stage kind) (vsl_set_tile_pages / vsl_tile_pages of the C ABI); `tune_shape` fills it for
 one level-set object by timing each kind's own operation (extension, reinitialization,
-advection) on that object's field for every candidate, with CUDA events, and keeping
+advection, ENORK2 extension) on that object's field for every candidate, with CUDA events, and keeping
 the fastest.  Tune before recording CUDA graphs: a graph keeps the launch shapes it was
 recorded with.
 """
@@ -16,8 +16,29 @@ import torch
 from ._lib import lib
 from .sdf3 import SDF3, colmajor_full
 
-KINDS = {"reinit": 0, "extend": 1, "advect": 2}
+KINDS = {"reinit": 0, "extend": 1, "advect": 2, "enork2_extend": 3}
 CANDIDATES = (4, 8, 16, 32, 64)
+TILE_ROWS, TILE_COLS = 32, 8  # tile of one block of the tiled kernels
+BLOCKS_PER_SM = 4  # resident blocks per SM of the tiled kernels (launch bounds)
+
+
+def wave_candidates(size, sms: int | None = None, fill: float = 0.85, max_waves: float = 4.0, lo: int = 2,
+                    hi: int = 64):
+    """Pages per block whose launch of at most `max_waves` waves of resident blocks fills
+    its last wave to at least `fill` (a launch of 1.42 waves leaves 29% of the second wave
+    idle; beyond a few waves the quantization hardly matters), together with CANDIDATES.
+    size = (rows, cols, pges)."""
+    rows, cols, pges = size
+    if sms is None:
+        sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    slots = sms * BLOCKS_PER_SM
+    tiles = -(-rows // TILE_ROWS) * -(-cols // TILE_COLS)
+    out = set(CANDIDATES)
+    for kz in range(lo, hi + 1):
+        waves = tiles * -(-pges // kz) / slots
+        if waves <= max_waves and waves / -(-waves // 1) >= fill:
+            out.add(kz)
+    return tuple(sorted(out))
 
 
 def get_pages(size, kind: str) -> int:
@@ -55,16 +76,21 @@ def _candidates(pges: int, candidates):
 def tune_shape(sdf: SDF3, candidates=CANDIDATES, iters: int = 2, reps: int = 3) -> dict:
     """Pick pages per block for each stage kind on sdf's grid shape; returns
     {kind: {"pages": best, "ms": {candidate: time}}}.  sdf must be FP32 with its
-    distances set (setDistance)."""
+    distances set (setDistance).  candidates="waves" takes wave_candidates(shape)."""
     if sdf.precision != "f32":
         raise ValueError("the tiled kernels are the FP32 form's")
     size = sdf.GD3.Size
+    if isinstance(candidates, str):
+        if candidates != "waves":
+            raise ValueError("candidates: a sequence of page counts or 'waves'")
+        candidates = wave_candidates(size)
     v = colmajor_full(size, 0.5, torch.float32)
     dt = 0.1 * min(sdf.GD3.Dx, sdf.GD3.Dy, sdf.GD3.Dz)
     ops = {
         "extend": lambda: sdf.WENO5RK3Extend(sdf.F, iters),
         "reinit": lambda: sdf.WENO5RK3Reinitialization(sdf.F, iters),
         "advect": lambda: sdf.WENO5RK3Advection(sdf.F, v, v, v, dt, iters),
+        "enork2_extend": lambda: sdf.ENORK2Extend(sdf.F, iters),
     }
     report = {}
     for kind, fn in ops.items():

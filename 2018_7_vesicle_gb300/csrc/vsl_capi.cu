@@ -612,6 +612,28 @@ int op_reinit_enork2(T *F, int iteration, int rows, int cols, int pges, double d
     return VSL_OK;
 }
 
+// crossing values of C, then `iters` Heun RK2 extension steps of C in place
+template <typename T>
+int enork2_extend_loop(T *C, int iters, Ptr6<const T> d, ExtendWork<T> &w, const Grid &g, cudaStream_t s)
+{
+    VSL_TRY(launch_enork2_crossing<T>(C, d, w.cp, w.flagged, g, s));
+    const Ptr6<const T> cp = cview(w.cp);
+    const Ptr3<const T> v = cview3(w.v);
+    if constexpr (std::is_same<T, float>::value) {
+        // tiled uniform nodes, the flagged list on the per-node code beside them
+        for (int it = 0; it < iters; ++it) {
+            VSL_TRY(tiled(3, false, w.band, C, C, w.b, w.flags, d, cp, v, nullptr, nullptr, 0, g, s, w.flagged));
+            VSL_TRY(tiled(3, false, w.band, w.b, C, C, w.flags, d, cp, v, nullptr, nullptr, 1, g, s, w.flagged));
+        }
+        return VSL_OK;
+    }
+    for (int it = 0; it < iters; ++it) {
+        VSL_TRY(launch_enork2_extend_stage<T>(C, C, w.b, w.flags, d, cp, v, g, 0, s));
+        VSL_TRY(launch_enork2_extend_stage<T>(w.b, C, C, w.flags, d, cp, v, g, 1, s));
+    }
+    return VSL_OK;
+}
+
 template <typename T>
 int op_extend_enork2(T *C, int iteration, const T *F, int rows, int cols, int pges, double dx, double dy, double dz,
                      void *ws, size_t bytes, cudaStream_t s)
@@ -627,28 +649,7 @@ int op_extend_enork2(T *C, int iteration, const T *F, int rows, int cols, int pg
     const Ptr6<const T> d = cview(w.dist);
     VSL_TRY(launch_enork2_velocity<T>(F, d, w.v, g, 1e-6, s));
     VSL_TRY(launch_classify<T>(F, d, w.flags, w.flagged, g, s));
-    VSL_TRY(launch_enork2_crossing<T>(C, d, w.cp, w.flagged, g, s));
-    const Ptr6<const T> cp = cview(w.cp);
-    const Ptr3<const T> v = cview3(w.v);
-    for (int it = 0; it < iteration; ++it) {
-        VSL_TRY(launch_enork2_extend_stage<T>(C, C, w.b, w.flags, d, cp, v, g, 0, s));
-        VSL_TRY(launch_enork2_extend_stage<T>(w.b, C, C, w.flags, d, cp, v, g, 1, s));
-    }
-    return VSL_OK;
-}
-
-// crossing values of C, then `iters` Heun RK2 extension steps of C in place
-template <typename T>
-int enork2_extend_loop(T *C, int iters, Ptr6<const T> d, ExtendWork<T> &w, const Grid &g, cudaStream_t s)
-{
-    VSL_TRY(launch_enork2_crossing<T>(C, d, w.cp, w.flagged, g, s));
-    const Ptr6<const T> cp = cview(w.cp);
-    const Ptr3<const T> v = cview3(w.v);
-    for (int it = 0; it < iters; ++it) {
-        VSL_TRY(launch_enork2_extend_stage<T>(C, C, w.b, w.flags, d, cp, v, g, 0, s));
-        VSL_TRY(launch_enork2_extend_stage<T>(w.b, C, C, w.flags, d, cp, v, g, 1, s));
-    }
-    return VSL_OK;
+    return enork2_extend_loop<T>(C, iteration, d, w, g, s);
 }
 
 // ENORK2ClosetPointSurfaceRedistance.m:4-128
@@ -936,7 +937,7 @@ int vsl_set_tile_pages(int rows, int cols, int pges, int kind, int pages)
 
 int vsl_tile_pages(int rows, int cols, int pges, int kind)
 {
-    if (rows <= 0 || cols <= 0 || pges <= 0 || kind < 0 || kind > 2) return 0;
+    if (rows <= 0 || cols <= 0 || pges <= 0 || kind < 0 || kind > 3) return 0;
     return tile_pages(make_grid(rows, cols, pges, 1.0, 1.0, 1.0), kind);
 }
 

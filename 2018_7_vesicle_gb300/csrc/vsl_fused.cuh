@@ -499,14 +499,13 @@ __global__ void __launch_bounds__(128) k_enork2_crossing(const T *__restrict__ c
     }
 }
 
+// one node of an ENORK2 extension stage, all reads from global memory (clamped)
 template <typename T>
-__global__ void __launch_bounds__(BX *BY) k_enork2_extend_stage(const T *__restrict__ c_s, const T *__restrict__ c_n,
-                                                                  T *__restrict__ out, const uint8_t *__restrict__ flags,
-                                                                  Ptr6<const T> d, Ptr6<const T> cp, Ptr3<const T> v,
-                                                                  Grid g, int stage)
+__device__ __forceinline__ void enork2_extend_node(const T *__restrict__ c_s, const T *__restrict__ c_n,
+                                                   T *__restrict__ out, const uint8_t *__restrict__ flags,
+                                                   const Ptr6<const T> &d, const Ptr6<const T> &cp,
+                                                   const Ptr3<const T> &v, const Grid &g, int stage, int i, int j, int k)
 {
-    int i, j, k;
-    if (!fused_node(g, i, j, k)) return;
     const long long c = node_index(g, i, j, k);
     const uint8_t fl = __ldg(flags + c);
     const T hs[3] = {(T)g.dx, (T)g.dy, (T)g.dz};
@@ -524,6 +523,17 @@ __global__ void __launch_bounds__(BX *BY) k_enork2_extend_stage(const T *__restr
                    pseudo_dt(fl, d, c, hs[0], hs[1], hs[2]);
     const T pn = stage == 0 ? T(0) : __ldg(c_n + c);
     out[c] = rk2_combine(stage, pn, __ldg(c_s + c), step);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BX *BY) k_enork2_extend_stage(const T *__restrict__ c_s, const T *__restrict__ c_n,
+                                                                  T *__restrict__ out, const uint8_t *__restrict__ flags,
+                                                                  Ptr6<const T> d, Ptr6<const T> cp, Ptr3<const T> v,
+                                                                  Grid g, int stage)
+{
+    int i, j, k;
+    if (!fused_node(g, i, j, k)) return;
+    enork2_extend_node<T>(c_s, c_n, out, flags, d, cp, v, g, stage, i, j, k);
 }
 
 }  // namespace

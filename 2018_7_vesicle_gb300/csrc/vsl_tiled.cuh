@@ -45,7 +45,8 @@ constexpr int SH = TX + 2 * HALO;
 constexpr int PLANE = SW * SH;
 constexpr int RING = 5;
 
-enum StageKind { SK_REINIT = 0, SK_EXTEND = 1, SK_ADVECT = 2 };
+// SK_ENO2: the ENORK2 extension (quadratic ENO derivatives, Heun RK2 stages)
+enum StageKind { SK_REINIT = 0, SK_EXTEND = 1, SK_ADVECT = 2, SK_ENO2 = 3 };
 
 struct TiledArgs {
     const float *phi_s;
@@ -66,6 +67,17 @@ struct TiledArgs {
 };
 
 constexpr int PER_THREAD = (PLANE + TY * TX - 1) / (TY * TX);  // halo elements per thread
+
+// Upwind quadratic-ENO derivative of a line with no crossing (eno2_pair with r1 = l1 = h:
+// (v2 - v0)/h - h * minmod/2h^2 forward, (v0 - v1)/h + h * minmod/2h^2 backward, folded
+// into one product with 1/h); back selects the backward one (speed > 0).
+__device__ __forceinline__ float eno2_upwind_uniform(const float p[7], bool back, float inv_h)
+{
+    const float v1 = p[2], v0 = p[3], v2 = p[4];
+    const float p2 = v1 - 2.f * v0 + v2;
+    if (back) return (v0 - v1 + 0.5f * minmod(p2, v0 - 2.f * v1 + p[1])) * inv_h;
+    return (v2 - v0 - 0.5f * minmod(p2, v0 - 2.f * v2 + p[5])) * inv_h;
+}
 
 template <int KIND>
 __global__ void __launch_bounds__(TY *TX, VSL_TILED_MIN_BLOCKS) k_stage_tiled(TiledArgs a)
@@ -121,8 +133,10 @@ __global__ void __launch_bounds__(TY *TX, VSL_TILED_MIN_BLOCKS) k_stage_tiled(Ti
 #pragma unroll
     for (int s = 3; s < 6; ++s) q[s] = sm[slot(k0 + s - 3)][ty + HALO][tx + HALO];
     // reciprocal smoothness weights of the z window of page k0 (backward derivative)
-    float zr1, zr2, zr3;
-    weno5_window_weights(q[1] - q[0], q[2] - q[1], q[3] - q[2], q[4] - q[3], q[5] - q[4], a.eps2[2], zr1, zr2, zr3);
+    float zr1 = 0.f, zr2 = 0.f, zr3 = 0.f;
+    if constexpr (KIND != SK_ENO2)
+        weno5_window_weights(q[1] - q[0], q[2] - q[1], q[3] - q[2], q[4] - q[3], q[5] - q[4], a.eps2[2], zr1, zr2,
+                             zr3);
 
     const unsigned lane = tid & 31;
     // ring slots of pages k, k+3 and k+4 (= k-1), advanced by one per page
@@ -158,8 +172,8 @@ __global__ void __launch_bounds__(TY *TX, VSL_TILED_MIN_BLOCKS) k_stage_tiled(Ti
         // backward derivative at the next page
         const float v1 = q[1] - q[0], v2 = q[2] - q[1], v3 = q[3] - q[2], v4 = q[4] - q[3], v5 = q[5] - q[4],
                     v6 = q[6] - q[5];
-        float nr1, nr2, nr3;
-        weno5_window_weights(v2, v3, v4, v5, v6, a.eps2[2], nr1, nr2, nr3);
+        float nr1 = 0.f, nr2 = 0.f, nr3 = 0.f;
+        if constexpr (KIND != SK_ENO2) weno5_window_weights(v2, v3, v4, v5, v6, a.eps2[2], nr1, nr2, nr3);
 
         bool band = false;
         if (active) {
@@ -176,7 +190,7 @@ __global__ void __launch_bounds__(TY *TX, VSL_TILED_MIN_BLOCKS) k_stage_tiled(Ti
             if (compute && KIND == SK_REINIT) {
                 band = px[2] * px[3] < 0.f || px[3] * px[4] < 0.f || py[2] * py[3] < 0.f || py[3] * py[4] < 0.f ||
                        q[2] * q[3] < 0.f || q[3] * q[4] < 0.f;
-            } else if (KIND == SK_EXTEND) {
+            } else if (KIND == SK_EXTEND || KIND == SK_ENO2) {
                 // every node of the static list (fixed ones too) belongs to the band kernel,
                 // which may run at the same time: each node has exactly one writer
                 band = (fl & 0x3F) != 0;
@@ -195,7 +209,13 @@ __global__ void __launch_bounds__(TY *TX, VSL_TILED_MIN_BLOCKS) k_stage_tiled(Ti
                 const float dtn = (fl & 0x3F) ? pseudo_dt(fl, a.d, c, a.h[0], a.h[1], a.h[2]) : a.dt_uniform;
                 const float gn = godunov_norm(neg, dxf, dxb, dyf, dyb, dz.y, dz.x);
                 step = (gn - 1.f) * dtn * (neg ? -1.f : 1.f);
-            } else if (compute && !band && KIND != SK_REINIT) {
+            } else if (compute && !band && KIND == SK_ENO2) {
+                // ENORK2 extension: the upwind quadratic-ENO derivative of each axis
+                const float tr = vx0 * eno2_upwind_uniform(px, vx0 > 0.f, a.inv_h[0]) +
+                                 vy0 * eno2_upwind_uniform(py, vy0 > 0.f, a.inv_h[1]) +
+                                 vz0 * eno2_upwind_uniform(q, vz0 > 0.f, a.inv_h[2]);
+                step = tr * a.dt_uniform;
+            } else if (compute && !band && (KIND == SK_EXTEND || KIND == SK_ADVECT)) {
                 // transport sum_ax min(0,v) D+ + max(0,v) D-: the velocity is fixed, so each
                 // axis needs only its upwind derivative (D- where v > 0); x and y share one
                 // packed evaluation, z reuses the carried window weights
@@ -211,7 +231,7 @@ __global__ void __launch_bounds__(TY *TX, VSL_TILED_MIN_BLOCKS) k_stage_tiled(Ti
                 const float tr = ux * dxy.x + uy * dxy.y + uz * dz;
                 step = KIND == SK_EXTEND ? tr * a.dt_uniform : (float)__ldg(a.dt) * tr;
             }
-            if (!band) a.out[c] = rk3_combine(a.stage, pn, ps - step);
+            if (!band) a.out[c] = KIND == SK_ENO2 ? rk2_combine(a.stage, pn, ps, step) : rk3_combine(a.stage, pn, ps - step);
         }
         if (KIND == SK_REINIT) {  // the extension's band is the static list of flagged nodes
             const unsigned m = __ballot_sync(0xffffffffu, band);
@@ -256,6 +276,8 @@ __global__ void __launch_bounds__(128) k_band_stage(TiledArgs a, Ptr6<const floa
         const int i = (int)(r - (long long)j * g.rows);
         if (KIND == SK_REINIT)
             reinit_node<float, ENO3, true>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
+        else if (KIND == SK_ENO2)
+            enork2_extend_node<float>(a.phi_s, a.phi_n, a.out, a.flags, a.d, cp, a.v, g, a.stage, i, j, k);
         else
             extend_node<float, ENO3, true>(a.phi_s, a.phi_n, a.out, a.flags, a.d, cp, a.v, g, a.stage, i, j, k);
     }
@@ -312,7 +334,7 @@ int tile_pages(const Grid &g, int kind)
 int set_tile_pages(int rows, int cols, int pges, int kind, int pages)
 {
     if (rows <= 0 || cols <= 0 || pges <= 0) return VSL_ERR_SHAPE;
-    if (kind < 0 || kind > 2 || pages < 0 || pages > 65535) return VSL_ERR_VALUE;
+    if (kind < 0 || kind > 3 || pages < 0 || pages > 65535) return VSL_ERR_VALUE;
     std::lock_guard<std::mutex> lock(tile_mutex);
     for (int e = 0; e < tile_count; ++e) {
         TileEntry &t = tile_table[e];
@@ -391,7 +413,7 @@ cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const 
     a.speed = st.speed;
     a.dt = st.dt;
     unsigned *next = nullptr;
-    if (kind == SK_EXTEND) {
+    if (kind == SK_EXTEND || kind == SK_ENO2) {
         a.queue = st.flagged.idx;
         a.counter = st.flagged.count;
     } else {
@@ -402,24 +424,33 @@ cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const 
     a.stage = st.stage;
     a.kz = tile_pages(g, kind);
     dim3 gr = tiled_grid(g, a.kz), bl(TY, TX);
-    if (kind == SK_EXTEND) {
+    if (kind == SK_EXTEND || kind == SK_ENO2) {
+        // the tiled kernel is submitted first so that its blocks are dispatched ahead of the
+        // band kernel's (a grid-stride kernel whose blocks mostly find no work)
         SideLane *ln = side_lane(s);
-        cudaStream_t bs = s;
         cudaError_t e;
+        if (ln && (e = cudaEventRecord(ln->fork, s)) != cudaSuccess) return e;
+        if (kind == SK_ENO2)
+            k_stage_tiled<SK_ENO2><<<gr, bl, 0, s>>>(a);
+        else
+            k_stage_tiled<SK_EXTEND><<<gr, bl, 0, s>>>(a);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        cudaStream_t bs = s;
         if (ln) {
-            if ((e = cudaEventRecord(ln->fork, s)) != cudaSuccess) return e;
             if ((e = cudaStreamWaitEvent(ln->side, ln->fork, 0)) != cudaSuccess) return e;
             bs = ln->side;
         }
-        if (eno3)
+        if (kind == SK_ENO2)
+            k_band_stage<SK_ENO2, false><<<band_blocks(), 128, 0, bs>>>(a, st.cp, next);
+        else if (eno3)
             k_band_stage<SK_EXTEND, true><<<band_blocks(), 128, 0, bs>>>(a, st.cp, next);
         else
             k_band_stage<SK_EXTEND, false><<<band_blocks(), 128, 0, bs>>>(a, st.cp, next);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        if (ln && (e = cudaEventRecord(ln->join, bs)) != cudaSuccess) return e;
-        k_stage_tiled<SK_EXTEND><<<gr, bl, 0, s>>>(a);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        if (ln && (e = cudaStreamWaitEvent(s, ln->join, 0)) != cudaSuccess) return e;
+        if (ln) {
+            if ((e = cudaEventRecord(ln->join, bs)) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(s, ln->join, 0)) != cudaSuccess) return e;
+        }
         return cudaSuccess;
     }
     if (kind == SK_REINIT)

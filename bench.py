@@ -487,7 +487,7 @@ def relax_measure(torch, pkg, S, n: int = 96, steps: int = 10, fp64_steps: int =
     # with its own graph, recorded after the tiles are set)
     out["f32_default_tiles_ms"] = timed("f32", steps)[3]
     m, _, _ = setup("f32")
-    out["autotune"] = importlib.import_module(PKG + ".autotune").tune_shape(m, candidates=(2, 4, 8, 16, 32, 64))
+    out["autotune"] = importlib.import_module(PKG + ".autotune").tune_shape(m, candidates="waves")
     del m
     res = {}
     for prec, k in (("f32", steps), ("f64", fp64_steps)):

@@ -120,6 +120,9 @@ def test_tile_pages_table(vsl):
     assert call("vsl_set_tile_pages", 40, 36, 52, 1, 0) == 0  # back to the default
     assert call("vsl_tile_pages", 40, 36, 52, 1) == 16
     assert call("vsl_set_tile_pages", 0, 36, 52, 1, 8) == 2
-    assert call("vsl_set_tile_pages", 40, 36, 52, 3, 8) == 3
+    assert call("vsl_set_tile_pages", 40, 36, 52, 3, 8) == 0  # kind 3: the ENORK2 extension
+    assert call("vsl_tile_pages", 40, 36, 52, 3) == 8
+    assert call("vsl_set_tile_pages", 40, 36, 52, 3, 0) == 0
+    assert call("vsl_set_tile_pages", 40, 36, 52, 4, 8) == 3
     assert call("vsl_set_tile_pages", 40, 36, 52, 1, -1) == 3
     assert call("vsl_tile_pages", 40, 36, 52, 7) == 0

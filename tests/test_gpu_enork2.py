@@ -135,3 +135,21 @@ def test_config1_fp32(pkg, oracle_mod, config1):
     rel = max_rel(got, ref)
     print("ENORK2 FP32 extension rel error", rel)
     assert rel <= 5e-5
+
+
+def test_fp32_extension_ragged_tiles(pkg, oracle_mod):
+    """FP32 ENORK2 extension on a grid with partial tiles in every axis (37 rows, 29
+    columns, 11 pages: 32 x 8 tiles and fewer pages than a block marches): tiled uniform
+    nodes and the flagged list together, against the oracle."""
+    O = oracle_mod
+    K = O.kernels("port")
+    x, y, z = S.meshgrid(np.linspace(-1, 1, 29), np.linspace(-0.95, 0.95, 37), np.linspace(-0.7, 0.7, 11))
+    F = S.perturbed_sphere(x, y, z, r=0.55, centre=(0.1, -0.05, 0.02))
+    g = O.grid_from_mesh(x, y, z)
+    m = pkg.SDF3(pkg.GD3(x, y, z), Val=F, precision="f32")
+    C = S.surface_field(x, y, z)
+    ref = O.extend_enork2(K, g, F, C, 20)
+    got = host(m.ENORK2Extend(dev(C), 20))
+    rel = max_rel(got, ref)
+    print("ENORK2 FP32 extension (ragged tiles) rel error", rel)
+    assert rel <= 5e-5
