@@ -359,18 +359,23 @@ class SDF3:
             info = torch.empty(11, dtype=torch.float64, device="cuda") if info is None else info
             launch(info)
             return info
-        key = (args, _ptr(self.F), tuple(map(_ptr, self._dist())), _ptr(ws))
-        if getattr(self, "_relax_graph_key", None) != key:
+        # one graph per argument set (a driver alternating steps with and without the
+        # reinitialization keeps two); a new field or workspace drops the recorded ones
+        bufs = (_ptr(self.F), tuple(map(_ptr, self._dist())), _ptr(ws))
+        if getattr(self, "_relax_graph_bufs", None) != bufs:
+            self._relax_graphs, self._relax_graph_bufs = {}, bufs
+        entry = self._relax_graphs.get(args)
+        if entry is None:
             out = torch.empty(11, dtype=torch.float64, device="cuda")
             g = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g):
                 launch(out)
-            self._relax_graph, self._relax_graph_info, self._relax_graph_key = g, out, key
-        self._relax_graph.replay()
+            entry = self._relax_graphs[args] = (g, out)
+        entry[0].replay()
         if info is not None:
-            info.copy_(self._relax_graph_info)
+            info.copy_(entry[1])
             return info
-        return self._relax_graph_info
+        return entry[1]
 
     def _vesicle_step_graph(self, ext_iters: int, reinit_iters: int, cfl: float) -> torch.Tensor:
         key = (ext_iters, reinit_iters, cfl, _ptr(self.F), tuple(map(_ptr, self._dist())))
