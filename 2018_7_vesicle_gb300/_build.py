@@ -31,6 +31,8 @@ FILE_FLAGS = {
     "vsl_relax_f64.cu": ["-fmad=false"],
     "vsl_relax_f32.cu": ["-prec-div=false", "-prec-sqrt=false"],
     "vsl_spectral.cu": ["-fmad=false"],
+    "vsl_auxi_f64.cu": ["-fmad=false"],
+    "vsl_auxi_f32.cu": ["-prec-div=false", "-prec-sqrt=false"],
 }
 
 

@@ -30,6 +30,7 @@ SIGNATURES = {
     "vsl_set_calculus_toolbox": "p" * 18 + "pp" + _G + "d" + "i" + "s",
     "vsl_advection_step": "ppppp" + _G + "s",
     "vsl_weno_derivative": "ppppppp" + _G + "s",
+    "vsl_auxi_set_calculus_toolbox": "p" * 27 + "pp" + "p" * 13 + _G + "d" + "i" + "s",
     # ENORK2 drop-ins (FP64, reference argument order)
     "vsl_enork2_boundary_correction": "ppppppp" + "i" + _G + "s",
     "vsl_enork2_re_step": "pppp" + "pppppp" + _G + "i" + "s",
@@ -62,6 +63,8 @@ for _suf in ("f64", "f32"):
             f"vsl_relax_step_{_suf}": "p" + "pppppp" + "dddddd" + "ii" + "p" + _G + "pz" + "s",
             f"vsl_weno5_rk3_advection_adjoint_{_suf}": "ppppp" + "pppp" + _G + "pz" + "s",
             f"vsl_weno5_rk3_reinitialization_adjoint_{_suf}": "pipp" + _G + "pz" + "s",
+            f"vsl_a_set_calculus_toolbox_{_suf}": "ppp" + _G + "pz" + "s",
+            f"vsl_masked_integral_{_suf}": "pppppp" + "p" + _G + "pz" + "s",
         }
     )
 
@@ -82,6 +85,8 @@ OP = {
     "surface_redistance_enork2": 14,
     "smooth": 15,
     "relax_step": 16,
+    "aux_toolbox": 17,
+    "masked_integral": 18,
 }
 
 

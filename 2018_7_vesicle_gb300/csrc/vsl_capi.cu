@@ -132,6 +132,22 @@ ReduceWork carve_reduce(Bump &w, const Grid &g, int ncomp)
     return r;
 }
 
+// the per-node values pass 2 of the auxiliary toolbox reads, where the caller does not
+// ask for them as outputs (sized for all of them)
+template <typename T> AuxKeep<T> carve_aux(Bump &w, const Grid &g)
+{
+    AuxKeep<T> k;
+    k.cx = w.take<T>(g.num);
+    k.cy = w.take<T>(g.num);
+    k.cz = w.take<T>(g.num);
+    k.ncr = w.take<T>(g.num);
+    k.agm = w.take<T>(g.num);
+    k.adelta = w.take<T>(g.num);
+    k.aheav = w.take<T>(g.num);
+    k.fheav = w.take<T>(g.num);
+    return k;
+}
+
 template <typename T> struct StepWork {
     T *vn;
     Ptr3<T> nrm;
@@ -239,6 +255,8 @@ size_t measure(int op, const Grid &g, int elem)
             break;
         }
         case VSL_OP_RELAX_STEP: carve_relax<T>(w, g); break;
+        case VSL_OP_AUX_TOOLBOX: carve_aux<T>(w, g); break;
+        case VSL_OP_MASKED_INTEGRAL: carve_reduce(w, g, 1); break;
         default: return false;
         }
         return true;
@@ -524,6 +542,53 @@ int op_area_volume(const T *F, double *av, int rows, int cols, int pges, double 
     int nb = 0;
     VSL_TRY(launch_toolbox<T>(F, none, g, ds, r.partials, &nb, s));
     VSL_TRY(launch_sum_partials(r.partials, nb, 2, std::pow(ds, 3), av, s));
+    return VSL_OK;
+}
+
+// GPUAsetCalculusToolBox.m:2-63 for the auxiliary level set A on F: out holds the 27 fields
+// of auxi_set_calculus_toolbox, then AFDiracDelta and ADiracDeltaDn; null entries are not
+// written.
+template <typename T>
+int op_aux_toolbox(const T *A, const T *F, T *const *out, int rows, int cols, int pges, double dx, double dy,
+                   double dz, void *ws, size_t bytes, cudaStream_t s)
+{
+    if (any_null(A, F, out)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    if (int st = check_ws(VSL_OP_AUX_TOOLBOX, g, sizeof(T), ws, bytes)) return st;
+    Bump b(ws);
+    AuxKeep<T> keep = carve_aux<T>(b, g);
+    AuxOut<T> o;
+    for (int q = 0; q < AUX_OUT_FIELDS; ++q) o.f[q] = out[q];
+    // pass 2 reads the caller's arrays where the caller asked for those fields
+    if (o.f[4]) keep.cx = o.f[4];
+    if (o.f[5]) keep.cy = o.f[5];
+    if (o.f[6]) keep.cz = o.f[6];
+    if (o.f[7]) keep.ncr = o.f[7];
+    if (o.f[3]) keep.agm = o.f[3];
+    if (o.f[26]) keep.adelta = o.f[26];
+    if (o.f[25]) keep.aheav = o.f[25];
+    VSL_TRY(launch_aux_toolbox<T>(A, F, o, keep, g, (dx + dy + dz) / 3, s));
+    return VSL_OK;
+}
+
+// sum over |F| < 2Ds (and |A| < 2Ds where A is given) of ((f0 f1) f2) (1 - one_minus) Ds^3,
+// the factors that are given, in FP64 (SDF3.m:82-85, 212-227)
+template <typename T>
+int op_masked_integral(const T *F, const T *A, const T *f0, const T *f1, const T *f2, const T *one_minus,
+                       double *result, int rows, int cols, int pges, double dx, double dy, double dz, void *ws,
+                       size_t bytes, cudaStream_t s)
+{
+    if (any_null(F, result)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    if (int st = check_ws(VSL_OP_MASKED_INTEGRAL, g, sizeof(T), ws, bytes)) return st;
+    Bump b(ws);
+    ReduceWork r = carve_reduce(b, g, 1);
+    const double ds = (dx + dy + dz) / 3;
+    int nb = 0;
+    VSL_TRY(launch_masked_sum<T>(F, A, f0, f1, f2, one_minus, g, ds, r.partials, &nb, s));
+    VSL_TRY(launch_sum_partials(r.partials, nb, 1, std::pow(ds, 3), result, s));
     return VSL_OK;
 }
 
@@ -1053,6 +1118,19 @@ size_t vsl_workspace_bytes(int op, int rows, int cols, int pges, int elem_bytes)
                                                      void *ws, size_t bytes, vsl_stream_t stream)                  \
     {                                                                                                              \
         return op_reinit_adjoint<T>(F0, iteration, lam, tape, rows, cols, pges, dx, dy, dz, ws, bytes, stream);    \
+    }                                                                                                              \
+    int vsl_a_set_calculus_toolbox_##SUF(const T *A, const T *F, T *const *out, int rows, int cols, int pges,      \
+                                         double dx, double dy, double dz, void *ws, size_t bytes,                  \
+                                         vsl_stream_t stream)                                                      \
+    {                                                                                                              \
+        return op_aux_toolbox<T>(A, F, out, rows, cols, pges, dx, dy, dz, ws, bytes, stream);                      \
+    }                                                                                                              \
+    int vsl_masked_integral_##SUF(const T *F, const T *A, const T *f0, const T *f1, const T *f2,                   \
+                                  const T *one_minus, double *result, int rows, int cols, int pges, double dx,     \
+                                  double dy, double dz, void *ws, size_t bytes, vsl_stream_t stream)               \
+    {                                                                                                              \
+        return op_masked_integral<T>(F, A, f0, f1, f2, one_minus, result, rows, cols, pges, dx, dy, dz, ws, bytes, \
+                                     stream);                                                                      \
     }
 
 VSL_TYPED(f64, double)

@@ -160,6 +160,34 @@ cudaError_t launch_time_step(const double *partials, int nblocks, double cfl_ds,
                              cudaStream_t s);
 int toolbox_partial_blocks(const Grid &g);
 
+// ---- auxiliary level set toolbox and masked integrals (vsl_auxi.cuh) -------------------
+// The 27 fields of auxi_set_calculus_toolbox in its argument order, then AFDiracDelta and
+// ADiracDeltaDn (null pointers are skipped).
+constexpr int AUX_OUT_FIELDS = 29;
+template <typename T> struct AuxOut {
+    T *f[AUX_OUT_FIELDS];
+};
+// F's toolbox inputs of the reference kernel: Fx Fy Fz FGradMag Nx Ny Nz Fxx Fyy Fzz Fxy Fyz Fzx
+template <typename T> struct AuxFIn {
+    const T *f[13];
+};
+// per-node values pass 2 of the fused form reads (outputs or workspace)
+template <typename T> struct AuxKeep {
+    T *cx, *cy, *cz, *ncr, *agm, *adelta, *aheav, *fheav;
+};
+template <typename T> struct AuxKeepC {
+    const T *cx, *cy, *cz, *ncr, *agm, *adelta, *aheav, *fheav;
+};
+template <typename T>
+cudaError_t launch_aux_toolbox(const T *A, const T *F, AuxOut<T> o, AuxKeep<T> keep, const Grid &g, double ds,
+                               cudaStream_t s);
+cudaError_t launch_auxi_dropin(AuxOut<double> o, const double *lsf, const double *ahp, AuxFIn<double> fin,
+                               const Grid &g, double ds, cudaStream_t s);
+// per-block FP64 partials of the masked product sum (see k_masked_sum)
+template <typename T>
+cudaError_t launch_masked_sum(const T *F, const T *A, const T *f0, const T *f1, const T *f2, const T *om,
+                              const Grid &g, double ds, double *partials, int *nblocks, cudaStream_t s);
+
 // ---- adjoint kernels (vsl_adjoint.cu), T in {float, double} ------------------------
 // W: 21 slot fields of g.num values each (slot ax*7 + o: line offset o - 3 along ax)
 template <typename T>

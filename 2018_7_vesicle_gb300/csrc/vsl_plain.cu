@@ -640,6 +640,31 @@ int vsl_set_calculus_toolbox(double *Fx, double *Fy, double *Fz, double *FGradMa
     return launch_status(cudaGetLastError());
 }
 
+int vsl_auxi_set_calculus_toolbox(
+    double *Ax, double *Ay, double *Az, double *AGradMag, double *Cx, double *Cy, double *Cz, double *NormCrossAF,
+    double *tx, double *ty, double *tz, double *nx, double *ny, double *nz, double *Axx, double *Ayy, double *Azz,
+    double *Axy, double *Ayz, double *Azx, double *ALaplacian, double *GeodesicCurvature, double *NormalCurvature,
+    double *GeodesicTorsion, double *BPerpendicular, double *AHeaviside, double *ADiracDelta, const double *lsf,
+    const double *AHPrimal, const double *Fx, const double *Fy, const double *Fz, const double *FGradMag,
+    const double *Nx, const double *Ny, const double *Nz, const double *Fxx, const double *Fyy, const double *Fzz,
+    const double *Fxy, const double *Fyz, const double *Fzx, int rows, int cols, int pges, double dx, double dy,
+    double dz, double ds, int num_ele, vsl_stream_t stream)
+{
+    AuxOut<double> o = {{Ax, Ay, Az, AGradMag, Cx, Cy, Cz, NormCrossAF, tx, ty, tz, nx, ny, nz, Axx, Ayy, Azz, Axy,
+                         Ayz, Azx, ALaplacian, GeodesicCurvature, NormalCurvature, GeodesicTorsion, BPerpendicular,
+                         AHeaviside, ADiracDelta, nullptr, nullptr}};
+    for (int q = 0; q < AUX_OUT_FIELDS - 2; ++q)
+        if (o.f[q] == nullptr) return VSL_ERR_NULL;
+    AuxFIn<double> fin = {{Fx, Fy, Fz, FGradMag, Nx, Ny, Nz, Fxx, Fyy, Fzz, Fxy, Fyz, Fzx}};
+    for (int q = 0; q < 13; ++q)
+        if (fin.f[q] == nullptr) return VSL_ERR_NULL;
+    if (any_null(lsf, AHPrimal)) return VSL_ERR_NULL;
+    if (int st = prologue(rows, cols, pges, dx, dy, dz, num_ele, true)) return st;
+    if (!(ds > 0)) return VSL_ERR_VALUE;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    return launch_status(launch_auxi_dropin(o, lsf, AHPrimal, fin, g, ds, (cudaStream_t)stream));
+}
+
 int vsl_advection_step(double *astep, const double *vx, const double *vy, const double *vz, const double *lsf,
                        int rows, int cols, int pges, double dx, double dy, double dz, vsl_stream_t stream)
 {

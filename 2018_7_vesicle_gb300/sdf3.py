@@ -150,6 +150,11 @@ class GD3:
 
 TOOLBOX_FIELDS = ("Fx", "Fy", "Fz", "FGradMag", "Nx", "Ny", "Nz", "Fxx", "Fyy", "Fzz", "Fxy", "Fyz", "Fzx",
                   "FLaplacian", "MeanCurvature", "GaussianCurvature", "Heaviside", "DiracDelta")
+# GPUAsetCalculusToolBox.m's fields: the 27 of auxi_set_calculus_toolbox in its argument
+# order, then AFDiracDelta and ADiracDeltaDn
+AUX_FIELDS = ("Ax", "Ay", "Az", "AGradMag", "Cx", "Cy", "Cz", "NormCrossAF", "tx", "ty", "tz", "nx", "ny", "nz",
+              "Axx", "Ayy", "Azz", "Axy", "Ayz", "Azx", "ALaplacian", "GeodesicCurvature", "NormalCurvature",
+              "GeodesicTorsion", "BPerpendicular", "AHeaviside", "ADiracDelta", "AFDiracDelta", "ADiracDeltaDn")
 
 
 class SDF3:
@@ -163,6 +168,7 @@ class SDF3:
         self.dtype = _DTYPES[precision]
         self.elem = 8 if precision == "f64" else 4
         self.F = None if Val is None else as_field(Val, self.dtype)
+        self.A = None  # the auxiliary level set of a multiphase vesicle (SDF3.m's A)
         self.xpr = self.xpl = self.ypf = self.ypb = self.zpu = self.zpd = None
         self._ws = {}
 
@@ -298,12 +304,62 @@ class SDF3:
     def calVolume(self) -> float:
         return float(self.area_volume()[1])
 
+    def _masked_integral(self, A, f0, f1, f2, one_minus) -> float:
+        out = torch.empty(1, dtype=torch.float64, device="cuda")
+        ws = self.workspace("masked_integral")
+        fs = [None if t is None else self._field(t) for t in (A, f0, f1, f2, one_minus)]
+        lib().call(self._fn("vsl_masked_integral"), _ptr(self.F), *map(_ptr, fs), _ptr(out), *self.GD3.args(),
+                   _ptr(ws), ws.numel(), _stream())
+        return float(out)
+
     def surfaceIntegral(self, field) -> float:
-        """SDF3.m:82-85; uses the toolbox fields of the last GPUsetCalculusToolBox."""
-        F = as_field(self.F, torch.float64)
-        mask = F.abs() < 2 * self.GD3.Ds
-        f = as_field(field, torch.float64)
-        return float((f[mask] * self.DiracDelta.double()[mask] * self.FGradMag.double()[mask]).sum()) * self.GD3.Ds ** 3
+        """SDF3.m:82-85: sum of (field DiracDelta) FGradMag over |F| < 2Ds, times Ds^3 (FP64);
+        the toolbox fields of the last GPUsetCalculusToolBox."""
+        return self._masked_integral(None, field, self.DiracDelta, self.FGradMag, None)
+
+    # -- the auxiliary level set of multiphase vesicles ----------------------------------
+    def GPUAsetCalculusToolBox(self, fields=None):
+        """GPUAsetCalculusToolBox.m:2-63: the toolbox of the auxiliary level set self.A on
+        self.F, stored as attributes (AUX_FIELDS; `fields` limits it to a subset), from A and F
+        alone.  AHPrimal = max(A, 0) as the MATLAB method sets it."""
+        if self.A is None:
+            raise ValueError("set the auxiliary level set (obj.A) first")
+        import ctypes
+
+        self.A = self._field(self.A)
+        names = AUX_FIELDS if fields is None else tuple(fields)
+        unknown = set(names) - set(AUX_FIELDS)
+        if unknown:
+            raise ValueError(f"unknown auxiliary toolbox fields: {sorted(unknown)}")
+        outs = {n: colmajor_empty(self.GD3.Size, self.dtype) for n in names}
+        ptrs = (ctypes.c_void_p * len(AUX_FIELDS))(*[_ptr(outs.get(n)) or None for n in AUX_FIELDS])
+        ws = self.workspace("aux_toolbox")
+        lib().call(self._fn("vsl_a_set_calculus_toolbox"), _ptr(self.A), _ptr(self.F), ctypes.addressof(ptrs),
+                   *self.GD3.args(), _ptr(ws), ws.numel(), _stream())
+        for n, t in outs.items():
+            setattr(self, n, t)
+        self.AHPrimal = torch.clamp(self.A, min=0)
+
+    def calLength(self) -> float:
+        """SDF3.m:212-215: length of the curve A = 0 on F = 0, sum of AFDiracDelta NormCrossAF
+        over |F|, |A| < 2Ds, times Ds^3 (FP64)."""
+        return self._masked_integral(self.A, self.AFDiracDelta, self.NormCrossAF, None, None)
+
+    def LineIntegral(self, field) -> float:
+        """SDF3.m:216-219: the integral of field along the curve A = 0 on F = 0."""
+        return self._masked_integral(self.A, field, self.AFDiracDelta, self.NormCrossAF, None)
+
+    def AcalArea(self) -> float:
+        """SDF3.m:220-223: area of the part of the surface where A < 0."""
+        return self._masked_integral(None, self.DiracDelta, None, None, self.AHeaviside)
+
+    def AsurfaceIntegral(self, field) -> float:
+        """SDF3.m:224-227: the surface integral of field over the part where A < 0."""
+        return self._masked_integral(None, field, self.DiracDelta, self.FGradMag, self.AHeaviside)
+
+    def BivalueField(self, valNeg, valPos):
+        """SDF3.m:228-232: valPos where A > 0 and valNeg where A < 0, blended by AHeaviside."""
+        return valPos * self.AHeaviside + valNeg * (1 - self.AHeaviside)
 
     # -- advection and the composite step ----------------------------------------------------
     def WENO5RK3Advection(self, F, vx, vy, vz, dt, steps: int = 1):

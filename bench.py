@@ -438,6 +438,41 @@ def differentiation_measure(torch, pkg, S, fd_check: bool = False, n: int = 128)
     return out
 
 
+def aux_measure(torch, pkg, S, n: int = N, reps: int = 5):
+    """The auxiliary level set toolbox of multiphase vesicles (GPUAsetCalculusToolBox.m) at
+    n^3: the 256^3 vesicle with a plane A = z - 0.1 marking two domains, all 29 fields
+    written, FP32 and FP64, CUDA events over `reps` calls after a warm-up.  Algorithmic
+    bytes: the reference kernel's own dataflow, 42 words per node (A, AHPrimal and 13 F
+    toolbox fields read, 27 fields written), the MATLAB glue not counted."""
+    x, y, z, F0 = S.vesicle_256(n, seed=0, device="cuda")
+    h = 3.0 / (n - 1)
+    grid = pkg.GD3(x, y, z, spacing=(h, h, h))
+    A = (z - 0.1).contiguous()
+    del x, y
+    grid.X = grid.Y = grid.Z = None
+    hbm, peak_kind = peaks()
+    out = {"workload": f"auxiliary toolbox {n}^3, all 29 fields", "algorithmic_words_per_node": 42}
+    for prec, w in (("f32", 4), ("f64", 8)):
+        m = pkg.SDF3(grid, Val=F0, precision=prec)
+        m.A = A
+        m.GPUAsetCalculusToolBox()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            m.GPUAsetCalculusToolBox()
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / reps
+        gbs = 42 * w * n**3 / (ms / 1e3) / 1e9
+        m.GPUsetCalculusToolBox()
+        out[prec] = {"ms": ms, "effective_gbs": gbs, "frac_of_" + peak_kind + "_hbm": gbs / hbm,
+                     "calLength": m.calLength(), "AcalArea": m.AcalArea()}
+        del m
+        torch.cuda.empty_cache()
+    return out
+
+
 RELAX_EXT, RELAX_RE = 100, 100  # p00_test_singlephase_relax.m:75, 86, 121, 192
 
 
@@ -534,6 +569,7 @@ def main():
     ap.add_argument("--no-differentiation", action="store_true")
     ap.add_argument("--no-precision", action="store_true")
     ap.add_argument("--no-relax", action="store_true")
+    ap.add_argument("--no-aux", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--fd-check", action="store_true",
                     help="also check the 128^3 amplitude gradient against FP64 central differences")
@@ -683,6 +719,11 @@ def main():
         torch.cuda.empty_cache()
         differentiation = differentiation_measure(torch, pkg, S, fd_check=args.fd_check)
 
+    aux = None
+    if not args.no_aux and rank == 0:
+        torch.cuda.empty_cache()
+        aux = aux_measure(torch, pkg, S)
+
     relax = None
     if not args.no_relax and rank == 0:
         torch.cuda.empty_cache()
@@ -718,6 +759,7 @@ def main():
         "precision": precision,
         "differentiation": differentiation,
         "relax": relax,
+        "auxiliary_toolbox": aux,
         "last_info": {"area": info_h[0], "volume": info_h[1], "dt": info_h[2], "max_speed": info_h[3]},
         "cpu_baseline": cpu,
     }

@@ -183,7 +183,9 @@ enum {
     VSL_OP_EXTEND_ENORK2 = 13,
     VSL_OP_SURFACE_REDISTANCE_ENORK2 = 14,
     VSL_OP_SMOOTH = 15,
-    VSL_OP_RELAX_STEP = 16
+    VSL_OP_RELAX_STEP = 16,
+    VSL_OP_AUX_TOOLBOX = 17,
+    VSL_OP_MASKED_INTEGRAL = 18
 };
 
 /* Tuning of the FP32 tiled stage kernels (no counterpart in the reference).  Each block
@@ -376,6 +378,58 @@ int vsl_relax_step_f32(float *F, float *xpr, float *xpl, float *ypf, float *ypb,
                        double V0, double kappa, double spon_c, double cfl, double alpha, int ext_iters,
                        int reinit_iters, double *info, int rows, int cols, int pges, double dx, double dy, double dz,
                        void *workspace, size_t workspace_bytes, vsl_stream_t stream);
+
+/* ---- the auxiliary level set of multiphase vesicles ----------------------------------
+ *
+ * A second level set A marks the domains on the vesicle surface F = 0; its zero set on the
+ * surface is the domain boundary (a curve). */
+
+/* ref: CUDA_Code/4_0_Calculus_ToolBox/auxi_set_calculus_toolbox.cu:10-11 (drop-in, FP64):
+ * A's central differences, the curve tangent t = (grad F x grad A) / |.|, the conormal
+ * n = t x N, geodesic and normal curvature, geodesic torsion, BPerpendicular, and A's
+ * Heaviside/Dirac functions from AHPrimal = max(A, 0); F's toolbox fields are inputs.
+ * Every output is written at every node. */
+int vsl_auxi_set_calculus_toolbox(
+    double *Ax, double *Ay, double *Az, double *AGradMag, double *Cx, double *Cy, double *Cz, double *NormCrossAF,
+    double *tx, double *ty, double *tz, double *nx, double *ny, double *nz, double *Axx, double *Ayy, double *Azz,
+    double *Axy, double *Ayz, double *Azx, double *ALaplacian, double *GeodesicCurvature, double *NormalCurvature,
+    double *GeodesicTorsion, double *BPerpendicular, double *AHeaviside, double *ADiracDelta, const double *lsf,
+    const double *AHPrimal, const double *Fx, const double *Fy, const double *Fz, const double *FGradMag,
+    const double *Nx, const double *Ny, const double *Nz, const double *Fxx, const double *Fyy, const double *Fzz,
+    const double *Fxy, const double *Fyz, const double *Fzx, int rows, int cols, int pges, double dx, double dy,
+    double dz, double ds, int num_ele, vsl_stream_t stream);
+
+/* ref: +SD/@SDF3/GPUAsetCalculusToolBox.m:2-63.  The auxiliary toolbox of A on F, reading
+ * only A and F (F's gradient, Hessian, normal and Heaviside function are recomputed with
+ * the calculus toolbox's own expressions).  out: a host array of 29 device pointers, the
+ * 27 fields of vsl_auxi_set_calculus_toolbox in its order, then AFDiracDelta = (C . (grad
+ * H_F x grad H_A)) / |C|^2 and ADiracDeltaDn = (Laplacian(AHeaviside) - ADiracDelta
+ * Laplacian(A)) / |grad A| (GD3's periodic operators); a null entry is not written.
+ * Ds = (dx + dy + dz) / 3.  Workspace op VSL_OP_AUX_TOOLBOX. */
+int vsl_a_set_calculus_toolbox_f64(const double *A, const double *F, double *const *out, int rows, int cols,
+                                   int pges, double dx, double dy, double dz, void *workspace,
+                                   size_t workspace_bytes, vsl_stream_t stream);
+int vsl_a_set_calculus_toolbox_f32(const float *A, const float *F, float *const *out, int rows, int cols,
+                                   int pges, double dx, double dy, double dz, void *workspace,
+                                   size_t workspace_bytes, vsl_stream_t stream);
+
+/* ref: +SD/@SDF3/SDF3.m:82-85 (surfaceIntegral), 212-219 (calLength, LineIntegral),
+ * 220-227 (AcalArea, AsurfaceIntegral).  *result (device) = Ds^3 times the FP64 sum over
+ * the nodes with |F| < 2Ds (and |A| < 2Ds where A is not null) of ((f0 f1) f2)
+ * (1 - one_minus), a null factor left out (a null f0 counts as 1):
+ *   surfaceIntegral(f)  = (F, null, f, DiracDelta, FGradMag, null)
+ *   calLength           = (F, A, AFDiracDelta, NormCrossAF, null, null)
+ *   LineIntegral(f)     = (F, A, f, AFDiracDelta, NormCrossAF, null)
+ *   AcalArea            = (F, null, DiracDelta, null, null, AHeaviside)
+ *   AsurfaceIntegral(f) = (F, null, f, DiracDelta, FGradMag, AHeaviside)
+ * Workspace op VSL_OP_MASKED_INTEGRAL. */
+int vsl_masked_integral_f64(const double *F, const double *A, const double *f0, const double *f1,
+                            const double *f2, const double *one_minus, double *result, int rows, int cols, int pges,
+                            double dx, double dy, double dz, void *workspace, size_t workspace_bytes,
+                            vsl_stream_t stream);
+int vsl_masked_integral_f32(const float *F, const float *A, const float *f0, const float *f1, const float *f2,
+                            const float *one_minus, double *result, int rows, int cols, int pges, double dx,
+                            double dy, double dz, void *workspace, size_t workspace_bytes, vsl_stream_t stream);
 
 /* ---- adjoints (no counterpart in the reference, which has no derivatives) -------------
  *

@@ -50,6 +50,7 @@ SIGNATURES = {
     "advection_step": "pppppiiiddd",
     "weno_derivative": "pppppppiiiddd",
     "set_calculus_toolbox": "ppppppppppppppppppppiiiddddi",
+    "auxi_set_calculus_toolbox": "p" * 42 + "iiiddddi",
     "enork2_boundary_correction": "pppppppiiiiddd",
     "enork2_re_step": "ppppppppppiiidddi",
     "enork2_upwind_normal": "ppppppppppiiidddi",
@@ -458,6 +459,73 @@ def calculus_toolbox(K, g: Grid, F):
     out = {n: zeros(g) for n in TOOLBOX_FIELDS}
     K.set_calculus_toolbox(*[out[n] for n in TOOLBOX_FIELDS], F, hp, *g.args(), g.ds, g.num_ele)
     return out
+
+
+AUX_FIELDS = ("Ax", "Ay", "Az", "AGradMag", "Cx", "Cy", "Cz", "NormCrossAF", "tx", "ty", "tz", "nx", "ny", "nz",
+              "Axx", "Ayy", "Azz", "Axy", "Ayz", "Azx", "ALaplacian", "GeodesicCurvature", "NormalCurvature",
+              "GeodesicTorsion", "BPerpendicular", "AHeaviside", "ADiracDelta")
+AUX_INPUTS = ("Fx", "Fy", "Fz", "FGradMag", "Nx", "Ny", "Nz", "Fxx", "Fyy", "Fzz", "Fxy", "Fyz", "Fzx")
+
+
+def periodic_gradient(g: Grid, f):
+    """GD3.Gradient (GD3.m:314-318): central differences with circshift neighbours,
+    (f(x + h) - f(x - h)) / (2 h) per axis; arrays are (rows = y, cols = x, pges = z)."""
+    f = F64(f)
+    fx = (np.roll(f, -1, axis=1) - np.roll(f, 1, axis=1)) / (2 * g.dx)
+    fy = (np.roll(f, -1, axis=0) - np.roll(f, 1, axis=0)) / (2 * g.dy)
+    fz = (np.roll(f, -1, axis=2) - np.roll(f, 1, axis=2)) / (2 * g.dz)
+    return F64(fx), F64(fy), F64(fz)
+
+
+def auxiliary_toolbox(K, g: Grid, F, A, tb=None):
+    """GPUAsetCalculusToolBox.m:2-63: the toolbox of the auxiliary level set A with F's
+    toolbox fields (`tb`, computed when not given): the 27 kernel fields, then
+    AFDiracDelta = (C . (grad H_F x grad H_A)) / |C|^2 and
+    ADiracDeltaDn = (Laplacian(H_A) - ADiracDelta Laplacian(A)) / |grad A| with the
+    periodic GD3 operators."""
+    F, A = F64(F), F64(A)
+    tb = calculus_toolbox(K, g, F) if tb is None else tb
+    out = {n: zeros(g) for n in AUX_FIELDS}
+    K.auxi_set_calculus_toolbox(*[out[n] for n in AUX_FIELDS], A, F64(np.maximum(A, 0)),
+                                *[F64(tb[n]) for n in AUX_INPUTS], *g.args(), g.ds, g.num_ele)
+    h1x, h1y, h1z = periodic_gradient(g, out["AHeaviside"])
+    h2x, h2y, h2z = periodic_gradient(g, tb["Heaviside"])
+    chx, chy, chz = h2y * h1z - h2z * h1y, h2z * h1x - h2x * h1z, h2x * h1y - h2y * h1x
+    dot = out["Cx"] * chx + out["Cy"] * chy + out["Cz"] * chz
+    out["AFDiracDelta"] = F64(dot / (out["NormCrossAF"] * out["NormCrossAF"]))
+    out["ADiracDeltaDn"] = F64((laplacian(g, out["AHeaviside"]) - out["ADiracDelta"] * laplacian(g, A))
+                               / out["AGradMag"])
+    return out, tb
+
+
+def line_mask(g: Grid, F, A):
+    return (np.abs(F64(F)) < 2 * g.ds) & (np.abs(F64(A)) < 2 * g.ds)
+
+
+def cal_length(g: Grid, F, A, aux) -> float:
+    """SDF3.calLength (SDF3.m:212-215): sum(AFDiracDelta .* NormCrossAF) over |F|, |A| < 2 Ds."""
+    m = line_mask(g, F, A)
+    return exact_sum(aux["AFDiracDelta"][m] * aux["NormCrossAF"][m]) * g.ds ** 3
+
+
+def line_integral(g: Grid, F, A, field, aux) -> float:
+    """SDF3.LineIntegral (SDF3.m:216-219): sum((f .* AFDiracDelta) .* NormCrossAF)."""
+    m = line_mask(g, F, A)
+    return exact_sum((F64(field)[m] * aux["AFDiracDelta"][m]) * aux["NormCrossAF"][m]) * g.ds ** 3
+
+
+def a_cal_area(g: Grid, F, tb, aux) -> float:
+    """SDF3.AcalArea (SDF3.m:220-223): sum(DiracDelta .* (1 - AHeaviside)) over |F| < 2 Ds."""
+    m = np.abs(F64(F)) < 2 * g.ds
+    return exact_sum(F64(tb["DiracDelta"])[m] * (1 - aux["AHeaviside"][m])) * g.ds ** 3
+
+
+def a_surface_integral(g: Grid, F, field, tb, aux) -> float:
+    """SDF3.AsurfaceIntegral (SDF3.m:224-227):
+    sum(((f .* DiracDelta) .* FGradMag) .* (1 - AHeaviside)) over |F| < 2 Ds."""
+    m = np.abs(F64(F)) < 2 * g.ds
+    return exact_sum(((F64(field)[m] * F64(tb["DiracDelta"])[m]) * F64(tb["FGradMag"])[m])
+                     * (1 - aux["AHeaviside"][m])) * g.ds ** 3
 
 
 def exact_sum(a) -> float:

@@ -14,7 +14,7 @@
  *                        boundary_interpolant.cu,extend_step.cu}
  *   2_1_WENORK3_Extend/wenork3_extend.cu
  *   1_0_ENORK2_Reinitialization/boundary_correction.cu, 2_0_ENORK2_Extend/enork2_extend.cu
- *   4_0_Calculus_ToolBox/{set_calculus_toolbox.cu,advection_step.cu}
+ *   4_0_Calculus_ToolBox/{set_calculus_toolbox.cu,auxi_set_calculus_toolbox.cu,advection_step.cu}
  *   5_0_Nonoscillating_Reconstruction/nonoscillating_interpolant.cu
  *
  * Arithmetic is kept in the reference's operation order (same association, same
@@ -1072,6 +1072,126 @@ void orc_enork2_extend_step(double *step, const double *deltat, const double *ls
         step[c] = (dmin(0, v[0][c]) * df[0] + dmax(0, v[0][c]) * db[0] + dmin(0, v[1][c]) * df[1] +
                    dmax(0, v[1][c]) * db[1] + dmin(0, v[2][c]) * df[2] + dmax(0, v[2][c]) * db[2]) *
                   deltat[c];
+    }
+}
+
+/* auxi_set_calculus_toolbox (auxi_set_calculus_toolbox.cu:10-199): the toolbox of the
+ * auxiliary level set A on the surface of F.  Central differences of A (clamped), the
+ * tangent t = (grad F x grad A) / |grad F x grad A| of the curve A = 0 on F = 0, the
+ * conormal n = t x N, geodesic and normal curvature, geodesic torsion, the perpendicular
+ * curvature, and the Heaviside/Dirac functions of A from the primal AHPrimal = max(A, 0);
+ * F's toolbox fields are inputs.  Vector norms are floored at 1e-14 (norm(),
+ * shared_utilities.cup:8-12). */
+static inline double norm3(double x, double y, double z) { return dmax(sqrt(x * x + y * y + z * z), 1e-14); }
+
+void orc_auxi_set_calculus_toolbox(
+    double *Ax, double *Ay, double *Az, double *AGradMag, double *ACx, double *ACy, double *ACz,
+    double *ANormCrossAF, double *Tx, double *Ty, double *Tz, double *Anx, double *Any, double *Anz, double *Axx,
+    double *Ayy, double *Azz, double *Axy, double *Ayz, double *Azx, double *ALaplacian, double *GeodesicCurvature,
+    double *NormalCurvature, double *GeodesicTorsion, double *BPerpendicular, double *AHeaviside,
+    double *ADiracDelta, const double *lsf, const double *AHPrimal, const double *Fx, const double *Fy,
+    const double *Fz, const double *FGradMag, const double *Nx, const double *Ny, const double *Nz,
+    const double *Fxx, const double *Fyy, const double *Fzz, const double *Fxy, const double *Fyz,
+    const double *Fzx, int rows, int cols, int pges, double dx, double dy, double dz, double ds, int num_ele)
+{
+    (void)num_ele;
+    grid3 g = {rows, cols, pges};
+    FOR_EACH_NODE(g)
+    {
+        int64_t c = node(&g, i, j, k);
+        int64_t xp = node(&g, i, j + 1, k), xm = node(&g, i, j - 1, k);
+        int64_t yp = node(&g, i + 1, j, k), ym = node(&g, i - 1, j, k);
+        int64_t zp = node(&g, i, j, k + 1), zm = node(&g, i, j, k - 1);
+        const double *a = lsf;
+        double ax = (a[xp] - a[xm]) / (2 * dx);
+        double ay = (a[yp] - a[ym]) / (2 * dy);
+        double az = (a[zp] - a[zm]) / (2 * dz);
+        double agm = norm3(ax, ay, az);
+        Ax[c] = ax;
+        Ay[c] = ay;
+        Az[c] = az;
+        AGradMag[c] = agm;
+
+        double fx = Fx[c], fy = Fy[c], fz = Fz[c];
+        double cx = fy * az - fz * ay, cy = fz * ax - fx * az, cz = fx * ay - fy * ax;
+        double ncr = norm3(cx, cy, cz);
+        ACx[c] = cx;
+        ACy[c] = cy;
+        ACz[c] = cz;
+        ANormCrossAF[c] = ncr;
+        double tx = cx / ncr, ty = cy / ncr, tz = cz / ncr;
+        Tx[c] = tx;
+        Ty[c] = ty;
+        Tz[c] = tz;
+        double fnx = Nx[c], fny = Ny[c], fnz = Nz[c];
+        double nx = ty * fnz - tz * fny, ny = tz * fnx - tx * fnz, nz = tx * fny - ty * fnx;
+        Anx[c] = nx;
+        Any[c] = ny;
+        Anz[c] = nz;
+
+        double axx = (a[xp] - 2 * a[c] + a[xm]) / (dx * dx);
+        double ayy = (a[yp] - 2 * a[c] + a[ym]) / (dy * dy);
+        double azz = (a[zp] - 2 * a[c] + a[zm]) / (dz * dz);
+        double axy = (a[node(&g, i + 1, j + 1, k)] + a[node(&g, i - 1, j - 1, k)] - a[node(&g, i + 1, j - 1, k)] -
+                      a[node(&g, i - 1, j + 1, k)]) / (4 * ds * ds);
+        double ayz = (a[node(&g, i + 1, j, k + 1)] + a[node(&g, i - 1, j, k - 1)] - a[node(&g, i + 1, j, k - 1)] -
+                      a[node(&g, i - 1, j, k + 1)]) / (4 * ds * ds);
+        double azx = (a[node(&g, i, j + 1, k + 1)] + a[node(&g, i, j - 1, k - 1)] - a[node(&g, i, j + 1, k - 1)] -
+                      a[node(&g, i, j - 1, k + 1)]) / (4 * ds * ds);
+        double alap = axx + ayy + azz;
+        Axx[c] = axx;
+        Ayy[c] = ayy;
+        Azz[c] = azz;
+        Axy[c] = axy;
+        Ayz[c] = ayz;
+        Azx[c] = azx;
+        ALaplacian[c] = alap;
+
+        double fxx = Fxx[c], fyy = Fyy[c], fzz = Fzz[c], fxy = Fxy[c], fyz = Fyz[c], fzx = Fzx[c];
+        double fgm = FGradMag[c];
+        /* geodesic curvature: n . ((H_F t) x grad A + grad F x (H_A t)) / |grad F x grad A| */
+        double vx = tx * fxx + ty * fxy + tz * fzx;
+        double vy = tx * fxy + ty * fyy + tz * fyz;
+        double vz = tx * fzx + ty * fyz + tz * fzz;
+        double w1x = vy * az - vz * ay, w1y = vz * ax - vx * az, w1z = vx * ay - vy * ax;
+        vx = tx * axx + ty * axy + tz * azx;
+        vy = tx * axy + ty * ayy + tz * ayz;
+        vz = tx * azx + ty * ayz + tz * azz;
+        double w2x = fy * vz - fz * vy, w2y = fz * vx - fx * vz, w2z = fx * vy - fy * vx;
+        GeodesicCurvature[c] = (nx * (w1x + w2x) + ny * (w1y + w2y) + nz * (w1z + w2z)) / ncr;
+
+        /* grad N = H_F / |grad F| - grad F (H_F grad F)^T / |grad F|^3, row by row */
+        double g3 = POW(fgm, 3);
+        double Nxx = fxx / fgm - fx * (fxx * fx + fxy * fy + fzx * fz) / g3;
+        double Nyx = fxy / fgm - fy * (fxx * fx + fxy * fy + fzx * fz) / g3;
+        double Nzx = fzx / fgm - fz * (fxx * fx + fxy * fy + fzx * fz) / g3;
+        double Nxy = fxy / fgm - fx * (fxy * fx + fyy * fy + fyz * fz) / g3;
+        double Nyy = fyy / fgm - fy * (fxy * fx + fyy * fy + fyz * fz) / g3;
+        double Nzy = fyz / fgm - fz * (fxy * fx + fyy * fy + fyz * fz) / g3;
+        double Nxz = fzx / fgm - fx * (fzx * fx + fyz * fy + fzz * fz) / g3;
+        double Nyz = fyz / fgm - fy * (fzx * fx + fyz * fy + fzz * fz) / g3;
+        double Nzz = fzz / fgm - fz * (fzx * fx + fyz * fy + fzz * fz) / g3;
+        vx = Nxx * tx + Nxy * ty + Nxz * tz;
+        vy = Nyx * tx + Nyy * ty + Nyz * tz;
+        vz = Nzx * tx + Nzy * ty + Nzz * tz;
+        NormalCurvature[c] = -(tx * vx + ty * vy + tz * vz);
+        vx = Nxx * nx + Nxy * ny + Nxz * nz;
+        vy = Nyx * nx + Nyy * ny + Nyz * nz;
+        vz = Nzx * nx + Nzy * ny + Nzz * nz;
+        GeodesicTorsion[c] = -(tx * vx + ty * vy + tz * vz);
+        BPerpendicular[c] = -(nx * vx + ny * vy + nz * vz);
+
+        const double *p = AHPrimal;
+        double px = (p[xp] - p[xm]) / (2 * dx);
+        double py = (p[yp] - p[ym]) / (2 * dy);
+        double pz = (p[zp] - p[zm]) / (2 * dz);
+        double dot = px * ax + py * ay + pz * az;
+        AHeaviside[c] = dot / POW(agm, 2);
+        double pxx = (p[xp] - 2 * p[c] + p[xm]) / (dx * dx);
+        double pyy = (p[yp] - 2 * p[c] + p[ym]) / (dy * dy);
+        double pzz = (p[zp] - 2 * p[c] + p[zm]) / (dz * dz);
+        double plap = pxx + pyy + pzz;
+        ADiracDelta[c] = plap / POW(agm, 2) - dot * alap / POW(agm, 4);
     }
 }
 

@@ -63,6 +63,15 @@ void orc_set_calculus_toolbox(double *Fx, double *Fy, double *Fz, double *FGradM
                               double *Fzx, double *FLaplacian, double *MeanCurvature, double *GaussianCurvature,
                               double *Heaviside, double *DiracDelta, const double *lsf, const double *HPrimal,
                               int rows, int cols, int pges, double dx, double dy, double dz, double ds, int num_ele);
+void orc_auxi_set_calculus_toolbox(
+    double *Ax, double *Ay, double *Az, double *AGradMag, double *ACx, double *ACy, double *ACz,
+    double *ANormCrossAF, double *Tx, double *Ty, double *Tz, double *Anx, double *Any, double *Anz, double *Axx,
+    double *Ayy, double *Azz, double *Axy, double *Ayz, double *Azx, double *ALaplacian, double *GeodesicCurvature,
+    double *NormalCurvature, double *GeodesicTorsion, double *BPerpendicular, double *AHeaviside,
+    double *ADiracDelta, const double *lsf, const double *AHPrimal, const double *Fx, const double *Fy,
+    const double *Fz, const double *FGradMag, const double *Nx, const double *Ny, const double *Nz,
+    const double *Fxx, const double *Fyy, const double *Fzz, const double *Fxy, const double *Fyz,
+    const double *Fzx, int rows, int cols, int pges, double dx, double dy, double dz, double ds, int num_ele);
 void orc_enork2_boundary_correction(double *xpr, double *xpl, double *ypf, double *ypb, double *zpu, double *zpd,
                                     const double *lsf, int num_ele, int rows, int cols, int pges, double dx,
                                     double dy, double dz);
