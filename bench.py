@@ -331,11 +331,28 @@ def relax_profile_case(torch, pkg, S, n: int = 96):
     m = pkg.SDF3(pkg.GD3(x, y, z), Val=F, precision="f32")
     m.setDistance()
     A0, V0 = (float(v) for v in m.area_volume().cpu())
+    # the tiles the autotuner picks for this grid (wave-aware candidates)
+    T = importlib.import_module(PKG + ".autotune")
+    for kind, pages in (("extend", 6), ("reinit", 3), ("advect", 6), ("enork2_extend", 6)):
+        T.set_pages((n, n, n), kind, pages)
     for _ in range(2):
         m.relax_step(A0, V0, kappa=1.0, spon_c=0.0, cfl=0.5, alpha=0.5, ext_iters=RELAX_EXT,
                      reinit_iters=RELAX_RE)
     torch.cuda.synchronize()
     print(json.dumps({"profile_case": "relax", "ok": True}))
+
+
+def aux_profile_case(torch, pkg, S, n: int = 160):
+    """Two FP32 auxiliary toolbox calls (all 29 fields) on the n^3 vesicle with a plane
+    domain: 0.5 GB of fields at 160^3, larger than L2 (the ncu capture case)."""
+    x, y, z, F0 = S.vesicle_256(n, seed=0, device="cuda")
+    h = 3.0 / (n - 1)
+    m = pkg.SDF3(pkg.GD3(x, y, z, spacing=(h, h, h)), Val=F0, precision="f32")
+    m.A = z - 0.1
+    for _ in range(2):
+        m.GPUAsetCalculusToolBox()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "aux", "ok": True}))
 
 
 def adjoint_profile_case(torch, pkg, S, n: int = 128):
@@ -573,7 +590,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--fd-check", action="store_true",
                     help="also check the 128^3 amplitude gradient against FP64 central differences")
-    ap.add_argument("--profile", choices=["extend", "reinit", "advect", "step", "step128", "adjoint", "relax"],
+    ap.add_argument("--profile", choices=["extend", "reinit", "advect", "step", "step128", "adjoint", "relax", "aux"],
                     help="run only a few launches of one operator at 256^3 (the ncu capture case)")
     args = ap.parse_args()
 
@@ -600,6 +617,8 @@ def main():
         return adjoint_profile_case(torch, pkg, S)
     if args.profile == "relax":
         return relax_profile_case(torch, pkg, S)
+    if args.profile == "aux":
+        return aux_profile_case(torch, pkg, S)
     if args.profile == "step128":
         return step128_profile_case(torch, pkg, S)
     x, y, z, F0 = S.vesicle_256(N, seed=rank, device="cuda")
