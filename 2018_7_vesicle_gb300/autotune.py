@@ -5,7 +5,7 @@ pages mean more blocks and more parallelism on small grids, more pages mean fewe
 reloads per node on large ones.  The library keeps a table of pages per (grid shape,
 stage kind) (vsl_set_tile_pages / vsl_tile_pages of the C ABI); `tune_shape` fills it for
 one level-set object by timing each kind's own operation (extension, reinitialization,
-advection, ENORK2 extension) on that object's field for every candidate, with CUDA events, and keeping
+advection, ENORK2 extension and reinitialization) on that object's field for every candidate, with CUDA events, and keeping
 the fastest.  Tune before recording CUDA graphs: a graph keeps the launch shapes it was
 recorded with.
 """
@@ -16,7 +16,7 @@ import torch
 from ._lib import lib
 from .sdf3 import SDF3, colmajor_full
 
-KINDS = {"reinit": 0, "extend": 1, "advect": 2, "enork2_extend": 3}
+KINDS = {"reinit": 0, "extend": 1, "advect": 2, "enork2_extend": 3, "enork2_reinit": 4}
 CANDIDATES = (4, 8, 16, 32, 64)
 TILE_ROWS, TILE_COLS = 32, 8  # tile of one block of the tiled kernels
 BLOCKS_PER_SM = 4  # resident blocks per SM of the tiled kernels (launch bounds)
@@ -91,6 +91,7 @@ def tune_shape(sdf: SDF3, candidates=CANDIDATES, iters: int = 2, reps: int = 3) 
         "reinit": lambda: sdf.WENO5RK3Reinitialization(sdf.F, iters),
         "advect": lambda: sdf.WENO5RK3Advection(sdf.F, v, v, v, dt, iters),
         "enork2_extend": lambda: sdf.ENORK2Extend(sdf.F, iters),
+        "enork2_reinit": lambda: sdf.ENORK2Reinitialization(sdf.F, iters),
     }
     report = {}
     for kind, fn in ops.items():

@@ -656,6 +656,24 @@ int op_vesicle_step(T *F, T *xpr, T *xpl, T *ypf, T *ypb, T *zpu, T *zpd, int ex
 // ENORK2 (ENORK2Reinitialization.m:3-45, ENORK2Extend.m:9-81)
 // ---------------------------------------------------------------------------------------
 
+// the FP32 reinitialization workspace's band storage as a node list (the FP64 form has none)
+template <typename T> NodeList band_list(ReinitWork<T> &w) { return NodeList{w.band.q.queue, w.band.q.counter}; }
+
+// one ENORK2 reinitialization stage; the FP32 form runs the tiled kernel on the uniform
+// nodes and the per-node code on the flagged list (from the classification) beside it
+template <typename T>
+int enork2_reinit_stage(const T *in, const T *n_in, T *out, ReinitWork<T> &w, Ptr6<const T> d, const Grid &g,
+                        int stage, cudaStream_t s)
+{
+    if constexpr (std::is_same<T, float>::value) {
+        VSL_TRY(tiled(4, false, w.band, in, n_in, out, w.flags, d, Ptr6<const float>{}, Ptr3<const float>{}, nullptr,
+                      nullptr, stage, g, s, band_list(w)));
+        return VSL_OK;
+    }
+    VSL_TRY(launch_enork2_reinit_stage<T>(in, n_in, out, w.flags, d, g, stage, s));
+    return VSL_OK;
+}
+
 template <typename T>
 int op_reinit_enork2(T *F, int iteration, int rows, int cols, int pges, double dx, double dy, double dz, void *ws,
                      size_t bytes, cudaStream_t s)
@@ -669,10 +687,10 @@ int op_reinit_enork2(T *F, int iteration, int rows, int cols, int pges, double d
     ReinitWork<T> w = carve_reinit<T>(b, g, true);
     VSL_TRY(launch_set_distance_eno2<T>(F, w.dist, g, w.edges, s));
     const Ptr6<const T> d = cview(w.dist);
-    VSL_TRY(launch_classify<T>(F, d, w.flags, NodeList{nullptr, nullptr}, g, s));
+    VSL_TRY(launch_classify<T>(F, d, w.flags, band_list(w), g, s));
     for (int it = 0; it < iteration; ++it) {
-        VSL_TRY(launch_enork2_reinit_stage<T>(F, F, w.b, w.flags, d, g, 0, s));
-        VSL_TRY(launch_enork2_reinit_stage<T>(w.b, F, F, w.flags, d, g, 1, s));
+        if (int st = enork2_reinit_stage<T>(F, F, w.b, w, d, g, 0, s)) return st;
+        if (int st = enork2_reinit_stage<T>(w.b, F, F, w, d, g, 1, s)) return st;
     }
     return VSL_OK;
 }
@@ -732,7 +750,7 @@ int op_redistance_enork2(T *A, int iter1, int iter2, const T *F, int rows, int c
     // A's distances, mask and pseudo time step (reinitialization)
     VSL_TRY(launch_set_distance_eno2<T>(A, w.re.dist, g, w.re.edges, s));
     const Ptr6<const T> dA = cview(w.re.dist);
-    VSL_TRY(launch_classify<T>(A, dA, w.re.flags, NodeList{nullptr, nullptr}, g, s));
+    VSL_TRY(launch_classify<T>(A, dA, w.re.flags, band_list(w.re), g, s));
     // F's distances, normals (floor 1e-14) and pseudo time step (extensions)
     VSL_TRY(launch_set_distance_eno2<T>(F, w.ext.dist, g, w.ext.edges, s));
     const Ptr6<const T> dF = cview(w.ext.dist);
@@ -741,9 +759,9 @@ int op_redistance_enork2(T *A, int iter1, int iter2, const T *F, int rows, int c
     T *t = w.re.b;
     for (int it = 0; it < iter1; ++it) {
         if (int st = enork2_extend_loop<T>(A, iter2, dF, w.ext, g, s)) return st;
-        VSL_TRY(launch_enork2_reinit_stage<T>(A, A, t, w.re.flags, dA, g, 0, s));
+        if (int st = enork2_reinit_stage<T>(A, A, t, w.re, dA, g, 0, s)) return st;
         if (int st = enork2_extend_loop<T>(t, iter2, dF, w.ext, g, s)) return st;
-        VSL_TRY(launch_enork2_reinit_stage<T>(t, A, A, w.re.flags, dA, g, 2, s));
+        if (int st = enork2_reinit_stage<T>(t, A, A, w.re, dA, g, 2, s)) return st;
     }
     return enork2_extend_loop<T>(A, iter2, dF, w.ext, g, s);
 }
@@ -1002,7 +1020,7 @@ int vsl_set_tile_pages(int rows, int cols, int pges, int kind, int pages)
 
 int vsl_tile_pages(int rows, int cols, int pges, int kind)
 {
-    if (rows <= 0 || cols <= 0 || pges <= 0 || kind < 0 || kind > 3) return 0;
+    if (rows <= 0 || cols <= 0 || pges <= 0 || kind < 0 || kind > 4) return 0;
     return tile_pages(make_grid(rows, cols, pges, 1.0, 1.0, 1.0), kind);
 }
 

@@ -429,14 +429,13 @@ __global__ void __launch_bounds__(128) k_dist_roots_eno2(const T *__restrict__ f
     }
 }
 
+// one node of an ENORK2 reinitialization stage, all reads from global memory (clamped)
 template <typename T>
-__global__ void __launch_bounds__(BX *BY) k_enork2_reinit_stage(const T *__restrict__ phi_s,
-                                                                  const T *__restrict__ phi_n, T *__restrict__ out,
-                                                                  const uint8_t *__restrict__ flags, Ptr6<const T> d,
-                                                                  Grid g, int stage)
+__device__ __forceinline__ void enork2_reinit_node(const T *__restrict__ phi_s, const T *__restrict__ phi_n,
+                                                   T *__restrict__ out, const uint8_t *__restrict__ flags,
+                                                   const Ptr6<const T> &d, const Grid &g, int stage, int i, int j,
+                                                   int k)
 {
-    int i, j, k;
-    if (!fused_node(g, i, j, k)) return;
     const long long c = node_index(g, i, j, k);
     const uint8_t fl = __ldg(flags + c);
     const T hs[3] = {(T)g.dx, (T)g.dy, (T)g.dz};
@@ -453,6 +452,17 @@ __global__ void __launch_bounds__(BX *BY) k_enork2_reinit_stage(const T *__restr
     const T step = (gn - T(1)) * pseudo_dt(fl, d, c, hs[0], hs[1], hs[2]) * (neg ? T(-1) : T(1));
     const T pn = stage == 0 ? T(0) : __ldg(phi_n + c);
     out[c] = rk2_combine(stage, pn, __ldg(phi_s + c), step);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BX *BY) k_enork2_reinit_stage(const T *__restrict__ phi_s,
+                                                                  const T *__restrict__ phi_n, T *__restrict__ out,
+                                                                  const uint8_t *__restrict__ flags, Ptr6<const T> d,
+                                                                  Grid g, int stage)
+{
+    int i, j, k;
+    if (!fused_node(g, i, j, k)) return;
+    enork2_reinit_node<T>(phi_s, phi_n, out, flags, d, g, stage, i, j, k);
 }
 
 // v = sign(F) * n / max(|n|, floor) with the ENO upwind normal (enork2_extend.cu:103-141,

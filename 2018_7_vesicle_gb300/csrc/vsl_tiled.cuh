@@ -45,8 +45,16 @@ constexpr int SH = TX + 2 * HALO;
 constexpr int PLANE = SW * SH;
 constexpr int RING = 5;
 
-// SK_ENO2: the ENORK2 extension (quadratic ENO derivatives, Heun RK2 stages)
-enum StageKind { SK_REINIT = 0, SK_EXTEND = 1, SK_ADVECT = 2, SK_ENO2 = 3 };
+// SK_ENO2 / SK_ENO2R: the ENORK2 extension / reinitialization (quadratic ENO derivatives,
+// Heun RK2 stages)
+enum StageKind { SK_REINIT = 0, SK_EXTEND = 1, SK_ADVECT = 2, SK_ENO2 = 3, SK_ENO2R = 4 };
+// kinds on the WENO5 stencils (their z window weights are carried from page to page)
+__host__ __device__ constexpr bool weno_kind(int kind) { return kind <= SK_ADVECT; }
+// kinds whose band is the static list of flagged nodes (the band kernel runs beside them)
+__host__ __device__ constexpr bool static_band_kind(int kind)
+{
+    return kind == SK_EXTEND || kind == SK_ENO2 || kind == SK_ENO2R;
+}
 
 struct TiledArgs {
     const float *phi_s;
@@ -77,6 +85,15 @@ __device__ __forceinline__ float eno2_upwind_uniform(const float p[7], bool back
     const float p2 = v1 - 2.f * v0 + v2;
     if (back) return (v0 - v1 + 0.5f * minmod(p2, v0 - 2.f * v1 + p[1])) * inv_h;
     return (v2 - v0 - 0.5f * minmod(p2, v0 - 2.f * v2 + p[5])) * inv_h;
+}
+
+// both quadratic-ENO derivatives of a line with no crossing
+__device__ __forceinline__ void eno2_pair_uniform(const float p[7], float inv_h, float &fore, float &back)
+{
+    const float v1 = p[2], v0 = p[3], v2 = p[4];
+    const float p2 = v1 - 2.f * v0 + v2;
+    fore = (v2 - v0 - 0.5f * minmod(p2, v0 - 2.f * v2 + p[5])) * inv_h;
+    back = (v0 - v1 + 0.5f * minmod(p2, v0 - 2.f * v1 + p[1])) * inv_h;
 }
 
 template <int KIND>
@@ -134,7 +151,7 @@ __global__ void __launch_bounds__(TY *TX, VSL_TILED_MIN_BLOCKS) k_stage_tiled(Ti
     for (int s = 3; s < 6; ++s) q[s] = sm[slot(k0 + s - 3)][ty + HALO][tx + HALO];
     // reciprocal smoothness weights of the z window of page k0 (backward derivative)
     float zr1 = 0.f, zr2 = 0.f, zr3 = 0.f;
-    if constexpr (KIND != SK_ENO2)
+    if constexpr (weno_kind(KIND))
         weno5_window_weights(q[1] - q[0], q[2] - q[1], q[3] - q[2], q[4] - q[3], q[5] - q[4], a.eps2[2], zr1, zr2,
                              zr3);
 
@@ -150,7 +167,7 @@ __global__ void __launch_bounds__(TY *TX, VSL_TILED_MIN_BLOCKS) k_stage_tiled(Ti
     auto load_node = [&](long long cc) {
         if (KIND != SK_ADVECT) fl_next = __ldg(a.flags + cc);
         if (a.stage != 0) pn_next = __ldg(a.phi_n + cc);
-        if (KIND != SK_REINIT) {
+        if (KIND == SK_EXTEND || KIND == SK_ADVECT || KIND == SK_ENO2) {
             v0_next = __ldg(a.v.p[0] + cc);
             v1_next = __ldg(a.v.p[1] + cc);
             v2_next = __ldg(a.v.p[2] + cc);
@@ -173,7 +190,7 @@ __global__ void __launch_bounds__(TY *TX, VSL_TILED_MIN_BLOCKS) k_stage_tiled(Ti
         const float v1 = q[1] - q[0], v2 = q[2] - q[1], v3 = q[3] - q[2], v4 = q[4] - q[3], v5 = q[5] - q[4],
                     v6 = q[6] - q[5];
         float nr1 = 0.f, nr2 = 0.f, nr3 = 0.f;
-        if constexpr (KIND != SK_ENO2) weno5_window_weights(v2, v3, v4, v5, v6, a.eps2[2], nr1, nr2, nr3);
+        if constexpr (weno_kind(KIND)) weno5_window_weights(v2, v3, v4, v5, v6, a.eps2[2], nr1, nr2, nr3);
 
         bool band = false;
         if (active) {
@@ -190,7 +207,7 @@ __global__ void __launch_bounds__(TY *TX, VSL_TILED_MIN_BLOCKS) k_stage_tiled(Ti
             if (compute && KIND == SK_REINIT) {
                 band = px[2] * px[3] < 0.f || px[3] * px[4] < 0.f || py[2] * py[3] < 0.f || py[3] * py[4] < 0.f ||
                        q[2] * q[3] < 0.f || q[3] * q[4] < 0.f;
-            } else if (KIND == SK_EXTEND || KIND == SK_ENO2) {
+            } else if (static_band_kind(KIND)) {
                 // every node of the static list (fixed ones too) belongs to the band kernel,
                 // which may run at the same time: each node has exactly one writer
                 band = (fl & 0x3F) != 0;
@@ -209,6 +226,15 @@ __global__ void __launch_bounds__(TY *TX, VSL_TILED_MIN_BLOCKS) k_stage_tiled(Ti
                 const float dtn = (fl & 0x3F) ? pseudo_dt(fl, a.d, c, a.h[0], a.h[1], a.h[2]) : a.dt_uniform;
                 const float gn = godunov_norm(neg, dxf, dxb, dyf, dyb, dz.y, dz.x);
                 step = (gn - 1.f) * dtn * (neg ? -1.f : 1.f);
+            } else if (compute && !band && KIND == SK_ENO2R) {
+                // ENORK2 reinitialization: Godunov norm of both quadratic-ENO derivatives
+                float xf, xb, yf, yb, zf, zb;
+                eno2_pair_uniform(px, a.inv_h[0], xf, xb);
+                eno2_pair_uniform(py, a.inv_h[1], yf, yb);
+                eno2_pair_uniform(q, a.inv_h[2], zf, zb);
+                const bool neg = fl & MASK_BIT;
+                const float gn = godunov_norm(neg, xf, xb, yf, yb, zf, zb);
+                step = (gn - 1.f) * a.dt_uniform * (neg ? -1.f : 1.f);
             } else if (compute && !band && KIND == SK_ENO2) {
                 // ENORK2 extension: the upwind quadratic-ENO derivative of each axis
                 const float tr = vx0 * eno2_upwind_uniform(px, vx0 > 0.f, a.inv_h[0]) +
@@ -231,7 +257,9 @@ __global__ void __launch_bounds__(TY *TX, VSL_TILED_MIN_BLOCKS) k_stage_tiled(Ti
                 const float tr = ux * dxy.x + uy * dxy.y + uz * dz;
                 step = KIND == SK_EXTEND ? tr * a.dt_uniform : (float)__ldg(a.dt) * tr;
             }
-            if (!band) a.out[c] = KIND == SK_ENO2 ? rk2_combine(a.stage, pn, ps, step) : rk3_combine(a.stage, pn, ps - step);
+            if (!band)
+                a.out[c] = (KIND == SK_ENO2 || KIND == SK_ENO2R) ? rk2_combine(a.stage, pn, ps, step)
+                                                                  : rk3_combine(a.stage, pn, ps - step);
         }
         if (KIND == SK_REINIT) {  // the extension's band is the static list of flagged nodes
             const unsigned m = __ballot_sync(0xffffffffu, band);
@@ -278,6 +306,8 @@ __global__ void __launch_bounds__(128) k_band_stage(TiledArgs a, Ptr6<const floa
             reinit_node<float, ENO3, true>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
         else if (KIND == SK_ENO2)
             enork2_extend_node<float>(a.phi_s, a.phi_n, a.out, a.flags, a.d, cp, a.v, g, a.stage, i, j, k);
+        else if (KIND == SK_ENO2R)
+            enork2_reinit_node<float>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
         else
             extend_node<float, ENO3, true>(a.phi_s, a.phi_n, a.out, a.flags, a.d, cp, a.v, g, a.stage, i, j, k);
     }
@@ -334,7 +364,7 @@ int tile_pages(const Grid &g, int kind)
 int set_tile_pages(int rows, int cols, int pges, int kind, int pages)
 {
     if (rows <= 0 || cols <= 0 || pges <= 0) return VSL_ERR_SHAPE;
-    if (kind < 0 || kind > 3 || pages < 0 || pages > 65535) return VSL_ERR_VALUE;
+    if (kind < 0 || kind > 4 || pages < 0 || pages > 65535) return VSL_ERR_VALUE;
     std::lock_guard<std::mutex> lock(tile_mutex);
     for (int e = 0; e < tile_count; ++e) {
         TileEntry &t = tile_table[e];
@@ -413,7 +443,7 @@ cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const 
     a.speed = st.speed;
     a.dt = st.dt;
     unsigned *next = nullptr;
-    if (kind == SK_EXTEND || kind == SK_ENO2) {
+    if (static_band_kind(kind)) {
         a.queue = st.flagged.idx;
         a.counter = st.flagged.count;
     } else {
@@ -424,7 +454,7 @@ cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const 
     a.stage = st.stage;
     a.kz = tile_pages(g, kind);
     dim3 gr = tiled_grid(g, a.kz), bl(TY, TX);
-    if (kind == SK_EXTEND || kind == SK_ENO2) {
+    if (static_band_kind(kind)) {
         // the tiled kernel is submitted first so that its blocks are dispatched ahead of the
         // band kernel's (a grid-stride kernel whose blocks mostly find no work)
         SideLane *ln = side_lane(s);
@@ -432,6 +462,8 @@ cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const 
         if (ln && (e = cudaEventRecord(ln->fork, s)) != cudaSuccess) return e;
         if (kind == SK_ENO2)
             k_stage_tiled<SK_ENO2><<<gr, bl, 0, s>>>(a);
+        else if (kind == SK_ENO2R)
+            k_stage_tiled<SK_ENO2R><<<gr, bl, 0, s>>>(a);
         else
             k_stage_tiled<SK_EXTEND><<<gr, bl, 0, s>>>(a);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -442,6 +474,8 @@ cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const 
         }
         if (kind == SK_ENO2)
             k_band_stage<SK_ENO2, false><<<band_blocks(), 128, 0, bs>>>(a, st.cp, next);
+        else if (kind == SK_ENO2R)
+            k_band_stage<SK_ENO2R, false><<<band_blocks(), 128, 0, bs>>>(a, st.cp, next);
         else if (eno3)
             k_band_stage<SK_EXTEND, true><<<band_blocks(), 128, 0, bs>>>(a, st.cp, next);
         else

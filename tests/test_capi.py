@@ -123,6 +123,8 @@ def test_tile_pages_table(vsl):
     assert call("vsl_set_tile_pages", 40, 36, 52, 3, 8) == 0  # kind 3: the ENORK2 extension
     assert call("vsl_tile_pages", 40, 36, 52, 3) == 8
     assert call("vsl_set_tile_pages", 40, 36, 52, 3, 0) == 0
-    assert call("vsl_set_tile_pages", 40, 36, 52, 4, 8) == 3
+    assert call("vsl_set_tile_pages", 40, 36, 52, 4, 8) == 0  # kind 4: the ENORK2 reinitialization
+    assert call("vsl_set_tile_pages", 40, 36, 52, 4, 0) == 0
+    assert call("vsl_set_tile_pages", 40, 36, 52, 5, 8) == 3
     assert call("vsl_set_tile_pages", 40, 36, 52, 1, -1) == 3
     assert call("vsl_tile_pages", 40, 36, 52, 7) == 0

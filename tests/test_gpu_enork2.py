@@ -153,3 +153,21 @@ def test_fp32_extension_ragged_tiles(pkg, oracle_mod):
     rel = max_rel(got, ref)
     print("ENORK2 FP32 extension (ragged tiles) rel error", rel)
     assert rel <= 5e-5
+
+
+def test_fp32_reinitialization_ragged_tiles(pkg, oracle_mod):
+    """FP32 ENORK2 reinitialization on the ragged grid: tiled uniform nodes and the flagged
+    list together, within 1e-5 dx of the oracle over the band |phi| < 3 dx."""
+    O = oracle_mod
+    K = O.kernels("port")
+    x, y, z = S.meshgrid(np.linspace(-1, 1, 29), np.linspace(-0.95, 0.95, 37), np.linspace(-0.7, 0.7, 11))
+    F = S.perturbed_sphere(x, y, z, r=0.55, centre=(0.1, -0.05, 0.02))
+    g = O.grid_from_mesh(x, y, z)
+    m = pkg.SDF3(pkg.GD3(x, y, z), Val=F, precision="f32")
+    ref = O.reinit_enork2(K, g, F, 30)
+    got = host(m.ENORK2Reinitialization(m.F, 30))
+    h = min(g.dx, g.dy, g.dz)
+    band = np.abs(ref) < 3 * h
+    err = np.abs(got - ref)[band].max() / h
+    print("ENORK2 FP32 reinitialization (ragged tiles) band error / dx", err)
+    assert err <= 1e-5
