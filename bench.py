@@ -50,6 +50,29 @@ BYTES_PER_NODE_STEP = EXT * BYTES_EXTEND + ADV * BYTES_ADVECT + RE * BYTES_REINI
 LAUNCHES_PER_STEP = 1 + 1 + 1 + 1 + 1 + 2 * 3 * EXT + 1 + 1 + 3 * ADV + 2 + 1 + 2 * 3 * RE
 
 
+def replica_seed(rank: int) -> int:
+    """Every rank advances its own vesicle (independent replicas, no data exchange): the
+    seed of its spherical-harmonic noise is its rank."""
+    return rank
+
+
+def max_over_ranks(x: float, dist, device) -> float:
+    """The largest of the ranks' values (the slowest rank's time); x itself on one rank."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_gpt_s(world: int, gpt_per_rank: float, seconds: float) -> float:
+    """Whole-job throughput: the grid-point updates of all ranks over the slowest rank's
+    time (every rank does the same work)."""
+    return world * gpt_per_rank / seconds / 1e9
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -621,7 +644,7 @@ def main():
         return aux_profile_case(torch, pkg, S)
     if args.profile == "step128":
         return step128_profile_case(torch, pkg, S)
-    x, y, z, F0 = S.vesicle_256(N, seed=rank, device="cuda")
+    x, y, z, F0 = S.vesicle_256(N, seed=replica_seed(rank), device="cuda")
     h = 3.0 / (N - 1)
     grid = pkg.GD3(x, y, z, spacing=(h, h, h))
     m = pkg.SDF3(grid, Val=F0, precision="f32")
@@ -654,13 +677,9 @@ def main():
             info = m.vesicle_step(EXT, RE, CFL, graph=True)
         ev1.record(stream)
         barrier()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, dist, "cuda")
     gpt_step = GPT_PER_NODE * N**3
-    value = world * gpt_step / (ms / 1e3) / 1e9
+    value = whole_job_gpt_s(world, gpt_step, ms / 1e3)
     info_h = info.cpu().tolist()
 
     # dominant kernel: the FP32 extension stage, timed live on the launching stream as
@@ -700,13 +719,13 @@ def main():
         F_out.copy_(Fv, non_blocking=True)
         info_out.copy_(inf, non_blocking=True)
     barrier()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    e2e_val = world * gpt_step / e2e_s / 1e9
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, dist, "cuda")
+    e2e_val = whole_job_gpt_s(world, gpt_step, e2e_s)
 
     # the plain FP64 form of the same step, for the FP32/FP64 throughput ratio
     fp64 = None
     if not args.no_fp64:
-        F0 = S.vesicle_256(N, seed=rank, device="cuda")[3]
+        F0 = S.vesicle_256(N, seed=replica_seed(rank), device="cuda")[3]
         m64 = pkg.SDF3(grid, Val=F0, precision="f64")
         del F0
         m64.setDistance()
