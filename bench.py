@@ -147,16 +147,17 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_sample(seconds: float = 10.0, seed: int = 0):
-    """The oracle on a bounded sample of the workload: full vesicle steps on a 32-page slab
-    through the middle of the 256^3 field, all host threads, repeated for >= `seconds`."""
+def cpu_sample(seconds: float = 10.0, seed: int = 0, pages: int = 32):
+    """The oracle on a bounded sample of the workload: full vesicle steps on a `pages`-page
+    slab through the middle of the 256^3 field, all host threads, repeated for >=
+    `seconds`."""
     from oracle import build_oracle
     from oracle import oracle as O
 
     build_oracle.build_port()
     S = importlib.import_module(PKG + ".shapes")
     K = O.kernels("port")
-    x, y, z, F = S.vesicle_256(N, seed=seed, pages=slice(N // 2 - 16, N // 2 + 16))
+    x, y, z, F = S.vesicle_256(N, seed=seed, pages=slice(N // 2 - pages // 2, N // 2 + pages - pages // 2))
     F = O.F64(F)
     g = O.Grid(F.shape[0], F.shape[1], F.shape[2], 3.0 / (N - 1), 3.0 / (N - 1), 3.0 / (N - 1))
     d = O.set_distance(K, g, F)
@@ -174,9 +175,48 @@ def cpu_sample(seconds: float = 10.0, seed: int = 0):
         "unit": UNIT,
         "cores": cores,
         "kind": "port",
-        "sample": f"{steps} full vesicle step(s) (30 ext + 1 adv + 20 reinit) on a 256x256x32 slab "
+        "sample": f"{steps} full vesicle step(s) (30 ext + 1 adv + 20 reinit) on a 256x256x{pages} slab "
                   f"of the 256^3 field, oracle C restatement, OpenMP over pages, {el:.1f} s",
     }
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu), or the machine type."""
+    import platform
+
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return platform.processor() or platform.machine()
+
+
+def cpu_sample_single_thread(seconds: float = 5.0, pages: int = 4) -> dict | None:
+    """cpu_sample on one thread (a child process with OMP_NUM_THREADS=1) on a thinner slab."""
+    code = ("import json, sys; sys.path.insert(0, %r); import bench; "
+            "print(json.dumps(bench.cpu_sample(seconds=%r, pages=%d)))" % (ROOT, seconds, pages))
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    try:
+        r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env,
+                           timeout=60 + 10 * seconds)
+        return json.loads(r.stdout.strip().splitlines()[-1]) if r.returncode == 0 else None
+    except (OSError, subprocess.SubprocessError, ValueError, IndexError):
+        return None
+
+
+def cpu_baseline(seconds: float = 10.0) -> dict:
+    """The oracle on all host threads (the baseline), with its one-thread rate, the core
+    count and the CPU model beside it."""
+    cpu = cpu_sample(seconds=seconds)
+    one = cpu_sample_single_thread()
+    cpu["single_thread"] = None if one is None else {"value": one["value"], "unit": one["unit"],
+                                                     "sample": one["sample"]}
+    cpu["nproc"] = os.cpu_count()
+    cpu["cpu_model"] = cpu_model()
+    return cpu
 
 
 def run_reference(args, rank, world):
@@ -199,7 +239,7 @@ def run_reference(args, rank, world):
         "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(args.gpus),
-        "cpu_baseline": {**base, "value": v},
+        "cpu_baseline": {**base, "value": v, "nproc": os.cpu_count(), "cpu_model": cpu_model()},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
     }
@@ -771,7 +811,7 @@ def main():
         if dist is not None:
             dist.barrier()
         return
-    cpu = None if args.no_cpu_baseline else cpu_sample(seconds=10.0)
+    cpu = None if args.no_cpu_baseline else cpu_baseline(seconds=10.0)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -786,7 +826,11 @@ def main():
                      "effective": "fused stage reads fewer bytes than the reference dataflow counts"},
         "step_hbm": {"algorithmic_bytes_per_step": BYTES_PER_NODE_STEP * N**3,
                      "achieved_gbs": BYTES_PER_NODE_STEP * N**3 / (ms / 1e3) / 1e9,
-                     "frac": BYTES_PER_NODE_STEP * N**3 / (ms / 1e3) / 1e9 / hbm},
+                     "frac": BYTES_PER_NODE_STEP * N**3 / (ms / 1e3) / 1e9 / hbm,
+                     # the compulsory minimum: phi read and written once per stage, 8w per Gpt
+                     "compulsory_bytes_per_step": 8 * W32 * gpt_step,
+                     "compulsory_gbs": 8 * W32 * gpt_step / (ms / 1e3) / 1e9,
+                     "compulsory_frac": 8 * W32 * gpt_step / (ms / 1e3) / 1e9 / hbm},
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 4 * N**3,
                 "d2h_bytes_per_step": 4 * N**3 + 32, "ms_per_step": e2e_s * 1e3},
         "gpu_launches": LAUNCHES_PER_STEP * args.steps,
