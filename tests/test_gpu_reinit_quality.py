@@ -13,9 +13,7 @@ phi0 = (sqrt(x^2+y^2+z^2) - 0.6) (0.1 + (x-0.35)^2 + (y-0.35)^2 + (z-0.35)^2), s
 GPU only."""
 import importlib
 
-import numpy as np
 import pytest
-import torch
 
 pytestmark = pytest.mark.gpu
 S = importlib.import_module("2018_7_vesicle_gb300.shapes")
