@@ -328,13 +328,14 @@ int reinit_loop(T *F, int iters, Ptr6<const T> d, ReinitWork<T> &w, const Grid &
             VSL_TRY(tiled(0, eno3, w.band, w.c, F, F, w.flags, d, none6, none3, nullptr, nullptr, 2, g, s));
         }
         return VSL_OK;
+    } else {
+        for (int it = 0; it < iters; ++it) {
+            VSL_TRY(launch_reinit_stage<T>(F, F, w.b, w.flags, d, g, 0, eno3, fast, s));
+            VSL_TRY(launch_reinit_stage<T>(w.b, F, w.c, w.flags, d, g, 1, eno3, fast, s));
+            VSL_TRY(launch_reinit_stage<T>(w.c, F, F, w.flags, d, g, 2, eno3, fast, s));
+        }
+        return VSL_OK;
     }
-    for (int it = 0; it < iters; ++it) {
-        VSL_TRY(launch_reinit_stage<T>(F, F, w.b, w.flags, d, g, 0, eno3, fast, s));
-        VSL_TRY(launch_reinit_stage<T>(w.b, F, w.c, w.flags, d, g, 1, eno3, fast, s));
-        VSL_TRY(launch_reinit_stage<T>(w.c, F, F, w.flags, d, g, 2, eno3, fast, s));
-    }
-    return VSL_OK;
 }
 
 // velocity and node classes of an extension off the zero set of F (distances d)
@@ -363,13 +364,14 @@ int extend_loop(T *C, int iters, Ptr6<const T> d, ExtendWork<T> &w, const Grid &
             VSL_TRY(tiled(1, eno3, w.band, w.c, C, C, w.flags, d, cp, v, nullptr, nullptr, 2, g, s, w.flagged));
         }
         return VSL_OK;
+    } else {
+        for (int it = 0; it < iters; ++it) {
+            VSL_TRY(launch_extend_stage<T>(C, C, w.b, w.flags, d, cp, v, g, 0, eno3, fast, s));
+            VSL_TRY(launch_extend_stage<T>(w.b, C, w.c, w.flags, d, cp, v, g, 1, eno3, fast, s));
+            VSL_TRY(launch_extend_stage<T>(w.c, C, C, w.flags, d, cp, v, g, 2, eno3, fast, s));
+        }
+        return VSL_OK;
     }
-    for (int it = 0; it < iters; ++it) {
-        VSL_TRY(launch_extend_stage<T>(C, C, w.b, w.flags, d, cp, v, g, 0, eno3, fast, s));
-        VSL_TRY(launch_extend_stage<T>(w.b, C, w.c, w.flags, d, cp, v, g, 1, eno3, fast, s));
-        VSL_TRY(launch_extend_stage<T>(w.c, C, C, w.flags, d, cp, v, g, 2, eno3, fast, s));
-    }
-    return VSL_OK;
 }
 
 template <typename T>
@@ -385,13 +387,14 @@ int advect_loop(T *F, Ptr3<const T> v, const T *speed, const double *dt, int ste
             VSL_TRY(tiled(2, false, w.band, w.c, F, F, nullptr, none6, none6, v, speed, dt, 2, g, s));
         }
         return VSL_OK;
+    } else {
+        for (int it = 0; it < steps; ++it) {
+            VSL_TRY(launch_advect_stage<T>(F, F, w.b, v, speed, dt, g, 0, fast, s));
+            VSL_TRY(launch_advect_stage<T>(w.b, F, w.c, v, speed, dt, g, 1, fast, s));
+            VSL_TRY(launch_advect_stage<T>(w.c, F, F, v, speed, dt, g, 2, fast, s));
+        }
+        return VSL_OK;
     }
-    for (int it = 0; it < steps; ++it) {
-        VSL_TRY(launch_advect_stage<T>(F, F, w.b, v, speed, dt, g, 0, fast, s));
-        VSL_TRY(launch_advect_stage<T>(w.b, F, w.c, v, speed, dt, g, 1, fast, s));
-        VSL_TRY(launch_advect_stage<T>(w.c, F, F, v, speed, dt, g, 2, fast, s));
-    }
-    return VSL_OK;
 }
 
 template <typename T> Ptr6<const T> six(const T *a, const T *b, const T *c, const T *d, const T *e, const T *f)
@@ -669,9 +672,10 @@ int enork2_reinit_stage(const T *in, const T *n_in, T *out, ReinitWork<T> &w, Pt
         VSL_TRY(tiled(4, false, w.band, in, n_in, out, w.flags, d, Ptr6<const float>{}, Ptr3<const float>{}, nullptr,
                       nullptr, stage, g, s, band_list(w)));
         return VSL_OK;
+    } else {
+        VSL_TRY(launch_enork2_reinit_stage<T>(in, n_in, out, w.flags, d, g, stage, s));
+        return VSL_OK;
     }
-    VSL_TRY(launch_enork2_reinit_stage<T>(in, n_in, out, w.flags, d, g, stage, s));
-    return VSL_OK;
 }
 
 template <typename T>
@@ -709,12 +713,13 @@ int enork2_extend_loop(T *C, int iters, Ptr6<const T> d, ExtendWork<T> &w, const
             VSL_TRY(tiled(3, false, w.band, w.b, C, C, w.flags, d, cp, v, nullptr, nullptr, 1, g, s, w.flagged));
         }
         return VSL_OK;
+    } else {
+        for (int it = 0; it < iters; ++it) {
+            VSL_TRY(launch_enork2_extend_stage<T>(C, C, w.b, w.flags, d, cp, v, g, 0, s));
+            VSL_TRY(launch_enork2_extend_stage<T>(w.b, C, C, w.flags, d, cp, v, g, 1, s));
+        }
+        return VSL_OK;
     }
-    for (int it = 0; it < iters; ++it) {
-        VSL_TRY(launch_enork2_extend_stage<T>(C, C, w.b, w.flags, d, cp, v, g, 0, s));
-        VSL_TRY(launch_enork2_extend_stage<T>(w.b, C, C, w.flags, d, cp, v, g, 1, s));
-    }
-    return VSL_OK;
 }
 
 template <typename T>
