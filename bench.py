@@ -257,6 +257,9 @@ def profile_case(which, m, torch):
         elif which == "advect":
             v = m.F.clone().fill_(0.5)
             m.WENO5RK3Advection(m.F, v, v, v, 1e-3, steps=2)
+        elif which == "enork2":
+            m.ENORK2Extend(C, 2)
+            m.ENORK2Reinitialization(m.F, 2)
         else:
             m.vesicle_step(2, 2, CFL)
     torch.cuda.synchronize()
@@ -653,7 +656,7 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--fd-check", action="store_true",
                     help="also check the 128^3 amplitude gradient against FP64 central differences")
-    ap.add_argument("--profile", choices=["extend", "reinit", "advect", "step", "step128", "adjoint", "relax", "aux"],
+    ap.add_argument("--profile", choices=["extend", "reinit", "advect", "step", "step128", "adjoint", "relax", "aux", "enork2"],
                     help="run only a few launches of one operator at 256^3 (the ncu capture case)")
     args = ap.parse_args()
 
