@@ -19,7 +19,7 @@ from .sdf3 import SDF3, colmajor_full
 KINDS = {"reinit": 0, "extend": 1, "advect": 2, "enork2_extend": 3, "enork2_reinit": 4}
 CANDIDATES = (4, 8, 16, 32, 64)
 TILE_ROWS, TILE_COLS = 32, 8  # tile of one block of the tiled kernels
-BLOCKS_PER_SM = 4  # resident blocks per SM of the tiled kernels (launch bounds)
+BLOCKS_PER_SM = 4  # resident blocks per SM of the tiled kernels (launch bounds; 5 for the ENORK2 extension)
 
 
 def wave_candidates(size, sms: int | None = None, fill: float = 0.85, max_waves: float = 4.0, lo: int = 2,

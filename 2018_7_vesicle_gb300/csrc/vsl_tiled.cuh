@@ -97,7 +97,11 @@ __device__ __forceinline__ void eno2_pair_uniform(const float p[7], float inv_h,
 }
 
 template <int KIND>
-__global__ void __launch_bounds__(TY *TX, VSL_TILED_MIN_BLOCKS) k_stage_tiled(TiledArgs a)
+// The ENORK2 extension kind, whose uniform path is light, is latency-bound at 4 blocks per SM
+// (long-scoreboard stalls, DRAM 35% of peak): 5 blocks (47 registers, no spills) took 100
+// pseudo-steps at 256^3 from 26.7 to 23.6 ms.  The ENORK2 reinitialization was slower at 5
+// (25.7 -> 27.7 ms) and keeps 4 with the WENO5 kinds.
+__global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_BLOCKS)) k_stage_tiled(TiledArgs a)
 {
     __shared__ float sm[RING][SH][SW];
     const Grid &g = a.g;
