@@ -124,7 +124,10 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
         const int sy = e / SW, sx = e - sy * SW;
         e_off[r] = clampi(j0 + sy - HALO, g.cols) * g.rows + clampi(i0 + sx - HALO, g.rows);
     }
-    auto page_base = [&](int p) { return a.phi_s + (long long)clampi(p, g.pges) * g.plane; };
+    // node offsets fit in 32 bits (grids hold at most 2^31 - 1 nodes), so an address is the
+    // base pointer plus one widened 32-bit offset
+    const unsigned plane = (unsigned)g.plane;
+    auto page_base = [&](int p) { return a.phi_s + (unsigned)clampi(p, g.pges) * plane; };
     float pre[PER_THREAD];
     auto fetch = [&](int p) {
         const float *src = page_base(p);
@@ -146,9 +149,9 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
     }
     {
         const int ic = clampi(i, g.rows), jc = clampi(j, g.cols);
-        const float *col = a.phi_s + (long long)jc * g.rows + ic;
+        const unsigned col = (unsigned)jc * (unsigned)g.rows + (unsigned)ic;
 #pragma unroll
-        for (int s = 0; s < 3; ++s) q[s] = __ldg(col + (long long)clampi(k0 - 3 + s, g.pges) * g.plane);
+        for (int s = 0; s < 3; ++s) q[s] = __ldg(a.phi_s + (col + (unsigned)clampi(k0 - 3 + s, g.pges) * plane));
     }
     __syncthreads();
 #pragma unroll
@@ -164,11 +167,11 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
     auto next_slot = [](int sl) { return sl == RING - 1 ? 0 : sl + 1; };
     int s_k = slot(k0), s_k3 = slot(k0 + 3), s_k4 = slot(k0 + 4);
     // per-node inputs of the next page, loaded one page ahead
-    const long long col_base = (long long)clampi(j, g.cols) * g.rows + clampi(i, g.rows);
-    long long c = col_base + (long long)k0 * g.plane;
+    const unsigned col_base = (unsigned)clampi(j, g.cols) * (unsigned)g.rows + (unsigned)clampi(i, g.rows);
+    unsigned c = col_base + (unsigned)k0 * plane;
     uint8_t fl_next = 0;
     float pn_next = 0.f, v0_next = 0.f, v1_next = 0.f, v2_next = 0.f, sp_next = 1.f;
-    auto load_node = [&](long long cc) {
+    auto load_node = [&](unsigned cc) {
         if (KIND != SK_ADVECT) fl_next = __ldg(a.flags + cc);
         if (a.stage != 0) pn_next = __ldg(a.phi_n + cc);
         if (KIND == SK_EXTEND || KIND == SK_ADVECT || KIND == SK_ENO2) {
@@ -179,7 +182,7 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
         }
     };
     if (active && k0 < k1) load_node(c);
-    for (int k = k0; k < k1; ++k, c += g.plane) {
+    for (int k = k0; k < k1; ++k, c += plane) {
         // every warp has finished page k-1 and stored page k+3
         __syncthreads();
         q[6] = sm[s_k3][ty + HALO][tx + HALO];
@@ -187,7 +190,7 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
         const float(*P)[SW] = sm[s_k];
         const uint8_t fl = fl_next;
         const float pn = pn_next, vx0 = v0_next, vy0 = v1_next, vz0 = v2_next, sp = sp_next;
-        if (active && k + 1 < k1) load_node(c + g.plane);
+        if (active && k + 1 < k1) load_node(c + plane);
 
         // z window of page k+1: its weights give the forward derivative here and the
         // backward derivative at the next page
@@ -227,7 +230,7 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
                 const float2 dz = mul2(weno5_combine2(q1, q2, q3, f2(zr1, nr3), f2(zr2, nr2), f2(zr3, nr1)),
                                        f2s(a.inv_h[2]));
                 const bool neg = fl & MASK_BIT;
-                const float dtn = (fl & 0x3F) ? pseudo_dt(fl, a.d, c, a.h[0], a.h[1], a.h[2]) : a.dt_uniform;
+                const float dtn = (fl & 0x3F) ? pseudo_dt(fl, a.d, (long long)c, a.h[0], a.h[1], a.h[2]) : a.dt_uniform;
                 const float gn = godunov_norm(neg, dxf, dxb, dyf, dyb, dz.y, dz.x);
                 step = (gn - 1.f) * dtn * (neg ? -1.f : 1.f);
             } else if (compute && !band && KIND == SK_ENO2R) {
@@ -274,7 +277,7 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
                 base = __shfl_sync(0xffffffffu, base, leader);
                 if (band) {
                     const unsigned rank = __popc(m & ((1u << lane) - 1u));
-                    a.queue[base + rank] = (unsigned)c;
+                    a.queue[base + rank] = c;
                 }
             }
         }
