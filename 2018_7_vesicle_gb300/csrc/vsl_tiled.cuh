@@ -76,6 +76,11 @@ struct TiledArgs {
 
 constexpr int PER_THREAD = (PLANE + TY * TX - 1) / (TY * TX);  // halo elements per thread
 
+// a ring slot known at compile time (the unrolled page loop)
+template <int N> struct RingSlot {
+    __host__ __device__ constexpr operator int() const { return N; }
+};
+
 // Upwind quadratic-ENO derivative of a line with no crossing (eno2_pair with r1 = l1 = h:
 // (v2 - v0)/h - h * minmod/2h^2 forward, (v0 - v1)/h + h * minmod/2h^2 backward, folded
 // into one product with 1/h); back selects the backward one (speed > 0).
@@ -112,7 +117,9 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
     const int k0 = blockIdx.z * a.kz;
     const int k1 = min(k0 + a.kz, g.pges);
     const bool active = i < g.rows && j < g.cols;
-    auto slot = [](int p) { return ((p % RING) + RING) % RING; };
+    // ring slot of page p (p >= k0): counted from the block's first page, so that in the
+    // loop unrolled by RING the slots are compile-time constants
+    auto slot = [k0](int p) { return (p - k0) % RING; };
 
     // this thread's share of a tile plane (with halo): smem index and in-page offset of up
     // to PER_THREAD elements; the same for every page, only the page base changes
@@ -163,9 +170,6 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
                              zr3);
 
     const unsigned lane = tid & 31;
-    // ring slots of pages k, k+3 and k+4 (= k-1), advanced by one per page
-    auto next_slot = [](int sl) { return sl == RING - 1 ? 0 : sl + 1; };
-    int s_k = slot(k0), s_k3 = slot(k0 + 3), s_k4 = slot(k0 + 4);
     // per-node inputs of the next page, loaded one page ahead
     const unsigned col_base = (unsigned)clampi(j, g.cols) * (unsigned)g.rows + (unsigned)clampi(i, g.rows);
     unsigned c = col_base + (unsigned)k0 * plane;
@@ -182,12 +186,14 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
         }
     };
     if (active && k0 < k1) load_node(c);
-    for (int k = k0; k < k1; ++k, c += plane) {
+    // one page: the slots of pages k, k+3 and k+4 (= k-1) are RingSlot constants in the
+    // unrolled loop and plain ints in the remainder
+    auto page = [&](auto sk, auto sk3, auto sk4, int k) {
         // every warp has finished page k-1 and stored page k+3
         __syncthreads();
-        q[6] = sm[s_k3][ty + HALO][tx + HALO];
+        q[6] = sm[int(sk3)][ty + HALO][tx + HALO];
         fetch(k + 4);  // loads in flight during this page's arithmetic, stored at its end
-        const float(*P)[SW] = sm[s_k];
+        const float(*P)[SW] = sm[int(sk)];
         const uint8_t fl = fl_next;
         const float pn = pn_next, vx0 = v0_next, vy0 = v1_next, vz0 = v2_next, sp = sp_next;
         if (active && k + 1 < k1) load_node(c + plane);
@@ -282,16 +288,30 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
             }
         }
         // page k+4 goes to the slot of page k-1, which no warp reads any more
-        store_slot(s_k4);
+        store_slot(int(sk4));
         zr1 = nr1;
         zr2 = nr2;
         zr3 = nr3;
 #pragma unroll
         for (int s = 0; s < 6; ++s) q[s] = q[s + 1];
-        s_k = next_slot(s_k);
-        s_k3 = next_slot(s_k3);
-        s_k4 = next_slot(s_k4);
+        c += plane;
+    };
+    using I0 = RingSlot<0>;
+    using I1 = RingSlot<1>;
+    using I2 = RingSlot<2>;
+    using I3 = RingSlot<3>;
+    using I4 = RingSlot<4>;
+    static_assert(RING == 5, "the unrolled page loop assumes a ring of 5 planes");
+    int k = k0;
+    for (; k + RING <= k1; k += RING) {
+        page(I0{}, I3{}, I4{}, k);
+        page(I1{}, I4{}, I0{}, k + 1);
+        page(I2{}, I0{}, I1{}, k + 2);
+        page(I3{}, I1{}, I2{}, k + 3);
+        page(I4{}, I2{}, I3{}, k + 4);
     }
+#pragma unroll 1
+    for (int r = 0; k < k1; ++k, ++r) page(r, (r + 3) % RING, (r + 4) % RING, k);
 }
 
 // Band nodes of one stage: the generic per-node update (interface-aware stencils),
