@@ -17,7 +17,8 @@ from ._lib import lib
 from .sdf3 import SDF3, colmajor_full
 
 KINDS = {"reinit": 0, "extend": 1, "advect": 2, "enork2_extend": 3, "enork2_reinit": 4}
-CANDIDATES = (4, 8, 16, 32, 64)
+CANDIDATES = (4, 8, 10, 15, 16, 20, 25, 30, 32, 40, 64)
+DEFAULT_PAGES = 20  # pages per block of a shape not in the table
 TILE_ROWS, TILE_COLS = 32, 8  # tile of one block of the tiled kernels
 BLOCKS_PER_SM = 4  # resident blocks per SM of the tiled kernels (launch bounds; 5 for the ENORK2 extension)
 
@@ -73,10 +74,15 @@ def _candidates(pges: int, candidates):
     return out
 
 
-def tune_shape(sdf: SDF3, candidates=CANDIDATES, iters: int = 2, reps: int = 3) -> dict:
+# the kinds a vesicle step (and a batch of them) launches
+STEP_KINDS = ("reinit", "extend", "advect")
+
+
+def tune_shape(sdf: SDF3, candidates=CANDIDATES, iters: int = 2, reps: int = 3, kinds=None) -> dict:
     """Pick pages per block for each stage kind on sdf's grid shape; returns
     {kind: {"pages": best, "ms": {candidate: time}}}.  sdf must be FP32 with its
-    distances set (setDistance).  candidates="waves" takes wave_candidates(shape)."""
+    distances set (setDistance).  candidates="waves" takes wave_candidates(shape); `kinds`
+    limits the tuning to those stage kinds (all of KINDS by default)."""
     if sdf.precision != "f32":
         raise ValueError("the tiled kernels are the FP32 form's")
     size = sdf.GD3.Size
@@ -95,6 +101,8 @@ def tune_shape(sdf: SDF3, candidates=CANDIDATES, iters: int = 2, reps: int = 3) 
     }
     report = {}
     for kind, fn in ops.items():
+        if kinds is not None and kind not in kinds:
+            continue
         times = {}
         for c in _candidates(size[2], candidates):
             set_pages(size, kind, c)

@@ -50,11 +50,11 @@ class VesicleBatch:
         shapes = {}
         for m in self.maps:
             shapes.setdefault(tuple(m.GD3.Size), m)
-        per_shape = {s: T.tune_shape(m, cand) for s, m in shapes.items()}
+        per_shape = {s: T.tune_shape(m, cand, kinds=T.STEP_KINDS) for s, m in shapes.items()}
         configs = {"tuned": {s: {k: r["pages"] for k, r in c.items()} for s, c in per_shape.items()},
-                   "default": {s: {k: 0 for k in T.KINDS} for s in shapes}}
+                   "default": {s: {k: 0 for k in T.STEP_KINDS} for s in shapes}}
         for c in cand:
-            configs[f"uniform_{c}"] = {s: {k: c for k in T.KINDS} for s in shapes}
+            configs[f"uniform_{c}"] = {s: {k: c for k in T.STEP_KINDS} for s in shapes}
 
         def apply(cfg):
             for s, kinds in cfg.items():

@@ -28,11 +28,11 @@ namespace {
 
 // Pages per block (a launch parameter: the default below, or the value the tuning table
 // holds for the grid shape and stage kind) and the occupancy target (compile time).
-// Measured on GB300 at 256^3 (vesicle step with graph replay): 16/32/64 pages x 4/5
-// blocks per SM gave 46.6/47.5/47.9 ms at 4 blocks (64 registers, no spills) and
-// 49.5/51.4/53.0 ms at 5 blocks (48 registers with spills).
+// Measured on GB300 at 256^3, vesicle step as a graph: 4 blocks per SM (64 registers) beat
+// 5 (48 registers with spills) at 16/32/64 pages; with the page loop unrolled by the ring
+// length, 10/15/16/20/25/30/32/40 pages gave 33.6/33.0/33.1/32.7/32.4/32.8/33.0/32.9 ms.
 #ifndef VSL_TILED_KZ
-#define VSL_TILED_KZ 16
+#define VSL_TILED_KZ 20
 #endif
 #ifndef VSL_TILED_MIN_BLOCKS
 #define VSL_TILED_MIN_BLOCKS 4

@@ -288,7 +288,7 @@ def batched_measure(torch, pkg, S, steps: int, seed: int = 0, tune: bool = True)
     nodes = batch.nodes()
     out = {"vesicles": len(maps), "nodes": nodes, "steps": steps}
     if tune:
-        out["autotune"] = batch.autotune()
+        out["autotune"] = batch.autotune(candidates=(8, 16, 20, 25, 32, 64))
     for name, fn in (("graph", batch.step), ("loop", batch.step_loop)):
         if tune and name == "loop":
             # the launch loop runs one vesicle at a time: the per-shape choices (each shape
@@ -708,7 +708,8 @@ def main():
     # pages per block of the tiled kernels for this grid, tuned before the graph is recorded
     tuning = None
     if not args.no_autotune:
-        tuning = importlib.import_module(PKG + ".autotune").tune_shape(m, candidates=(8, 16, 32, 64))
+        T = importlib.import_module(PKG + ".autotune")
+        tuning = T.tune_shape(m, candidates=(10, 15, 16, 20, 25, 30, 32, 40), kinds=T.STEP_KINDS)
     # each step replays one CUDA graph holding the step's whole launch sequence
     for _ in range(args.warmup):
         m.vesicle_step(EXT, RE, CFL, graph=True)

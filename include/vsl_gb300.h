@@ -193,7 +193,7 @@ enum {
  * pges, kind), kind 0 reinitialization, 1 extension, 2 advection, 3 ENORK2 extension, 4
  * ENORK2 reinitialization, used by every later launch of that shape (a CUDA graph keeps the
  * value it was recorded with).
- * Shapes not in the table use 16.  vsl_set_tile_pages(..., pages = 0) removes an entry; it returns
+ * Shapes not in the table use 20.  vsl_set_tile_pages(..., pages = 0) removes an entry; it returns
  * VSL_ERR_SHAPE / VSL_ERR_VALUE for a bad shape, kind or pages (1..65535), or a full
  * table (512 entries).  vsl_tile_pages returns the value in effect (0 for bad input). */
 int vsl_set_tile_pages(int rows, int cols, int pges, int kind, int pages);

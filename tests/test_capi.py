@@ -108,17 +108,17 @@ def test_workspace_sizes(vsl):
 
 
 def test_tile_pages_table(vsl):
-    """The pages-per-block table of the tiled kernels: default 16, set / replace / remove,
+    """The pages-per-block table of the tiled kernels: default 20, set / replace / remove,
     argument checks (host only, no launch)."""
     call = vsl.raw
-    assert call("vsl_tile_pages", 40, 36, 52, 1) == 16
+    assert call("vsl_tile_pages", 40, 36, 52, 1) == 20
     assert call("vsl_set_tile_pages", 40, 36, 52, 1, 8) == 0
     assert call("vsl_tile_pages", 40, 36, 52, 1) == 8
-    assert call("vsl_tile_pages", 40, 36, 52, 0) == 16  # other kind untouched
+    assert call("vsl_tile_pages", 40, 36, 52, 0) == 20  # other kind untouched
     assert call("vsl_set_tile_pages", 40, 36, 52, 1, 4) == 0
     assert call("vsl_tile_pages", 40, 36, 52, 1) == 4
     assert call("vsl_set_tile_pages", 40, 36, 52, 1, 0) == 0  # back to the default
-    assert call("vsl_tile_pages", 40, 36, 52, 1) == 16
+    assert call("vsl_tile_pages", 40, 36, 52, 1) == 20
     assert call("vsl_set_tile_pages", 0, 36, 52, 1, 8) == 2
     assert call("vsl_set_tile_pages", 40, 36, 52, 3, 8) == 0  # kind 3: the ENORK2 extension
     assert call("vsl_tile_pages", 40, 36, 52, 3) == 8

@@ -37,7 +37,7 @@ def test_tune_shape_fills_table(pkg, T):
         assert T.get_pages(size, kind) == report[kind]["pages"]
         assert all(ms > 0 for ms in report[kind]["ms"].values())
     T.clear_shape(size)
-    assert all(T.get_pages(size, k) == 16 for k in T.KINDS)
+    assert all(T.get_pages(size, k) == T.DEFAULT_PAGES for k in T.KINDS)
 
 
 def test_pages_change_only_the_launch_shape(pkg, T):
