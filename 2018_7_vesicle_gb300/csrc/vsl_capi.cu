@@ -344,7 +344,7 @@ int extend_setup(const T *F, Ptr6<const T> d, const ExtendWork<T> &w, const Grid
                  cudaStream_t s)
 {
     VSL_TRY(launch_classify<T>(F, d, w.flags, w.flagged, g, s));
-    VSL_TRY(launch_extension_velocity<T>(F, w.flags, d, w.v, g, eno3, floor, s));
+    VSL_TRY(launch_extension_velocity<T>(F, w.flags, d, w.v, g, eno3, floor, w.flagged, s));
     return VSL_OK;
 }
 

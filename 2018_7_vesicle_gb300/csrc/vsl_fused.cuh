@@ -227,13 +227,13 @@ __global__ void __launch_bounds__(BX *BY) k_reinit_stage(const T *__restrict__ p
 // ---------------------------------------------------------------------------------------
 // The classification byte says which distances differ from the spacing (only those are
 // read); away from the interface the mixed form takes the packed fast WENO5 pair.
+// one node of the extension velocity (the generic form: interface-aware one-sided
+// derivatives on the axes with a crossing)
 template <typename T, bool ENO3>
-__global__ void __launch_bounds__(BX *BY) k_extension_velocity(const T *__restrict__ phi,
-                                                                 const uint8_t *__restrict__ flags, Ptr6<const T> d,
-                                                                 Ptr3<T> v, Grid g, T floor)
+__device__ __forceinline__ void extension_velocity_node(const T *__restrict__ phi, const uint8_t *__restrict__ flags,
+                                                        const Ptr6<const T> &d, Ptr3<T> &v, const Grid &g, T floor,
+                                                        int i, int j, int k)
 {
-    int i, j, k;
-    if (!fused_node(g, i, j, k)) return;
     const long long c = node_index(g, i, j, k);
     const uint8_t fl = __ldg(flags + c);
     T n[3];
@@ -258,6 +258,62 @@ __global__ void __launch_bounds__(BX *BY) k_extension_velocity(const T *__restri
     const T s = f0 > T(0) ? T(1) : (f0 < T(0) ? T(-1) : T(0));
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax) v.p[ax][c] = s * (n[ax] / grad);
+}
+
+template <typename T, bool ENO3>
+__global__ void __launch_bounds__(BX *BY) k_extension_velocity(const T *__restrict__ phi,
+                                                                 const uint8_t *__restrict__ flags, Ptr6<const T> d,
+                                                                 Ptr3<T> v, Grid g, T floor)
+{
+    int i, j, k;
+    if (!fused_node(g, i, j, k)) return;
+    extension_velocity_node<T, ENO3>(phi, flags, d, v, g, floor, i, j, k);
+}
+
+// The mixed form splits the extension velocity: nodes without a distance flag take the
+// uniform path alone, and only the side each axis keeps (n = D+ where |p4| < |p2|, else
+// D-) is reconstructed, x and y as the two lanes of one packed WENO5, z with itself in
+// both lanes; each lane is the arithmetic of the corresponding lane of weno5_pair_fast2,
+// so the velocity is the same to the bit.  The flagged nodes (the classification's list)
+// run the generic form in k_velocity_list.
+__global__ void __launch_bounds__(BX *BY) k_velocity_uniform(const float *__restrict__ phi,
+                                                               const uint8_t *__restrict__ flags, Ptr3<float> v,
+                                                               Grid g, float floor)
+{
+    int i, j, k;
+    if (!fused_node(g, i, j, k)) return;
+    const long long c = node_index(g, i, j, k);
+    if (__ldg(flags + c) & 0x3F) return;
+    float px[7], py[7], pz[7];
+    load_line7(phi, axis_line(g, i, j, k, AX_X), px);
+    load_line7(phi, axis_line(g, i, j, k, AX_Y), py);
+    load_line7(phi, axis_line(g, i, j, k, AX_Z), pz);
+    const float hx = (float)g.dx, hy = (float)g.dy, hz = (float)g.dz;
+    const bool bx = !(fabsf(px[4]) < fabsf(px[2])), by = !(fabsf(py[4]) < fabsf(py[2]));
+    const bool bz = !(fabsf(pz[4]) < fabsf(pz[2]));
+    const float2 dxy = weno5_upwind2(px, bx, py, by, f2(1.0f / hx, 1.0f / hy), f2(1e-6f * hx * hx, 1e-6f * hy * hy));
+    const float2 dzz = weno5_upwind2(pz, bz, pz, bz, f2s(1.0f / hz), f2s(1e-6f * hz * hz));
+    const float n[3] = {dxy.x, dxy.y, dzz.x};
+    const float grad = vmax(sqrtf(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]), floor);
+    const float f0 = px[3];
+    const float s = f0 > 0.f ? 1.f : (f0 < 0.f ? -1.f : 0.f);
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) v.p[ax][c] = s * (n[ax] / grad);
+}
+
+// the flagged nodes of the extension velocity (the classification's list), generic form
+template <bool ENO3>
+__global__ void __launch_bounds__(128) k_velocity_list(const float *__restrict__ phi, const uint8_t *__restrict__ flags,
+                                                       Ptr6<const float> d, Ptr3<float> v, NodeList list, Grid g,
+                                                       float floor)
+{
+    const unsigned n = *list.count;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const long long c = list.idx[t];
+        int i, j, k;
+        node_of(g, c, i, j, k);
+        extension_velocity_node<float, ENO3>(phi, flags, d, v, g, floor, i, j, k);
+    }
 }
 
 // crossing values (boundary_interpolant.cu:78-141 / wenork3_extend.cu:296-365), at the
@@ -610,8 +666,20 @@ cudaError_t launch_reinit_stage(const T *phi_s, const T *phi_n, T *out, const ui
 
 template <typename T>
 cudaError_t launch_extension_velocity(const T *phi, const uint8_t *flags, Ptr6<const T> dist, Ptr3<T> v, const Grid &g,
-                                      bool eno3, double floor, cudaStream_t s)
+                                      bool eno3, double floor, NodeList flagged, cudaStream_t s)
 {
+    if constexpr (std::is_same<T, float>::value) {
+        if (flagged.idx) {
+            k_velocity_uniform<<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, flags, v, g, (float)floor);
+            cudaError_t err = cudaGetLastError();
+            if (err != cudaSuccess) return err;
+            if (eno3)
+                k_velocity_list<true><<<list_blocks(), 128, 0, s>>>(phi, flags, dist, v, flagged, g, (float)floor);
+            else
+                k_velocity_list<false><<<list_blocks(), 128, 0, s>>>(phi, flags, dist, v, flagged, g, (float)floor);
+            return cudaGetLastError();
+        }
+    }
     if (eno3)
         k_extension_velocity<T, true><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, flags, dist, v, g, (T)floor);
     else
@@ -710,7 +778,7 @@ cudaError_t launch_enork2_extend_stage(const T *c_s, const T *c_n, T *out, const
     template cudaError_t launch_reinit_stage<T>(const T *, const T *, T *, const uint8_t *, Ptr6<const T>,          \
                                                 const Grid &, int, bool, bool, cudaStream_t);                       \
     template cudaError_t launch_extension_velocity<T>(const T *, const uint8_t *, Ptr6<const T>, Ptr3<T>,           \
-                                                      const Grid &, bool, double, cudaStream_t);                    \
+                                                      const Grid &, bool, double, NodeList, cudaStream_t);          \
     template cudaError_t launch_crossing<T>(const T *, Ptr6<const T>, Ptr6<T>, NodeList, const Grid &, bool,        \
                                             cudaStream_t);                                                          \
     template cudaError_t launch_extend_stage<T>(const T *, const T *, T *, const uint8_t *, Ptr6<const T>,          \

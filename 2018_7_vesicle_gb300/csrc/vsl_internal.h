@@ -58,10 +58,11 @@ cudaError_t launch_classify(const T *phi0, Ptr6<const T> dist, uint8_t *flags, N
 template <typename T>
 cudaError_t launch_reinit_stage(const T *phi_s, const T *phi_n, T *out, const uint8_t *flags, Ptr6<const T> dist,
                                 const Grid &g, int stage, bool eno3, bool fast, cudaStream_t s);
-// flags: the classification bytes of phi with these distances (launch_classify)
+// flags: the classification bytes of phi with these distances (launch_classify); flagged:
+// its list of flagged nodes (the FP32 form then runs the uniform nodes and the list apart)
 template <typename T>
 cudaError_t launch_extension_velocity(const T *phi, const uint8_t *flags, Ptr6<const T> dist, Ptr3<T> v, const Grid &g,
-                                      bool eno3, double floor, cudaStream_t s);
+                                      bool eno3, double floor, NodeList flagged, cudaStream_t s);
 // crossing values at the listed (flagged) nodes only; other entries of cp are not written
 template <typename T>
 cudaError_t launch_crossing(const T *c, Ptr6<const T> dist, Ptr6<T> cp, NodeList list, const Grid &g, bool cubic,
