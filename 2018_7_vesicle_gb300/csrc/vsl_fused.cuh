@@ -173,6 +173,64 @@ __global__ void __launch_bounds__(BX *BY) k_classify(const T *__restrict__ phi0,
     if (list.idx) warp_append((fl & 0x3F) != 0, (unsigned)c, list.idx, list.count);
 }
 
+// The FP32 classification with four consecutive nodes per thread: the classification is
+// elementwise in the linear index, so the field and the six distances are read as 16-byte
+// vectors and the four flag bytes written as one word (node count a multiple of 4, every
+// array 16-byte aligned; the launcher checks).  The flags are k_classify's.
+__global__ void __launch_bounds__(256) k_classify4(const float *__restrict__ phi0, Ptr6<const float> d,
+                                                   uint8_t *flags, NodeList list, long long n4, float hx, float hy,
+                                                   float hz, float tiny)
+{
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = t < n4;
+    const float h[3] = {hx, hy, hz};
+    uint8_t fl[4] = {0, 0, 0, 0};
+    if (in) {
+        bool fixed[4] = {false, false, false, false};
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const float4 v = __ldg(reinterpret_cast<const float4 *>(d.p[q]) + t);
+            const float e[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                if (e[r] != h[q / 2]) fl[r] |= (uint8_t)(1u << q);
+                fixed[r] |= e[r] < tiny;
+            }
+        }
+        const float4 f = __ldg(reinterpret_cast<const float4 *>(phi0) + t);
+        const float fv[4] = {f.x, f.y, f.z, f.w};
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            if (fv[r] < 0.f) fl[r] |= MASK_BIT;
+            if (fixed[r]) fl[r] |= FIXED_BIT;
+        }
+        reinterpret_cast<uchar4 *>(flags)[t] = make_uchar4(fl[0], fl[1], fl[2], fl[3]);
+    }
+    if (list.idx) {
+        // append the flagged nodes in node order (as k_classify's warps do): a warp-wide
+        // exclusive scan of the per-lane counts, one atomic per warp
+        const unsigned lane = threadIdx.x & 31u;
+        unsigned mine = 0;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) mine += (fl[r] & 0x3F) ? 1u : 0u;
+        unsigned incl = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+            if ((int)lane >= o) incl += y;
+        }
+        const unsigned total = __shfl_sync(0xffffffffu, incl, 31);
+        if (total) {
+            unsigned base = 0;
+            if (lane == 31) base = atomicAdd(list.count, total);
+            base = __shfl_sync(0xffffffffu, base, 31) + incl - mine;
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+                if (fl[r] & 0x3F) list.idx[base++] = (unsigned)(4 * t + r);
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------------------
 // reinitialization stage (re_step.cu:283-393 / weno_rk3_reinitialization.cu:295-406)
 // ---------------------------------------------------------------------------------------
@@ -640,6 +698,17 @@ cudaError_t launch_classify(const T *phi0, Ptr6<const T> dist, uint8_t *flags, N
     if (list.idx) {
         cudaError_t err = cudaMemsetAsync(list.count, 0, sizeof(unsigned), s);
         if (err != cudaSuccess) return err;
+    }
+    if constexpr (std::is_same<T, float>::value) {
+        auto aligned = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
+        bool vec = g.num % 4 == 0 && aligned(phi0) && aligned(flags);
+        for (int q = 0; q < 6; ++q) vec = vec && aligned(dist.p[q]);
+        if (vec) {
+            const long long n4 = g.num / 4;
+            k_classify4<<<(unsigned)((n4 + 255) / 256), 256, 0, s>>>(phi0, dist, flags, list, n4, (float)g.dx,
+                                                                   (float)g.dy, (float)g.dz, (float)(1e-6 * g.dx));
+            return cudaGetLastError();
+        }
     }
     k_classify<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi0, dist, flags, list, g);
     return cudaGetLastError();
