@@ -101,7 +101,7 @@ __device__ __forceinline__ void eno2_pair_uniform(const float p[7], float inv_h,
     back = (v0 - v1 + 0.5f * minmod(p2, v0 - 2.f * v1 + p[1])) * inv_h;
 }
 
-template <int KIND>
+template <int KIND, int STAGE>
 // The ENORK2 extension kind, whose uniform path is light, is latency-bound at 4 blocks per SM
 // (long-scoreboard stalls, DRAM 35% of peak): 5 blocks (47 registers, no spills) took 100
 // pseudo-steps at 256^3 from 26.7 to 23.6 ms.  The ENORK2 reinitialization was slower at 5
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
     float pn_next = 0.f, v0_next = 0.f, v1_next = 0.f, v2_next = 0.f, sp_next = 1.f;
     auto load_node = [&](unsigned cc) {
         if (KIND != SK_ADVECT) fl_next = __ldg(a.flags + cc);
-        if (a.stage != 0) pn_next = __ldg(a.phi_n + cc);
+        if (STAGE != 0) pn_next = __ldg(a.phi_n + cc);
         if (KIND == SK_EXTEND || KIND == SK_ADVECT || KIND == SK_ENO2) {
             v0_next = __ldg(a.v.p[0] + cc);
             v1_next = __ldg(a.v.p[1] + cc);
@@ -271,8 +271,8 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
                 step = KIND == SK_EXTEND ? tr * a.dt_uniform : (float)__ldg(a.dt) * tr;
             }
             if (!band)
-                a.out[c] = (KIND == SK_ENO2 || KIND == SK_ENO2R) ? rk2_combine(a.stage, pn, ps, step)
-                                                                  : rk3_combine(a.stage, pn, ps - step);
+                a.out[c] = (KIND == SK_ENO2 || KIND == SK_ENO2R) ? rk2_combine(STAGE, pn, ps, step)
+                                                                  : rk3_combine(STAGE, pn, ps - step);
         }
         if (KIND == SK_REINIT) {  // the extension's band is the static list of flagged nodes
             const unsigned m = __ballot_sync(0xffffffffu, band);
@@ -458,6 +458,18 @@ SideLane *side_lane(cudaStream_t s)
 }
 }  // namespace
 
+// the RK stage is a template parameter of the tiled kernel (its combination and whether it
+// reads the step-start field are then fixed at compile time); the ENORK2 kinds have two
+template <int KIND> void launch_stage_kind(int stage, dim3 gr, dim3 bl, cudaStream_t s, const TiledArgs &a)
+{
+    if (stage == 0)
+        k_stage_tiled<KIND, 0><<<gr, bl, 0, s>>>(a);
+    else if (stage == 1 || KIND == SK_ENO2 || KIND == SK_ENO2R)
+        k_stage_tiled<KIND, 1><<<gr, bl, 0, s>>>(a);
+    else
+        k_stage_tiled<KIND, 2><<<gr, bl, 0, s>>>(a);
+}
+
 cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const Grid &g, cudaStream_t s)
 {
     TiledArgs a = tiled_args(g);
@@ -488,11 +500,11 @@ cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const 
         cudaError_t e;
         if (ln && (e = cudaEventRecord(ln->fork, s)) != cudaSuccess) return e;
         if (kind == SK_ENO2)
-            k_stage_tiled<SK_ENO2><<<gr, bl, 0, s>>>(a);
+            launch_stage_kind<SK_ENO2>(a.stage, gr, bl, s, a);
         else if (kind == SK_ENO2R)
-            k_stage_tiled<SK_ENO2R><<<gr, bl, 0, s>>>(a);
+            launch_stage_kind<SK_ENO2R>(a.stage, gr, bl, s, a);
         else
-            k_stage_tiled<SK_EXTEND><<<gr, bl, 0, s>>>(a);
+            launch_stage_kind<SK_EXTEND>(a.stage, gr, bl, s, a);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         cudaStream_t bs = s;
         if (ln) {
@@ -515,9 +527,9 @@ cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const 
         return cudaSuccess;
     }
     if (kind == SK_REINIT)
-        k_stage_tiled<SK_REINIT><<<gr, bl, 0, s>>>(a);
+        launch_stage_kind<SK_REINIT>(a.stage, gr, bl, s, a);
     else
-        k_stage_tiled<SK_ADVECT><<<gr, bl, 0, s>>>(a);
+        launch_stage_kind<SK_ADVECT>(a.stage, gr, bl, s, a);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || kind == SK_ADVECT) return e;
     // the reinitialization's band is queued by the tiled kernel, so its kernel follows it
