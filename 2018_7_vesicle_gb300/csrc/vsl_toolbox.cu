@@ -12,6 +12,8 @@ __global__ void __launch_bounds__(1024) k_sum_partials(const double *__restrict_
     __shared__ double s[32];
     for (int q = 0; q < ncomp; ++q) {
         double acc = 0.0;
+        // unrolled so that the loads are in flight together; the additions keep their order
+#pragma unroll 8
         for (int b = threadIdx.x; b < nblocks; b += blockDim.x) acc += partials[(long long)ncomp * b + q];
         acc = warp_sum(acc);
         if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = acc;
@@ -30,6 +32,7 @@ __global__ void __launch_bounds__(1024) k_time_step(const double *__restrict__ p
 {
     __shared__ double s[32];
     double m = 0.0;
+#pragma unroll 8
     for (int b = threadIdx.x; b < nblocks; b += blockDim.x) m = fmax(m, partials[b]);
     m = warp_max(m);
     if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = m;

@@ -57,12 +57,18 @@ __global__ void __launch_bounds__(NT) k_toolbox(const T *__restrict__ f, Toolbox
     bool unit = false;  // a volume term equal to exactly 1
     if (i < g.rows && j < g.cols) {
         const long long c = node_index(g, i, j, k);
-        auto F = [&](int a, int b, int e) { return __ldg(f + clamped_index(g, a, b, e)); };
-        auto H = [&](int a, int b, int e) { return vmax(__ldg(f + clamped_index(g, a, b, e)), T(0)); };
+        // the clamped neighbour coordinates once; node offsets in 32 bits (grids hold fewer
+        // than 2^31 nodes)
+        const int im = clampi(i - 1, g.rows), ip = clampi(i + 1, g.rows);
+        const int jm = clampi(j - 1, g.cols), jp = clampi(j + 1, g.cols);
+        const int km = clampi(k - 1, g.pges), kp = clampi(k + 1, g.pges);
+        const unsigned rows = (unsigned)g.rows, plane = (unsigned)g.plane;
+        auto F = [&](int a, int b, int e) { return __ldg(f + ((unsigned)e * plane + (unsigned)b * rows + (unsigned)a)); };
+        auto H = [&](int a, int b, int e) { return vmax(F(a, b, e), T(0)); };
         const T dx = (T)g.dx, dy = (T)g.dy, dz = (T)g.dz, ds = (T)ds_;
         const T fc = __ldg(f + c);
-        const T fxp = F(i, j + 1, k), fxm = F(i, j - 1, k), fyp = F(i + 1, j, k), fym = F(i - 1, j, k);
-        const T fzp = F(i, j, k + 1), fzm = F(i, j, k - 1);
+        const T fxp = F(i, jp, k), fxm = F(i, jm, k), fyp = F(ip, j, k), fym = F(im, j, k);
+        const T fzp = F(i, j, kp), fzm = F(i, j, km);
         T fx = (fxp - fxm) / (2 * dx);
         T fy = (fyp - fym) / (2 * dy);
         T fz = (fzp - fzm) / (2 * dz);
@@ -70,9 +76,9 @@ __global__ void __launch_bounds__(NT) k_toolbox(const T *__restrict__ f, Toolbox
         T fxx = (fxp - 2 * fc + fxm) / (dx * dx);
         T fyy = (fyp - 2 * fc + fym) / (dy * dy);
         T fzz = (fzp - 2 * fc + fzm) / (dz * dz);
-        T fxy = (F(i + 1, j + 1, k) + F(i - 1, j - 1, k) - F(i + 1, j - 1, k) - F(i - 1, j + 1, k)) / (4 * ds * ds);
-        T fyz = (F(i + 1, j, k + 1) + F(i - 1, j, k - 1) - F(i + 1, j, k - 1) - F(i - 1, j, k + 1)) / (4 * ds * ds);
-        T fzx = (F(i, j + 1, k + 1) + F(i, j - 1, k - 1) - F(i, j + 1, k - 1) - F(i, j - 1, k + 1)) / (4 * ds * ds);
+        T fxy = (F(ip, jp, k) + F(im, jm, k) - F(ip, jm, k) - F(im, jp, k)) / (4 * ds * ds);
+        T fyz = (F(ip, j, kp) + F(im, j, km) - F(ip, j, km) - F(im, j, kp)) / (4 * ds * ds);
+        T fzx = (F(i, jp, kp) + F(i, jm, km) - F(i, jp, km) - F(i, jm, kp)) / (4 * ds * ds);
         T lap = fxx + fyy + fzz;
         T r1 = fxx * fx + fxy * fy + fzx * fz;
         T r2 = fxy * fx + fyy * fy + fyz * fz;
@@ -81,8 +87,8 @@ __global__ void __launch_bounds__(NT) k_toolbox(const T *__restrict__ f, Toolbox
         T mean = -lap / gm + (fx * r1 + fy * r2 + fz * r3) / cube(gm);
         const T gm4 = fourth(gm);
         T hc = vmax(fc, T(0));
-        T hxp = H(i, j + 1, k), hxm = H(i, j - 1, k), hyp = H(i + 1, j, k), hym = H(i - 1, j, k);
-        T hzp = H(i, j, k + 1), hzm = H(i, j, k - 1);
+        T hxp = H(i, jp, k), hxm = H(i, jm, k), hyp = H(ip, j, k), hym = H(im, j, k);
+        T hzp = H(i, j, kp), hzm = H(i, j, km);
         T px = (hxp - hxm) / (2 * dx), py = (hyp - hym) / (2 * dy), pz = (hzp - hzm) / (2 * dz);
         T dot = px * fx + py * fy + pz * fz;
         T pxx = (hxp - 2 * hc + hxm) / (dx * dx);
