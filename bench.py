@@ -43,11 +43,12 @@ BYTES_ADVECT = 17 * W32
 # toolbox + reductions 1w, plus a second setDistance 7w)
 BYTES_SETUP = (7 + 10 + 13 + 1 + 7) * W32
 BYTES_PER_NODE_STEP = EXT * BYTES_EXTEND + ADV * BYTES_ADVECT + RE * BYTES_REINIT + BYTES_SETUP
-# kernels launched per vesicle step: toolbox, sum, velocity, classify, crossing,
-# 3*EXT extension stages each with its band kernel, band max, time step, 3 advection
-# stages, setDistance (scan + roots), classify, 3*RE reinitialization stages each with
-# its band kernel (memsets of the list counters are not kernels)
-LAUNCHES_PER_STEP = 1 + 1 + 1 + 1 + 1 + 2 * 3 * EXT + 1 + 1 + 3 * ADV + 2 + 1 + 2 * 3 * RE
+# kernels launched per vesicle step: toolbox, sum, classify, velocity (uniform nodes and
+# the flagged list), crossing, 3*EXT extension stages each with its band kernel, band
+# max, time step, 3 advection stages, setDistance (scan + roots), classify, 3*RE
+# reinitialization stages each with its band kernel (memsets of the list counters are
+# not kernels)
+LAUNCHES_PER_STEP = 1 + 1 + 1 + 2 + 1 + 2 * 3 * EXT + 1 + 1 + 3 * ADV + 2 + 1 + 2 * 3 * RE
 
 
 def replica_seed(rank: int) -> int:
