@@ -110,6 +110,10 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
 {
     __shared__ float sm[RING][SH][SW];
     const Grid &g = a.g;
+    // the launch is always TY x TX threads: the first two elements of every thread's share
+    // of a plane are then in the plane without a test
+    __builtin_assume(threadIdx.x < TY);
+    __builtin_assume(threadIdx.y < TX);
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * TY + tx;
     const int i0 = blockIdx.x * TY, j0 = blockIdx.y * TX;
@@ -134,7 +138,8 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
     // node offsets fit in 32 bits (grids hold at most 2^31 - 1 nodes), so an address is the
     // base pointer plus one widened 32-bit offset
     const unsigned plane = (unsigned)g.plane;
-    auto page_base = [&](int p) { return a.phi_s + (unsigned)clampi(p, g.pges) * plane; };
+    // pages are fetched at p >= k0 >= 0: only the top edge clamps
+    auto page_base = [&](int p) { return a.phi_s + (unsigned)min(p, g.pges - 1) * plane; };
     float pre[PER_THREAD];
     auto fetch = [&](int p) {
         const float *src = page_base(p);
