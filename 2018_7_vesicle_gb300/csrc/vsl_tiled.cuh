@@ -175,6 +175,8 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
                              zr3);
 
     const unsigned lane = tid & 31;
+    // the advection's time step (formed on the device by an earlier launch): read once
+    const float dt_adv = KIND == SK_ADVECT ? (float)__ldg(a.dt) : 0.f;
     // per-node inputs of the next page, loaded one page ahead
     const unsigned col_base = (unsigned)clampi(j, g.cols) * (unsigned)g.rows + (unsigned)clampi(i, g.rows);
     unsigned c = col_base + (unsigned)k0 * plane;
@@ -273,7 +275,7 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
                                                     zb ? v5 : v2, zb ? zr1 : nr3, zb ? zr2 : nr2, zb ? zr3 : nr1) *
                                  a.inv_h[2];
                 const float tr = ux * dxy.x + uy * dxy.y + uz * dz;
-                step = KIND == SK_EXTEND ? tr * a.dt_uniform : (float)__ldg(a.dt) * tr;
+                step = KIND == SK_EXTEND ? tr * a.dt_uniform : dt_adv * tr;
             }
             if (!band)
                 a.out[c] = (KIND == SK_ENO2 || KIND == SK_ENO2R) ? rk2_combine(STAGE, pn, ps, step)
@@ -322,8 +324,13 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
 // Band nodes of one stage: the generic per-node update (interface-aware stencils),
 // grid-stride over the queue (reinitialization: also clears the other stage's counter for
 // its next use) or over the static flagged list (extension).
+// The static-band kinds' kernel runs beside the tiled stage: at 8 blocks per SM (64
+// registers) it leaves the tiled kernel more room (256^3: 30 extension pseudo-steps
+// 15.53 -> 15.34 ms); the reinitialization's, which runs alone, has no occupancy target
+// (75 registers; 8 blocks per SM gained nothing there).
 template <int KIND, bool ENO3>
-__global__ void __launch_bounds__(128) k_band_stage(TiledArgs a, Ptr6<const float> cp, unsigned *next_counter)
+__global__ void __launch_bounds__(128, (KIND == SK_REINIT ? 0 : 8))
+    k_band_stage(TiledArgs a, Ptr6<const float> cp, unsigned *next_counter)
 {
     const unsigned n = *a.counter;
     if (next_counter && blockIdx.x == 0 && threadIdx.x == 0) *next_counter = 0u;
