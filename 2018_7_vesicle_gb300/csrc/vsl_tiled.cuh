@@ -474,12 +474,16 @@ SideLane *side_lane(cudaStream_t s)
 // reads the step-start field are then fixed at compile time); the ENORK2 kinds have two
 template <int KIND> void launch_stage_kind(int stage, dim3 gr, dim3 bl, cudaStream_t s, const TiledArgs &a)
 {
-    if (stage == 0)
+    if (stage == 0) {
         k_stage_tiled<KIND, 0><<<gr, bl, 0, s>>>(a);
-    else if (stage == 1 || KIND == SK_ENO2 || KIND == SK_ENO2R)
+    } else if constexpr (KIND == SK_ENO2 || KIND == SK_ENO2R) {
         k_stage_tiled<KIND, 1><<<gr, bl, 0, s>>>(a);
-    else
-        k_stage_tiled<KIND, 2><<<gr, bl, 0, s>>>(a);
+    } else {
+        if (stage == 1)
+            k_stage_tiled<KIND, 1><<<gr, bl, 0, s>>>(a);
+        else
+            k_stage_tiled<KIND, 2><<<gr, bl, 0, s>>>(a);
+    }
 }
 
 cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const Grid &g, cudaStream_t s)
