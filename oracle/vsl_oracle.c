@@ -2,7 +2,7 @@
  * vsl_oracle.c -- CPU restatement of the level-set hot path of the vesicle code.
  *
  * TEST INFRASTRUCTURE ONLY.  This file is the oracle: the tests, the smoke check and the
- * bench's CPU-baseline leg use it as the checker.  The product (the CUDA library in the
+ * bench's CPU-baseline leg compare against it.  The product (the CUDA library in the
  * package) never links, loads or calls it.
  *
  * Every function restates one reference kernel or device helper (FP64, one "thread" per
@@ -34,8 +34,8 @@
  * oracle instead rounds those powers once (the running product kept exactly as a
  * double-double via fma), which is how the CUDA plain form forms them; glibc's pow is
  * accurate to 0.52 ulp but not always correctly rounded, so the two builds can differ in
- * the last bit of a power.  Comparing the CUDA form with this build isolates everything
- * else to the bit. */
+ * the last bit of a power.  Comparing the CUDA form with the VSL_ORACLE_CR_POW variant
+ * isolates everything else to the bit. */
 #ifdef VSL_ORACLE_CR_POW
 static double cr_pow(double t, double pd)
 {
