@@ -133,18 +133,18 @@ __global__ void __launch_bounds__(BX *BY) k_dist_scan(const T *__restrict__ f, P
 template <typename T, bool QUINTIC>
 __global__ void __launch_bounds__(128) k_dist_roots(const T *__restrict__ f, Ptr6<T> d, EdgeLists e, Grid g)
 {
-    for (int ax = 0; ax < 3; ++ax) {
-        const unsigned n = *(e.count + ax);
+    // the three axes' lists as one, so that a thread solves one root rather than one per axis
+    const unsigned n0 = e.count[0], n01 = n0 + e.count[1], n = n01 + e.count[2];
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int ax = t < n0 ? 0 : (t < n01 ? 1 : 2);
+        const long long c = e.idx[ax][t - (ax == 0 ? 0u : (ax == 1 ? n0 : n01))];
         const double h = axis_h(g, ax);
-        for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-            const long long c = e.idx[ax][t];
-            int i, j, k;
-            node_of(g, c, i, j, k);
-            const AxisLine L = axis_line(g, i, j, k, ax);
-            const double dist = fore_distance<QUINTIC>(f, L, h);
-            d.p[2 * ax][c] = (T)dist;
-            d.p[2 * ax + 1][c + L.stride] = (T)(h - dist);
-        }
+        int i, j, k;
+        node_of(g, c, i, j, k);
+        const AxisLine L = axis_line(g, i, j, k, ax);
+        const double dist = fore_distance<QUINTIC>(f, L, h);
+        d.p[2 * ax][c] = (T)dist;
+        d.p[2 * ax + 1][c + L.stride] = (T)(h - dist);
     }
 }
 
@@ -528,18 +528,17 @@ template <typename T> __device__ __forceinline__ T rk2_combine(int stage, T phi_
 template <typename T>
 __global__ void __launch_bounds__(128) k_dist_roots_eno2(const T *__restrict__ f, Ptr6<T> d, EdgeLists e, Grid g)
 {
-    for (int ax = 0; ax < 3; ++ax) {
-        const unsigned n = *(e.count + ax);
+    const unsigned n0 = e.count[0], n01 = n0 + e.count[1], n = n01 + e.count[2];
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int ax = t < n0 ? 0 : (t < n01 ? 1 : 2);
+        const long long c = e.idx[ax][t - (ax == 0 ? 0u : (ax == 1 ? n0 : n01))];
         const double h = axis_h(g, ax);
-        for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-            const long long c = e.idx[ax][t];
-            int i, j, k;
-            node_of(g, c, i, j, k);
-            const AxisLine L = axis_line(g, i, j, k, ax);
-            const double dist = eno2_fore_distance(f, L, h);
-            d.p[2 * ax][c] = (T)dist;
-            d.p[2 * ax + 1][c + L.stride] = (T)(h - dist);
-        }
+        int i, j, k;
+        node_of(g, c, i, j, k);
+        const AxisLine L = axis_line(g, i, j, k, ax);
+        const double dist = eno2_fore_distance(f, L, h);
+        d.p[2 * ax][c] = (T)dist;
+        d.p[2 * ax + 1][c + L.stride] = (T)(h - dist);
     }
 }
 
@@ -685,9 +684,9 @@ cudaError_t launch_set_distance(const T *phi, Ptr6<T> dist, const Grid &g, bool 
     if (err != cudaSuccess) return err;
     k_dist_scan<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, dist, e, g);
     if (quintic)
-        k_dist_roots<T, true><<<list_blocks(), 128, 0, s>>>(phi, dist, e, g);
+        k_dist_roots<T, true><<<list_blocks() * 4, 128, 0, s>>>(phi, dist, e, g);
     else
-        k_dist_roots<T, false><<<list_blocks(), 128, 0, s>>>(phi, dist, e, g);
+        k_dist_roots<T, false><<<list_blocks() * 4, 128, 0, s>>>(phi, dist, e, g);
     return cudaGetLastError();
 }
 
@@ -804,7 +803,7 @@ cudaError_t launch_set_distance_eno2(const T *phi, Ptr6<T> dist, const Grid &g, 
     cudaError_t err = cudaMemsetAsync(e.count, 0, 3 * sizeof(unsigned), s);
     if (err != cudaSuccess) return err;
     k_dist_scan<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, dist, e, g);
-    k_dist_roots_eno2<T><<<list_blocks(), 128, 0, s>>>(phi, dist, e, g);
+    k_dist_roots_eno2<T><<<list_blocks() * 4, 128, 0, s>>>(phi, dist, e, g);
     return cudaGetLastError();
 }
 
