@@ -11,16 +11,19 @@
 // The per-block partial sums of the reduction, which vsl_area_volume_f64 keeps in the
 // caller's workspace, live here in one file-scope __device__ array of
 // VSL_NOALLOC_SCRATCH_BYTES (1 MiB).  Every device that loads this library holds that
-// array until the process exits.  Its device address is looked up once per device, by the
-// first call made while that device is current.  The entry point allocates nothing: no
-// cudaMalloc, no cudaFree, no allocating library routine.
+// array until the process exits.  Host code cannot use the array's name as a device
+// address, so every call looks the address up (cudaGetSymbolAddress, a host-side query)
+// on the device current at the call.  Nothing is cached: after a cudaDeviceReset the
+// module is loaded again and the next call finds the new address.  The first call on a
+// device is the one that loads the module there (lazy loading), so make it before any
+// stream capture.  The entry point allocates nothing: no cudaMalloc, no cudaFree, no
+// allocating library routine.
 //
 // The array is shared by every call on a device and keeps the last call's contents.
 // Nothing in it needs to start at zero: the toolbox launch of a call writes every partial
 // slot that the call's fixed-order sum reads.  Two calls whose launches can overlap on the
 // GPU (unordered streams, or several host threads) race on the array.
 #include <cmath>
-#include <mutex>
 
 #include "vsl_internal.h"
 
@@ -29,22 +32,12 @@ namespace {
 
 static __device__ __align__(256) double noalloc_scratch[VSL_NOALLOC_SCRATCH_BYTES / sizeof(double)];
 
-constexpr int kMaxDevices = 64;
-std::mutex scratch_mutex;
-void *scratch_ptr[kMaxDevices];
-
-// device address of noalloc_scratch on the current device (looked up on first use)
+// device address of noalloc_scratch on the current device
 int scratch_address(double **out)
 {
-    int dev = -1;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return VSL_ERR_CUDA;
-    std::lock_guard<std::mutex> lock(scratch_mutex);
-    if (scratch_ptr[dev] == nullptr) {
-        void *p = nullptr;
-        if (cudaGetSymbolAddress(&p, noalloc_scratch) != cudaSuccess || p == nullptr) return VSL_ERR_CUDA;
-        scratch_ptr[dev] = p;
-    }
-    *out = static_cast<double *>(scratch_ptr[dev]);
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, noalloc_scratch) != cudaSuccess || p == nullptr) return VSL_ERR_CUDA;
+    *out = static_cast<double *>(p);
     return VSL_OK;
 }
 

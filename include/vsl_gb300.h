@@ -273,11 +273,12 @@ int vsl_area_volume_f32(const float *F, double *area_volume, int rows, int cols,
  * is one static device array of VSL_NOALLOC_SCRATCH_BYTES, held by every device that loads
  * the library until the process exits.  Limit: ceil(rows/32) * ceil(cols/8) * pges <=
  * VSL_NOALLOC_SCRATCH_BYTES / 16 = 65536 (every grid up to 256^3); larger grids return
- * VSL_ERR_SCRATCH_LIMIT before anything is launched.  The first call on a device looks up
- * the array's address with that device current (make that first call before any stream
- * capture).  All calls on a device share the array: calls that can overlap on the GPU
- * race, so order them (one stream, or events).  Results are bitwise those of
- * vsl_area_volume_f64. */
+ * VSL_ERR_SCRATCH_LIMIT before anything is launched.  Every call looks up the array's
+ * address on the device current at the call (nothing is cached, so the address stays right
+ * after a cudaDeviceReset); the first call on a device loads the library's device code
+ * there, so make that first call before any stream capture.  All calls on a device share
+ * the array: calls that can overlap on the GPU race, so order them (one stream, or
+ * events).  Results are bitwise those of vsl_area_volume_f64. */
 #define VSL_NOALLOC_SCRATCH_BYTES 1048576
 int vsl_area_volume_noalloc_f64(const double *F, double *area_volume, int rows, int cols, int pges, double dx,
                                 double dy, double dz, vsl_stream_t stream);

@@ -12,7 +12,24 @@ import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE_KERNELS = "/root/reference/src/7_0_paper/2_0_Vesicle/CUDA_Code"
+# The reference checkout is read in place.  VSL_REFERENCE names its root; when it is unset
+# the recipes look at the development container's read-only mount.
+DEFAULT_REFERENCE = "/root/reference"
+VESICLE = os.path.join("src", "7_0_paper", "2_0_Vesicle")
+
+
+def reference_root() -> str:
+    return os.environ.get("VSL_REFERENCE", DEFAULT_REFERENCE)
+
+
+def reference_vesicle() -> str:
+    """The vesicle project inside the reference checkout (the survey's V/)."""
+    return os.path.join(reference_root(), VESICLE)
+
+
+def reference_kernels() -> str:
+    return os.path.join(reference_vesicle(), "CUDA_Code")
+
 
 CFLAGS = ["-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-std=c11", "-Wall"]
 
@@ -32,9 +49,10 @@ def build_port(force: bool = False) -> str:
 
 def build_ref() -> str | None:
     """Compile the reference kernels for the host; None when the checkout is absent."""
-    if not os.path.isdir(REFERENCE_KERNELS):
+    kernels = reference_kernels()
+    if not os.path.isdir(kernels):
         return None
-    subprocess.run(["make", "-s", "-j8", "-C", os.path.join(HERE, "ref"), f"REF={REFERENCE_KERNELS}"], check=True)
+    subprocess.run(["make", "-s", "-j8", "-C", os.path.join(HERE, "ref"), f"REF={kernels}"], check=True)
     return os.path.join(HERE, "_ref", "libvsl_ref.so")
 
 

@@ -23,12 +23,12 @@ sys.path.insert(0, ROOT)
 from oracle import build_oracle  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
-PEAR = "/root/reference/src/7_0_paper/2_0_Vesicle/pear.mat"
+PEAR = os.path.join(build_oracle.reference_vesicle(), "pear.mat")
 
 
 def reference_digest() -> str:
     h = hashlib.sha256()
-    base = build_oracle.REFERENCE_KERNELS
+    base = build_oracle.reference_kernels()
     for sub in sorted(os.listdir(base)):
         d = os.path.join(base, sub)
         for f in sorted(os.listdir(d)):

@@ -19,12 +19,17 @@ fixture is committed.
 from __future__ import annotations
 
 import os
+import sys
 
 import numpy as np
 import scipy.io as sio
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRC = "/root/reference/src/7_0_paper/2_0_Vesicle"
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from oracle import build_oracle  # noqa: E402
+
+SRC = build_oracle.reference_vesicle()
 FIRST = 8
 FIELDS = ("t", "ene", "da", "dv", "P", "ten")
 # file -> (variable suffix, grid edge, CFL number)
