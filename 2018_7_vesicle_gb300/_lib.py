@@ -42,12 +42,25 @@ SIGNATURES = {
     "vsl_tile_pages": "iiii",
     # no-allocation variant (static device scratch, no workspace argument)
     "vsl_area_volume_noalloc_f64": "pp" + _G + "s",
+    # a batch of vesicle steps: host array of VesicleF32, count, ext/reinit pseudo-steps, CFL
+    "vsl_vesicle_step_batch_f32": "piiid" + "s",
 }
+
+
+class VesicleF32(ctypes.Structure):
+    """vsl_vesicle_f32 of the C ABI: one vesicle of vsl_vesicle_step_batch_f32."""
+
+    _fields_ = [("F", ctypes.c_void_p), ("xpr", ctypes.c_void_p), ("xpl", ctypes.c_void_p), ("ypf", ctypes.c_void_p),
+                ("ypb", ctypes.c_void_p), ("zpu", ctypes.c_void_p), ("zpd", ctypes.c_void_p),
+                ("info", ctypes.c_void_p), ("rows", ctypes.c_int), ("cols", ctypes.c_int), ("pges", ctypes.c_int),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
+                ("workspace", ctypes.c_void_p), ("workspace_bytes", ctypes.c_size_t)]
 for _suf in ("f64", "f32"):
     SIGNATURES.update(
         {
             f"vsl_set_distance_{_suf}": "ppppppp" + _G + "pz" + "s",
             f"vsl_weno5_rk3_reinitialization_{_suf}": "pi" + "pppppp" + _G + "pz" + "s",
+            f"vsl_weno5_rk3_reinitialization_tol_{_suf}": "pidd" + "pppppp" + _G + "pp" + "pz" + "s",
             f"vsl_wenork3_reinitialization_{_suf}": "pi" + _G + "pz" + "s",
             f"vsl_weno5_rk3_extend_{_suf}": "pip" + "pppppp" + _G + "pz" + "s",
             f"vsl_wenork3_extend_{_suf}": "pip" + _G + "pz" + "s",
@@ -87,6 +100,7 @@ OP = {
     "relax_step": 16,
     "aux_toolbox": 17,
     "masked_integral": 18,
+    "reinit_tol": 19,
 }
 
 

@@ -1,16 +1,25 @@
 """Many independent vesicles advanced together.
 
-A batch step is one CUDA graph: the graph forks into `streams` parallel branches and each
-vesicle's whole vesicle-step launch sequence (toolbox, extension, time step, advection,
-setDistance, reinitialization) is recorded on one branch, vesicles dealt round-robin.
-Small grids, which cannot fill the GPU alone, then run concurrently, and the host issues
-one graph launch per batch step instead of a few hundred launches per vesicle.  The
-vesicles share nothing: each has its own field, distances and workspace.
+Two batch steps:
+
+* `step_batched` (FP32): vsl_vesicle_step_batch_f32, one persistent launch per RK stage
+  running that stage of every vesicle (a work list of all the vesicles' tiles), with the
+  per-vesicle set-up passes between them; recorded once as a CUDA graph and replayed.  A
+  batch step of 64 vesicles is then ~1,300 launches instead of ~20,000, and the small
+  grids share the GPU inside each launch.
+* `step` (either precision): one CUDA graph that forks into `streams` parallel branches,
+  each vesicle's whole vesicle-step launch sequence recorded on one branch, vesicles dealt
+  round-robin.
+
+The vesicles share nothing: each has its own field, distances and workspace.
 """
 from __future__ import annotations
 
+import ctypes
+
 import torch
 
+from ._lib import VesicleF32, lib
 from .sdf3 import SDF3
 
 
@@ -26,6 +35,47 @@ class VesicleBatch:
         self.infos = [torch.zeros(4, dtype=torch.float64, device="cuda") for _ in self.maps]
         self._tuning = {}
 
+    def _descriptors(self):
+        arr = (VesicleF32 * len(self.maps))()
+        for d, m, info in zip(arr, self.maps, self.infos):
+            ws = m.workspace("vesicle_step")
+            dist = m._dist()
+            d.F = m.F.data_ptr()
+            d.xpr, d.xpl, d.ypf, d.ypb, d.zpu, d.zpd = (t.data_ptr() for t in dist)
+            d.info = info.data_ptr()
+            d.rows, d.cols, d.pges = m.GD3.Size
+            d.dx, d.dy, d.dz = m.GD3.Dx, m.GD3.Dy, m.GD3.Dz
+            d.workspace, d.workspace_bytes = ws.data_ptr(), ws.numel()
+        return arr
+
+    def step_batched(self, ext_iters: int = 30, reinit_iters: int = 20, cfl: float = 0.5, graph: bool = True):
+        """One batch step with each RK stage of all the vesicles as one persistent launch
+        (vsl_vesicle_step_batch_f32; FP32 vesicles only).  graph=True records the step's
+        launches once as a CUDA graph and replays it (re-recorded when the arguments
+        change); bitwise the results of `step_loop`."""
+        if any(m.precision != "f32" for m in self.maps):
+            raise ValueError("step_batched runs the FP32 mixed form")
+        key = (int(ext_iters), int(reinit_iters), float(cfl))
+
+        def launch():
+            arr = self._descriptors()
+            lib().call("vsl_vesicle_step_batch_f32", ctypes.addressof(arr), len(self.maps), *key,
+                       torch.cuda.current_stream().cuda_stream)
+
+        if not graph:
+            launch()
+            return self.infos
+        if getattr(self, "_bkey", None) != key:
+            for m in self.maps:
+                m.workspace("vesicle_step")  # allocated before recording
+            torch.cuda.synchronize()
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                launch()
+            self._bgraph, self._bkey = g, key
+        self._bgraph.replay()
+        return self.infos
+
     def nodes(self) -> int:
         return sum(m.GD3.NumElt for m in self.maps)
 
@@ -37,13 +87,13 @@ class VesicleBatch:
         return self.infos
 
     def autotune(self, candidates=None, steps: int = 2, ext_iters: int = 30, reinit_iters: int = 20,
-                 cfl: float = 0.5) -> dict:
+                 cfl: float = 0.5, mode: str = "graph") -> dict:
         """Pick pages per block of the tiled kernels for the batch's grid shapes by the
-        batch step's own time (graph replay).  Configurations compared: the per-shape
-        choices (each shape timed alone on one of its vesicles), every candidate applied
-        to all shapes, and the default.  Concurrent branches favour other choices than a
-        vesicle timed alone, which is why the whole step decides.  Returns the timings and
-        the configuration kept."""
+        batch step's own time (graph replay of `step`, mode "graph", or of `step_batched`,
+        mode "batched").  Configurations compared: the per-shape choices (each shape timed
+        alone on one of its vesicles), every candidate applied to all shapes, and the
+        default.  Concurrent vesicles favour other choices than a vesicle timed alone, which
+        is why the whole step decides.  Returns the timings and the configuration kept."""
         from . import autotune as T
 
         cand = T.CANDIDATES if candidates is None else candidates
@@ -61,14 +111,17 @@ class VesicleBatch:
                 for k, p in kinds.items():
                     T.set_pages(s, k, p)
 
+        fn = self.step_batched if mode == "batched" else self.step
+
         def batch_ms():
             self._graph, self._key = None, None  # re-record with the current table
-            self.step(ext_iters, reinit_iters, cfl)
+            self._bgraph, self._bkey = None, None
+            fn(ext_iters, reinit_iters, cfl)
             torch.cuda.synchronize()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record()
             for _ in range(steps):
-                self.step(ext_iters, reinit_iters, cfl)
+                fn(ext_iters, reinit_iters, cfl)
             b.record()
             torch.cuda.synchronize()
             return a.elapsed_time(b) / steps
@@ -80,8 +133,9 @@ class VesicleBatch:
         best = min(times, key=times.get)
         apply(configs[best])
         self._graph, self._key = None, None
+        self._bgraph, self._bkey = None, None
         self._tuning = configs
-        return {"shapes": len(shapes), "ms": times, "kept": best.split("_")[0] if best.startswith("uniform") else best,
+        return {"mode": mode, "shapes": len(shapes), "ms": times, "kept": best.split("_")[0] if best.startswith("uniform") else best,
                 "config": best,
                 "pages": {"x".join(map(str, s)): v for s, v in configs[best].items()}}
 
@@ -94,6 +148,7 @@ class VesicleBatch:
             for k, p in kinds.items():
                 T.set_pages(s, k, p)
         self._graph, self._key = None, None
+        self._bgraph, self._bkey = None, None
 
     def step(self, ext_iters: int = 30, reinit_iters: int = 20, cfl: float = 0.5):
         """One batch step by graph replay (recorded on first use or when arguments change)."""

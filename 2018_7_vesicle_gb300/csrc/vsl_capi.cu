@@ -1,7 +1,9 @@
 // vsl_capi.cu -- method-level entry points of the C ABI (include/vsl_gb300.h): argument
 // checks, workspace carving and the launch sequences of the TVD-RK3 loops.  Everything
 // is enqueued on the caller's stream; nothing here allocates or synchronises.
+#include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <type_traits>
 
 #include "vsl_internal.h"
@@ -77,7 +79,9 @@ template <typename T> ReinitWork<T> carve_reinit(Bump &w, const Grid &g, bool ow
 
 template <typename T> struct ExtendWork {
     Ptr3<T> v;
-    Ptr6<T> cp;
+    Ptr6<T> cp;         // FP64 form: crossing values
+    Ptr6<double> cp64;  // FP32 form: FP64 crossing values and the band's shadow fields
+    double *sh[3];
     T *b, *c;
     uint8_t *flags;
     NodeList flagged;  // nodes with a distance flag: crossing values and the band
@@ -89,7 +93,12 @@ template <typename T> ExtendWork<T> carve_extend(Bump &w, const Grid &g, bool ow
 {
     ExtendWork<T> e{};
     for (int q = 0; q < 3; ++q) e.v.p[q] = w.take<T>(g.num);
-    for (int q = 0; q < 6; ++q) e.cp.p[q] = w.take<T>(g.num);
+    if (std::is_same<T, float>::value) {
+        for (int q = 0; q < 6; ++q) e.cp64.p[q] = w.take<double>(g.num);
+        for (int q = 0; q < 3; ++q) e.sh[q] = w.take<double>(g.num);
+    } else {
+        for (int q = 0; q < 6; ++q) e.cp.p[q] = w.take<T>(g.num);
+    }
     e.b = w.take<T>(g.num);
     e.c = w.take<T>(g.num);
     e.flags = w.take<uint8_t>(g.num);
@@ -98,6 +107,22 @@ template <typename T> ExtendWork<T> carve_extend(Bump &w, const Grid &g, bool ow
     e.edges = own_dist ? carve_edges(w, g) : EdgeLists{};
     e.band = carve_band<T>(w, g);
     return e;
+}
+
+// the residual-driven reinitialization: the reinitialization workspace and the residual's
+// two reduction words
+template <typename T> struct TolWork {
+    ReinitWork<T> re;
+    unsigned long long *max_bits;
+    unsigned *ticket;
+};
+template <typename T> TolWork<T> carve_tol(Bump &w, const Grid &g)
+{
+    TolWork<T> t;
+    t.re = carve_reinit<T>(w, g, false);
+    t.max_bits = w.take<unsigned long long>(2);  // the ticket shares the second word
+    t.ticket = t.max_bits ? reinterpret_cast<unsigned *>(t.max_bits + 1) : nullptr;
+    return t;
 }
 
 // zero the band counters before the first tiled stage of an operation
@@ -257,6 +282,7 @@ size_t measure(int op, const Grid &g, int elem)
         case VSL_OP_RELAX_STEP: carve_relax<T>(w, g); break;
         case VSL_OP_AUX_TOOLBOX: carve_aux<T>(w, g); break;
         case VSL_OP_MASKED_INTEGRAL: carve_reduce(w, g, 1); break;
+        case VSL_OP_REINIT_TOL: carve_tol<T>(w, g); break;
         default: return false;
         }
         return true;
@@ -305,11 +331,11 @@ template <typename T> Ptr3<const T> cview3(const Ptr3<T> &p)
 
 // one stage through the tiled FP32 kernels (stage input s_in, RK3 base n_in, output out)
 inline cudaError_t tiled(int kind, bool eno3, Band &band, const float *s_in, const float *n_in, float *out,
-                         const uint8_t *flags, Ptr6<const float> d, Ptr6<const float> cp, Ptr3<const float> v,
+                         const uint8_t *flags, Ptr6<const float> d, BandShadow sh, Ptr3<const float> v,
                          const float *speed, const double *dt, int stage, const Grid &g, cudaStream_t s,
                          NodeList flagged = NodeList{nullptr, nullptr})
 {
-    TiledStage st{s_in, n_in, out, flags, d, cp, v, speed, dt, band.q, flagged, stage, band.seq++};
+    TiledStage st{s_in, n_in, out, flags, d, sh, v, speed, dt, band.q, flagged, stage, band.seq++};
     return launch_tiled_stage(kind, eno3, st, g, s);
 }
 
@@ -320,12 +346,12 @@ int reinit_loop(T *F, int iters, Ptr6<const T> d, ReinitWork<T> &w, const Grid &
     const bool fast = fast_form<T>();
     if constexpr (std::is_same<T, float>::value) {
         if (int st = band_reset(w.band, s)) return st;
-        const Ptr6<const float> none6{};
+        const BandShadow none{};
         const Ptr3<const float> none3{};
         for (int it = 0; it < iters; ++it) {
-            VSL_TRY(tiled(0, eno3, w.band, F, F, w.b, w.flags, d, none6, none3, nullptr, nullptr, 0, g, s));
-            VSL_TRY(tiled(0, eno3, w.band, w.b, F, w.c, w.flags, d, none6, none3, nullptr, nullptr, 1, g, s));
-            VSL_TRY(tiled(0, eno3, w.band, w.c, F, F, w.flags, d, none6, none3, nullptr, nullptr, 2, g, s));
+            VSL_TRY(tiled(0, eno3, w.band, F, F, w.b, w.flags, d, none, none3, nullptr, nullptr, 0, g, s));
+            VSL_TRY(tiled(0, eno3, w.band, w.b, F, w.c, w.flags, d, none, none3, nullptr, nullptr, 1, g, s));
+            VSL_TRY(tiled(0, eno3, w.band, w.c, F, F, w.flags, d, none, none3, nullptr, nullptr, 2, g, s));
         }
         return VSL_OK;
     } else {
@@ -336,6 +362,27 @@ int reinit_loop(T *F, int iters, Ptr6<const T> d, ReinitWork<T> &w, const Grid &
         }
         return VSL_OK;
     }
+}
+
+// one TVD-RK3 reinitialization pseudo-step of F in place, kernel launches only (the FP32
+// band counters must be zero, as band_reset leaves them; the third stage leaves counter 0
+// set and counter 1 zero)
+template <typename T>
+int reinit_pseudo_step(T *F, Ptr6<const T> d, ReinitWork<T> &w, const Grid &g, cudaStream_t s)
+{
+    if constexpr (std::is_same<T, float>::value) {
+        const BandShadow none{};
+        const Ptr3<const float> none3{};
+        w.band.seq = 0;
+        VSL_TRY(tiled(0, false, w.band, F, F, w.b, w.flags, d, none, none3, nullptr, nullptr, 0, g, s));
+        VSL_TRY(tiled(0, false, w.band, w.b, F, w.c, w.flags, d, none, none3, nullptr, nullptr, 1, g, s));
+        VSL_TRY(tiled(0, false, w.band, w.c, F, F, w.flags, d, none, none3, nullptr, nullptr, 2, g, s));
+    } else {
+        VSL_TRY(launch_reinit_stage<T>(F, F, w.b, w.flags, d, g, 0, false, false, s));
+        VSL_TRY(launch_reinit_stage<T>(w.b, F, w.c, w.flags, d, g, 1, false, false, s));
+        VSL_TRY(launch_reinit_stage<T>(w.c, F, F, w.flags, d, g, 2, false, false, s));
+    }
+    return VSL_OK;
 }
 
 // velocity and node classes of an extension off the zero set of F (distances d)
@@ -353,18 +400,25 @@ template <typename T>
 int extend_loop(T *C, int iters, Ptr6<const T> d, ExtendWork<T> &w, const Grid &g, bool eno3, cudaStream_t s)
 {
     const bool fast = fast_form<T>();
-    VSL_TRY(launch_crossing<T>(C, d, w.cp, w.flagged, g, eno3, s));
-    Ptr6<const T> cp = cview(w.cp);
     Ptr3<const T> v = cview3(w.v);
     if constexpr (std::is_same<T, float>::value) {
+        // FP64 crossing values and the band's FP64 shadow of C (BandShadow)
+        VSL_TRY(launch_crossing_mixed(C, d, w.cp64, w.flagged, g, eno3, s));
+        VSL_TRY(launch_shadow_init(C, w.sh[0], w.flagged, s));
+        const Ptr6<const double> cp = cview(w.cp64);
         if (int st = band_reset(w.band, s)) return st;
         for (int it = 0; it < iters; ++it) {
-            VSL_TRY(tiled(1, eno3, w.band, C, C, w.b, w.flags, d, cp, v, nullptr, nullptr, 0, g, s, w.flagged));
-            VSL_TRY(tiled(1, eno3, w.band, w.b, C, w.c, w.flags, d, cp, v, nullptr, nullptr, 1, g, s, w.flagged));
-            VSL_TRY(tiled(1, eno3, w.band, w.c, C, C, w.flags, d, cp, v, nullptr, nullptr, 2, g, s, w.flagged));
+            VSL_TRY(tiled(1, eno3, w.band, C, C, w.b, w.flags, d, BandShadow{w.sh[0], w.sh[0], w.sh[1], cp}, v,
+                          nullptr, nullptr, 0, g, s, w.flagged));
+            VSL_TRY(tiled(1, eno3, w.band, w.b, C, w.c, w.flags, d, BandShadow{w.sh[1], w.sh[0], w.sh[2], cp}, v,
+                          nullptr, nullptr, 1, g, s, w.flagged));
+            VSL_TRY(tiled(1, eno3, w.band, w.c, C, C, w.flags, d, BandShadow{w.sh[2], w.sh[0], w.sh[0], cp}, v,
+                          nullptr, nullptr, 2, g, s, w.flagged));
         }
         return VSL_OK;
     } else {
+        VSL_TRY(launch_crossing<T>(C, d, w.cp, w.flagged, g, eno3, s));
+        Ptr6<const T> cp = cview(w.cp);
         for (int it = 0; it < iters; ++it) {
             VSL_TRY(launch_extend_stage<T>(C, C, w.b, w.flags, d, cp, v, g, 0, eno3, fast, s));
             VSL_TRY(launch_extend_stage<T>(w.b, C, w.c, w.flags, d, cp, v, g, 1, eno3, fast, s));
@@ -382,9 +436,9 @@ int advect_loop(T *F, Ptr3<const T> v, const T *speed, const double *dt, int ste
     if constexpr (std::is_same<T, float>::value) {
         const Ptr6<const float> none6{};
         for (int it = 0; it < steps; ++it) {
-            VSL_TRY(tiled(2, false, w.band, F, F, w.b, nullptr, none6, none6, v, speed, dt, 0, g, s));
-            VSL_TRY(tiled(2, false, w.band, w.b, F, w.c, nullptr, none6, none6, v, speed, dt, 1, g, s));
-            VSL_TRY(tiled(2, false, w.band, w.c, F, F, nullptr, none6, none6, v, speed, dt, 2, g, s));
+            VSL_TRY(tiled(2, false, w.band, F, F, w.b, nullptr, none6, BandShadow{}, v, speed, dt, 0, g, s));
+            VSL_TRY(tiled(2, false, w.band, w.b, F, w.c, nullptr, none6, BandShadow{}, v, speed, dt, 1, g, s));
+            VSL_TRY(tiled(2, false, w.band, w.c, F, F, nullptr, none6, BandShadow{}, v, speed, dt, 2, g, s));
         }
         return VSL_OK;
     } else {
@@ -512,7 +566,7 @@ int op_redistance(T *A, int iter1, int iter2, const T *F, int rows, int cols, in
     // one reinitialization stage of A's pseudo-time loop (tiled kernels for FP32)
     auto re_stage = [&](const T *in, T *out, int stage) -> cudaError_t {
         if constexpr (std::is_same<T, float>::value)
-            return tiled(0, false, w.re.band, in, A, out, w.re.flags, dA, Ptr6<const float>{}, Ptr3<const float>{},
+            return tiled(0, false, w.re.band, in, A, out, w.re.flags, dA, BandShadow{}, Ptr3<const float>{},
                          nullptr, nullptr, stage, g, s);
         else
             return launch_reinit_stage<T>(in, A, out, w.re.flags, dA, g, stage, false, fast, s);
@@ -656,6 +710,267 @@ int op_vesicle_step(T *F, T *xpr, T *xpl, T *ypf, T *ypb, T *zpu, T *zpd, int ex
 }
 
 // ---------------------------------------------------------------------------------------
+// residual-driven reinitialization (no counterpart in the reference, whose loop runs a
+// fixed count, WENO5RK3Reinitialization.m:15).  One CUDA graph: a prelude (classification,
+// the residual of the input) and a conditional WHILE node whose body is one pseudo-step
+// followed by the residual, which sets the loop condition on the device.  The host neither
+// waits nor reads anything back.
+// ---------------------------------------------------------------------------------------
+// two internal streams per device to record the graph on: one for the prelude (when the
+// caller's stream is not being captured itself) and one for the loop body.  Created on first
+// use with this thread's capture mode relaxed, so that a first use inside the caller's own
+// capture is legal; the mutex also serialises the recordings.
+struct CaptureLanes {
+    int device;
+    cudaStream_t main, body;
+};
+constexpr int MAX_CAPTURE_DEVICES = 64;
+std::mutex capture_mutex;
+CaptureLanes capture_lanes[MAX_CAPTURE_DEVICES];
+int n_capture_lanes = 0;
+
+CaptureLanes *capture_lanes_for_current_device()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    for (int e = 0; e < n_capture_lanes; ++e)
+        if (capture_lanes[e].device == dev) return &capture_lanes[e];
+    if (n_capture_lanes == MAX_CAPTURE_DEVICES) return nullptr;
+    CaptureLanes ln{dev, nullptr, nullptr};
+    cudaStreamCaptureMode mode = cudaStreamCaptureModeRelaxed;
+    if (cudaThreadExchangeStreamCaptureMode(&mode) != cudaSuccess) return nullptr;
+    bool ok = cudaStreamCreateWithFlags(&ln.main, cudaStreamNonBlocking) == cudaSuccess;
+    ok = ok && cudaStreamCreateWithFlags(&ln.body, cudaStreamNonBlocking) == cudaSuccess;
+    cudaThreadExchangeStreamCaptureMode(&mode);
+    if (!ok) {
+        if (ln.body) cudaStreamDestroy(ln.body);
+        if (ln.main) cudaStreamDestroy(ln.main);
+        return nullptr;
+    }
+    capture_lanes[n_capture_lanes] = ln;
+    return &capture_lanes[n_capture_lanes++];
+}
+
+// Records the prelude and the WHILE node on `cap` (the caller's capturing stream, or an
+// internal stream capturing into a fresh graph).
+template <typename T>
+int record_reinit_tol(T *F, int max_iters, double tol, double band, Ptr6<const T> d, TolWork<T> &w, const Grid &g,
+                      int *status, double *history, cudaStream_t cap, cudaStream_t body_stream)
+{
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t graph = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    const cudaGraphEdgeData *edges = nullptr;
+    size_t ndeps = 0;
+    VSL_TRY(cudaStreamGetCaptureInfo(cap, &cs, nullptr, &graph, &deps, &edges, &ndeps));
+    if (cs != cudaStreamCaptureStatusActive || graph == nullptr) return VSL_ERR_CUDA;
+    cudaGraphConditionalHandle handle;
+    VSL_TRY(cudaGraphConditionalHandleCreate(&handle, graph, 0, cudaGraphCondAssignDefault));
+    // the FP32 band counter that the body's last stage leaves set (zeroed by the residual)
+    unsigned *left_set = std::is_same<T, float>::value ? w.re.band.q.counter : nullptr;
+    ResidualState rs{w.max_bits, w.ticket, status, history, left_set, tol, max_iters, 0, 1, handle};
+    // prelude: counters, the classification (mask = F < 0 on entry), the input's residual
+    VSL_TRY(cudaMemsetAsync(status, 0, 2 * sizeof(int), cap));
+    VSL_TRY(cudaMemsetAsync(w.max_bits, 0, 2 * sizeof(unsigned long long), cap));
+    if (int st = band_reset(w.re.band, cap)) return st;
+    VSL_TRY(launch_classify<T>(F, d, w.re.flags, NodeList{nullptr, nullptr}, g, cap));
+    VSL_TRY(launch_reinit_residual<T>(F, w.re.flags, d, g, band, rs, cap));
+    // the WHILE node after the prelude
+    VSL_TRY(cudaStreamGetCaptureInfo(cap, &cs, nullptr, &graph, &deps, &edges, &ndeps));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    VSL_TRY(cudaGraphAddNode(&node, graph, deps, edges, ndeps, &cp));
+    VSL_TRY(cudaStreamUpdateCaptureDependencies(cap, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    // body (kernel nodes only): condition to 0 first (only a completed residual evaluation
+    // continues the loop), one pseudo-step, the residual (counts the step, records it, sets
+    // the condition, zeroes the band counter the next pseudo-step's first stage appends to)
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    VSL_TRY(cudaStreamBeginCaptureToGraph(body_stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    int st = launch_condition_reset(handle, body_stream) == cudaSuccess ? VSL_OK : VSL_ERR_CUDA;
+    if (st == VSL_OK) st = reinit_pseudo_step<T>(F, d, w.re, g, body_stream);
+    rs.advance = 1;
+    if (st == VSL_OK && launch_reinit_residual<T>(F, w.re.flags, d, g, band, rs, body_stream) != cudaSuccess)
+        st = VSL_ERR_CUDA;
+    cudaGraph_t out = nullptr;
+    if (cudaStreamEndCapture(body_stream, &out) != cudaSuccess && st == VSL_OK) st = VSL_ERR_CUDA;
+    return st;
+}
+
+template <typename T>
+int op_reinit_tol(T *F, int max_iters, double tol, double band, const T *xpr, const T *xpl, const T *ypf,
+                  const T *ypb, const T *zpu, const T *zpd, int rows, int cols, int pges, double dx, double dy,
+                  double dz, int *status, double *history, void *ws, size_t bytes, cudaStream_t s)
+{
+    if (any_null(F, xpr, xpl, ypf, ypb, zpu, zpd, status)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    if (max_iters < 0 || !(tol >= 0) || !(band > 0)) return VSL_ERR_VALUE;
+    Grid g = make_grid(rows, cols, pges, dx, dy, dz);
+    if (int st = check_ws(VSL_OP_REINIT_TOL, g, sizeof(T), ws, bytes)) return st;
+    Bump b(ws);
+    TolWork<T> w = carve_tol<T>(b, g);
+    Ptr6<const T> d = six(xpr, xpl, ypf, ypb, zpu, zpd);
+    cudaStreamCaptureStatus cs;
+    VSL_TRY(cudaStreamIsCapturing(s, &cs));
+    std::lock_guard<std::mutex> lock(capture_mutex);
+    CaptureLanes *ln = capture_lanes_for_current_device();
+    if (ln == nullptr) return VSL_ERR_CUDA;
+    if (cs == cudaStreamCaptureStatusActive)  // inside the caller's capture: add to its graph
+        return record_reinit_tol<T>(F, max_iters, tol, band, d, w, g, status, history, s, ln->body);
+    if (cs != cudaStreamCaptureStatusNone) return VSL_ERR_CUDA;
+    // record a graph of its own, launch it on the caller's stream and release it (an
+    // executable graph destroyed while in flight is freed once its launch completes)
+    VSL_TRY(cudaStreamBeginCapture(ln->main, cudaStreamCaptureModeThreadLocal));
+    int st = record_reinit_tol<T>(F, max_iters, tol, band, d, w, g, status, history, ln->main, ln->body);
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamEndCapture(ln->main, &graph) != cudaSuccess && st == VSL_OK) st = VSL_ERR_CUDA;
+    cudaGraphExec_t exec = nullptr;
+    if (st == VSL_OK && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) st = VSL_ERR_CUDA;
+    if (st == VSL_OK && cudaGraphLaunch(exec, s) != cudaSuccess) st = VSL_ERR_CUDA;
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    return st;
+}
+
+// ---------------------------------------------------------------------------------------
+// a batch of vesicle steps (FP32): the composite step of op_vesicle_step for every vesicle,
+// with each RK stage of all the vesicles as one persistent launch (launch_tiled_batch); the
+// per-vesicle set-up passes (toolbox, extension velocity and crossing values, time step,
+// setDistance, classification) stay per vesicle.  Vesicles are taken TILED_BATCH_MAX at a
+// time.
+// ---------------------------------------------------------------------------------------
+struct BatchMember {
+    Grid g;
+    float *F;
+    Ptr6<float> dist;
+    double *info;
+    StepWork<float> w;
+    ReinitWork<float> adv, re;  // the advection and reinitialization views of w.ext
+};
+
+int check_vesicle(const vsl_vesicle_f32 &v)
+{
+    if (any_null(v.F, v.xpr, v.xpl, v.ypf, v.ypb, v.zpu, v.zpd, v.info)) return VSL_ERR_NULL;
+    if (int st = check_grid(v.rows, v.cols, v.pges, v.dx, v.dy, v.dz)) return st;
+    const Grid g = make_grid(v.rows, v.cols, v.pges, v.dx, v.dy, v.dz);
+    return check_ws(VSL_OP_VESICLE_STEP, g, sizeof(float), v.workspace, v.workspace_bytes);
+}
+
+int batch_chunk(const vsl_vesicle_f32 *ves, int n, int ext_iters, int reinit_iters, double cfl, cudaStream_t s)
+{
+    BatchMember m[TILED_BATCH_MAX];
+    TiledStage st[TILED_BATCH_MAX];
+    Grid grids[TILED_BATCH_MAX];
+    for (int v = 0; v < n; ++v) {
+        const vsl_vesicle_f32 &d = ves[v];
+        BatchMember &b = m[v];
+        b.g = grids[v] = make_grid(d.rows, d.cols, d.pges, d.dx, d.dy, d.dz);
+        b.F = d.F;
+        b.dist = Ptr6<float>{{d.xpr, d.xpl, d.ypf, d.ypb, d.zpu, d.zpd}};
+        b.info = d.info;
+        Bump bump(d.workspace);
+        b.w = carve_step<float>(bump, b.g);
+        b.adv = ReinitWork<float>{};
+        b.adv.b = b.w.ext.b;
+        b.adv.c = b.w.ext.c;
+        b.adv.band = b.w.ext.band;
+        b.re = b.adv;
+        b.re.flags = b.w.ext.flags;
+    }
+    // per vesicle: toolbox (mean curvature, normals, area, volume), the extension's
+    // velocity, classification and crossing values of the mean curvature, its shadow
+    for (int v = 0; v < n; ++v) {
+        BatchMember &b = m[v];
+        const double ds = (b.g.dx + b.g.dy + b.g.dz) / 3;
+        ToolboxOut<float> tb{};
+        tb.f[4] = b.w.nrm.p[0];
+        tb.f[5] = b.w.nrm.p[1];
+        tb.f[6] = b.w.nrm.p[2];
+        tb.f[14] = b.w.vn;
+        int nb = 0;
+        VSL_TRY(launch_toolbox<float>(b.F, tb, b.g, ds, b.w.red.partials, &nb, s));
+        VSL_TRY(launch_sum_partials(b.w.red.partials, nb, 2, std::pow(ds, 3), b.info, s));
+        const Ptr6<const float> d = cview(b.dist);
+        if (int r = extend_setup<float>(b.F, d, b.w.ext, b.g, false, 1e-6, s)) return r;
+        VSL_TRY(launch_crossing_mixed(b.w.vn, d, b.w.ext.cp64, b.w.ext.flagged, b.g, false, s));
+        VSL_TRY(launch_shadow_init(b.w.vn, b.w.ext.sh[0], b.w.ext.flagged, s));
+        if (int r = band_reset(b.w.ext.band, s)) return r;
+    }
+    // extension of the normal speed: each stage of all vesicles as one launch
+    for (int it = 0; it < ext_iters; ++it) {
+        for (int stage = 0; stage < 3; ++stage) {
+            for (int v = 0; v < n; ++v) {
+                BatchMember &b = m[v];
+                ExtendWork<float> &e = b.w.ext;
+                float *in = stage == 0 ? b.w.vn : (stage == 1 ? e.b : e.c);
+                float *out = stage == 0 ? e.b : (stage == 1 ? e.c : b.w.vn);
+                double *s_in = e.sh[stage], *s_out = e.sh[stage == 2 ? 0 : stage + 1];
+                st[v] = TiledStage{in, b.w.vn, out, e.flags, cview(b.dist),
+                                   BandShadow{s_in, e.sh[0], s_out, cview(e.cp64)}, cview3(e.v), nullptr, nullptr,
+                                   e.band.q, e.flagged, stage, e.band.seq++};
+            }
+            VSL_TRY(launch_tiled_batch(1, false, st, grids, n, s));
+        }
+    }
+    // per vesicle: dt = cfl * Ds / max |Vn| over |F| < 2 Ds
+    for (int v = 0; v < n; ++v) {
+        BatchMember &b = m[v];
+        const double ds = (b.g.dx + b.g.dy + b.g.dz) / 3;
+        int nb = 0;
+        VSL_TRY(launch_band_maxabs<float>(b.w.vn, b.F, 2 * ds, b.g, b.w.red.partials, &nb, s));
+        VSL_TRY(launch_time_step(b.w.red.partials, nb, cfl * ds, b.info + 2, b.info + 3, s));
+    }
+    // one WENO5 TVD-RK3 advection step along Vn * N
+    for (int stage = 0; stage < 3; ++stage) {
+        for (int v = 0; v < n; ++v) {
+            BatchMember &b = m[v];
+            float *in = stage == 0 ? b.F : (stage == 1 ? b.adv.b : b.adv.c);
+            float *out = stage == 0 ? b.adv.b : (stage == 1 ? b.adv.c : b.F);
+            st[v] = TiledStage{in, b.F, out, nullptr, Ptr6<const float>{}, BandShadow{}, cview3(b.w.nrm), b.w.vn,
+                               b.info + 2, b.adv.band.q, NodeList{nullptr, nullptr}, stage, b.adv.band.seq++};
+        }
+        VSL_TRY(launch_tiled_batch(2, false, st, grids, n, s));
+    }
+    // per vesicle: setDistance and the classification of the reinitialization
+    for (int v = 0; v < n; ++v) {
+        BatchMember &b = m[v];
+        VSL_TRY(launch_set_distance<float>(b.F, b.dist, b.g, true, b.w.edges, s));
+        VSL_TRY(launch_classify<float>(b.F, cview(b.dist), b.re.flags, NodeList{nullptr, nullptr}, b.g, s));
+        if (int r = band_reset(b.re.band, s)) return r;
+    }
+    for (int it = 0; it < reinit_iters; ++it) {
+        for (int stage = 0; stage < 3; ++stage) {
+            for (int v = 0; v < n; ++v) {
+                BatchMember &b = m[v];
+                float *in = stage == 0 ? b.F : (stage == 1 ? b.re.b : b.re.c);
+                float *out = stage == 0 ? b.re.b : (stage == 1 ? b.re.c : b.F);
+                st[v] = TiledStage{in, b.F, out, b.re.flags, cview(b.dist), BandShadow{}, Ptr3<const float>{},
+                                   nullptr, nullptr, b.re.band.q, NodeList{nullptr, nullptr}, stage,
+                                   b.re.band.seq++};
+            }
+            VSL_TRY(launch_tiled_batch(0, false, st, grids, n, s));
+        }
+    }
+    return VSL_OK;
+}
+
+int op_vesicle_step_batch(const vsl_vesicle_f32 *ves, int count, int ext_iters, int reinit_iters, double cfl,
+                          cudaStream_t s)
+{
+    if (ves == nullptr && count > 0) return VSL_ERR_NULL;
+    if (count < 0 || ext_iters < 0 || reinit_iters < 0 || !(cfl > 0)) return VSL_ERR_VALUE;
+    for (int v = 0; v < count; ++v)
+        if (int st = check_vesicle(ves[v])) return st;
+    for (int v0 = 0; v0 < count; v0 += TILED_BATCH_MAX)
+        if (int st = batch_chunk(ves + v0, std::min(TILED_BATCH_MAX, count - v0), ext_iters, reinit_iters, cfl, s))
+            return st;
+    return VSL_OK;
+}
+
+// ---------------------------------------------------------------------------------------
 // ENORK2 (ENORK2Reinitialization.m:3-45, ENORK2Extend.m:9-81)
 // ---------------------------------------------------------------------------------------
 
@@ -669,7 +984,7 @@ int enork2_reinit_stage(const T *in, const T *n_in, T *out, ReinitWork<T> &w, Pt
                         int stage, cudaStream_t s)
 {
     if constexpr (std::is_same<T, float>::value) {
-        VSL_TRY(tiled(4, false, w.band, in, n_in, out, w.flags, d, Ptr6<const float>{}, Ptr3<const float>{}, nullptr,
+        VSL_TRY(tiled(4, false, w.band, in, n_in, out, w.flags, d, BandShadow{}, Ptr3<const float>{}, nullptr,
                       nullptr, stage, g, s, band_list(w)));
         return VSL_OK;
     } else {
@@ -703,17 +1018,23 @@ int op_reinit_enork2(T *F, int iteration, int rows, int cols, int pges, double d
 template <typename T>
 int enork2_extend_loop(T *C, int iters, Ptr6<const T> d, ExtendWork<T> &w, const Grid &g, cudaStream_t s)
 {
-    VSL_TRY(launch_enork2_crossing<T>(C, d, w.cp, w.flagged, g, s));
-    const Ptr6<const T> cp = cview(w.cp);
     const Ptr3<const T> v = cview3(w.v);
     if constexpr (std::is_same<T, float>::value) {
-        // tiled uniform nodes, the flagged list on the per-node code beside them
+        // tiled uniform nodes, the flagged list on the per-node code beside them with the FP64
+        // crossing values and shadow of C
+        VSL_TRY(launch_enork2_crossing_mixed(C, d, w.cp64, w.flagged, g, s));
+        VSL_TRY(launch_shadow_init(C, w.sh[0], w.flagged, s));
+        const Ptr6<const double> cp = cview(w.cp64);
         for (int it = 0; it < iters; ++it) {
-            VSL_TRY(tiled(3, false, w.band, C, C, w.b, w.flags, d, cp, v, nullptr, nullptr, 0, g, s, w.flagged));
-            VSL_TRY(tiled(3, false, w.band, w.b, C, C, w.flags, d, cp, v, nullptr, nullptr, 1, g, s, w.flagged));
+            VSL_TRY(tiled(3, false, w.band, C, C, w.b, w.flags, d, BandShadow{w.sh[0], w.sh[0], w.sh[1], cp}, v,
+                          nullptr, nullptr, 0, g, s, w.flagged));
+            VSL_TRY(tiled(3, false, w.band, w.b, C, C, w.flags, d, BandShadow{w.sh[1], w.sh[0], w.sh[0], cp}, v,
+                          nullptr, nullptr, 1, g, s, w.flagged));
         }
         return VSL_OK;
     } else {
+        VSL_TRY(launch_enork2_crossing<T>(C, d, w.cp, w.flagged, g, s));
+        const Ptr6<const T> cp = cview(w.cp);
         for (int it = 0; it < iters; ++it) {
             VSL_TRY(launch_enork2_extend_stage<T>(C, C, w.b, w.flags, d, cp, v, g, 0, s));
             VSL_TRY(launch_enork2_extend_stage<T>(w.b, C, C, w.flags, d, cp, v, g, 1, s));
@@ -908,8 +1229,8 @@ int advect_stages(const T *F, Ptr3<const T> v, const double *dt, ReinitWork<T> &
 {
     if constexpr (std::is_same<T, float>::value) {
         const Ptr6<const float> none6{};
-        VSL_TRY(tiled(2, false, w.band, F, F, w.b, nullptr, none6, none6, v, nullptr, dt, 0, g, s));
-        VSL_TRY(tiled(2, false, w.band, w.b, F, w.c, nullptr, none6, none6, v, nullptr, dt, 1, g, s));
+        VSL_TRY(tiled(2, false, w.band, F, F, w.b, nullptr, none6, BandShadow{}, v, nullptr, dt, 0, g, s));
+        VSL_TRY(tiled(2, false, w.band, w.b, F, w.c, nullptr, none6, BandShadow{}, v, nullptr, dt, 1, g, s));
     } else {
         VSL_TRY(launch_advect_stage<T>(F, F, w.b, v, nullptr, dt, g, 0, false, s));
         VSL_TRY(launch_advect_stage<T>(w.b, F, w.c, v, nullptr, dt, g, 1, false, s));
@@ -925,8 +1246,8 @@ int reinit_stages(const T *F, Ptr6<const T> d, ReinitWork<T> &w, const Grid &g, 
         if (int st = band_reset(w.band, s)) return st;
         const Ptr6<const float> none6{};
         const Ptr3<const float> none3{};
-        VSL_TRY(tiled(0, false, w.band, F, F, w.b, w.flags, d, none6, none3, nullptr, nullptr, 0, g, s));
-        VSL_TRY(tiled(0, false, w.band, w.b, F, w.c, w.flags, d, none6, none3, nullptr, nullptr, 1, g, s));
+        VSL_TRY(tiled(0, false, w.band, F, F, w.b, w.flags, d, BandShadow{}, none3, nullptr, nullptr, 0, g, s));
+        VSL_TRY(tiled(0, false, w.band, w.b, F, w.c, w.flags, d, BandShadow{}, none3, nullptr, nullptr, 1, g, s));
     } else {
         VSL_TRY(launch_reinit_stage<T>(F, F, w.b, w.flags, d, g, 0, false, false, s));
         VSL_TRY(launch_reinit_stage<T>(w.b, F, w.c, w.flags, d, g, 1, false, false, s));
@@ -1001,6 +1322,12 @@ using namespace vsl;
 
 extern "C" {
 
+int vsl_vesicle_step_batch_f32(const vsl_vesicle_f32 *vesicles, int count, int ext_iters, int reinit_iters,
+                               double cfl, vsl_stream_t stream)
+{
+    return op_vesicle_step_batch(vesicles, count, ext_iters, reinit_iters, cfl, reinterpret_cast<cudaStream_t>(stream));
+}
+
 const char *vsl_status_string(int status)
 {
     switch (status) {
@@ -1051,6 +1378,15 @@ size_t vsl_workspace_bytes(int op, int rows, int cols, int pges, int elem_bytes)
     {                                                                                                              \
         return op_reinit_weno5<T>(F, iteration, xpr, xpl, ypf, ypb, zpu, zpd, rows, cols, pges, dx, dy, dz, ws,    \
                                   bytes, stream);                                                                  \
+    }                                                                                                              \
+    int vsl_weno5_rk3_reinitialization_tol_##SUF(T *F, int max_iters, double tol, double band, const T *xpr,       \
+                                                 const T *xpl, const T *ypf, const T *ypb, const T *zpu,           \
+                                                 const T *zpd, int rows, int cols, int pges, double dx, double dy, \
+                                                 double dz, int *status, double *residual, void *ws, size_t bytes, \
+                                                 vsl_stream_t stream)                                              \
+    {                                                                                                              \
+        return op_reinit_tol<T>(F, max_iters, tol, band, xpr, xpl, ypf, ypb, zpu, zpd, rows, cols, pges, dx, dy,   \
+                                dz, status, residual, ws, bytes, stream);                                          \
     }                                                                                                              \
     int vsl_wenork3_reinitialization_##SUF(T *F, int iteration, int rows, int cols, int pges, double dx,           \
                                            double dy, double dz, void *ws, size_t bytes, vsl_stream_t stream)      \

@@ -557,6 +557,153 @@ __device__ __forceinline__ void interface_pair(const T p[7], T r1, T l1, T h, T 
         weno_nonuniform_pair(xs, hs, d_fore, d_back);
 }
 
+// ---------------------------------------------------------------------------------------
+// The interface-aware pair of the mixed (FP32) form, written on the gaps between the seven
+// stencil points rather than on their positions.
+//
+// With the interface at r1 close to h, the position form takes the short gap between the
+// interface and the next node as h - r1 in FP32, where r1 is the FP32 rounding of the FP64
+// root: a gap of 4e-5 h keeps only about three significant digits, and the one-sided
+// divided difference across it (and the WENO weights built on it) inherit that error -- a
+// 1e-3 dx error in one pseudo-step at such nodes of a 256^3 grid.  The neighbour beyond the
+// crossing stores that same gap as its own distance (h - dist, rounded once from the FP64
+// root), so the gap form takes it from there: rc = h - r1 and lc = h - l1 to FP32 relative
+// precision.  Every difference of two stencil points is then a sum of positive gaps (no
+// cancellation).  Same formulas as the position form (the differences are the same
+// quantities), different rounding.
+// ---------------------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void insert_interface_gaps(const T p[7], T r1, T rc, T l1, T lc, T h, T hf, T hb, T G[6],
+                                                      T hs[7])
+{
+    hs[3] = p[3];
+    if (r1 < h) {
+        G[3] = r1; G[4] = rc; G[5] = h;
+        hs[4] = hf; hs[5] = p[4]; hs[6] = p[5];
+    } else {
+        G[3] = h; G[4] = h; G[5] = h;
+        hs[4] = p[4]; hs[5] = p[5]; hs[6] = p[6];
+    }
+    if (l1 < h) {
+        G[2] = l1; G[1] = lc; G[0] = h;
+        hs[2] = hb; hs[1] = p[2]; hs[0] = p[1];
+    } else {
+        G[2] = h; G[1] = h; G[0] = h;
+        hs[2] = p[2]; hs[1] = p[1]; hs[0] = p[0];
+    }
+}
+
+// differences e[b] - e[a] of six faces from the five gaps between consecutive faces
+template <typename T> struct FaceSpan {
+    T d01, d12, d23, d34, d45, d02, d13, d24, d35, d03, d14, d25, d04, d15, d05;
+    __device__ __forceinline__ explicit FaceSpan(const T g[5])
+    {
+        d01 = g[0]; d12 = g[1]; d23 = g[2]; d34 = g[3]; d45 = g[4];
+        d02 = d01 + d12; d13 = d12 + d23; d24 = d23 + d34; d35 = d34 + d45;
+        d03 = d02 + d23; d14 = d13 + d34; d25 = d24 + d45;
+        d04 = d03 + d34; d15 = d14 + d45; d05 = d04 + d45;
+    }
+};
+
+// nu_smoothness on face spans (faces xm25, xm15, xm05, x05, x15, x25 = e[0..5])
+template <typename T> __device__ __forceinline__ void nu_smoothness_gaps(const FaceSpan<T> &D, const T u[5], T s[3])
+{
+    const T um2 = u[0], um1 = u[1], u0 = u[2], u1 = u[3], u2 = u[4];
+    const T w = D.d23;
+    s[0] = T(4.0) * sqr(w / D.d25) *
+           (sqr((u2 - u1) / D.d35) * (T(10.0) * sqr(w) + D.d24 * D.d34) +
+            (u2 - u1) * (u0 - u1) / (D.d35 * D.d24) *
+                (T(20.0) * sqr(w) + T(2.0) * D.d24 * D.d34 + D.d25 * (D.d34 + D.d24)) +
+            sqr((u0 - u1) / D.d24) * (T(10.0) * sqr(w) + (D.d25 + D.d24) * (D.d35 + D.d24)));
+    s[1] = T(4.0) * sqr(w / D.d14) *
+           (sqr((um1 - u0) / D.d13) * (T(10.0) * sqr(w) + D.d24 * D.d34) +
+            (u1 - u0) * (um1 - u0) / (D.d24 * D.d13) * (T(20.0) * sqr(w) - D.d34 * D.d12 - D.d24 * D.d13) +
+            sqr((u1 - u0) / D.d24) * (T(10.0) * sqr(w) + D.d12 * D.d13));
+    s[2] = T(4.0) * sqr(w / D.d03) *
+           (sqr((um2 - um1) / D.d02) * (T(10.0) * sqr(w) + D.d13 * D.d12) +
+            (u0 - um1) * (um2 - um1) / (D.d13 * D.d02) *
+                (T(20.0) * sqr(w) + T(2.0) * D.d13 * D.d12 + D.d03 * (D.d13 + D.d12)) +
+            sqr((u0 - um1) / D.d13) * (T(10.0) * sqr(w) + (D.d03 + D.d13) * (D.d13 + D.d02)));
+}
+
+// weno_nonuniform_pair on the gaps G[m] = xs[m+1] - xs[m] and the divided differences
+// dd[m] = (hs[m+1] - hs[m]) / G[m]
+template <typename T>
+__device__ __noinline__ void weno_nonuniform_pair_dd(const T G[6], const T dd[6], T &d_fore, T &d_back)
+{
+    T u[5], v[3], c[3], s[3];
+    {  // forward bias: faces xs[1..6], cells dd[1..5]
+        const FaceSpan<T> D(G + 1);
+#pragma unroll
+        for (int m = 0; m < 5; ++m) u[m] = dd[m + 1];
+        const T um2 = u[0], um1 = u[1], u0 = u[2], u1 = u[3], u2 = u[4];
+        v[0] = u1 + (u0 - u1) * (T(1.0) + D.d23 / D.d24 + D.d23 / D.d25) + (u2 - u1) * (D.d23 / D.d25) * (D.d24 / D.d35);
+        v[1] = u0 + (um1 - u0) * (D.d23 / D.d14) * (D.d24 / D.d13) - (u1 - u0) * (D.d23 / D.d14) * (D.d12 / D.d24);
+        v[2] = um1 + (u0 - um1) * (D.d12 / D.d03) * (D.d02 / D.d13) - (um2 - um1) * (D.d12 / D.d03) * (D.d23 / D.d02);
+        c[0] = (D.d12 / D.d05) * (D.d02 / D.d15);
+        c[1] = (D.d02 / D.d05) * (D.d25 / D.d15) * (T(1.0) + D.d15 / D.d04);
+        c[2] = (D.d24 / D.d05) * (D.d25 / D.d04);
+        nu_smoothness_gaps(D, u, s);
+        d_fore = nu_combine(v, c, s);
+    }
+    {  // backward bias: faces xs[0..5], cells dd[0..4]
+        const FaceSpan<T> D(G);
+#pragma unroll
+        for (int m = 0; m < 5; ++m) u[m] = dd[m];
+        const T um2 = u[0], um1 = u[1], u0 = u[2], u1 = u[3], u2 = u[4];
+        v[0] = u1 + (u0 - u1) * (D.d34 / D.d25) * (D.d35 / D.d24) - (u2 - u1) * (D.d34 / D.d25) * (D.d23 / D.d35);
+        v[1] = u0 + (u1 - u0) * (D.d23 / D.d14) * (D.d13 / D.d24) - (um1 - u0) * (D.d23 / D.d14) * (D.d34 / D.d13);
+        v[2] = um1 + (um2 - um1) * (D.d23 / D.d02) * (D.d13 / D.d03) + (u0 - um1) * (T(1.0) + D.d23 / D.d13 + D.d23 / D.d03);
+        c[0] = (D.d03 / D.d05) * (D.d13 / D.d15);
+        c[1] = (D.d03 / D.d05) * (D.d35 / D.d15) * (T(1.0) + D.d15 / D.d04);
+        c[2] = (D.d34 / D.d05) * (D.d35 / D.d04);
+        nu_smoothness_gaps(D, u, s);
+        d_back = nu_combine(v, c, s);
+    }
+}
+
+// eno3_nonuniform_pair on the gaps G[m] = xs[m+1] - xs[m] and the divided differences
+// dd[m] = (hs[m+1] - hs[m]) / G[m]
+template <typename T>
+__device__ __noinline__ void eno3_nonuniform_pair_dd(const T G[6], const T dd[6], T &d_fore, T &d_back)
+{
+    const T f25 = dd[5], f15 = dd[4], f05 = dd[3], fm05 = dd[2], fm15 = dd[1], fm25 = dd[0];
+    T g2 = (f25 - f15) / (G[4] + G[5]);
+    T g1 = (f15 - f05) / (G[3] + G[4]);
+    T g0 = (f05 - fm05) / (G[2] + G[3]);
+    T gm1 = (fm05 - fm15) / (G[1] + G[2]);
+    T gm2 = (fm15 - fm25) / (G[0] + G[1]);
+    T t15 = (g2 - g1) / (G[3] + G[4] + G[5]);
+    T t05 = (g1 - g0) / (G[2] + G[3] + G[4]);
+    T tm05 = (g0 - gm1) / (G[1] + G[2] + G[3]);
+    T tm15 = (gm1 - gm2) / (G[0] + G[1] + G[2]);
+    // x0 - x1m = G[2], x0 - x2m = G[1] + G[2], x0 - x1 = -G[3], x0 - x2 = -(G[3] + G[4])
+    T a1 = G[2] * (G[1] + G[2]) * minabs(tm05, tm15);
+    T a2 = -(G[2] * G[3]) * minabs(tm05, t05);
+    T a = (fabs(gm1) < fabs(g0)) ? a1 : a2;
+    T b1 = -(G[2] * G[3]) * minabs(tm05, t05);
+    T b2 = G[3] * (G[3] + G[4]) * minabs(t05, t15);
+    T b = (fabs(g0) < fabs(g1)) ? b1 : b2;
+    d_back = fm05 + minmod(gm1, g0) * G[2] + a;
+    d_fore = f05 - minmod(g0, g1) * G[3] + b;
+}
+
+// Interface-aware pair of the mixed form: rc / lc are h - r1 / h - l1 as the neighbours
+// beyond the crossings store them (read only where r1 / l1 < h).
+template <typename T>
+__device__ __forceinline__ void interface_pair_gaps(const T p[7], T r1, T rc, T l1, T lc, T h, T hf, T hb, bool eno3,
+                                                    T &d_fore, T &d_back)
+{
+    T G[6], hs[7], dd[6];
+    insert_interface_gaps(p, r1, rc, l1, lc, h, hf, hb, G, hs);
+#pragma unroll
+    for (int m = 0; m < 6; ++m) dd[m] = (hs[m + 1] - hs[m]) / G[m];
+    if (eno3)
+        eno3_nonuniform_pair_dd(G, dd, d_fore, d_back);
+    else
+        weno_nonuniform_pair_dd(G, dd, d_fore, d_back);
+}
+
 // Godunov |grad phi| for the reinitialization Hamiltonian; `neg` is the mask (phi0 < 0)
 // (re_step.cu:382-392).
 template <typename T>
@@ -719,52 +866,34 @@ __device__ __forceinline__ float2 weno5_upwind2(const float pa[7], bool back_a, 
 }
 
 // Crossing values for the mixed-precision form: the same interpolating polynomials
-// (degree 5 through six nodes, or the cubic through four) evaluated in FP32 in Lagrange
-// product form with the equispaced denominators folded into constants, at the normalised
-// abscissa t (node spacing 1).  The reference builds monomial coefficients in FP64
-// (boundary_interpolant.cu:78-99, wenork3_extend.cu:296-328); the product form is the
-// better-conditioned evaluation of the same polynomial.
-template <int NPT>
-__device__ __forceinline__ float lagrange_equispaced(const float *y, float t)
+// (degree 5 through six nodes, or the cubic through four) evaluated in Lagrange product
+// form at the normalised abscissa t (node spacing 1), in FP64 on the promoted FP32 values.
+// The reference builds monomial coefficients in FP64 (boundary_interpolant.cu:78-99,
+// wenork3_extend.cu:296-328); the product form is the better-conditioned evaluation of the
+// same polynomial, and reproduces the node values exactly at the nodes.
+template <int NPT, typename T>
+__device__ __forceinline__ T lagrange_equispaced(const T *y, T t)
 {
     // nodes 0..NPT-1; weight_m = prod_{q != m} (t - q) / prod_{q != m} (m - q)
-    float d[NPT], pre[NPT], suf[NPT];
+    T d[NPT], pre[NPT], suf[NPT];
 #pragma unroll
-    for (int q = 0; q < NPT; ++q) d[q] = t - (float)q;
-    pre[0] = 1.f;
+    for (int q = 0; q < NPT; ++q) d[q] = t - (T)q;
+    pre[0] = T(1);
 #pragma unroll
     for (int q = 1; q < NPT; ++q) pre[q] = pre[q - 1] * d[q - 1];
-    suf[NPT - 1] = 1.f;
+    suf[NPT - 1] = T(1);
 #pragma unroll
     for (int q = NPT - 2; q >= 0; --q) suf[q] = suf[q + 1] * d[q + 1];
-    float v = 0.f;
+    T v = T(0);
 #pragma unroll
     for (int m = 0; m < NPT; ++m) {
-        float den = 1.f;
+        T den = T(1);
 #pragma unroll
         for (int q = 0; q < NPT; ++q)
-            if (q != m) den *= (float)(m - q);
-        v += y[m] * (pre[m] * suf[m]) * (1.f / den);
+            if (q != m) den *= (T)(m - q);
+        v += y[m] * (pre[m] * suf[m]) * (T(1) / den);
     }
     return v;
-}
-
-__device__ __forceinline__ void crossing_quintic_fast(const float p[7], float dis_f, float dis_b, float h,
-                                                      float &cf, float &cb)
-{
-    cf = 0.f;
-    cb = 0.f;
-    if (dis_f < h) cf = lagrange_equispaced<6>(p + 1, 2.f + dis_f / h);  // nodes p[1..6] at 0..5
-    if (dis_b < h) cb = lagrange_equispaced<6>(p, 3.f - dis_b / h);      // nodes p[0..5] at 0..5
-}
-
-__device__ __forceinline__ void crossing_cubic_fast(const float p[7], float dis_f, float dis_b, float h, float &cf,
-                                                    float &cb)
-{
-    cf = 0.f;
-    cb = 0.f;
-    if (dis_f < h) cf = lagrange_equispaced<4>(p + 2, 1.f + dis_f / h);  // nodes p[2..5] at 0..3
-    if (dis_b < h) cb = lagrange_equispaced<4>(p + 1, 2.f - dis_b / h);  // nodes p[1..4] at 0..3
 }
 
 // ---------------------------------------------------------------------------------------

@@ -18,6 +18,7 @@
 // defaults, so the dense per-stage traffic is phi_s (stencil), phi_n, flags and out.
 #pragma once
 
+#include <math_constants.h>
 #include <type_traits>
 
 #include "vsl_internal.h"
@@ -231,6 +232,41 @@ __global__ void __launch_bounds__(256) k_classify4(const float *__restrict__ phi
     }
 }
 
+// The short gaps beyond the crossings of node c on line L (FP32 distances): h - r1 and
+// h - l1 as the neighbours beyond the crossings store them (their own distance, h - dist
+// rounded once from the FP64 root), where they agree with h - r1 / h - l1 to 1e-6 h (so
+// distances from any source stay safe); h - r1 / h - l1 otherwise and at the line's ends.
+__device__ __forceinline__ void crossing_gaps(const AxisLine &L, int ax, const Ptr6<const float> &d, long long c,
+                                              float r1, float l1, float h, float &rc, float &lc)
+{
+    rc = h - r1;
+    lc = h - l1;
+    if (r1 < h && L.c + 1 < L.n) {
+        const float nb = __ldg(d.p[2 * ax + 1] + c + L.stride);
+        if (fabsf(r1 + nb - h) <= 1e-6f * h) rc = nb;
+    }
+    if (l1 < h && L.c > 0) {
+        const float nb = __ldg(d.p[2 * ax] + c - L.stride);
+        if (fabsf(l1 + nb - h) <= 1e-6f * h) lc = nb;
+    }
+}
+
+// The interface-aware pair at node c of axis line L (r1 / l1: the node's distances, hf /
+// hb: the values at the crossings).  The plain FP64 form takes the reference's position
+// form.  The mixed FP32 form takes the gap form with the short gaps of crossing_gaps.
+template <typename T, bool ENO3>
+__device__ __forceinline__ void node_interface_pair(const T p[7], const AxisLine &L, int ax, const Ptr6<const T> &d,
+                                                    long long c, T r1, T l1, T h, T hf, T hb, T &df, T &db)
+{
+    if constexpr (std::is_same<T, float>::value) {
+        T rc, lc;
+        crossing_gaps(L, ax, d, c, r1, l1, h, rc, lc);
+        interface_pair_gaps(p, r1, rc, l1, lc, h, hf, hb, ENO3, df, db);
+    } else {
+        interface_pair(p, r1, l1, h, hf, hb, ENO3, df, db);
+    }
+}
+
 // ---------------------------------------------------------------------------------------
 // reinitialization stage (re_step.cu:283-393 / weno_rk3_reinitialization.cu:295-406)
 // ---------------------------------------------------------------------------------------
@@ -250,12 +286,13 @@ __device__ __forceinline__ void reinit_node(const T *__restrict__ phi_s, const T
 #pragma unroll
         for (int ax = 0; ax < 3; ++ax) {
             T p[7];
-            load_line7(phi_s, axis_line(g, i, j, k, ax), p);
+            const AxisLine L = axis_line(g, i, j, k, ax);
+            load_line7(phi_s, L, p);
             const T h = ax == 0 ? hx : (ax == 1 ? hy : hz);
             if (p[2] * p[3] < T(0) || p[3] * p[4] < T(0)) {
                 const T r1 = flagged_distance(fl, 2 * ax, d, c, h);
                 const T l1 = flagged_distance(fl, 2 * ax + 1, d, c, h);
-                interface_pair(p, r1, l1, h, T(0), T(0), ENO3, df[ax], db[ax]);
+                node_interface_pair<T, ENO3>(p, L, ax, d, c, r1, l1, h, T(0), T(0), df[ax], db[ax]);
             } else {
                 uniform_pair<T, FAST>(p, h, df[ax], db[ax]);
             }
@@ -279,6 +316,85 @@ __global__ void __launch_bounds__(BX *BY) k_reinit_stage(const T *__restrict__ p
 }
 
 // ---------------------------------------------------------------------------------------
+// reinitialization residual
+// ---------------------------------------------------------------------------------------
+// | |grad phi|_G - 1 | at node c in FP64 (the Godunov norm of re_step.cu:382-392 with the
+// stage's stencil choice: the interface-aware pair where the line changes sign).  The plain
+// form takes reinit_node's FP64 arithmetic; the mixed form promotes its FP32 values and
+// takes the gap form of its distances.
+template <typename T>
+__device__ __forceinline__ double residual_node(const T *__restrict__ phi, uint8_t fl, const Ptr6<const T> &d,
+                                                const Grid &g, int i, int j, int k, long long c)
+{
+    double df[3], db[3];
+#pragma unroll 1
+    for (int ax = 0; ax < 3; ++ax) {
+        const AxisLine L = axis_line(g, i, j, k, ax);
+        T pt[7];
+        load_line7(phi, L, pt);
+        double p[7];
+#pragma unroll
+        for (int m = 0; m < 7; ++m) p[m] = (double)pt[m];
+        const double h = axis_h(g, ax);
+        if (p[2] * p[3] < 0.0 || p[3] * p[4] < 0.0) {
+            if constexpr (std::is_same<T, float>::value) {
+                const float hf = (float)h;
+                const float r1 = flagged_distance(fl, 2 * ax, d, c, hf), l1 = flagged_distance(fl, 2 * ax + 1, d, c, hf);
+                float rc, lc;
+                crossing_gaps(L, ax, d, c, r1, l1, hf, rc, lc);
+                interface_pair_gaps<double>(p, r1, rc, l1, lc, hf, 0.0, 0.0, false, df[ax], db[ax]);
+            } else {
+                const double r1 = flagged_distance(fl, 2 * ax, d, c, h), l1 = flagged_distance(fl, 2 * ax + 1, d, c, h);
+                interface_pair<double>(p, r1, l1, h, 0.0, 0.0, false, df[ax], db[ax]);
+            }
+        } else {
+            weno5_pair_plain<double>(p, h, df[ax], db[ax]);
+        }
+    }
+    const double gn = godunov_norm((fl & MASK_BIT) != 0, df[0], db[0], df[1], db[1], df[2], db[2]);
+    return fabs(gn - 1.0);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(BX *BY) k_reinit_residual(const T *__restrict__ phi, const uint8_t *__restrict__ flags,
+                                                              Ptr6<const T> d, Grid g, double band, ResidualState st)
+{
+    const int i = blockIdx.x * BX + threadIdx.x, j = blockIdx.y * BY + threadIdx.y, k = blockIdx.z;
+    double r = 0.0;
+    if (i < g.rows && j < g.cols) {
+        const long long c = node_index(g, i, j, k);
+        const uint8_t fl = __ldg(flags + c);
+        if (fabs((double)__ldg(phi + c)) < band && !(fl & FIXED_BIT)) r = residual_node<T>(phi, fl, d, g, i, j, k, c);
+        if (r != r) r = CUDART_INF;  // a NaN never counts as converged
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r = fmax(r, __shfl_down_sync(0xffffffffu, r, o));
+    __shared__ double sm[BX * BY / 32];
+    const int t = threadIdx.y * BX + threadIdx.x;
+    if ((t & 31) == 0) sm[t >> 5] = r;
+    __syncthreads();
+    if (t != 0) return;
+    for (int w = 1; w < BX * BY / 32; ++w) r = fmax(r, sm[w]);
+    // non-negative doubles order as their bit patterns
+    atomicMax(st.max_bits, (unsigned long long)__double_as_longlong(r));
+    __threadfence();
+    const unsigned nb = gridDim.x * gridDim.y * gridDim.z;
+    if (atomicAdd(st.ticket, 1u) != nb - 1) return;
+    // the last block: every other block's maximum is in (each fenced before its ticket)
+    const double res = __longlong_as_double((long long)atomicExch(st.max_bits, 0ull));
+    *st.ticket = 0u;
+    const int it = st.status[0] + st.advance;
+    st.status[0] = it;
+    if (st.history) st.history[it] = res;
+    const bool conv = res <= st.tol;
+    st.status[1] = conv ? 1 : 0;
+    if (st.zero_counter) *st.zero_counter = 0u;
+    if (st.has_handle) cudaGraphSetConditional(st.handle, (!conv && it < st.cap) ? 1u : 0u);
+}
+
+__global__ void k_condition_reset(cudaGraphConditionalHandle handle) { cudaGraphSetConditional(handle, 0u); }
+
+// ---------------------------------------------------------------------------------------
 // extension set-up: v = sign(F) * grad / max(|grad|, floor) with the upwind normal of
 // upwind_normal.cu:4-104 (WENORK3: wenork3_extend.cu:192-292) and the normalisation of
 // WENO5RK3Extend.m:23-31
@@ -298,11 +414,12 @@ __device__ __forceinline__ void extension_velocity_node(const T *__restrict__ ph
 #pragma unroll
     for (int ax = 0; ax < 3; ++ax) {
         T p[7], df, db;
-        load_line7(phi, axis_line(g, i, j, k, ax), p);
+        const AxisLine L = axis_line(g, i, j, k, ax);
+        load_line7(phi, L, p);
         const T h = (T)axis_h(g, ax);
         const T r1 = flagged_distance(fl, 2 * ax, d, c, h), l1 = flagged_distance(fl, 2 * ax + 1, d, c, h);
         if (r1 < h || l1 < h) {
-            interface_pair(p, r1, l1, h, T(0), T(0), ENO3, df, db);
+            node_interface_pair<T, ENO3>(p, L, ax, d, c, r1, l1, h, T(0), T(0), df, db);
         } else {
             if constexpr (std::is_same<T, float>::value)
                 weno5_pair_fast2(p, 1.0f / h, 1e-6f * h * h, df, db);
@@ -376,8 +493,8 @@ __global__ void __launch_bounds__(128) k_velocity_list(const float *__restrict__
 
 // crossing values (boundary_interpolant.cu:78-141 / wenork3_extend.cu:296-365), at the
 // listed nodes only (a node without a distance flag has no crossing, and its entries are
-// never read): the reference's FP64 construction for the plain form, the FP32 product
-// form for the mixed form
+// never read): the reference's FP64 construction (the mixed form's extension takes its
+// FP64 crossing values from k_crossing_mixed)
 template <typename T, bool CUBIC>
 __global__ void __launch_bounds__(128) k_crossing(const T *__restrict__ cfield, Ptr6<const T> d, Ptr6<T> cp,
                                                   NodeList list, Grid g)
@@ -394,27 +511,14 @@ __global__ void __launch_bounds__(128) k_crossing(const T *__restrict__ cfield, 
             double cf = 0.0, cb = 0.0;
             if (r1 < h || l1 < h) {
                 AxisLine L = axis_line(g, i, j, k, ax);
-                if constexpr (std::is_same<T, float>::value) {
-                    float p[7], ff, fb;
+                double p[7];
 #pragma unroll
-                    for (int s = -3; s <= 3; ++s)
-                        p[s + 3] = __ldg(cfield + L.base + (long long)clampi(L.c + s, L.n) * L.stride);
-                    if (CUBIC)
-                        crossing_cubic_fast(p, (float)r1, (float)l1, (float)h, ff, fb);
-                    else
-                        crossing_quintic_fast(p, (float)r1, (float)l1, (float)h, ff, fb);
-                    cf = ff;
-                    cb = fb;
-                } else {
-                    double p[7];
-#pragma unroll
-                    for (int s = -3; s <= 3; ++s)
-                        p[s + 3] = (double)__ldg(cfield + L.base + (long long)clampi(L.c + s, L.n) * L.stride);
-                    if (CUBIC)
-                        crossing_cubic(p, r1, l1, h, cf, cb);
-                    else
-                        crossing_quintic(p, r1, l1, h, cf, cb);
-                }
+                for (int s = -3; s <= 3; ++s)
+                    p[s + 3] = (double)__ldg(cfield + L.base + (long long)clampi(L.c + s, L.n) * L.stride);
+                if (CUBIC)
+                    crossing_cubic(p, r1, l1, h, cf, cb);
+                else
+                    crossing_quintic(p, r1, l1, h, cf, cb);
             }
             cp.p[2 * ax][c] = (T)cf;
             cp.p[2 * ax + 1][c] = (T)cb;
@@ -442,14 +546,15 @@ __device__ __forceinline__ void extend_node(const T *__restrict__ c_s, const T *
 #pragma unroll
         for (int ax = 0; ax < 3; ++ax) {
             T p[7];
-            load_line7(c_s, axis_line(g, i, j, k, ax), p);
+            const AxisLine L = axis_line(g, i, j, k, ax);
+            load_line7(c_s, L, p);
             const T h = ax == 0 ? hx : (ax == 1 ? hy : hz);
             const T r1 = flagged_distance(fl, 2 * ax, d, c, h);
             const T l1 = flagged_distance(fl, 2 * ax + 1, d, c, h);
             if (r1 < h || l1 < h) {
                 const T hf = r1 < h ? __ldg(cp.p[2 * ax] + c) : T(0);
                 const T hb = l1 < h ? __ldg(cp.p[2 * ax + 1] + c) : T(0);
-                interface_pair(p, r1, l1, h, hf, hb, ENO3, df[ax], db[ax]);
+                node_interface_pair<T, ENO3>(p, L, ax, d, c, r1, l1, h, hf, hb, df[ax], db[ax]);
             } else {
                 uniform_pair<T, FAST>(p, h, df[ax], db[ax]);
             }
@@ -839,6 +944,14 @@ cudaError_t launch_enork2_extend_stage(const T *c_s, const T *c_n, T *out, const
     return cudaGetLastError();
 }
 
+template <typename T>
+cudaError_t launch_reinit_residual(const T *phi, const uint8_t *flags, Ptr6<const T> dist, const Grid &g, double band,
+                                   const ResidualState &st, cudaStream_t s)
+{
+    k_reinit_residual<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, flags, dist, g, band, st);
+    return cudaGetLastError();
+}
+
 #define VSL_INSTANTIATE_FUSED(T)                                                                                   \
     template cudaError_t launch_set_distance<T>(const T *, Ptr6<T>, const Grid &, bool, EdgeLists, cudaStream_t);   \
     template cudaError_t launch_classify<T>(const T *, Ptr6<const T>, uint8_t *, NodeList, const Grid &,            \
@@ -847,6 +960,8 @@ cudaError_t launch_enork2_extend_stage(const T *c_s, const T *c_n, T *out, const
                                                 const Grid &, int, bool, bool, cudaStream_t);                       \
     template cudaError_t launch_extension_velocity<T>(const T *, const uint8_t *, Ptr6<const T>, Ptr3<T>,           \
                                                       const Grid &, bool, double, NodeList, cudaStream_t);          \
+    template cudaError_t launch_reinit_residual<T>(const T *, const uint8_t *, Ptr6<const T>, const Grid &, double, \
+                                                   const ResidualState &, cudaStream_t);                           \
     template cudaError_t launch_crossing<T>(const T *, Ptr6<const T>, Ptr6<T>, NodeList, const Grid &, bool,        \
                                             cudaStream_t);                                                          \
     template cudaError_t launch_extend_stage<T>(const T *, const T *, T *, const uint8_t *, Ptr6<const T>,          \

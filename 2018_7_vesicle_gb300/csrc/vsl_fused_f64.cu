@@ -5,4 +5,10 @@
 
 namespace vsl {
 VSL_INSTANTIATE_FUSED(double)
+
+cudaError_t launch_condition_reset(cudaGraphConditionalHandle handle, cudaStream_t s)
+{
+    k_condition_reset<<<1, 1, 0, s>>>(handle);
+    return cudaGetLastError();
+}
 }  // namespace vsl

@@ -75,6 +75,29 @@ template <typename T>
 cudaError_t launch_advect_stage(const T *phi_s, const T *phi_n, T *out, Ptr3<const T> v, const T *speed,
                                 const double *dt, const Grid &g, int stage, bool fast, cudaStream_t s);
 
+// Reinitialization residual (no counterpart in the reference, whose loops run a fixed
+// count): the FP64 maximum over the band |phi| < band of | |grad phi|_G - 1 |, the Godunov
+// norm the stage takes, at the non-fixed nodes.  The last block to finish records it and
+// decides whether a residual-driven loop goes on (see ResidualState).
+struct ResidualState {
+    unsigned long long *max_bits;  // running maximum, the bits of a non-negative double (zero between uses)
+    unsigned *ticket;              // blocks finished (zero between uses)
+    int *status;                   // [pseudo-steps done, 1 if the residual is <= tol]
+    double *history;               // residual after each pseudo-step, [0] on entry (may be null)
+    unsigned *zero_counter;        // a band counter the next pseudo-step needs zeroed (may be null)
+    double tol;
+    int cap;                       // most pseudo-steps
+    int advance;                   // 1: one more pseudo-step was taken before this evaluation
+    int has_handle;                // inside a residual-driven loop (a conditional graph node)
+    cudaGraphConditionalHandle handle;  // the loop's condition, set to (residual > tol && steps < cap)
+};
+template <typename T>
+cudaError_t launch_reinit_residual(const T *phi, const uint8_t *flags, Ptr6<const T> dist, const Grid &g, double band,
+                                   const ResidualState &st, cudaStream_t s);
+// 1 thread: the loop condition of a residual-driven loop set to 0 (the first node of each
+// iteration, so that only a completed residual evaluation can continue the loop)
+cudaError_t launch_condition_reset(cudaGraphConditionalHandle handle, cudaStream_t s);
+
 // ENORK2 (second-order ENO, Heun RK2 stages 0 and 1): quadratic-ENO distances, the
 // reinitialization and extension stages, the extension velocity and crossing values
 template <typename T>
@@ -122,13 +145,25 @@ struct BandQueue {
     unsigned *queue;
     unsigned *counter;
 };
+// The mixed form's FP64 interface data of an extension stage: the crossing values and an
+// FP64 copy ("shadow") of the flagged nodes' values of the stage input, the step-start
+// field and the stage output.  A one-sided divided difference across a short gap g between
+// a node and a crossing, (C_node - C_cross) / g, amplifies the FP32 rounding of C_node and
+// C_cross by h / g (a gap of 2e-4 h turns an FP32 ulp into a 5e-3 relative error of the
+// derivative), so those values stay FP64 where the band kernel forms such differences.
+struct BandShadow {
+    const double *s_in;
+    const double *s_n;
+    double *s_out;
+    Ptr6<const double> cp;
+};
 struct TiledStage {
     const float *phi_s;
     const float *phi_n;
     float *out;
     const uint8_t *flags;
     Ptr6<const float> d;
-    Ptr6<const float> cp;
+    BandShadow shadow;  // extension kinds only
     Ptr3<const float> v;
     const float *speed;
     const double *dt;
@@ -139,6 +174,18 @@ struct TiledStage {
 };
 // kind: 0 reinitialization, 1 extension, 2 advection
 cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const Grid &g, cudaStream_t s);
+// the same stage (same kind and RK stage) of `count` <= TILED_BATCH_MAX grids as one
+// persistent launch over all their tiles, and one launch for all their band nodes
+constexpr int TILED_BATCH_MAX = 64;
+cudaError_t launch_tiled_batch(int kind, bool eno3, const TiledStage *st, const Grid *grids, int count, cudaStream_t s);
+// the mixed form's extension set-up at the listed (flagged) nodes: FP64 crossing values on
+// the promoted FP32 field (degree-5 / cubic product form, or the ENORK2 quadratic), and the
+// shadow of the field's values
+cudaError_t launch_crossing_mixed(const float *c, Ptr6<const float> dist, Ptr6<double> cp, NodeList list,
+                                  const Grid &g, bool cubic, cudaStream_t s);
+cudaError_t launch_enork2_crossing_mixed(const float *c, Ptr6<const float> dist, Ptr6<double> cp, NodeList list,
+                                         const Grid &g, cudaStream_t s);
+cudaError_t launch_shadow_init(const float *c, double *shadow, NodeList list, cudaStream_t s);
 // pages per block of the tiled kernels for a grid shape and kind (the tuning table, or the
 // default); set_tile_pages(..., 0) restores the default
 int tile_pages(const Grid &g, int kind);

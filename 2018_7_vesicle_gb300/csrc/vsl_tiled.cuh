@@ -19,6 +19,7 @@
 // test): a static list, so the band kernel runs beside the tiled kernel on a side stream.
 #pragma once
 
+#include <algorithm>
 #include <mutex>
 
 #include "vsl_fused.cuh"
@@ -101,14 +102,12 @@ __device__ __forceinline__ void eno2_pair_uniform(const float p[7], float inv_h,
     back = (v0 - v1 + 0.5f * minmod(p2, v0 - 2.f * v1 + p[1])) * inv_h;
 }
 
+// One tile of one stage: the TY x TX block's tile (bx, by) marching pages bz * kz ..
+// (bz + 1) * kz - 1 of the grid of `a` (the work of one block of k_stage_tiled, or of one
+// work item of the batched kernel).  sm: the block's plane ring.
 template <int KIND, int STAGE>
-// The ENORK2 extension kind, whose uniform path is light, is latency-bound at 4 blocks per SM
-// (long-scoreboard stalls, DRAM 35% of peak): 5 blocks (47 registers, no spills) took 100
-// pseudo-steps at 256^3 from 26.7 to 23.6 ms.  The ENORK2 reinitialization was slower at 5
-// (25.7 -> 27.7 ms) and keeps 4 with the WENO5 kinds.
-__global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_BLOCKS)) k_stage_tiled(TiledArgs a)
+__device__ __forceinline__ void stage_tile(const TiledArgs &a, float (*sm)[SH][SW], int bx, int by, int bz)
 {
-    __shared__ float sm[RING][SH][SW];
     const Grid &g = a.g;
     // the launch is always TY x TX threads: the first two elements of every thread's share
     // of a plane are then in the plane without a test
@@ -116,9 +115,9 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
     __builtin_assume(threadIdx.y < TX);
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * TY + tx;
-    const int i0 = blockIdx.x * TY, j0 = blockIdx.y * TX;
+    const int i0 = bx * TY, j0 = by * TX;
     const int i = i0 + tx, j = j0 + ty;
-    const int k0 = blockIdx.z * a.kz;
+    const int k0 = bz * a.kz;
     const int k1 = min(k0 + a.kz, g.pges);
     const bool active = i < g.rows && j < g.cols;
     // ring slot of page p (p >= k0): counted from the block's first page, so that in the
@@ -321,6 +320,128 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
     for (int r = 0; k < k1; ++k, ++r) page(r, (r + 3) % RING, (r + 4) % RING, k);
 }
 
+// The ENORK2 extension kind, whose uniform path is light, is latency-bound at 4 blocks per SM
+// (long-scoreboard stalls, DRAM 35% of peak): 5 blocks (47 registers, no spills) took 100
+// pseudo-steps at 256^3 from 26.7 to 23.6 ms.  The ENORK2 reinitialization was slower at 5
+// (25.7 -> 27.7 ms) and keeps 4 with the WENO5 kinds.
+template <int KIND, int STAGE>
+__global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_BLOCKS)) k_stage_tiled(TiledArgs a)
+{
+    __shared__ float sm[RING][SH][SW];
+    stage_tile<KIND, STAGE>(a, sm, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// ---------------------------------------------------------------------------------------
+// Extension band of the mixed form with FP64 interface data.  Next to a crossing at a
+// short distance from a node, the one-sided divided difference between the node (or its
+// neighbour) and the crossing value divides the difference of two O(|C|) values by a gap
+// of a small fraction of h: in FP32 both values carry an independent rounding of |C| 6e-8,
+// which the gap multiplies by h / gap.  The crossing values (computed in FP64 from the FP32
+// field) and the flagged nodes' values (kept in FP64 beside the FP32 field, "shadows", and
+// updated here) give those differences in FP64; the rest of the stencil arithmetic stays
+// FP32 on divided differences of ordinary size.  Nodes off the band (the tiled kernel)
+// never form such a difference.
+// ---------------------------------------------------------------------------------------
+
+// the stage input at node n next to a crossing: its shadow where n is flagged (every node
+// next to a crossing is, unless its own distance rounded to the spacing), else its FP32 value
+__device__ __forceinline__ double shadow_or(const BandShadow &sh, const uint8_t *flags, long long n, float v)
+{
+    return (__ldg(flags + n) & 0x3F) ? __ldg(sh.s_in + n) : (double)v;
+}
+
+// one band node of a WENO5 / WENORK3 extension stage (extend_node with the FP64 interface data)
+template <bool ENO3>
+__device__ __forceinline__ void extend_node_mixed(const TiledArgs &a, const BandShadow &sh, int i, int j, int k)
+{
+    const Grid &g = a.g;
+    const long long c = node_index(g, i, j, k);
+    const uint8_t fl = __ldg(a.flags + c);
+    const double cs = __ldg(sh.s_in + c);
+    float step = 0.f;
+    if (!(fl & FIXED_BIT)) {
+        float df[3], db[3];
+#pragma unroll 1
+        for (int ax = 0; ax < 3; ++ax) {
+            float p[7];
+            const AxisLine L = axis_line(g, i, j, k, ax);
+            load_line7(a.phi_s, L, p);
+            const float h = a.h[ax];
+            const float r1 = flagged_distance(fl, 2 * ax, a.d, c, h);
+            const float l1 = flagged_distance(fl, 2 * ax + 1, a.d, c, h);
+            if (r1 < h || l1 < h) {
+                float rc, lc;
+                crossing_gaps(L, ax, a.d, c, r1, l1, h, rc, lc);
+                float G[6], pv[7];
+                insert_interface_gaps(p, r1, rc, l1, lc, h, 0.f, 0.f, G, pv);
+                double hs[7];
+#pragma unroll
+                for (int m = 0; m < 7; ++m) hs[m] = (double)pv[m];
+                hs[3] = cs;
+                if (r1 < h) {
+                    hs[4] = __ldg(sh.cp.p[2 * ax] + c);
+                    hs[5] = shadow_or(sh, a.flags, c + L.stride, p[4]);
+                }
+                if (l1 < h) {
+                    hs[2] = __ldg(sh.cp.p[2 * ax + 1] + c);
+                    hs[1] = shadow_or(sh, a.flags, c - L.stride, p[2]);
+                }
+                float dd[6];
+#pragma unroll
+                for (int m = 0; m < 6; ++m) dd[m] = (float)((hs[m + 1] - hs[m]) / (double)G[m]);
+                if (ENO3)
+                    eno3_nonuniform_pair_dd(G, dd, df[ax], db[ax]);
+                else
+                    weno_nonuniform_pair_dd(G, dd, df[ax], db[ax]);
+            } else {
+                weno5_pair_fast(p, a.inv_h[ax], a.eps2[ax], df[ax], db[ax]);
+            }
+        }
+        step = upwind_dot(__ldg(a.v.p[0] + c), __ldg(a.v.p[1] + c), __ldg(a.v.p[2] + c), df[0], db[0], df[1], db[1],
+                          df[2], db[2]) *
+               pseudo_dt(fl, a.d, c, a.h[0], a.h[1], a.h[2]);
+    }
+    const double pn = a.stage == 0 ? 0.0 : __ldg(sh.s_n + c);
+    const double val = rk3_combine(a.stage, pn, cs - (double)step);
+    a.out[c] = (float)val;
+    sh.s_out[c] = val;
+}
+
+// one band node of an ENORK2 extension stage (enork2_extend_node with the FP64 interface data)
+__device__ __forceinline__ void enork2_extend_node_mixed(const TiledArgs &a, const BandShadow &sh, int i, int j, int k)
+{
+    const Grid &g = a.g;
+    const long long c = node_index(g, i, j, k);
+    const uint8_t fl = __ldg(a.flags + c);
+    const double cs = __ldg(sh.s_in + c);
+    float df[3], db[3];
+#pragma unroll
+    for (int ax = 0; ax < 3; ++ax) {
+        float p[7];
+        load_line7(a.phi_s, axis_line(g, i, j, k, ax), p);
+        const float h = a.h[ax];
+        const bool ff = fl & (1u << (2 * ax)), fb = fl & (1u << (2 * ax + 1));
+        const float r1 = ff ? __ldg(a.d.p[2 * ax] + c) : h, l1 = fb ? __ldg(a.d.p[2 * ax + 1] + c) : h;
+        // eno2_pair: the one-sided differences to a crossing in FP64 (crossing value and shadow)
+        const float v4 = p[1], v1 = p[2], v0 = p[3], v2 = p[4], v3 = p[5];
+        const float h2 = h * h;
+        const float p2 = v1 - 2.f * v0 + v2;
+        float p2m = 0.5f * minmod(p2, v0 - 2.f * v2 + v3) / h2;
+        const float sr = (r1 == h) ? (v2 - v0) / r1 : (float)((__ldg(sh.cp.p[2 * ax] + c) - cs) / (double)r1);
+        df[ax] = sr - r1 * p2m;
+        p2m = 0.5f * minmod(p2, v0 - 2.f * v1 + v4) / h2;
+        const float sl = (l1 == h) ? (v0 - v1) / l1 : (float)((cs - __ldg(sh.cp.p[2 * ax + 1] + c)) / (double)l1);
+        db[ax] = sl + l1 * p2m;
+    }
+    const float step = upwind_dot(__ldg(a.v.p[0] + c), __ldg(a.v.p[1] + c), __ldg(a.v.p[2] + c), df[0], db[0], df[1],
+                                  db[1], df[2], db[2]) *
+                       pseudo_dt(fl, a.d, c, a.h[0], a.h[1], a.h[2]);
+    const double pn = a.stage == 0 ? 0.0 : __ldg(sh.s_n + c);
+    const double val = rk2_combine(a.stage, pn, cs, (double)step);
+    a.out[c] = (float)val;
+    sh.s_out[c] = val;
+}
+
 // Band nodes of one stage: the generic per-node update (interface-aware stencils),
 // grid-stride over the queue (reinitialization: also clears the other stage's counter for
 // its next use) or over the static flagged list (extension).
@@ -330,7 +451,7 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
 // (75 registers; 8 blocks per SM gained nothing there).
 template <int KIND, bool ENO3>
 __global__ void __launch_bounds__(128, (KIND == SK_REINIT ? 0 : 8))
-    k_band_stage(TiledArgs a, Ptr6<const float> cp, unsigned *next_counter)
+    k_band_stage(TiledArgs a, BandShadow sh, unsigned *next_counter)
 {
     const unsigned n = *a.counter;
     if (next_counter && blockIdx.x == 0 && threadIdx.x == 0) *next_counter = 0u;
@@ -344,11 +465,94 @@ __global__ void __launch_bounds__(128, (KIND == SK_REINIT ? 0 : 8))
         if (KIND == SK_REINIT)
             reinit_node<float, ENO3, true>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
         else if (KIND == SK_ENO2)
-            enork2_extend_node<float>(a.phi_s, a.phi_n, a.out, a.flags, a.d, cp, a.v, g, a.stage, i, j, k);
+            enork2_extend_node_mixed(a, sh, i, j, k);
         else if (KIND == SK_ENO2R)
             enork2_reinit_node<float>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
         else
-            extend_node<float, ENO3, true>(a.phi_s, a.phi_n, a.out, a.flags, a.d, cp, a.v, g, a.stage, i, j, k);
+            extend_node_mixed<ENO3>(a, sh, i, j, k);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Batched stages: one persistent launch runs one RK stage of up to BATCH_MAX grids (a batch
+// of vesicles).  The work list is every grid's tiles (tile x, tile y, page slab) in order;
+// the launch's blocks walk it grid-stride, so small grids that could not fill the GPU alone
+// share its SMs, and a batch step issues one launch per stage instead of one per vesicle.
+// The stages' order is the launches' order on the stream: no block waits for another.
+// Every grid's arguments travel in the kernel parameter (a __grid_constant__ table indexed
+// by the block-uniform grid number).
+// ---------------------------------------------------------------------------------------
+constexpr int BATCH_MAX = TILED_BATCH_MAX;
+struct TiledBatch {
+    TiledArgs v[BATCH_MAX];
+    int start[BATCH_MAX + 1];  // first work item of each grid; start[count] = all items
+    int nx[BATCH_MAX], ny[BATCH_MAX];  // tiles along rows and columns
+    int count;
+};
+static_assert(sizeof(TiledBatch) <= 32000, "kernel parameter space");
+
+// the grid of work item w: the last g with start[g] <= w (start is block-uniform)
+__device__ __forceinline__ int batch_member(const int *start, int count, int w)
+{
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (start[mid] <= w)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int KIND, int STAGE>
+__global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_BLOCKS))
+    k_stage_tiled_batch(const __grid_constant__ TiledBatch B)
+{
+    __shared__ float sm[RING][SH][SW];
+    const int total = B.start[B.count];
+    for (int w = blockIdx.x; w < total; w += gridDim.x) {
+        const int v = batch_member(B.start, B.count, w);
+        const int local = w - B.start[v];
+        const int rest = local / B.nx[v];
+        stage_tile<KIND, STAGE>(B.v[v], sm, local - rest * B.nx[v], rest % B.ny[v], rest / B.ny[v]);
+        __syncthreads();  // the next item's prologue rewrites the plane ring
+    }
+}
+
+// The band nodes of one stage of every grid of a batch (k_band_stage per grid, one after
+// the other in one grid-stride launch).
+struct BandBatch {
+    TiledArgs v[BATCH_MAX];
+    BandShadow sh[BATCH_MAX];
+    unsigned *next[BATCH_MAX];  // reinitialization: the other stage's counter, zeroed here
+    int count;
+};
+static_assert(sizeof(BandBatch) <= 32000, "kernel parameter space");
+
+template <int KIND, bool ENO3>
+__global__ void __launch_bounds__(128, (KIND == SK_REINIT ? 0 : 8)) k_band_stage_batch(const __grid_constant__ BandBatch B)
+{
+    if (blockIdx.x == 0 && (int)threadIdx.x < B.count && B.next[threadIdx.x]) *B.next[threadIdx.x] = 0u;
+    for (int v = 0; v < B.count; ++v) {
+        const TiledArgs &a = B.v[v];
+        const Grid &g = a.g;
+        const unsigned n = *a.counter;
+        for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+            const long long c = a.queue[t];
+            const int k = (int)(c / g.plane);
+            const long long r = c - (long long)k * g.plane;
+            const int j = (int)(r / g.rows);
+            const int i = (int)(r - (long long)j * g.rows);
+            if (KIND == SK_REINIT)
+                reinit_node<float, ENO3, true>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
+            else if (KIND == SK_ENO2)
+                enork2_extend_node_mixed(a, B.sh[v], i, j, k);
+            else if (KIND == SK_ENO2R)
+                enork2_reinit_node<float>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
+            else
+                extend_node_mixed<ENO3>(a, B.sh[v], i, j, k);
+        }
     }
 }
 
@@ -528,13 +732,13 @@ cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const 
             bs = ln->side;
         }
         if (kind == SK_ENO2)
-            k_band_stage<SK_ENO2, false><<<band_blocks(), 128, 0, bs>>>(a, st.cp, next);
+            k_band_stage<SK_ENO2, false><<<band_blocks(), 128, 0, bs>>>(a, st.shadow, next);
         else if (kind == SK_ENO2R)
-            k_band_stage<SK_ENO2R, false><<<band_blocks(), 128, 0, bs>>>(a, st.cp, next);
+            k_band_stage<SK_ENO2R, false><<<band_blocks(), 128, 0, bs>>>(a, st.shadow, next);
         else if (eno3)
-            k_band_stage<SK_EXTEND, true><<<band_blocks(), 128, 0, bs>>>(a, st.cp, next);
+            k_band_stage<SK_EXTEND, true><<<band_blocks(), 128, 0, bs>>>(a, st.shadow, next);
         else
-            k_band_stage<SK_EXTEND, false><<<band_blocks(), 128, 0, bs>>>(a, st.cp, next);
+            k_band_stage<SK_EXTEND, false><<<band_blocks(), 128, 0, bs>>>(a, st.shadow, next);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         if (ln) {
             if ((e = cudaEventRecord(ln->join, bs)) != cudaSuccess) return e;
@@ -550,9 +754,229 @@ cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const 
     if (e != cudaSuccess || kind == SK_ADVECT) return e;
     // the reinitialization's band is queued by the tiled kernel, so its kernel follows it
     if (eno3)
-        k_band_stage<SK_REINIT, true><<<band_blocks(), 128, 0, s>>>(a, st.cp, next);
+        k_band_stage<SK_REINIT, true><<<band_blocks(), 128, 0, s>>>(a, st.shadow, next);
     else
-        k_band_stage<SK_REINIT, false><<<band_blocks(), 128, 0, s>>>(a, st.cp, next);
+        k_band_stage<SK_REINIT, false><<<band_blocks(), 128, 0, s>>>(a, st.shadow, next);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------
+// batched stages (k_stage_tiled_batch, k_band_stage_batch)
+// ---------------------------------------------------------------------------------------
+namespace {
+// resident blocks per SM of a batched stage kernel (its occupancy; the persistent grid)
+template <int KIND, int STAGE> int batch_blocks()
+{
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_stage_tiled_batch<KIND, STAGE>, TY * TX, 0);
+        n = (sms > 0 ? sms : 132) * (per > 0 ? per : 1);
+    }
+    return n;
+}
+
+template <int KIND> cudaError_t launch_batch_kind(int stage, const TiledBatch &B, int total, cudaStream_t s)
+{
+    const dim3 bl(TY, TX);
+    auto go = [&](auto kernel, int blocks) {
+        kernel<<<std::min(total, blocks), bl, 0, s>>>(B);
+        return cudaGetLastError();
+    };
+    if (stage == 0) return go(k_stage_tiled_batch<KIND, 0>, batch_blocks<KIND, 0>());
+    if constexpr (KIND == SK_ENO2 || KIND == SK_ENO2R) {
+        return go(k_stage_tiled_batch<KIND, 1>, batch_blocks<KIND, 1>());
+    } else {
+        if (stage == 1) return go(k_stage_tiled_batch<KIND, 1>, batch_blocks<KIND, 1>());
+        return go(k_stage_tiled_batch<KIND, 2>, batch_blocks<KIND, 2>());
+    }
+}
+}  // namespace
+
+cudaError_t launch_tiled_batch(int kind, bool eno3, const TiledStage *st, const Grid *grids, int count, cudaStream_t s)
+{
+    if (count <= 0) return cudaSuccess;
+    if (count > BATCH_MAX) return cudaErrorInvalidValue;
+    // the tables are large (kernel parameters of ~16 and ~21 KB): one per host thread
+    static thread_local TiledBatch B;
+    static thread_local BandBatch BB;
+    B.count = BB.count = count;
+    int total = 0;
+    for (int v = 0; v < count; ++v) {
+        const Grid &g = grids[v];
+        TiledArgs a = tiled_args(g);
+        a.phi_s = st[v].phi_s;
+        a.phi_n = st[v].phi_n;
+        a.out = st[v].out;
+        a.flags = st[v].flags;
+        a.d = st[v].d;
+        a.v = st[v].v;
+        a.speed = st[v].speed;
+        a.dt = st[v].dt;
+        unsigned *next = nullptr;
+        if (static_band_kind(kind)) {
+            a.queue = st[v].flagged.idx;
+            a.counter = st[v].flagged.count;
+        } else {
+            a.queue = st[v].band.queue;
+            a.counter = st[v].band.counter + (st[v].seq & 1);
+            next = st[v].band.counter + ((st[v].seq + 1) & 1);
+        }
+        a.stage = st[v].stage;
+        a.kz = tile_pages(g, kind);
+        const dim3 gr = tiled_grid(g, a.kz);
+        B.v[v] = a;
+        B.nx[v] = (int)gr.x;
+        B.ny[v] = (int)gr.y;
+        B.start[v] = total;
+        total += (int)(gr.x * gr.y * gr.z);
+        BB.v[v] = a;
+        BB.sh[v] = st[v].shadow;
+        BB.next[v] = next;
+    }
+    B.start[count] = total;
+    const int stage = st[0].stage;
+    cudaError_t e;
+    if (static_band_kind(kind)) {
+        SideLane *ln = side_lane(s);
+        if (ln && (e = cudaEventRecord(ln->fork, s)) != cudaSuccess) return e;
+        if (kind == SK_ENO2)
+            e = launch_batch_kind<SK_ENO2>(stage, B, total, s);
+        else if (kind == SK_ENO2R)
+            e = launch_batch_kind<SK_ENO2R>(stage, B, total, s);
+        else
+            e = launch_batch_kind<SK_EXTEND>(stage, B, total, s);
+        if (e != cudaSuccess) return e;
+        cudaStream_t bs = s;
+        if (ln) {
+            if ((e = cudaStreamWaitEvent(ln->side, ln->fork, 0)) != cudaSuccess) return e;
+            bs = ln->side;
+        }
+        if (kind == SK_ENO2)
+            k_band_stage_batch<SK_ENO2, false><<<band_blocks(), 128, 0, bs>>>(BB);
+        else if (kind == SK_ENO2R)
+            k_band_stage_batch<SK_ENO2R, false><<<band_blocks(), 128, 0, bs>>>(BB);
+        else if (eno3)
+            k_band_stage_batch<SK_EXTEND, true><<<band_blocks(), 128, 0, bs>>>(BB);
+        else
+            k_band_stage_batch<SK_EXTEND, false><<<band_blocks(), 128, 0, bs>>>(BB);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if (ln) {
+            if ((e = cudaEventRecord(ln->join, bs)) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(s, ln->join, 0)) != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    }
+    e = kind == SK_REINIT ? launch_batch_kind<SK_REINIT>(stage, B, total, s) : launch_batch_kind<SK_ADVECT>(stage, B, total, s);
+    if (e != cudaSuccess || kind == SK_ADVECT) return e;
+    if (eno3)
+        k_band_stage_batch<SK_REINIT, true><<<band_blocks(), 128, 0, s>>>(BB);
+    else
+        k_band_stage_batch<SK_REINIT, false><<<band_blocks(), 128, 0, s>>>(BB);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------------------
+// set-up of the mixed form's extension band: FP64 crossing values and the shadows
+// ---------------------------------------------------------------------------------------
+namespace {
+// crossing values at the listed nodes (boundary_interpolant.cu:78-141 /
+// wenork3_extend.cu:296-365): the degree-5 / cubic interpolant of the promoted FP32
+// values in FP64, product (Lagrange) form
+template <bool CUBIC>
+__global__ void __launch_bounds__(128) k_crossing_mixed(const float *__restrict__ cfield, Ptr6<const float> d,
+                                                        Ptr6<double> cp, NodeList list, Grid g)
+{
+    const unsigned n = *list.count;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const long long c = list.idx[t];
+        int i, j, k;
+        node_of(g, c, i, j, k);
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            const float hf = (float)axis_h(g, ax);
+            const float r1 = __ldg(d.p[2 * ax] + c), l1 = __ldg(d.p[2 * ax + 1] + c);
+            double cf = 0.0, cb = 0.0;
+            if (r1 < hf || l1 < hf) {
+                const AxisLine L = axis_line(g, i, j, k, ax);
+                double p[7];
+#pragma unroll
+                for (int s = -3; s <= 3; ++s)
+                    p[s + 3] = (double)__ldg(cfield + L.base + (long long)clampi(L.c + s, L.n) * L.stride);
+                const double h = (double)hf, rf = (double)r1, rb = (double)l1;
+                if (CUBIC) {
+                    if (r1 < hf) cf = lagrange_equispaced<4, double>(p + 2, 1.0 + rf / h);
+                    if (l1 < hf) cb = lagrange_equispaced<4, double>(p + 1, 2.0 - rb / h);
+                } else {
+                    if (r1 < hf) cf = lagrange_equispaced<6, double>(p + 1, 2.0 + rf / h);
+                    if (l1 < hf) cb = lagrange_equispaced<6, double>(p, 3.0 - rb / h);
+                }
+            }
+            cp.p[2 * ax][c] = cf;
+            cp.p[2 * ax + 1][c] = cb;
+        }
+    }
+}
+
+// ENORK2 crossing values (enork2_extend.cu:144-211) in FP64 on the promoted FP32 values
+__global__ void __launch_bounds__(128) k_enork2_crossing_mixed(const float *__restrict__ cfield, Ptr6<const float> d,
+                                                               Ptr6<double> cp, NodeList list, Grid g)
+{
+    const unsigned n = *list.count;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const long long c = list.idx[t];
+        int i, j, k;
+        node_of(g, c, i, j, k);
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            const AxisLine L = axis_line(g, i, j, k, ax);
+            double p[7], cf, cb;
+#pragma unroll
+            for (int s = -3; s <= 3; ++s)
+                p[s + 3] = (double)__ldg(cfield + L.base + (long long)clampi(L.c + s, L.n) * L.stride);
+            const float hf = (float)axis_h(g, ax);
+            const float r1 = __ldg(d.p[2 * ax] + c), l1 = __ldg(d.p[2 * ax + 1] + c);
+            // the tests r1 != h, l1 != h of the FP32 distances hold unchanged once promoted
+            eno2_crossing<double>(p, (double)r1, (double)l1, (double)hf, cf, cb);
+            cp.p[2 * ax][c] = cf;
+            cp.p[2 * ax + 1][c] = cb;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_shadow_init(const float *__restrict__ c, double *__restrict__ shadow,
+                                                     NodeList list)
+{
+    const unsigned n = *list.count;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const unsigned q = list.idx[t];
+        shadow[q] = (double)__ldg(c + q);
+    }
+}
+}  // namespace
+
+cudaError_t launch_crossing_mixed(const float *c, Ptr6<const float> dist, Ptr6<double> cp, NodeList list,
+                                  const Grid &g, bool cubic, cudaStream_t s)
+{
+    if (cubic)
+        k_crossing_mixed<true><<<list_blocks(), 128, 0, s>>>(c, dist, cp, list, g);
+    else
+        k_crossing_mixed<false><<<list_blocks(), 128, 0, s>>>(c, dist, cp, list, g);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_enork2_crossing_mixed(const float *c, Ptr6<const float> dist, Ptr6<double> cp, NodeList list,
+                                         const Grid &g, cudaStream_t s)
+{
+    k_enork2_crossing_mixed<<<list_blocks(), 128, 0, s>>>(c, dist, cp, list, g);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_shadow_init(const float *c, double *shadow, NodeList list, cudaStream_t s)
+{
+    k_shadow_init<<<list_blocks(), 128, 0, s>>>(c, shadow, list);
     return cudaGetLastError();
 }
 

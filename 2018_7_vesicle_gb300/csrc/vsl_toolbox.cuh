@@ -9,6 +9,7 @@
 
 #include <cmath>
 #include <limits>
+#include <type_traits>
 
 #include "vsl_internal.h"
 
@@ -97,16 +98,54 @@ __global__ void __launch_bounds__(NT) k_toolbox(const T *__restrict__ f, Toolbox
         T plap = pxx + pyy + pzz;
         T heav = dot / gm2;
         T delta = plap / gm2 - dot * lap / gm4;
-        if (fabs(fc) < thr2ds) area = (double)delta;
-        if (fc < thr2ds) {
-            // 1 - heav in FP64; heav == 0 (no positive neighbour) gives exactly 1
-            if (heav == T(0)) {
-                unit = true;
-            } else {
-                vol = 1 - (double)heav;
-                if (vol == 1.0) {
+        if constexpr (std::is_same<T, float>::value) {
+            // The mixed form's area and volume terms in FP64 on the promoted FP32 values:
+            // the FP32 quotients and second differences above carry a relative error of
+            // ~1e-7 per node that does not average out in the sums (4e-8 of the area at
+            // 256^3).  Only nodes with a positive value among the seven carry a nonzero
+            // term, so the FP64 arithmetic runs on the interface band alone.
+            const bool pos = hc > T(0) || hxp > T(0) || hxm > T(0) || hyp > T(0) || hym > T(0) || hzp > T(0) ||
+                             hzm > T(0);
+            if (fc < thr2ds && pos) {
+                const double Dx = g.dx, Dy = g.dy, Dz = g.dz;
+                const double c0 = fc, xp = fxp, xm = fxm, yp = fyp, ym = fym, zp = fzp, zm = fzm;
+                const double gx = (xp - xm) / (2 * Dx), gy = (yp - ym) / (2 * Dy), gz = (zp - zm) / (2 * Dz);
+                const double g2 = fmax(sqrt(gx * gx + gy * gy + gz * gz), 1e-14);
+                const double l = (xp - 2 * c0 + xm) / (Dx * Dx) + (yp - 2 * c0 + ym) / (Dy * Dy) +
+                                 (zp - 2 * c0 + zm) / (Dz * Dz);
+                const double q0 = fmax(c0, 0.0);
+                const double qxp = fmax(xp, 0.0), qxm = fmax(xm, 0.0), qyp = fmax(yp, 0.0), qym = fmax(ym, 0.0);
+                const double qzp = fmax(zp, 0.0), qzm = fmax(zm, 0.0);
+                const double d = (qxp - qxm) / (2 * Dx) * gx + (qyp - qym) / (2 * Dy) * gy + (qzp - qzm) / (2 * Dz) * gz;
+                const double pl = (qxp - 2 * q0 + qxm) / (Dx * Dx) + (qyp - 2 * q0 + qym) / (Dy * Dy) +
+                                  (qzp - 2 * q0 + qzm) / (Dz * Dz);
+                const double gg = g2 * g2;
+                const double h64 = d / gg;
+                if (fabs(fc) < thr2ds) area = pl / gg - d * l / (gg * gg);
+                if (h64 == 0.0) {
                     unit = true;
-                    vol = 0.0;
+                } else {
+                    vol = 1 - h64;
+                    if (vol == 1.0) {
+                        unit = true;
+                        vol = 0.0;
+                    }
+                }
+            } else if (fc < thr2ds) {
+                unit = true;  // no positive value among the seven: Heaviside 0, Dirac 0
+            }
+        } else {
+            if (fabs(fc) < thr2ds) area = (double)delta;
+            if (fc < thr2ds) {
+                // 1 - heav in FP64; heav == 0 (no positive neighbour) gives exactly 1
+                if (heav == T(0)) {
+                    unit = true;
+                } else {
+                    vol = 1 - (double)heav;
+                    if (vol == 1.0) {
+                        unit = true;
+                        vol = 0.0;
+                    }
                 }
             }
         }

@@ -218,6 +218,24 @@ class SDF3:
                    *self.GD3.args(), _ptr(ws), ws.numel(), _stream())
         return out
 
+    def WENO5RK3ReinitializationTol(self, F, max_iters: int, tol: float, band: float | None = None,
+                                    history: bool = True):
+        """WENO5RK3Reinitialization run until its residual is at most `tol` (no counterpart in
+        the reference, whose loop runs a fixed count): the FP64 maximum over |F| < band
+        (default 3 Ds) of | |grad F|_G - 1 |, tested on the device after every pseudo-step,
+        at most `max_iters` pseudo-steps.  Returns (F, status, residual) as device tensors:
+        status = [pseudo-steps taken, 1 if converged], residual[n] after n pseudo-steps
+        (entries past the stop stay NaN), or None with history=False."""
+        out = self._field(F).clone()
+        ws = self.workspace("reinit_tol")
+        band = 3 * self.GD3.Ds if band is None else float(band)
+        status = torch.zeros(2, dtype=torch.int32, device="cuda")
+        res = torch.full((int(max_iters) + 1,), float("nan"), dtype=torch.float64, device="cuda") if history else None
+        lib().call(self._fn("vsl_weno5_rk3_reinitialization_tol"), _ptr(out), int(max_iters), float(tol), band,
+                   *map(_ptr, self._dist()), *self.GD3.args(), _ptr(status), _ptr(res), _ptr(ws), ws.numel(),
+                   _stream())
+        return out, status, res
+
     def WENORK3Reinitialization(self, F, iteration: int):
         """WENORK3Reinitialization.m:3-61 (cubic distances recomputed from F)."""
         out = self._field(F).clone()

@@ -144,12 +144,42 @@ def vesicle_256(n: int = 256, seed: int = 0, reduced_volume: float = 0.65, pages
     return x, y, z, noisy_oblate(x, y, z, axes=(1.0, 1.0, c), seed=seed)
 
 
-def oblate_ellipsoid(size=(96, 96, 96), reduced_volume: float = 0.6, ratio: float = 0.35, device=None):
-    """The relaxation driver's initial shape, SD.Shape.Ellipsoid(size, rv, 'O', ratio)
-    (Ellipsoid.m:7-47, p00_test_singlephase_relax.m:24): x = linspace(-1, 1, size[0]),
-    y and z centred on 0 with the same spacing ((1-n)/2 : (n-1)/2 times dx), half axes
-    a = b = 2 ratio and c = a cq, cq interpolated linearly in the table of reduced volumes
-    of (1, 1, c) at c = 0.01 : 0.01 : 0.99.  Returns x, y, z and the field."""
+def ellipsoid_reduced_volume(a: float, b: float, c: float) -> float:
+    """Reduced volume (3V/4pi)(4pi/A)^(3/2) of the ellipsoid with half axes a >= b >= c
+    (Ellipsoid.m:74-85).  The area is Legendre's form 2 pi c^2 + 2 pi a b (E(phi, m) sin^2 phi
+    + F(phi, m) cos^2 phi) / sin phi with cos phi = c / a; as in the reference, the value
+    k = a sqrt(b^2 - c^2) / (b sqrt(a^2 - c^2)) is passed as the integrals' second argument
+    (the parameter m of MATLAB's ellipticE/ellipticF and of scipy's ellipeinc/ellipkinc).
+    Both branches the reference uses have k = 0 (prolate, b = c) or k = 1 (oblate, a = b),
+    where the integrals are elementary and taken in closed form; other axes go through
+    scipy."""
+    volume = 4 * math.pi * a * b * c / 3
+    phi = math.atan2(math.sqrt(a * a - c * c), c)
+    cos_phi = c / a
+    sin_phi = math.sqrt(a * a - c * c) / a
+    if b == c:  # k = 0: E(phi, 0) = F(phi, 0) = phi
+        e_int = f_int = phi
+    elif a == b:  # k = 1: E(phi, 1) = sin phi, F(phi, 1) = atanh(sin phi)
+        e_int, f_int = sin_phi, math.atanh(sin_phi)
+    else:
+        from scipy.special import ellipeinc, ellipkinc
+
+        k = a * math.sqrt(b * b - c * c) / b / math.sqrt(a * a - c * c)
+        e_int, f_int = float(ellipeinc(phi, k)), float(ellipkinc(phi, k))
+    area = 2 * math.pi * c * c + 2 * math.pi * a * b * (e_int * sin_phi**2 + f_int * cos_phi**2) / sin_phi
+    return (3 * volume / 4 / math.pi) * (4 * math.pi / area) ** 1.5
+
+
+def ellipsoid(size=(96, 96, 96), reduced_volume: float = 0.6, kind: str = "O", ratio: float = 0.35, device=None):
+    """SD.Shape.Ellipsoid(Size, reducedVolume, TYPE, ratio) (Ellipsoid.m:5-72):
+    x = linspace(-1, 1, size[0]), y and z centred on 0 with the same spacing
+    ((1-n)/2 : (n-1)/2 times dx).  The axis ratio cq is interpolated linearly in the table
+    of reduced volumes at c = 0.01 : 0.01 : 0.99 (interp1 of the reference).
+      kind 'O' (oblate): half axes a = b = ratio (xmax - xmin) = 2 ratio, c = a cq, table of
+        ReducedVolume(1, 1, c); field sqrt(x^2/a^2 + y^2/b^2 + z^2/c^2) - 1.
+      kind 'P' (prolate): a = ratio (zmax - zmin), b = c = a cq, table of
+        ReducedVolume(1, c, c); field sqrt(x^2/b^2 + y^2/c^2 + z^2/a^2) - 1 (long axis z).
+    Returns x, y, z, the field and the half axes (a, b, c)."""
     nx, ny, nz = size
     xv = np.linspace(-1.0, 1.0, nx)
     dx = xv[1] - xv[0]
@@ -157,11 +187,29 @@ def oblate_ellipsoid(size=(96, 96, 96), reduced_volume: float = 0.6, ratio: floa
     zv = (np.arange(nz) + (1 - nz) / 2.0) * dx
     x, y, z = meshgrid(xv, yv, zv, device=device)
     cs = np.arange(1, 100) / 100.0
-    rv = np.array([oblate_reduced_volume(c) for c in cs])
-    a = ratio * 2.0
-    c = a * float(np.interp(reduced_volume, rv, cs))
+    kind = kind.upper()[:1]
     xp = _Ops(x)
-    return x, y, z, xp.fortran(xp.sqrt(x**2 / a**2 + y**2 / a**2 + z**2 / c**2) - 1)
+    if kind == "O":
+        rv = np.array([ellipsoid_reduced_volume(1.0, 1.0, c) for c in cs])
+        a = ratio * 2.0
+        b = a
+        c = a * float(np.interp(reduced_volume, rv, cs))
+        f = xp.sqrt(x**2 / a**2 + y**2 / b**2 + z**2 / c**2) - 1
+    elif kind == "P":
+        rv = np.array([ellipsoid_reduced_volume(1.0, c, c) for c in cs])
+        a = ratio * (float(zv[-1]) - float(zv[0]))
+        b = a * float(np.interp(reduced_volume, rv, cs))
+        c = b
+        f = xp.sqrt(x**2 / b**2 + y**2 / c**2 + z**2 / a**2) - 1
+    else:
+        raise ValueError("kind must be 'O' (oblate) or 'P' (prolate)")
+    return x, y, z, xp.fortran(f), (a, b, c)
+
+
+def oblate_ellipsoid(size=(96, 96, 96), reduced_volume: float = 0.6, ratio: float = 0.35, device=None):
+    """The relaxation driver's initial shape, SD.Shape.Ellipsoid(size, rv, 'O', ratio)
+    (p00_test_singlephase_relax.m:24); see `ellipsoid`.  Returns x, y, z and the field."""
+    return ellipsoid(size, reduced_volume, "O", ratio, device)[:4]
 
 
 def surface_field(x, y, z):

@@ -24,6 +24,8 @@ import subprocess
 import sys
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -43,6 +45,10 @@ BYTES_ADVECT = 17 * W32
 # toolbox + reductions 1w, plus a second setDistance 7w)
 BYTES_SETUP = (7 + 10 + 13 + 1 + 7) * W32
 BYTES_PER_NODE_STEP = EXT * BYTES_EXTEND + ADV * BYTES_ADVECT + RE * BYTES_REINIT + BYTES_SETUP
+# the same per node for FP64 fields (w = 8), and a reinitialization pseudo-step's alone
+W64 = 8
+BYTES_PER_NODE_STEP64 = EXT * 56 * W64 + ADV * 17 * W64 + RE * (29 * W64 + 3) + (7 + 10 + 13 + 1 + 7) * W64
+BYTES_REINIT64 = 29 * W64 + 3
 # kernels launched per vesicle step: toolbox, sum, classify, velocity (uniform nodes and
 # the flagged list), crossing, 3*EXT extension stages each with its band kernel, band
 # max, time step, 3 advection stages, setDistance (scan + roots), classify, 3*RE
@@ -83,16 +89,42 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "extend_stage_f32_256.md")
+def profiled(summary: str, key: str):
+    """A per-launch figure from a committed one-kernel ncu summary (`key: value` lines of
+    profiles/<summary>): DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) or warp
+    instructions (smsp__inst_executed.sum) of one 256^3 launch."""
+    path = os.path.join(ROOT, "profiles", summary)
     try:
         for line in open(path):
-            if line.startswith("dram_bytes_per_launch_256:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":", 1)[1].split()[0])
     except OSError:
         pass
     return None
+
+
+def stage_roofline(name, kernel, stage_ms, alg_bytes, summary, hbm, peak_kind, sm_mhz, sms):
+    """Roofline entry of one tiled stage (tiled launch plus its band launch), timed live:
+    the effective fraction (the reference dataflow's algorithmic bytes over the time), the
+    DRAM fraction (the bytes ncu measured for one launch over the time) and the issue
+    fraction (the launch's warp instructions over the issue slots of the time: SMs x 4
+    schedulers x the sampled SM clock)."""
+    traffic = profiled(summary, "dram_bytes_per_launch_256")
+    winst = profiled(summary, "warp_instructions_per_launch_256")
+    sec = stage_ms / 1e3
+    achieved = alg_bytes / sec / 1e9
+    out = {"kernel": kernel, "stage_ms": stage_ms, "algorithmic_bytes_per_launch": alg_bytes, "achieved": achieved,
+           "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
+           "frac_kind": "effective (algorithmic bytes of the reference dataflow over the time)",
+           "traffic": traffic, "traffic_source": f"ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/{summary}"}
+    if traffic is not None:
+        out["dram_gbs"] = traffic / sec / 1e9
+        out["dram_frac"] = out["dram_gbs"] / hbm
+    if winst is not None and sm_mhz:
+        out["warp_instructions_per_launch"] = winst
+        out["issue_frac"] = winst / (sms * 4 * sm_mhz * 1e6) / sec
+        out["issue_basis"] = f"{sms} SMs x 4 schedulers x {sm_mhz:.0f} MHz (median SM clock sampled in the timed region)"
+    return out
 
 
 class ClockSampler:
@@ -243,8 +275,158 @@ def run_reference(args, rank, world):
         "cpu_baseline": {**base, "value": v, "nproc": os.cpu_count(), "cpu_model": cpu_model()},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
+        "cpu_configs": cpu_configs(),
     }
+    # beside the CPU path (the line's value): the reference's own kernels on the GPU
+    try:
+        line["reference_gpu"] = reference_gpu_measure()
+    except Exception as e:  # no GPU, or the driver refused the module
+        line["reference_gpu"] = {"unavailable": f"{type(e).__name__}: {e}"}
     print(json.dumps(line), flush=True)
+
+
+def config_cases(S, device, count: int = 3):
+    """The three workload sizes of the comparison of forms: (name, grid edge, x, y, z, F,
+    operation, pseudo-steps, Gpt per node).  64^3: the reinitialization workload (the
+    perturbed sphere on [-1, 1]^3, setDistance and 100 WENO5 TVD-RK3 pseudo-steps); 128^3:
+    one vesicle step of the noisy oblate (axes 1, 1, 0.55) on [-1.5, 1.5]^3; 256^3: one
+    vesicle step of the headline workload."""
+    out = []
+    x, y, z = S.meshgrid(*(np.linspace(-1.0, 1.0, 64),) * 3, device=device)
+    F = (torch_sqrt(x, y, z) - 0.6) * (0.1 + (x - 0.35) ** 2 + (y - 0.35) ** 2 + (z - 0.35) ** 2)
+    out.append(("reinit_64", 64, x, y, z, F, "reinit", 100, 100))
+    x, y, z = S.meshgrid(*(np.linspace(-1.5, 1.5, 128),) * 3, device=device)
+    out.append(("step_128", 128, x, y, z, S.noisy_oblate(x, y, z, axes=(1.0, 1.0, 0.55), seed=0), "step", 1,
+                GPT_PER_NODE))
+    if count > 2:
+        x, y, z, F = S.vesicle_256(N, seed=0, device=device)
+        out.append(("step_256", N, x, y, z, F, "step", 1, GPT_PER_NODE))
+    return out
+
+
+def torch_sqrt(x, y, z):
+    return (x**2 + y**2 + z**2) ** 0.5
+
+
+def forms_measure(torch, pkg, S, fp64_reps: int = 3):
+    """This library's FP32 and FP64 forms at the three workload sizes of config_cases, each
+    timed with CUDA events (FP32 over 5 runs, FP64 over `fp64_reps`), as Gpt/s and FP64
+    algorithmic HBM GB/s (the reference dataflow's bytes, w = 8, over the time)."""
+    out = {}
+    stream = torch.cuda.current_stream()
+    for name, n, x, y, z, F, op, iters, gpt in config_cases(S, "cuda"):
+        h = float(x[0, 1, 0] - x[0, 0, 0])
+        grid = pkg.GD3(x, y, z, spacing=(h, h, h))
+        grid.X = grid.Y = grid.Z = None
+        rec = {"grid": [n, n, n]}
+        for prec, reps in (("f32", 5), ("f64", fp64_reps)):
+            m = pkg.SDF3(grid, Val=F, precision=prec)
+            m.setDistance()
+            F0, d0 = m.F.clone(), [t.clone() for t in m._dist()]
+
+            def once():
+                if op == "reinit":
+                    m.setDistance()
+                    m.WENO5RK3Reinitialization(m.F, iters)
+                else:
+                    m.vesicle_step(EXT, RE, CFL)
+
+            once()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            total = 0.0
+            for _ in range(reps):
+                m.F.copy_(F0)
+                for t, s0 in zip(m._dist(), d0):
+                    t.copy_(s0)
+                torch.cuda.synchronize()
+                a.record(stream)
+                once()
+                b.record(stream)
+                torch.cuda.synchronize()
+                total += a.elapsed_time(b)
+            ms = total / reps
+            nodes = n**3
+            rate = gpt * nodes / (ms / 1e3) / 1e9
+            bytes_node = iters * BYTES_REINIT64 if op == "reinit" else BYTES_PER_NODE_STEP64
+            rec[prec] = {"ms": ms, "value": rate, "unit": UNIT}
+            if prec == "f64":
+                rec[prec]["hbm_gbs_algorithmic_fp64"] = bytes_node * nodes / (ms / 1e3) / 1e9
+            del m, F0, d0
+            torch.cuda.empty_cache()
+        rec["ratio_fp32_over_fp64"] = rec["f32"]["value"] / rec["f64"]["value"]
+        out[name] = rec
+    return out
+
+
+def reference_gpu_measure(reps: int = 2) -> dict:
+    """The reference's own CUDA kernels on the GPU (oracle/refgpu.py: the reference's .cu
+    files compiled for sm_103a with its Makefile flags, launched with its geometry, the
+    MATLAB glue as torch FP64 operations) at the three workload sizes of config_cases."""
+    import torch
+
+    from oracle import refgpu
+
+    if not refgpu.available():
+        return {"unavailable": "the reference's PTX is built from the reference checkout, absent on this machine"}
+    S = importlib.import_module(PKG + ".shapes")
+    K = refgpu.RefKernels()
+    out = {"form": "the reference's FP64 kernels, reference launch geometry, torch FP64 glue"}
+    stream = torch.cuda.current_stream()
+    for name, n, x, y, z, F, op, iters, gpt in config_cases(S, "cuda"):
+        h = float(x[0, 1, 0] - x[0, 0, 0])
+        R = refgpu.RefGpu(refgpu.Grid(n, n, n, h, h, h), K)
+        F = refgpu.field(F)
+        del x, y, z
+        d = R.set_distance(F)
+
+        def once():
+            if op == "reinit":
+                R.reinit_weno5(F, iters, R.set_distance(F))
+            else:
+                R.vesicle_step(F, d, EXT, RE, CFL)
+
+        once()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            once()
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / reps
+        out[name] = {"grid": [n, n, n], "ms": ms, "value": gpt * n**3 / (ms / 1e3) / 1e9, "unit": UNIT}
+        del R, F, d
+        torch.cuda.empty_cache()
+    return out
+
+
+def cpu_configs(seconds: float = 6.0) -> dict:
+    """The oracle (the reference kernels' arithmetic, all host threads) on the two smaller
+    workloads of config_cases: the 64^3 reinitialization (100 pseudo-steps) and the 128^3
+    vesicle step, each run at least once and for about `seconds`."""
+    from oracle import build_oracle
+    from oracle import oracle as O
+
+    build_oracle.build_port()
+    S = importlib.import_module(PKG + ".shapes")
+    K = O.kernels("port")
+    out = {}
+    for name, n, x, y, z, F, op, iters, gpt in config_cases(S, None, count=2):
+        F = O.F64(F)
+        g = O.grid_from_mesh(x, y, z)
+        runs, t0 = 0, time.perf_counter()
+        while True:
+            if op == "reinit":
+                O.reinit_weno5(K, g, F, iters, O.set_distance(K, g, F))
+            else:
+                O.vesicle_step(K, g, F, O.set_distance(K, g, F), EXT, RE, CFL)
+            runs += 1
+            el = time.perf_counter() - t0
+            if el >= seconds:
+                break
+        out[name] = {"grid": [n, n, n], "runs": runs, "value": gpt * n**3 * runs / el / 1e9, "unit": UNIT}
+    return out
 
 
 def profile_case(which, m, torch):
@@ -270,10 +452,12 @@ def profile_case(which, m, torch):
 def batched_measure(torch, pkg, S, steps: int, seed: int = 0, tune: bool = True):
     """The batched workload: 64 vesicles with node counts per axis drawn from
     {48, 64, 96, 128, 160} and half axes U[0.4, 1.0], FP32, advanced `steps` vesicle steps
-    as one CUDA graph per batch step (parallel branches) and, for comparison, by the
-    per-vesicle launch loop; with `tune`, pages per block of the tiled kernels are first
-    autotuned (VesicleBatch.autotune: the configuration with the fastest graph step), and
-    the loop runs with the per-shape choices, its own best."""
+    with each RK stage of all the vesicles as one persistent launch (step_batched, a graph
+    per batch step) and, for comparison, as one CUDA graph of parallel per-vesicle branches
+    and by the per-vesicle launch loop.  With `tune`, pages per block of the tiled kernels
+    are first autotuned for the batched step (VesicleBatch.autotune, mode "batched"); the
+    branch graph runs with the same table and the loop with the per-shape choices, its own
+    best."""
     B = importlib.import_module(PKG + ".batch")
     maps = []
     for xv, yv, zv, axes in S.random_vesicles(64, seed=seed):
@@ -289,8 +473,8 @@ def batched_measure(torch, pkg, S, steps: int, seed: int = 0, tune: bool = True)
     nodes = batch.nodes()
     out = {"vesicles": len(maps), "nodes": nodes, "steps": steps}
     if tune:
-        out["autotune"] = batch.autotune(candidates=(8, 16, 20, 25, 32, 64))
-    for name, fn in (("graph", batch.step), ("loop", batch.step_loop)):
+        out["autotune"] = batch.autotune(candidates=(4, 8, 16, 20, 25, 32, 64), mode="batched")
+    for name, fn in (("batched_stages", batch.step_batched), ("graph", batch.step), ("loop", batch.step_loop)):
         if tune and name == "loop":
             # the launch loop runs one vesicle at a time: the per-shape choices (each shape
             # timed alone) are its tuning
@@ -307,6 +491,7 @@ def batched_measure(torch, pkg, S, steps: int, seed: int = 0, tune: bool = True)
         ms = a.elapsed_time(b) / steps
         out[name] = {"ms_per_step": ms, "value": GPT_PER_NODE * nodes / (ms / 1e3) / 1e9, "unit": UNIT}
     out["speedup_graph_over_loop"] = out["loop"]["ms_per_step"] / out["graph"]["ms_per_step"]
+    out["speedup_batched_over_loop"] = out["loop"]["ms_per_step"] / out["batched_stages"]["ms_per_step"]
     # the flow is explicit: vesicles whose time step fell below the parabolic limit can
     # blow up (FP32 overflow gives NaN); count the ones still finite
     out["finite_vesicles"] = sum(int(bool(torch.all(torch.isfinite(m.F)))) for m in maps)
@@ -742,10 +927,33 @@ def main():
         torch.cuda.synchronize()
         return a.elapsed_time(b) / reps
     stage_ms = (t_ext(EXT) - t_ext(0)) / (3 * EXT)
+
+    # the second dominant kernel: the FP32 reinitialization stage (tiled launch and the band
+    # launch that follows it), timed the same way over 60 launches
+    R = m.F.clone()
+
+    def t_re(iters, reps=3):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            m.WENO5RK3Reinitialization(R, iters)
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    t_re(RE)
+    re_stage_ms = (t_re(RE) - t_re(0)) / (3 * RE)
+    del R
     hbm, peak_kind = peaks()
-    alg_bytes_launch = BYTES_EXTEND / 3 * N**3
-    achieved = alg_bytes_launch / (stage_ms / 1e3) / 1e9
-    traffic = profiled_traffic()
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    sm_mhz = clk.summary()["sm_mhz"]
+    ext_roof = stage_roofline("extension", "one FP32 WENO5 RK3 extension stage: k_stage_tiled<SK_EXTEND> + "
+                              "k_band_stage<SK_EXTEND> (side stream)", stage_ms, BYTES_EXTEND / 3 * N**3,
+                              "extend_stage_f32_256.md", hbm, peak_kind, sm_mhz, sms)
+    re_roof = stage_roofline("reinitialization", "one FP32 WENO5 RK3 reinitialization stage: k_stage_tiled<SK_REINIT> "
+                             "+ k_band_stage<SK_REINIT>", re_stage_ms, BYTES_REINIT / 3 * N**3,
+                             "reinit_stage_f32_256.md", hbm, peak_kind, sm_mhz, sms)
 
     # end to end through the public API with host buffers: H2D of F, setDistance, one
     # vesicle step, D2H of F and of [area, volume, dt, max|Vn|]
@@ -767,24 +975,17 @@ def main():
     e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, dist, "cuda")
     e2e_val = whole_job_gpt_s(world, gpt_step, e2e_s)
 
-    # the plain FP64 form of the same step, for the FP32/FP64 throughput ratio
-    fp64 = None
-    if not args.no_fp64:
-        F0 = S.vesicle_256(N, seed=replica_seed(rank), device="cuda")[3]
-        m64 = pkg.SDF3(grid, Val=F0, precision="f64")
-        del F0
-        m64.setDistance()
-        m64.vesicle_step(EXT, RE, CFL)
-        torch.cuda.synchronize()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        m64.vesicle_step(EXT, RE, CFL)
-        b.record(stream)
-        torch.cuda.synchronize()
-        ms64 = a.elapsed_time(b)
-        fp64 = {"value": gpt_step / (ms64 / 1e3) / 1e9, "unit": UNIT, "ms_per_step": ms64,
-                "ratio_fp32_over_fp64": (gpt_step / (ms / 1e3)) / (gpt_step / (ms64 / 1e3))}
-        del m64
+    # the plain FP64 form of the same step over three steps (FP32/FP64 ratio, FP64 HBM GB/s),
+    # and both forms at the reinitialization workload (64^3) and the 128^3 vesicle step
+    fp64, forms = None, None
+    if not args.no_fp64 and rank == 0:
+        torch.cuda.empty_cache()
+        forms = forms_measure(torch, pkg, S)
+        f = forms["step_256"]["f64"]
+        fp64 = {"value": f["value"], "unit": UNIT, "ms_per_step": f["ms"], "steps_timed": 3,
+                "hbm_gbs_algorithmic_fp64": f["hbm_gbs_algorithmic_fp64"],
+                "hbm_frac_algorithmic_fp64": f["hbm_gbs_algorithmic_fp64"] / peaks()[0],
+                "ratio_fp32_over_fp64": (gpt_step / (ms / 1e3)) / (gpt_step / (f["ms"] / 1e3))}
 
     batched = None
     if not args.no_batched and rank == 0:
@@ -821,14 +1022,11 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(world),
-        "roofline": {"bound": "hbm",
-                     "kernel": "one FP32 WENO5 RK3 extension stage: k_stage_tiled<SK_EXTEND> + k_band_stage<SK_EXTEND>",
-                     "achieved": achieved, "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": traffic,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_stage_tiled<SK_EXTEND> at 256^3 (band launch not included)",
-                     "stage_ms": stage_ms,
-                     "algorithmic_bytes_per_launch": alg_bytes_launch,
-                     "effective": "fused stage reads fewer bytes than the reference dataflow counts"},
+        "roofline": {"bound": "hbm", **ext_roof,
+                     "note": "bound and frac on the dominant kernel as the reference dataflow counts bytes "
+                             "(effective); the kernels are instruction-issue bound: see dram_frac and issue_frac, "
+                             "and the second dominant kernel under 'reinitialization'",
+                     "reinitialization": re_roof},
         "step_hbm": {"algorithmic_bytes_per_step": BYTES_PER_NODE_STEP * N**3,
                      "achieved_gbs": BYTES_PER_NODE_STEP * N**3 / (ms / 1e3) / 1e9,
                      "frac": BYTES_PER_NODE_STEP * N**3 / (ms / 1e3) / 1e9 / hbm,
@@ -842,6 +1040,7 @@ def main():
         "clocks": clk.summary(),
         "autotune": tuning,
         "fp64_plain": fp64,
+        "forms": forms,
         "batched": batched,
         "precision": precision,
         "differentiation": differentiation,

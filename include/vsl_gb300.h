@@ -185,7 +185,8 @@ enum {
     VSL_OP_SMOOTH = 15,
     VSL_OP_RELAX_STEP = 16,
     VSL_OP_AUX_TOOLBOX = 17,
-    VSL_OP_MASKED_INTEGRAL = 18
+    VSL_OP_MASKED_INTEGRAL = 18,
+    VSL_OP_REINIT_TOL = 19
 };
 
 /* Tuning of the FP32 tiled stage kernels (no counterpart in the reference).  Each block
@@ -223,6 +224,31 @@ int vsl_weno5_rk3_reinitialization_f32(float *F, int iteration, const float *xpr
                                        const float *ypf, const float *ypb, const float *zpu, const float *zpd,
                                        int rows, int cols, int pges, double dx, double dy, double dz,
                                        void *workspace, size_t workspace_bytes, vsl_stream_t stream);
+
+/* The reinitialization of vsl_weno5_rk3_reinitialization_* run until its residual is small
+ * (no counterpart in the reference, whose loop runs a fixed count,
+ * +SD/@SDF3/WENO5RK3Reinitialization.m:15; the fixed-count entry point above stays the
+ * drop-in).  The residual is the FP64 maximum, over the nodes with |F| < band that are not
+ * fixed, of | |grad F|_G - 1 |, with the Godunov norm and stencil choice of the
+ * pseudo-step.  Pseudo-steps run while the residual exceeds tol and fewer than max_iters
+ * were taken; the test runs on the device (a CUDA graph with a conditional loop node), so
+ * the call neither waits nor reads back.  Results on the device: status[0] = pseudo-steps
+ * taken, status[1] = 1 if the last residual is <= tol (0: stopped by max_iters; a NaN
+ * residual never converges); residual[n] (optional, max_iters + 1 doubles) = the residual
+ * after n pseudo-steps, residual[0] that of the input.  Each call records and instantiates a
+ * small graph (driver resources, no device-memory allocation of its own); called while the
+ * caller's stream is being captured, it adds its nodes to the caller's graph instead.
+ * VSL_ERR_VALUE for max_iters < 0, tol < 0 or band <= 0.  Workspace op VSL_OP_REINIT_TOL. */
+int vsl_weno5_rk3_reinitialization_tol_f64(double *F, int max_iters, double tol, double band, const double *xpr,
+                                           const double *xpl, const double *ypf, const double *ypb,
+                                           const double *zpu, const double *zpd, int rows, int cols, int pges,
+                                           double dx, double dy, double dz, int *status, double *residual,
+                                           void *workspace, size_t workspace_bytes, vsl_stream_t stream);
+int vsl_weno5_rk3_reinitialization_tol_f32(float *F, int max_iters, double tol, double band, const float *xpr,
+                                           const float *xpl, const float *ypf, const float *ypb, const float *zpu,
+                                           const float *zpd, int rows, int cols, int pges, double dx, double dy,
+                                           double dz, int *status, double *residual, void *workspace,
+                                           size_t workspace_bytes, vsl_stream_t stream);
 
 /* ref: +SD/@SDF3/WENORK3Reinitialization.m:3-61 (cubic distances recomputed from F). */
 int vsl_wenork3_reinitialization_f64(double *F, int iteration, int rows, int cols, int pges, double dx, double dy,
@@ -309,6 +335,26 @@ int vsl_vesicle_step_f32(float *F, float *xpr, float *xpl, float *ypf, float *yp
                          int ext_iters, int reinit_iters, double cfl, double *info, int rows, int cols, int pges,
                          double dx, double dy, double dz, void *workspace, size_t workspace_bytes,
                          vsl_stream_t stream);
+
+/* A batch of vesicle steps, FP32 mixed form (no counterpart in the reference, which
+ * advances one vesicle per MATLAB process).  Every vesicle gets the step of
+ * vsl_vesicle_step_f32 (its own field, cached distances, info output and workspace of
+ * vsl_workspace_bytes(VSL_OP_VESICLE_STEP, its grid, 4)); each RK stage of all the
+ * vesicles runs as one persistent launch over all their tiles, 64 vesicles at a time, and
+ * the per-vesicle set-up passes stay per vesicle.  Results are bitwise those of
+ * vsl_vesicle_step_f32 called per vesicle.  `vesicles` is a HOST array read during the
+ * call; the pointers in it are device pointers. */
+typedef struct {
+    float *F;
+    float *xpr, *xpl, *ypf, *ypb, *zpu, *zpd;
+    double *info; /* [area, volume, dt, max |Vn|] */
+    int rows, cols, pges;
+    double dx, dy, dz;
+    void *workspace;
+    size_t workspace_bytes;
+} vsl_vesicle_f32;
+int vsl_vesicle_step_batch_f32(const vsl_vesicle_f32 *vesicles, int count, int ext_iters, int reinit_iters,
+                               double cfl, vsl_stream_t stream);
 
 /* ref: +SD/@SDF3/ENORK2Reinitialization.m:3-45.  Quadratic-ENO distances recomputed from
  * F, then `iteration` Heun RK2 pseudo-steps F1 = F - step(F), F = (F + F1 - step(F1)) / 2

@@ -239,6 +239,44 @@ def reinit_weno5(K, g: Grid, F, iteration: int, dist: Distances):
     return F
 
 
+def reinit_residual(K, g: Grid, F, mask, dist: Distances, band: float) -> float:
+    """Residual of the reinitialization at F: the maximum over the nodes with |F| < band of
+    | |grad F|_G - 1 |, the Godunov norm of re_step (re_step.cu:382-392) with the call's
+    mask, recovered as |step| / deltat (deltat = 0.3 min_dist); fixed nodes (step 0) count 0.
+    No counterpart in the reference, whose loop runs a fixed count."""
+    F = F64(F)
+    deltat = F64(0.3 * dist.min_dist)
+    step = zeros(g)
+    K.re_step(step, F, mask, deltat, *dist.six(), *g.args(), g.num_ele)
+    sel = (np.abs(F) < band) & (deltat > 0)
+    if not np.any(sel):
+        return 0.0
+    r = np.abs(step[sel]) / deltat[sel]
+    return float(np.inf) if np.any(np.isnan(r)) else float(np.max(r))
+
+
+def reinit_weno5_tol(K, g: Grid, F, max_iters: int, tol: float, band: float, dist: Distances):
+    """WENO5RK3Reinitialization run while the residual exceeds tol, at most max_iters
+    pseudo-steps (mask = F < 0 on entry, the cached distances).  Returns (F, steps taken,
+    converged, residual history [0..steps])."""
+    F = F64(F).copy(order="F")
+    mask = np.asfortranarray(F < 0)
+    deltat = F64(0.3 * dist.min_dist)
+    step = zeros(g)
+
+    def stage(Fs):
+        K.re_step(step, F64(Fs), mask, deltat, *dist.six(), *g.args(), g.num_ele)
+        return step.copy(order="F")
+
+    hist = [reinit_residual(K, g, F, mask, dist, band)]
+    n = 0
+    while hist[-1] > tol and n < max_iters:
+        F = F64(_rk3(F, stage))
+        n += 1
+        hist.append(reinit_residual(K, g, F, mask, dist, band))
+    return F, n, hist[-1] <= tol, hist
+
+
 def reinit_eno3(K, g: Grid, F, iteration: int):
     """WENORK3Reinitialization(F, iteration): cubic distances recomputed from F."""
     F = F64(F).copy(order="F")

@@ -36,3 +36,115 @@ def test_batch_graph_matches_loop(pkg, vsl, precision):
         assert np.array_equal(host(m1.F), host(m2.F))
     # anisotropic grids really are anisotropic
     assert len({m.GD3.Size for m in loop.maps}) > 1
+
+
+def oracle_steps(O, K, x, y, z, F, steps, ext, re):
+    g = O.grid_from_mesh(x, y, z)
+    d = O.set_distance(K, g, F)
+    for _ in range(steps):
+        F, d, info = O.vesicle_step(K, g, F, d, ext, re, 0.5)
+    return g, F, info
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_batch_members_match_the_oracle(pkg, vsl, oracle_mod, precision):
+    """Every member of a graph-replayed batch against the oracle's steps of the same vesicle:
+    bitwise against the oracle built with integer powers rounded once (FP64 form), within
+    1e-5 dx over the band |phi| < 3 dx (FP32 form)."""
+    O = oracle_mod
+    K = O.kernels("port_crpow")
+    vs = S.random_vesicles(3, seed=5, edges=(24, 32, 40))
+    fields = [S.ellipsoid_field(xv, yv, zv, axes) for xv, yv, zv, axes in vs]
+    maps = []
+    for x, y, z, F in fields:
+        m = pkg.SDF3(pkg.GD3(x, y, z), Val=F, precision=precision)
+        m.setDistance()
+        maps.append(m)
+    batch = B.VesicleBatch(maps, streams=2)
+    for _ in range(2):
+        infos = [i.cpu().numpy().copy() for i in batch.step(8, 5, 0.5)]
+    for (x, y, z, F), m, info in zip(fields, maps, infos):
+        g, Fo, oi = oracle_steps(O, K, x, y, z, F, 2, 8, 5)
+        got = host(m.F)
+        if precision == "f64":
+            assert np.array_equal(got, Fo)
+            assert info[2] == oi["dt"]
+        else:
+            band = np.abs(Fo) < 3 * g.dx
+            assert np.max(np.abs(got[band] - Fo[band])) <= 1e-5 * g.dx
+            assert abs(info[2] / oi["dt"] - 1) <= 1e-5
+
+
+def test_edge_mix_with_tuned_pages(pkg, vsl, oracle_mod):
+    """The batched workload's edge mix {48, 64, 96, 128, 160} with a non-default pages-per-block
+    table for every shape (as the autotuner leaves it): the graph replay equals the launch
+    loop bit for bit, and the smallest member (FP32) is within 1e-5 dx of the oracle."""
+    T = importlib.import_module("2018_7_vesicle_gb300.autotune")
+    O = oracle_mod
+    vs = S.random_vesicles(4, seed=7)
+    fields = [S.ellipsoid_field(xv, yv, zv, axes) for xv, yv, zv, axes in vs]
+    shapes = {f[3].shape for f in fields}
+    assert len(shapes) > 1
+    pages = {"reinit": 7, "extend": 13, "advect": 9}
+    try:
+        for sz in shapes:
+            for kind, p in pages.items():
+                T.set_pages(sz, kind, p)
+
+        def make():
+            out = []
+            for x, y, z, F in fields:
+                m = pkg.SDF3(pkg.GD3(x, y, z), Val=F, precision="f32")
+                m.setDistance()
+                out.append(m)
+            return out
+
+        loop = B.VesicleBatch(make(), streams=2)
+        graph = B.VesicleBatch(make(), streams=2)
+        a = [i.cpu().numpy().copy() for i in loop.step_loop(30, 20, 0.5)]
+        b = [i.cpu().numpy().copy() for i in graph.step(30, 20, 0.5)]
+        for u, v in zip(a, b):
+            assert np.array_equal(u, v)
+        for m1, m2 in zip(loop.maps, graph.maps):
+            assert np.array_equal(host(m1.F), host(m2.F))
+        q = min(range(len(fields)), key=lambda t: fields[t][3].size)
+        x, y, z, F = fields[q]
+        g, Fo, oi = oracle_steps(O, O.kernels("port"), x, y, z, F, 1, 30, 20)
+        got = host(graph.maps[q].F)
+        band = np.abs(Fo) < 3 * g.dx
+        err = float(np.max(np.abs(got[band] - Fo[band]))) / g.dx
+        print(f"\nsmallest member {F.shape}: band max {err:.2e} dx")
+        assert err <= 1e-5
+    finally:
+        for sz in shapes:
+            for kind in pages:
+                T.set_pages(sz, kind, 0)
+
+
+@pytest.mark.parametrize("count,edges,iters", [(5, (24, 32, 40), (8, 5)), (66, (16, 20, 24), (4, 3))])
+def test_batched_stages_match_loop(pkg, vsl, count, edges, iters):
+    """vsl_vesicle_step_batch_f32 (each RK stage of all the vesicles as one persistent launch;
+    66 vesicles run as two launches' worth, 64 + 2) gives bitwise the per-vesicle steps,
+    as a graph replay and as direct launches, over two batch steps."""
+    loop = B.VesicleBatch(make_batch_edges(pkg, count, edges), streams=2)
+    graph = B.VesicleBatch(make_batch_edges(pkg, count, edges), streams=2)
+    direct = B.VesicleBatch(make_batch_edges(pkg, count, edges), streams=2)
+    for _ in range(2):
+        a = [i.cpu().numpy().copy() for i in loop.step_loop(*iters, 0.5)]
+        b = [i.cpu().numpy().copy() for i in graph.step_batched(*iters, 0.5)]
+        c = [i.cpu().numpy().copy() for i in direct.step_batched(*iters, 0.5, graph=False)]
+        for u, v, w in zip(a, b, c):
+            assert np.array_equal(u, v) and np.array_equal(u, w)
+    for m1, m2, m3 in zip(loop.maps, graph.maps, direct.maps):
+        f = host(m1.F)
+        assert np.array_equal(f, host(m2.F)) and np.array_equal(f, host(m3.F))
+
+
+def make_batch_edges(pkg, n, edges):
+    maps = []
+    for xv, yv, zv, axes in S.random_vesicles(n, seed=11, edges=edges):
+        x, y, z, F = S.ellipsoid_field(xv, yv, zv, axes)
+        m = pkg.SDF3(pkg.GD3(x, y, z), Val=F, precision="f32")
+        m.setDistance()
+        maps.append(m)
+    return maps

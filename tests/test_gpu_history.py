@@ -3,9 +3,10 @@
 mean curvature, 30 extension + 1 advection (CFL 0.5) + 20 reinitialization pseudo-steps
 per step, after the driver's set-up (setDistance and 500 reinitialization pseudo-steps).
 
-At this size the oracle is too slow for a step-by-step comparison (the FP64 step is
-bitwise equal to the oracle on the smaller grids of test_gpu_methods), so the history is
-checked through properties that hold at any size.  Mean-curvature flow moves the surface
+The first two FP64 steps from the set-up state are compared with the oracle: bitwise
+against the oracle built with integer powers rounded once (the FP64 form's arithmetic),
+area and volume within 1e-14 (fixed-order tree against a correctly rounded sum).  The
+50-step history is checked through properties that hold at any size.  Mean-curvature flow moves the surface
 inward: the enclosed volume shrinks every step and the area shrinks overall.  The
 advective CFL 0.5 time step is above the parabolic stability limit of an explicit
 curvature flow (about dx^2 / 6), so after a few steps a grid-scale oscillation grows until
@@ -25,9 +26,7 @@ STEPS = 50
 N = 128
 
 
-def history(pkg, precision):
-    import torch
-
+def setup(pkg, precision):
     S = importlib.import_module(pkg.__name__ + ".shapes")
     v = np.linspace(-1.5, 1.5, N)
     x, y, z = S.meshgrid(v, v, v, device="cuda")
@@ -40,6 +39,34 @@ def history(pkg, precision):
     m.setDistance()
     m.F = m.WENO5RK3Reinitialization(m.F, 500)
     m.setDistance()
+    return m
+
+
+def test_fp64_steps_match_oracle_128(pkg, vsl, oracle_mod):
+    from gpu_util import host
+
+    O = oracle_mod
+    m = setup(pkg, "f64")
+    h = 3.0 / (N - 1)  # the spacing the level-set object was given
+    g = O.Grid(N, N, N, h, h, h)
+    KC = O.kernels("port_crpow")
+    Fo = host(m.F)
+    do = O.Distances(*(host(t) for t in m._dist()))
+    for _ in range(2):
+        info = m.vesicle_step(30, 20, 0.5).cpu().numpy()
+        Fo, do, oi = O.vesicle_step(KC, g, Fo, do, 30, 20, 0.5)
+        assert abs(info[0] - oi["area"]) <= 1e-14 * oi["area"]
+        assert abs(info[1] - oi["volume"]) <= 1e-14 * oi["volume"]
+        assert info[2] == oi["dt"] and info[3] == oi["vmax"]
+        assert np.array_equal(host(m.F), Fo)
+        for a, b in zip(m._dist(), do.six()):
+            assert np.array_equal(host(a), b)
+
+
+def history(pkg, precision):
+    import torch
+
+    m = setup(pkg, precision)
     rows = []
     for _ in range(STEPS):
         rows.append(m.vesicle_step(30, 20, 0.5).cpu().numpy().copy())
