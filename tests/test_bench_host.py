@@ -20,11 +20,26 @@ def test_step_counts():
     assert bench.LAUNCHES_PER_STEP == 314
 
 
-def test_profiled_traffic_matches_summary():
-    t = bench.profiled_traffic()
-    assert t is not None and 2.5e8 < t < 5e8  # about 20 bytes per node at 256^3
-    with open(os.path.join(ROOT, "profiles", "extend_stage_f32_256.md")) as f:
-        assert any(line.startswith("dram_bytes_per_launch_256:") for line in f)
+def test_profiled_figures_match_summaries():
+    """The per-launch DRAM bytes of both dominant kernels come from their committed ncu
+    summaries (about 20 and 7 bytes per node at 256^3)."""
+    t = bench.profiled("extend_stage_f32_256.md", "dram_bytes_per_launch_256")
+    assert t is not None and 2.5e8 < t < 5e8
+    r = bench.profiled("reinit_stage_f32_256.md", "dram_bytes_per_launch_256")
+    assert r is not None and 5e7 < r < 3e8
+    assert bench.profiled("extend_stage_f32_256.md", "no_such_key") is None
+    assert bench.profiled("no_such_summary.md", "dram_bytes_per_launch_256") is None
+
+
+def test_stage_roofline_fractions():
+    """Effective, DRAM and issue fractions of a stage from its time, its algorithmic bytes,
+    the summary's per-launch figures and the sampled clock."""
+    e = bench.stage_roofline("extension", "k", 0.2, 1.0e9, "extend_stage_f32_256.md", 5000.0, "measured", 2000.0, 100)
+    assert abs(e["achieved"] - 5000.0) < 1e-9 and abs(e["frac"] - 1.0) < 1e-12
+    assert abs(e["dram_gbs"] - e["traffic"] / 0.2e-3 / 1e9) < 1e-6
+    if "warp_instructions_per_launch" in e:
+        slots = 100 * 4 * 2000.0e6 * 0.2e-3
+        assert abs(e["issue_frac"] - e["warp_instructions_per_launch"] / slots) < 1e-12
 
 
 def test_whole_job_throughput():
