@@ -386,9 +386,10 @@ __device__ __forceinline__ void extend_node_mixed(const TiledArgs &a, const Band
                     hs[2] = __ldg(sh.cp.p[2 * ax + 1] + c);
                     hs[1] = shadow_or(sh, a.flags, c - L.stride, p[2]);
                 }
+                // the differences in FP64 (where the digits cancel), the quotients in FP32
                 float dd[6];
 #pragma unroll
-                for (int m = 0; m < 6; ++m) dd[m] = (float)((hs[m + 1] - hs[m]) / (double)G[m]);
+                for (int m = 0; m < 6; ++m) dd[m] = (float)(hs[m + 1] - hs[m]) / G[m];
                 if (ENO3)
                     eno3_nonuniform_pair_dd(G, dd, df[ax], db[ax]);
                 else
@@ -427,10 +428,10 @@ __device__ __forceinline__ void enork2_extend_node_mixed(const TiledArgs &a, con
         const float h2 = h * h;
         const float p2 = v1 - 2.f * v0 + v2;
         float p2m = 0.5f * minmod(p2, v0 - 2.f * v2 + v3) / h2;
-        const float sr = (r1 == h) ? (v2 - v0) / r1 : (float)((__ldg(sh.cp.p[2 * ax] + c) - cs) / (double)r1);
+        const float sr = (r1 == h) ? (v2 - v0) / r1 : (float)(__ldg(sh.cp.p[2 * ax] + c) - cs) / r1;
         df[ax] = sr - r1 * p2m;
         p2m = 0.5f * minmod(p2, v0 - 2.f * v1 + v4) / h2;
-        const float sl = (l1 == h) ? (v0 - v1) / l1 : (float)((cs - __ldg(sh.cp.p[2 * ax + 1] + c)) / (double)l1);
+        const float sl = (l1 == h) ? (v0 - v1) / l1 : (float)(cs - __ldg(sh.cp.p[2 * ax + 1] + c)) / l1;
         db[ax] = sl + l1 * p2m;
     }
     const float step = upwind_dot(__ldg(a.v.p[0] + c), __ldg(a.v.p[1] + c), __ldg(a.v.p[2] + c), df[0], db[0], df[1],

@@ -45,11 +45,16 @@ template <typename T> __device__ __forceinline__ T fourth(T x);
 template <> __device__ __forceinline__ double fourth<double>(double x) { return pow_cr<4>(x); }
 template <> __device__ __forceinline__ float fourth<float>(float x) { return (x * x) * (x * x); }
 
+// reciprocals of the spacings for the mixed form's FP64 area and volume terms
+struct Recips {
+    double i2x, i2y, i2z, ixx, iyy, izz;  // 1 / (2 d), 1 / d^2 per axis
+};
+
 // thr2ds: 2 Ds as the smallest T not below it, so that x < thr2ds in T is exactly
 // (double)x < 2 Ds for every x of type T (the reference's FP64 band tests)
 template <typename T>
 __global__ void __launch_bounds__(NT) k_toolbox(const T *__restrict__ f, ToolboxOut<T> o, Grid g, double ds_,
-                                                T thr2ds, double *__restrict__ partials)
+                                                T thr2ds, double *__restrict__ partials, Recips rc)
 {
     const int i = blockIdx.x * BX + threadIdx.x;
     const int j = blockIdx.y * BY + threadIdx.y;
@@ -107,21 +112,21 @@ __global__ void __launch_bounds__(NT) k_toolbox(const T *__restrict__ f, Toolbox
             const bool pos = hc > T(0) || hxp > T(0) || hxm > T(0) || hyp > T(0) || hym > T(0) || hzp > T(0) ||
                              hzm > T(0);
             if (fc < thr2ds && pos) {
-                const double Dx = g.dx, Dy = g.dy, Dz = g.dz;
+                // FP64 divisions and square roots are slow on this GPU: reciprocals of the
+                // spacings from the host, |grad|^2 clamped instead of |grad|, one division
                 const double c0 = fc, xp = fxp, xm = fxm, yp = fyp, ym = fym, zp = fzp, zm = fzm;
-                const double gx = (xp - xm) / (2 * Dx), gy = (yp - ym) / (2 * Dy), gz = (zp - zm) / (2 * Dz);
-                const double g2 = fmax(sqrt(gx * gx + gy * gy + gz * gz), 1e-14);
-                const double l = (xp - 2 * c0 + xm) / (Dx * Dx) + (yp - 2 * c0 + ym) / (Dy * Dy) +
-                                 (zp - 2 * c0 + zm) / (Dz * Dz);
+                const double gx = (xp - xm) * rc.i2x, gy = (yp - ym) * rc.i2y, gz = (zp - zm) * rc.i2z;
+                const double gg = fmax(gx * gx + gy * gy + gz * gz, 1e-28);
+                const double l = (xp - 2 * c0 + xm) * rc.ixx + (yp - 2 * c0 + ym) * rc.iyy + (zp - 2 * c0 + zm) * rc.izz;
                 const double q0 = fmax(c0, 0.0);
                 const double qxp = fmax(xp, 0.0), qxm = fmax(xm, 0.0), qyp = fmax(yp, 0.0), qym = fmax(ym, 0.0);
                 const double qzp = fmax(zp, 0.0), qzm = fmax(zm, 0.0);
-                const double d = (qxp - qxm) / (2 * Dx) * gx + (qyp - qym) / (2 * Dy) * gy + (qzp - qzm) / (2 * Dz) * gz;
-                const double pl = (qxp - 2 * q0 + qxm) / (Dx * Dx) + (qyp - 2 * q0 + qym) / (Dy * Dy) +
-                                  (qzp - 2 * q0 + qzm) / (Dz * Dz);
-                const double gg = g2 * g2;
-                const double h64 = d / gg;
-                if (fabs(fc) < thr2ds) area = pl / gg - d * l / (gg * gg);
+                const double d = (qxp - qxm) * rc.i2x * gx + (qyp - qym) * rc.i2y * gy + (qzp - qzm) * rc.i2z * gz;
+                const double pl = (qxp - 2 * q0 + qxm) * rc.ixx + (qyp - 2 * q0 + qym) * rc.iyy +
+                                  (qzp - 2 * q0 + qzm) * rc.izz;
+                const double ig = 1.0 / gg;
+                const double h64 = d * ig;
+                if (fabs(fc) < thr2ds) area = (pl - d * l * ig) * ig;
                 if (h64 == 0.0) {
                     unit = true;
                 } else {
@@ -248,7 +253,9 @@ cudaError_t launch_toolbox(const T *phi, ToolboxOut<T> out, const Grid &g, doubl
                            int *nblocks, cudaStream_t s)
 {
     if (nblocks) *nblocks = toolbox_partial_blocks(g);
-    k_toolbox<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, out, g, ds, round_up<T>(2 * ds), partials);
+    const Recips rc{1 / (2 * g.dx), 1 / (2 * g.dy), 1 / (2 * g.dz), 1 / (g.dx * g.dx), 1 / (g.dy * g.dy),
+                    1 / (g.dz * g.dz)};
+    k_toolbox<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, out, g, ds, round_up<T>(2 * ds), partials, rc);
     return cudaGetLastError();
 }
 
