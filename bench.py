@@ -50,11 +50,11 @@ W64 = 8
 BYTES_PER_NODE_STEP64 = EXT * 56 * W64 + ADV * 17 * W64 + RE * (29 * W64 + 3) + (7 + 10 + 13 + 1 + 7) * W64
 BYTES_REINIT64 = 29 * W64 + 3
 # kernels launched per vesicle step: toolbox, sum, classify, velocity (uniform nodes and
-# the flagged list), crossing, 3*EXT extension stages each with its band kernel, band
-# max, time step, 3 advection stages, setDistance (scan + roots), classify, 3*RE
-# reinitialization stages each with its band kernel (memsets of the list counters are
-# not kernels)
-LAUNCHES_PER_STEP = 1 + 1 + 1 + 2 + 1 + 2 * 3 * EXT + 1 + 1 + 3 * ADV + 2 + 1 + 2 * 3 * RE
+# the flagged list), crossing values, the band's FP64 shadow, 3*EXT extension stages each
+# with its band kernel, band max, time step, 3 advection stages, setDistance (scan +
+# roots), classify, 3*RE reinitialization stages each with its band kernel (memsets of the
+# list counters are not kernels)
+LAUNCHES_PER_STEP = 1 + 1 + 1 + 2 + 1 + 1 + 2 * 3 * EXT + 1 + 1 + 3 * ADV + 2 + 1 + 2 * 3 * RE
 
 
 def replica_seed(rank: int) -> int:
