@@ -309,6 +309,11 @@ int check_ws(int op, const Grid &g, int elem, void *ws, size_t bytes)
         cudaError_t e_ = (expr);                                                                                   \
         if (e_ != cudaSuccess) return VSL_ERR_CUDA;                                                                \
     } while (0)
+#define VSL_TRY_CUDA(expr)                                                                                         \
+    do {                                                                                                           \
+        cudaError_t e_ = (expr);                                                                                   \
+        if (e_ != cudaSuccess) return e_;                                                                          \
+    } while (0)
 
 template <typename T> constexpr bool fast_form() { return std::is_same<T, float>::value; }
 
@@ -839,9 +844,80 @@ int op_reinit_tol(T *F, int max_iters, double tol, double band, const T *xpr, co
 // a batch of vesicle steps (FP32): the composite step of op_vesicle_step for every vesicle,
 // with each RK stage of all the vesicles as one persistent launch (launch_tiled_batch); the
 // per-vesicle set-up passes (toolbox, extension velocity and crossing values, time step,
-// setDistance, classification) stay per vesicle.  Vesicles are taken TILED_BATCH_MAX at a
-// time.
+// setDistance, classification) stay per vesicle, spread over BATCH_LANES streams forked
+// from and joined back into the caller's stream (parallel branches under stream capture).
+// Vesicles are taken TILED_BATCH_MAX at a time.
 // ---------------------------------------------------------------------------------------
+constexpr int BATCH_LANES = 8;
+struct BatchLanes {
+    int device;
+    cudaStream_t user;
+    cudaStream_t lane[BATCH_LANES];
+    cudaEvent_t fork, join[BATCH_LANES];
+};
+constexpr int MAX_BATCH_LANE_SETS = 64;
+std::mutex batch_lane_mutex;
+BatchLanes batch_lane_sets[MAX_BATCH_LANE_SETS];
+int n_batch_lane_sets = 0;
+
+// the lanes of (current device, caller stream), created on first use with this thread's
+// capture mode relaxed; nullptr (everything on the caller's stream) when the pool is full or
+// a creation fails
+BatchLanes *batch_lanes(cudaStream_t s)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> lock(batch_lane_mutex);
+    for (int e = 0; e < n_batch_lane_sets; ++e)
+        if (batch_lane_sets[e].device == dev && batch_lane_sets[e].user == s) return &batch_lane_sets[e];
+    if (n_batch_lane_sets == MAX_BATCH_LANE_SETS) return nullptr;
+    BatchLanes ln{};
+    ln.device = dev;
+    ln.user = s;
+    cudaStreamCaptureMode mode = cudaStreamCaptureModeRelaxed;
+    if (cudaThreadExchangeStreamCaptureMode(&mode) != cudaSuccess) return nullptr;
+    bool ok = cudaEventCreateWithFlags(&ln.fork, cudaEventDisableTiming) == cudaSuccess;
+    for (int l = 0; l < BATCH_LANES && ok; ++l) {
+        ok = cudaStreamCreateWithFlags(&ln.lane[l], cudaStreamNonBlocking) == cudaSuccess;
+        ok = ok && cudaEventCreateWithFlags(&ln.join[l], cudaEventDisableTiming) == cudaSuccess;
+    }
+    cudaThreadExchangeStreamCaptureMode(&mode);
+    if (!ok) {
+        for (int l = 0; l < BATCH_LANES; ++l) {
+            if (ln.join[l]) cudaEventDestroy(ln.join[l]);
+            if (ln.lane[l]) cudaStreamDestroy(ln.lane[l]);
+        }
+        if (ln.fork) cudaEventDestroy(ln.fork);
+        return nullptr;
+    }
+    batch_lane_sets[n_batch_lane_sets] = ln;
+    return &batch_lane_sets[n_batch_lane_sets++];
+}
+
+// per-vesicle passes fanned out over the lanes: open() forks them from the caller's stream,
+// lane(v) is vesicle v's stream, close() joins them back
+struct Fan {
+    BatchLanes *ln;
+    cudaStream_t s;
+    cudaError_t open()
+    {
+        if (!ln) return cudaSuccess;
+        VSL_TRY_CUDA(cudaEventRecord(ln->fork, s));
+        for (int l = 0; l < BATCH_LANES; ++l) VSL_TRY_CUDA(cudaStreamWaitEvent(ln->lane[l], ln->fork, 0));
+        return cudaSuccess;
+    }
+    cudaStream_t lane(int v) const { return ln ? ln->lane[v % BATCH_LANES] : s; }
+    cudaError_t close()
+    {
+        if (!ln) return cudaSuccess;
+        for (int l = 0; l < BATCH_LANES; ++l) {
+            VSL_TRY_CUDA(cudaEventRecord(ln->join[l], ln->lane[l]));
+            VSL_TRY_CUDA(cudaStreamWaitEvent(s, ln->join[l], 0));
+        }
+        return cudaSuccess;
+    }
+};
+
 struct BatchMember {
     Grid g;
     float *F;
@@ -882,8 +958,11 @@ int batch_chunk(const vsl_vesicle_f32 *ves, int n, int ext_iters, int reinit_ite
     }
     // per vesicle: toolbox (mean curvature, normals, area, volume), the extension's
     // velocity, classification and crossing values of the mean curvature, its shadow
+    Fan fan{batch_lanes(s), s};
+    VSL_TRY(fan.open());
     for (int v = 0; v < n; ++v) {
         BatchMember &b = m[v];
+        const cudaStream_t s = fan.lane(v);
         const double ds = (b.g.dx + b.g.dy + b.g.dz) / 3;
         ToolboxOut<float> tb{};
         tb.f[4] = b.w.nrm.p[0];
@@ -899,6 +978,7 @@ int batch_chunk(const vsl_vesicle_f32 *ves, int n, int ext_iters, int reinit_ite
         VSL_TRY(launch_shadow_init(b.w.vn, b.w.ext.sh[0], b.w.ext.flagged, s));
         if (int r = band_reset(b.w.ext.band, s)) return r;
     }
+    VSL_TRY(fan.close());
     // extension of the normal speed: each stage of all vesicles as one launch
     for (int it = 0; it < ext_iters; ++it) {
         for (int stage = 0; stage < 3; ++stage) {
@@ -916,13 +996,16 @@ int batch_chunk(const vsl_vesicle_f32 *ves, int n, int ext_iters, int reinit_ite
         }
     }
     // per vesicle: dt = cfl * Ds / max |Vn| over |F| < 2 Ds
+    VSL_TRY(fan.open());
     for (int v = 0; v < n; ++v) {
         BatchMember &b = m[v];
+        const cudaStream_t s = fan.lane(v);
         const double ds = (b.g.dx + b.g.dy + b.g.dz) / 3;
         int nb = 0;
         VSL_TRY(launch_band_maxabs<float>(b.w.vn, b.F, 2 * ds, b.g, b.w.red.partials, &nb, s));
         VSL_TRY(launch_time_step(b.w.red.partials, nb, cfl * ds, b.info + 2, b.info + 3, s));
     }
+    VSL_TRY(fan.close());
     // one WENO5 TVD-RK3 advection step along Vn * N
     for (int stage = 0; stage < 3; ++stage) {
         for (int v = 0; v < n; ++v) {
@@ -935,12 +1018,15 @@ int batch_chunk(const vsl_vesicle_f32 *ves, int n, int ext_iters, int reinit_ite
         VSL_TRY(launch_tiled_batch(2, false, st, grids, n, s));
     }
     // per vesicle: setDistance and the classification of the reinitialization
+    VSL_TRY(fan.open());
     for (int v = 0; v < n; ++v) {
         BatchMember &b = m[v];
+        const cudaStream_t s = fan.lane(v);
         VSL_TRY(launch_set_distance<float>(b.F, b.dist, b.g, true, b.w.edges, s));
         VSL_TRY(launch_classify<float>(b.F, cview(b.dist), b.re.flags, NodeList{nullptr, nullptr}, b.g, s));
         if (int r = band_reset(b.re.band, s)) return r;
     }
+    VSL_TRY(fan.close());
     for (int it = 0; it < reinit_iters; ++it) {
         for (int stage = 0; stage < 3; ++stage) {
             for (int v = 0; v < n; ++v) {
@@ -1244,7 +1330,6 @@ int reinit_stages(const T *F, Ptr6<const T> d, ReinitWork<T> &w, const Grid &g, 
 {
     if constexpr (std::is_same<T, float>::value) {
         if (int st = band_reset(w.band, s)) return st;
-        const Ptr6<const float> none6{};
         const Ptr3<const float> none3{};
         VSL_TRY(tiled(0, false, w.band, F, F, w.b, w.flags, d, BandShadow{}, none3, nullptr, nullptr, 0, g, s));
         VSL_TRY(tiled(0, false, w.band, w.b, F, w.c, w.flags, d, BandShadow{}, none3, nullptr, nullptr, 1, g, s));

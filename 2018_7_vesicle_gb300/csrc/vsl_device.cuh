@@ -332,7 +332,18 @@ __device__ __forceinline__ T weno5_plain(T v1, T v2, T v3, T v4, T v5)
 }
 
 // a / b: the hardware reciprocal-based quotient for float (about 2 ulp), IEEE for double
-__device__ __forceinline__ float fast_div(float a, float b) { return __fdividef(a, b); }
+// The hardware approximate reciprocal (PTX rcp.approx.ftz.f32).  The WENO5 weights and
+// quotients divide by (S + eps)^2 and by sums of such weights: normal numbers far inside the
+// FP32 range for any grid spacing above ~1e-6, where a * rcp_ftz(b) is the value
+// __fdividef(a, b) returns (checked bitwise on the GPU against the __fdividef form) without
+// the subnormal and range handling a general quotient carries.
+__device__ __forceinline__ float rcp_ftz(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float fast_div(float a, float b) { return a * rcp_ftz(b); }
 __device__ __forceinline__ double fast_div(double a, double b) { return a / b; }
 
 // The same reconstruction from UNSCALED differences u = h*v with eps2 = eps*h^2 and the
@@ -364,9 +375,9 @@ __device__ __forceinline__ void weno5_window_weights(float u1, float u2, float u
     const float s1 = (13.f / 12.f) * sqr(u1 - 2 * u2 + u3) + 0.25f * sqr(u1 - 4 * u2 + 3 * u3);
     const float s2 = (13.f / 12.f) * sqr(u2 - 2 * u3 + u4) + 0.25f * sqr(u2 - u4);
     const float s3 = (13.f / 12.f) * sqr(u3 - 2 * u4 + u5) + 0.25f * sqr(3 * u3 - 4 * u4 + u5);
-    r1 = __fdividef(1.f, sqr(s1 + eps2));
-    r2 = __fdividef(1.f, sqr(s2 + eps2));
-    r3 = __fdividef(1.f, sqr(s3 + eps2));
+    r1 = rcp_ftz(sqr(s1 + eps2));
+    r2 = rcp_ftz(sqr(s2 + eps2));
+    r3 = rcp_ftz(sqr(s3 + eps2));
 }
 
 // WENO5 one-sided derivative (unscaled differences, biased toward u3) with the reciprocal
@@ -378,7 +389,7 @@ __device__ __forceinline__ float weno5_with_weights(float u1, float u2, float u3
     const float q2 = (-1.f / 6.f) * u2 + (5.f / 6.f) * u3 + (1.f / 3.f) * u4;
     const float q3 = (1.f / 3.f) * u3 + (5.f / 6.f) * u4 - (1.f / 6.f) * u5;
     const float a1 = 0.1f * r1, a2 = 0.6f * r2, a3 = 0.3f * r3;
-    return __fdividef(a1 * q1 + a2 * q2 + a3 * q3, a1 + a2 + a3);
+    return (a1 * q1 + a2 * q2 + a3 * q3) * rcp_ftz(a1 + a2 + a3);
 }
 
 // Seven-point stencil with the interface inserted at r1 (forward) / l1 (backward) when
@@ -784,7 +795,8 @@ __device__ __forceinline__ float2 f2s(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float2 fdiv2(float2 a, float2 b) { return f2(__fdividef(a.x, b.x), __fdividef(a.y, b.y)); }
+__device__ __forceinline__ float2 rcp2(float2 b) { return f2(rcp_ftz(b.x), rcp_ftz(b.y)); }
+__device__ __forceinline__ float2 fdiv2(float2 a, float2 b) { return mul2(a, rcp2(b)); }
 
 // Candidate values of the three stencils for packed differences u1..u5.
 __device__ __forceinline__ void weno5_candidates2(float2 u1, float2 u2, float2 u3, float2 u4, float2 u5, float2 &q1,
@@ -810,10 +822,9 @@ __device__ __forceinline__ void weno5_weights2(float2 u1, float2 u2, float2 u3, 
     const float2 s2 = fma2(c13, mul2(t3, t3), mul2(c14, mul2(t4, t4)));
     const float2 s3 = fma2(c13, mul2(t5, t5), mul2(c14, mul2(t6, t6)));
     const float2 e1 = add2(s1, eps2), e2 = add2(s2, eps2), e3 = add2(s3, eps2);
-    const float2 one = f2s(1.f);
-    r1 = fdiv2(one, mul2(e1, e1));
-    r2 = fdiv2(one, mul2(e2, e2));
-    r3 = fdiv2(one, mul2(e3, e3));
+    r1 = rcp2(mul2(e1, e1));
+    r2 = rcp2(mul2(e2, e2));
+    r3 = rcp2(mul2(e3, e3));
 }
 
 // Weighted combination sum(d_k r_k q_k) / sum(d_k r_k), d = (0.1, 0.6, 0.3).

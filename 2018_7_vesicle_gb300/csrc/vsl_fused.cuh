@@ -446,35 +446,11 @@ __global__ void __launch_bounds__(BX *BY) k_extension_velocity(const T *__restri
 }
 
 // The mixed form splits the extension velocity: nodes without a distance flag take the
-// uniform path alone, and only the side each axis keeps (n = D+ where |p4| < |p2|, else
-// D-) is reconstructed, x and y as the two lanes of one packed WENO5, z with itself in
-// both lanes; each lane is the arithmetic of the corresponding lane of weno5_pair_fast2,
-// so the velocity is the same to the bit.  The flagged nodes (the classification's list)
-// run the generic form in k_velocity_list.
-__global__ void __launch_bounds__(BX *BY) k_velocity_uniform(const float *__restrict__ phi,
-                                                               const uint8_t *__restrict__ flags, Ptr3<float> v,
-                                                               Grid g, float floor)
-{
-    int i, j, k;
-    if (!fused_node(g, i, j, k)) return;
-    const long long c = node_index(g, i, j, k);
-    if (__ldg(flags + c) & 0x3F) return;
-    float px[7], py[7], pz[7];
-    load_line7(phi, axis_line(g, i, j, k, AX_X), px);
-    load_line7(phi, axis_line(g, i, j, k, AX_Y), py);
-    load_line7(phi, axis_line(g, i, j, k, AX_Z), pz);
-    const float hx = (float)g.dx, hy = (float)g.dy, hz = (float)g.dz;
-    const bool bx = !(fabsf(px[4]) < fabsf(px[2])), by = !(fabsf(py[4]) < fabsf(py[2]));
-    const bool bz = !(fabsf(pz[4]) < fabsf(pz[2]));
-    const float2 dxy = weno5_upwind2(px, bx, py, by, f2(1.0f / hx, 1.0f / hy), f2(1e-6f * hx * hx, 1e-6f * hy * hy));
-    const float2 dzz = weno5_upwind2(pz, bz, pz, bz, f2s(1.0f / hz), f2s(1e-6f * hz * hz));
-    const float n[3] = {dxy.x, dxy.y, dzz.x};
-    const float grad = vmax(sqrtf(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]), floor);
-    const float f0 = px[3];
-    const float s = f0 > 0.f ? 1.f : (f0 < 0.f ? -1.f : 0.f);
-#pragma unroll
-    for (int ax = 0; ax < 3; ++ax) v.p[ax][c] = s * (n[ax] / grad);
-}
+// uniform path on 2.5D tiles (stage kind SK_VELOCITY), where only the side each axis keeps
+// (n = D+ where |p4| < |p2|, else D-) is reconstructed, x and y as the two lanes of one
+// packed WENO5, z with itself in both lanes; each lane is the arithmetic of the
+// corresponding lane of weno5_pair_fast2, so the velocity is the same to the bit.  The
+// flagged nodes (the classification's list) run the generic form in k_velocity_list.
 
 // the flagged nodes of the extension velocity (the classification's list), generic form
 template <bool ENO3>
@@ -843,8 +819,7 @@ cudaError_t launch_extension_velocity(const T *phi, const uint8_t *flags, Ptr6<c
 {
     if constexpr (std::is_same<T, float>::value) {
         if (flagged.idx) {
-            k_velocity_uniform<<<node_grid(g), dim3(BX, BY), 0, s>>>(phi, flags, v, g, (float)floor);
-            cudaError_t err = cudaGetLastError();
+            cudaError_t err = launch_velocity_tiled(phi, flags, v, g, (float)floor, s);
             if (err != cudaSuccess) return err;
             if (eno3)
                 k_velocity_list<true><<<list_blocks(), 128, 0, s>>>(phi, flags, dist, v, flagged, g, (float)floor);

@@ -174,6 +174,9 @@ struct TiledStage {
 };
 // kind: 0 reinitialization, 1 extension, 2 advection
 cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const Grid &g, cudaStream_t s);
+// the mixed form's extension velocity of the nodes without a distance flag, on 2.5D tiles
+cudaError_t launch_velocity_tiled(const float *phi, const uint8_t *flags, Ptr3<float> v, const Grid &g, float floor,
+                                  cudaStream_t s);
 // the same stage (same kind and RK stage) of `count` <= TILED_BATCH_MAX grids as one
 // persistent launch over all their tiles, and one launch for all their band nodes
 constexpr int TILED_BATCH_MAX = 64;

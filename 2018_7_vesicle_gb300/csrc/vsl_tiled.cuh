@@ -47,8 +47,9 @@ constexpr int PLANE = SW * SH;
 constexpr int RING = 5;
 
 // SK_ENO2 / SK_ENO2R: the ENORK2 extension / reinitialization (quadratic ENO derivatives,
-// Heun RK2 stages)
-enum StageKind { SK_REINIT = 0, SK_EXTEND = 1, SK_ADVECT = 2, SK_ENO2 = 3, SK_ENO2R = 4 };
+// Heun RK2 stages); SK_VELOCITY: the extension velocity of the nodes without a distance
+// flag (a single pass writing three fields, not an RK stage)
+enum StageKind { SK_REINIT = 0, SK_EXTEND = 1, SK_ADVECT = 2, SK_ENO2 = 3, SK_ENO2R = 4, SK_VELOCITY = 5 };
 // kinds on the WENO5 stencils (their z window weights are carried from page to page)
 __host__ __device__ constexpr bool weno_kind(int kind) { return kind <= SK_ADVECT; }
 // kinds whose band is the static list of flagged nodes (the band kernel runs beside them)
@@ -73,6 +74,8 @@ struct TiledArgs {
     float h[3], inv_h[3], eps2[3];
     float dt_uniform;  // 0.3 * min spacing: the pseudo time step of a node with no crossing
     int kz;            // pages per block
+    Ptr3<float> w;     // SK_VELOCITY: the velocity written
+    float floor;       // SK_VELOCITY: the floor of |grad phi|
 };
 
 constexpr int PER_THREAD = (PLANE + TY * TX - 1) / (TY * TX);  // halo elements per thread
@@ -222,11 +225,11 @@ __device__ __forceinline__ void stage_tile(const TiledArgs &a, float (*sm)[SH][S
             const float ps = q[3];
             float step = 0.f;
             bool compute = true;
-            if (KIND != SK_ADVECT && (fl & FIXED_BIT)) compute = false;
+            if (KIND != SK_ADVECT && KIND != SK_VELOCITY && (fl & FIXED_BIT)) compute = false;
             if (compute && KIND == SK_REINIT) {
                 band = px[2] * px[3] < 0.f || px[3] * px[4] < 0.f || py[2] * py[3] < 0.f || py[3] * py[4] < 0.f ||
                        q[2] * q[3] < 0.f || q[3] * q[4] < 0.f;
-            } else if (static_band_kind(KIND)) {
+            } else if (static_band_kind(KIND) || KIND == SK_VELOCITY) {
                 // every node of the static list (fixed ones too) belongs to the band kernel,
                 // which may run at the same time: each node has exactly one writer
                 band = (fl & 0x3F) != 0;
@@ -276,9 +279,24 @@ __device__ __forceinline__ void stage_tile(const TiledArgs &a, float (*sm)[SH][S
                 const float tr = ux * dxy.x + uy * dxy.y + uz * dz;
                 step = KIND == SK_EXTEND ? tr * a.dt_uniform : dt_adv * tr;
             }
-            if (!band)
+            if (!band && KIND == SK_VELOCITY) {
+                // k_velocity_uniform's arithmetic: each axis reconstructs the side it keeps
+                // (D+ where |p4| < |p2|, else D-), x and y as the lanes of one packed WENO5,
+                // z with itself in both lanes, so the velocity is the same to the bit
+                const bool bx = !(fabsf(px[4]) < fabsf(px[2])), by = !(fabsf(py[4]) < fabsf(py[2]));
+                const bool bz = !(fabsf(q[4]) < fabsf(q[2]));
+                const float2 dxy =
+                    weno5_upwind2(px, bx, py, by, f2(a.inv_h[0], a.inv_h[1]), f2(a.eps2[0], a.eps2[1]));
+                const float2 dzz = weno5_upwind2(q, bz, q, bz, f2s(a.inv_h[2]), f2s(a.eps2[2]));
+                const float n[3] = {dxy.x, dxy.y, dzz.x};
+                const float grad = vmax(sqrtf(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]), a.floor);
+                const float sg = ps > 0.f ? 1.f : (ps < 0.f ? -1.f : 0.f);
+#pragma unroll
+                for (int ax = 0; ax < 3; ++ax) a.w.p[ax][c] = sg * (n[ax] / grad);
+            } else if (!band) {
                 a.out[c] = (KIND == SK_ENO2 || KIND == SK_ENO2R) ? rk2_combine(STAGE, pn, ps, step)
                                                                   : rk3_combine(STAGE, pn, ps - step);
+            }
         }
         if (KIND == SK_REINIT) {  // the extension's band is the static list of flagged nodes
             const unsigned m = __ballot_sync(0xffffffffu, band);
@@ -521,8 +539,8 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
     }
 }
 
-// The band nodes of one stage of every grid of a batch (k_band_stage per grid, one after
-// the other in one grid-stride launch).
+// The band nodes of one stage of every grid of a batch (k_band_stage per grid, all the
+// grids' band nodes as one work list in one launch).
 struct BandBatch {
     TiledArgs v[BATCH_MAX];
     BandShadow sh[BATCH_MAX];
@@ -534,26 +552,45 @@ static_assert(sizeof(BandBatch) <= 32000, "kernel parameter space");
 template <int KIND, bool ENO3>
 __global__ void __launch_bounds__(128, (KIND == SK_REINIT ? 0 : 8)) k_band_stage_batch(const __grid_constant__ BandBatch B)
 {
+    // one work list of every grid's band nodes: the grids' counts, prefix-summed per block,
+    // place work item t at node t - first[v] of grid v (first[v] <= t < first[v + 1]), so the
+    // blocks share the band nodes of all the grids evenly, whatever the sizes of the bands
+    static_assert(BATCH_MAX <= 128, "one counter per thread");
+    __shared__ unsigned first[BATCH_MAX + 1];
+    if ((int)threadIdx.x < B.count) first[threadIdx.x + 1] = *B.v[threadIdx.x].counter;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        first[0] = 0u;
+        for (int v = 0; v < B.count; ++v) first[v + 1] += first[v];
+    }
+    __syncthreads();
+    // the reinitialization clears the other stage's counters, which this launch does not read
     if (blockIdx.x == 0 && (int)threadIdx.x < B.count && B.next[threadIdx.x]) *B.next[threadIdx.x] = 0u;
-    for (int v = 0; v < B.count; ++v) {
-        const TiledArgs &a = B.v[v];
-        const Grid &g = a.g;
-        const unsigned n = *a.counter;
-        for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-            const long long c = a.queue[t];
-            const int k = (int)(c / g.plane);
-            const long long r = c - (long long)k * g.plane;
-            const int j = (int)(r / g.rows);
-            const int i = (int)(r - (long long)j * g.rows);
-            if (KIND == SK_REINIT)
-                reinit_node<float, ENO3, true>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
-            else if (KIND == SK_ENO2)
-                enork2_extend_node_mixed(a, B.sh[v], i, j, k);
-            else if (KIND == SK_ENO2R)
-                enork2_reinit_node<float>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
+    const unsigned total = first[B.count];
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        int lo = 0, hi = B.count - 1;  // the last grid v with first[v] <= t
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (first[mid] <= t)
+                lo = mid;
             else
-                extend_node_mixed<ENO3>(a, B.sh[v], i, j, k);
+                hi = mid - 1;
         }
+        const TiledArgs &a = B.v[lo];
+        const Grid &g = a.g;
+        const long long c = a.queue[t - first[lo]];
+        const int k = (int)(c / g.plane);
+        const long long r = c - (long long)k * g.plane;
+        const int j = (int)(r / g.rows);
+        const int i = (int)(r - (long long)j * g.rows);
+        if (KIND == SK_REINIT)
+            reinit_node<float, ENO3, true>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
+        else if (KIND == SK_ENO2)
+            enork2_extend_node_mixed(a, B.sh[lo], i, j, k);
+        else if (KIND == SK_ENO2R)
+            enork2_reinit_node<float>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
+        else
+            extend_node_mixed<ENO3>(a, B.sh[lo], i, j, k);
     }
 }
 
@@ -761,6 +798,21 @@ cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const 
     return cudaGetLastError();
 }
 
+// the extension velocity of the nodes without a distance flag on the tiles (the flagged
+// nodes are k_velocity_list's)
+cudaError_t launch_velocity_tiled(const float *phi, const uint8_t *flags, Ptr3<float> v, const Grid &g, float floor,
+                                  cudaStream_t s)
+{
+    TiledArgs a = tiled_args(g);
+    a.phi_s = phi;
+    a.flags = flags;
+    a.w = v;
+    a.floor = floor;
+    a.kz = tile_pages(g, SK_VELOCITY);
+    k_stage_tiled<SK_VELOCITY, 0><<<tiled_grid(g, a.kz), dim3(TY, TX), 0, s>>>(a);
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------------------
 // batched stages (k_stage_tiled_batch, k_band_stage_batch)
 // ---------------------------------------------------------------------------------------
@@ -839,6 +891,7 @@ cudaError_t launch_tiled_batch(int kind, bool eno3, const TiledStage *st, const 
     }
     B.start[count] = total;
     const int stage = st[0].stage;
+    const int bgrid = band_blocks();
     cudaError_t e;
     if (static_band_kind(kind)) {
         SideLane *ln = side_lane(s);
@@ -856,13 +909,13 @@ cudaError_t launch_tiled_batch(int kind, bool eno3, const TiledStage *st, const 
             bs = ln->side;
         }
         if (kind == SK_ENO2)
-            k_band_stage_batch<SK_ENO2, false><<<band_blocks(), 128, 0, bs>>>(BB);
+            k_band_stage_batch<SK_ENO2, false><<<bgrid, 128, 0, bs>>>(BB);
         else if (kind == SK_ENO2R)
-            k_band_stage_batch<SK_ENO2R, false><<<band_blocks(), 128, 0, bs>>>(BB);
+            k_band_stage_batch<SK_ENO2R, false><<<bgrid, 128, 0, bs>>>(BB);
         else if (eno3)
-            k_band_stage_batch<SK_EXTEND, true><<<band_blocks(), 128, 0, bs>>>(BB);
+            k_band_stage_batch<SK_EXTEND, true><<<bgrid, 128, 0, bs>>>(BB);
         else
-            k_band_stage_batch<SK_EXTEND, false><<<band_blocks(), 128, 0, bs>>>(BB);
+            k_band_stage_batch<SK_EXTEND, false><<<bgrid, 128, 0, bs>>>(BB);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         if (ln) {
             if ((e = cudaEventRecord(ln->join, bs)) != cudaSuccess) return e;
@@ -873,9 +926,9 @@ cudaError_t launch_tiled_batch(int kind, bool eno3, const TiledStage *st, const 
     e = kind == SK_REINIT ? launch_batch_kind<SK_REINIT>(stage, B, total, s) : launch_batch_kind<SK_ADVECT>(stage, B, total, s);
     if (e != cudaSuccess || kind == SK_ADVECT) return e;
     if (eno3)
-        k_band_stage_batch<SK_REINIT, true><<<band_blocks(), 128, 0, s>>>(BB);
+        k_band_stage_batch<SK_REINIT, true><<<bgrid, 128, 0, s>>>(BB);
     else
-        k_band_stage_batch<SK_REINIT, false><<<band_blocks(), 128, 0, s>>>(BB);
+        k_band_stage_batch<SK_REINIT, false><<<bgrid, 128, 0, s>>>(BB);
     return cudaGetLastError();
 }
 
