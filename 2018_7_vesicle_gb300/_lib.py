@@ -40,6 +40,10 @@ SIGNATURES = {
     # tuning table of the tiled kernels (pages per block)
     "vsl_set_tile_pages": "iiiii",
     "vsl_tile_pages": "iiii",
+    # plane loads of the tiled kernels (1 TMA, 0 registers) and the TMA wait-timeout count
+    "vsl_set_plane_loads": "i",
+    "vsl_plane_loads": "",
+    "vsl_tma_wait_timeouts": "p",
     # no-allocation variant (static device scratch, no workspace argument)
     "vsl_area_volume_noalloc_f64": "pp" + _G + "s",
     # a batch of vesicle steps: host array of VesicleF32, count, ext/reinit pseudo-steps, CFL

@@ -51,6 +51,26 @@ def set_pages(size, kind: str, pages: int) -> None:
     lib().call("vsl_set_tile_pages", *size, KINDS[kind], int(pages))
 
 
+def set_plane_loads(mode: int) -> None:
+    """Plane loads of the tiled kernels, process-wide: 1 TMA tensor copies (where the field
+    allows), 0 through registers; the results are the same either way."""
+    lib().call("vsl_set_plane_loads", int(mode))
+
+
+def plane_loads() -> int:
+    return int(lib().raw("vsl_plane_loads"))
+
+
+def tma_wait_timeouts() -> int:
+    """Bounded waits for a tensor copy that gave up since the library was loaded (0 unless a
+    copy failed to complete)."""
+    import ctypes
+
+    n = ctypes.c_uint(0)
+    lib().call("vsl_tma_wait_timeouts", ctypes.addressof(n))
+    return int(n.value)
+
+
 def _elapsed_ms(fn, reps: int) -> float:
     fn()  # warm-up (workspace, first launch of the shape)
     torch.cuda.synchronize()

@@ -1435,6 +1435,16 @@ int vsl_set_tile_pages(int rows, int cols, int pges, int kind, int pages)
     return set_tile_pages(rows, cols, pges, kind, pages);
 }
 
+int vsl_set_plane_loads(int mode) { return set_plane_loads(mode); }
+
+int vsl_plane_loads(void) { return get_plane_loads(); }
+
+int vsl_tma_wait_timeouts(unsigned *count)
+{
+    if (count == nullptr) return VSL_ERR_NULL;
+    return tma_timeouts(count) == cudaSuccess ? VSL_OK : VSL_ERR_CUDA;
+}
+
 int vsl_tile_pages(int rows, int cols, int pges, int kind)
 {
     if (rows <= 0 || cols <= 0 || pges <= 0 || kind < 0 || kind > 4) return 0;

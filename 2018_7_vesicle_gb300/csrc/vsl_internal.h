@@ -174,6 +174,10 @@ struct TiledStage {
 };
 // kind: 0 reinitialization, 1 extension, 2 advection
 cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const Grid &g, cudaStream_t s);
+// plane loads of the 2.5D-tiled stage kernels: 1 = TMA for the inner tiles, 0 = registers
+int set_plane_loads(int mode);
+int get_plane_loads();
+cudaError_t tma_timeouts(unsigned *count);
 // the mixed form's extension velocity of the nodes without a distance flag, on 2.5D tiles
 cudaError_t launch_velocity_tiled(const float *phi, const uint8_t *flags, Ptr3<float> v, const Grid &g, float floor,
                                   cudaStream_t s);

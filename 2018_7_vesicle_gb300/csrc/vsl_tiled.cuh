@@ -20,9 +20,12 @@
 #pragma once
 
 #include <algorithm>
+#include <atomic>
+#include <cudaTypedefs.h>
 #include <mutex>
 
 #include "vsl_fused.cuh"
+#include "vsl_tma.cuh"
 
 namespace vsl {
 namespace {
@@ -79,6 +82,8 @@ struct TiledArgs {
 };
 
 constexpr int PER_THREAD = (PLANE + TY * TX - 1) / (TY * TX);  // halo elements per thread
+// cells of a TMA ring slot per thread (the fix-up of an edge tile's halo)
+constexpr int TMA_FIX = (TMA_BOX_ROWS * TMA_BOX_COLS + TY * TX - 1) / (TY * TX);
 
 // a ring slot known at compile time (the unrolled page loop)
 template <int N> struct RingSlot {
@@ -107,10 +112,28 @@ __device__ __forceinline__ void eno2_pair_uniform(const float p[7], float inv_h,
 
 // One tile of one stage: the TY x TX block's tile (bx, by) marching pages bz * kz ..
 // (bz + 1) * kz - 1 of the grid of `a` (the work of one block of k_stage_tiled, or of one
-// work item of the batched kernel).  sm: the block's plane ring.
-template <int KIND, int STAGE>
-__device__ __forceinline__ void stage_tile(const TiledArgs &a, float (*sm)[SH][SW], int bx, int by, int bz)
+// work item of the batched kernel).  smem: the block's plane ring.
+//
+// Planes reach the ring in one of two ways.  Without TMA every thread loads its share of a
+// plane (clamped halo) into registers one page ahead and stores it after the page's reads.
+// With TMA thread 0 issues one tensor copy per plane, which completes on the slot's
+// mbarrier; thread 0 waits for page k+3 before the barrier of page k, which passes the
+// landed plane on to the other threads.  A slot's plane is then
+// TMA_BOX_ROWS wide, its first row 4 rows below the tile (the copy's innermost coordinate
+// is a multiple of 16 bytes).  A copy reads zeros outside the grid; on tiles at the grid's
+// edge each thread then gives its (at most three) cells outside the grid the value of the
+// nearest cell inside, the clamped halo of the register path, so both paths see the same
+// planes.
+template <int KIND, int STAGE, bool TMA = false>
+__device__ __forceinline__ void stage_tile(const TiledArgs &a, float *smem, int bx, int by, int bz,
+                                           const CUtensorMap *tm = nullptr, uint64_t *bars = nullptr,
+                                           unsigned *fixtab = nullptr)
 {
+    constexpr int PITCH = TMA ? TMA_BOX_ROWS : SW;  // ring row extent (rows of the grid)
+    constexpr int PSTR = TMA ? TMA_SLOT_FLOATS : PLANE;  // floats per ring slot
+    constexpr int XO = TMA ? 4 : HALO;  // ring index of the tile's first row
+    // ring slot sl, tile column jj (0 .. SH-1, halo included), ring row ii
+    auto S = [smem](int sl, int jj, int ii) -> float & { return smem[sl * PSTR + jj * PITCH + ii]; };
     const Grid &g = a.g;
     // the launch is always TY x TX threads: the first two elements of every thread's share
     // of a plane are then in the plane without a test
@@ -131,11 +154,13 @@ __device__ __forceinline__ void stage_tile(const TiledArgs &a, float (*sm)[SH][S
     // to PER_THREAD elements; the same for every page, only the page base changes
     // element tid + r*TY*TX of the plane; offsets are within one page (< 2^31)
     int e_off[PER_THREAD];
+    if constexpr (!TMA) {
 #pragma unroll
-    for (int r = 0; r < PER_THREAD; ++r) {
-        const int e = tid + r * TY * TX;
-        const int sy = e / SW, sx = e - sy * SW;
-        e_off[r] = clampi(j0 + sy - HALO, g.cols) * g.rows + clampi(i0 + sx - HALO, g.rows);
+        for (int r = 0; r < PER_THREAD; ++r) {
+            const int e = tid + r * TY * TX;
+            const int sy = e / SW, sx = e - sy * SW;
+            e_off[r] = clampi(j0 + sy - HALO, g.cols) * g.rows + clampi(i0 + sx - HALO, g.rows);
+        }
     }
     // node offsets fit in 32 bits (grids hold at most 2^31 - 1 nodes), so an address is the
     // base pointer plus one widened 32-bit offset
@@ -150,16 +175,79 @@ __device__ __forceinline__ void stage_tile(const TiledArgs &a, float (*sm)[SH][S
             if (tid + r * TY * TX < PLANE) pre[r] = __ldg(src + e_off[r]);
     };
     auto store_slot = [&](int sl) {
-        float *dst = &sm[sl][0][0];
+        float *dst = &S(sl, 0, 0);
 #pragma unroll
         for (int r = 0; r < PER_THREAD; ++r)
             if (tid + r * TY * TX < PLANE) dst[tid + r * TY * TX] = pre[r];
     };
+    // TMA: the copy of page p into slot sl and the wait for a slot's next fill (thread 0); a
+    // slot's n-th fill completes phase n of its barrier (ph: the parity each slot waits for).
+    // A wait that gave up (a copy that never completed) is counted and thread 0 waits for no
+    // later copy, so that the block ends in bounded time on stale planes.
+    unsigned ph = 0u;
+    bool gave_up = false;
+    // edge tiles: fixtab[r][tid] = this thread's cell e = tid + r*TY*TX of a slot when it lies
+    // outside the grid, as (e << 16) | (offset of the clamped cell) + 1, else 0 (in shared
+    // memory: no registers held through the page loop)
+    const bool edge =
+        TMA && !(i0 >= XO && i0 + TY + HALO <= g.rows && j0 >= HALO && j0 + TX + HALO <= g.cols);
+    if constexpr (TMA) {
+        if (edge) {
+#pragma unroll
+            for (int r = 0; r < TMA_FIX; ++r) {
+                unsigned f = 0u;
+                const int e = tid + r * TY * TX;
+                if (e < TMA_BOX_ROWS * TMA_BOX_COLS) {
+                    const int jj = e / TMA_BOX_ROWS, ii = e - jj * TMA_BOX_ROWS;
+                    const int gj = j0 - HALO + jj, gi = i0 - XO + ii;
+                    if (gj < 0 || gj >= g.cols || gi < 0 || gi >= g.rows) {
+                        const int src =
+                            (clampi(gj, g.cols) - j0 + HALO) * TMA_BOX_ROWS + clampi(gi, g.rows) - i0 + XO;
+                        f = ((unsigned)e << 16) | (unsigned)(src + 1);
+                    }
+                }
+                fixtab[r * TY * TX + tid] = f;
+            }
+        }
+    }
+    // after the copy of slot sl has landed: the cells outside the grid (each thread its own
+    // entries, so no barrier), then the proxy fence that orders these writes before a later
+    // copy into the slot
+    auto fix_slot = [&](int sl) {
+        if constexpr (TMA) {
+            if (edge) {
+                float *pl = &S(sl, 0, 0);
+#pragma unroll
+                for (int r = 0; r < TMA_FIX; ++r) {
+                    const unsigned f = fixtab[r * TY * TX + tid];
+                    if (f) pl[f >> 16] = pl[(f & 0xFFFFu) - 1u];
+                }
+                fence_proxy_async();
+            }
+        }
+    };
+    auto tma_fetch = [&](int p, int sl) {
+        mbar_expect_tx(&bars[sl], TMA_PLANE_BYTES);
+        tma_load_box(&S(sl, 0, 0), tm, i0 - XO, j0 - HALO, min(p, g.pges - 1), &bars[sl]);
+    };
+    auto tma_wait = [&](int sl) {
+        if (!gave_up) gave_up = !mbar_wait(&bars[sl], (ph >> sl) & 1u);
+        ph ^= 1u << sl;
+    };
 
     float q[7];  // phi_s(i, j, k-3 .. k+3)
-    for (int p = k0; p < k0 + 4; ++p) {
-        fetch(p);
-        store_slot(slot(p));
+    if constexpr (TMA) {
+        // pages k0 .. k0+3 (k1 > k0, so all of them are read); thread 0 alone waits for a
+        // copy, and the block barrier after its wait passes the plane on to the other threads
+        if (tid == 0) {
+            for (int p = k0; p < k0 + 4; ++p) tma_fetch(p, slot(p));
+            for (int p = k0; p < k0 + 3; ++p) tma_wait(slot(p));
+        }
+    } else {
+        for (int p = k0; p < k0 + 4; ++p) {
+            fetch(p);
+            store_slot(slot(p));
+        }
     }
     {
         const int ic = clampi(i, g.rows), jc = clampi(j, g.cols);
@@ -168,8 +256,13 @@ __device__ __forceinline__ void stage_tile(const TiledArgs &a, float (*sm)[SH][S
         for (int s = 0; s < 3; ++s) q[s] = __ldg(a.phi_s + (col + (unsigned)clampi(k0 - 3 + s, g.pges) * plane));
     }
     __syncthreads();
+    if constexpr (TMA) {
+        // the halo cells outside the grid; an active node's own cell is never one of them, and
+        // the barrier of page k0 orders these writes before the stencil reads
+        for (int p = k0; p < k0 + 3; ++p) fix_slot(slot(p));
+    }
 #pragma unroll
-    for (int s = 3; s < 6; ++s) q[s] = sm[slot(k0 + s - 3)][ty + HALO][tx + HALO];
+    for (int s = 3; s < 6; ++s) q[s] = S(slot(k0 + s - 3), ty + HALO, tx + XO);
     // reciprocal smoothness weights of the z window of page k0 (backward derivative)
     float zr1 = 0.f, zr2 = 0.f, zr3 = 0.f;
     if constexpr (weno_kind(KIND))
@@ -198,11 +291,23 @@ __device__ __forceinline__ void stage_tile(const TiledArgs &a, float (*sm)[SH][S
     // one page: the slots of pages k, k+3 and k+4 (= k-1) are RingSlot constants in the
     // unrolled loop and plain ints in the remainder
     auto page = [&](auto sk, auto sk3, auto sk4, int k) {
-        // every warp has finished page k-1 and stored page k+3
+        // every warp has finished page k-1 and stored page k+3 (TMA: thread 0 has seen the
+        // copy of page k+3 land)
+        if constexpr (TMA) {
+            if (tid == 0) tma_wait(int(sk3));
+        }
         __syncthreads();
-        q[6] = sm[int(sk3)][ty + HALO][tx + HALO];
-        fetch(k + 4);  // loads in flight during this page's arithmetic, stored at its end
-        const float(*P)[SW] = sm[int(sk)];
+        if constexpr (TMA) {
+            // page k+4 into the slot of page k-1; pages past k1+2 are never read
+            if (tid == 0 && k + 4 <= k1 + 2) {
+                fence_proxy_async();
+                tma_fetch(k + 4, int(sk4));
+            }
+            fix_slot(int(sk3));  // page k+3, read as a stencil plane three barriers later
+        }
+        q[6] = S(int(sk3), ty + HALO, tx + XO);
+        if constexpr (!TMA) fetch(k + 4);  // loads in flight during this page's arithmetic, stored at its end
+        const float *P = &S(int(sk), 0, 0);
         const uint8_t fl = fl_next;
         const float pn = pn_next, vx0 = v0_next, vy0 = v1_next, vz0 = v2_next, sp = sp_next;
         if (active && k + 1 < k1) load_node(c + plane);
@@ -219,8 +324,8 @@ __device__ __forceinline__ void stage_tile(const TiledArgs &a, float (*sm)[SH][S
             float px[7], py[7];
 #pragma unroll
             for (int s = 0; s < 7; ++s) {
-                px[s] = P[ty + s][tx + HALO];
-                py[s] = P[ty + HALO][tx + s];
+                px[s] = P[(ty + s) * PITCH + tx + XO];
+                py[s] = P[(ty + HALO) * PITCH + tx + XO - HALO + s];
             }
             const float ps = q[3];
             float step = 0.f;
@@ -312,7 +417,7 @@ __device__ __forceinline__ void stage_tile(const TiledArgs &a, float (*sm)[SH][S
             }
         }
         // page k+4 goes to the slot of page k-1, which no warp reads any more
-        store_slot(int(sk4));
+        if constexpr (!TMA) store_slot(int(sk4));
         zr1 = nr1;
         zr2 = nr2;
         zr3 = nr3;
@@ -342,11 +447,27 @@ __device__ __forceinline__ void stage_tile(const TiledArgs &a, float (*sm)[SH][S
 // (long-scoreboard stalls, DRAM 35% of peak): 5 blocks (47 registers, no spills) took 100
 // pseudo-steps at 256^3 from 26.7 to 23.6 ms.  The ENORK2 reinitialization was slower at 5
 // (25.7 -> 27.7 ms) and keeps 4 with the WENO5 kinds.
-template <int KIND, int STAGE>
-__global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_BLOCKS)) k_stage_tiled(TiledArgs a)
+//
+// TMA: the planes by tensor copies (the launch's tensor map of phi_s), else through registers.
+template <int KIND, int STAGE, bool TMA>
+__global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_BLOCKS))
+    k_stage_tiled(const __grid_constant__ TiledArgs a, const __grid_constant__ CUtensorMap tm)
 {
-    __shared__ float sm[RING][SH][SW];
-    stage_tile<KIND, STAGE>(a, sm, blockIdx.x, blockIdx.y, blockIdx.z);
+    static_assert(SH == TMA_BOX_COLS && PLANE <= TMA_SLOT_FLOATS, "ring layouts");
+    if constexpr (TMA) {
+        __shared__ __align__(128) float smem[RING * TMA_SLOT_FLOATS];
+        __shared__ __align__(8) uint64_t bars[RING];
+        __shared__ unsigned fixtab[TMA_FIX * TY * TX];
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            for (int s = 0; s < RING; ++s) mbar_init(&bars[s], 1);
+            mbar_init_fence();
+        }
+        __syncthreads();
+        stage_tile<KIND, STAGE, true>(a, smem, blockIdx.x, blockIdx.y, blockIdx.z, &tm, bars, fixtab);
+    } else {
+        __shared__ float smem[RING * PLANE];
+        stage_tile<KIND, STAGE, false>(a, smem, blockIdx.x, blockIdx.y, blockIdx.z);
+    }
 }
 
 // ---------------------------------------------------------------------------------------
@@ -528,13 +649,13 @@ template <int KIND, int STAGE>
 __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_BLOCKS))
     k_stage_tiled_batch(const __grid_constant__ TiledBatch B)
 {
-    __shared__ float sm[RING][SH][SW];
+    __shared__ float smem[RING * PLANE];
     const int total = B.start[B.count];
     for (int w = blockIdx.x; w < total; w += gridDim.x) {
         const int v = batch_member(B.start, B.count, w);
         const int local = w - B.start[v];
         const int rest = local / B.nx[v];
-        stage_tile<KIND, STAGE>(B.v[v], sm, local - rest * B.nx[v], rest % B.ny[v], rest / B.ny[v]);
+        stage_tile<KIND, STAGE>(B.v[v], smem, local - rest * B.nx[v], rest % B.ny[v], rest / B.ny[v]);
         __syncthreads();  // the next item's prologue rewrites the plane ring
     }
 }
@@ -712,20 +833,92 @@ SideLane *side_lane(cudaStream_t s)
 }
 }  // namespace
 
+// ---------------------------------------------------------------------------------------
+// TMA plane loads: the driver's tensor-map encoder (looked up once through the runtime) and
+// the process-wide choice of plane loads (vsl_set_plane_loads)
+// ---------------------------------------------------------------------------------------
+namespace {
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+// Register plane loads are the default: measured on GB300 at 256^3, the TMA path ran the
+// reinitialization stage in 203 us against 189 us (ncu), 340 against 329 warp instructions
+// per node: the stage kernels are issue-bound at the 64-register cap, and the copies' waits,
+// the branches of the issuing thread and the edge fix-up cost more issue slots than the
+// three loads and three shared stores per node they replace.
+#ifndef VSL_PLANE_LOADS
+#define VSL_PLANE_LOADS 0
+#endif
+std::atomic<int> plane_loads{VSL_PLANE_LOADS};  // 1: TMA where the field allows, 0: registers only
+}  // namespace
+
+int set_plane_loads(int mode)
+{
+    if (mode != 0 && mode != 1) return VSL_ERR_VALUE;
+    plane_loads.store(mode);
+    return VSL_OK;
+}
+int get_plane_loads() { return plane_loads.load(); }
+
+// bounded TMA waits that gave up since the library was loaded (zero unless a copy failed
+// to complete)
+cudaError_t tma_timeouts(unsigned *count) { return cudaMemcpyFromSymbol(count, tma_wait_timeouts, sizeof(unsigned)); }
+
+// The tensor map of a stage input for TMA plane loads; false (registers only) where the
+// field cannot take them: TMA off, rows not a multiple of 4 (a copy's row stride is a
+// multiple of 16 bytes), a base address not 16-byte aligned, or no encoder.
+bool encode_plane_map(CUtensorMap &tm, const float *f, const Grid &g)
+{
+    if (plane_loads.load() == 0) return false;
+    if (g.rows % 4 != 0 || (reinterpret_cast<uintptr_t>(f) & 15u) != 0u) return false;
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)g.rows, (cuuint64_t)g.cols, (cuuint64_t)g.pges};
+    const cuuint64_t strides[2] = {(cuuint64_t)g.rows * 4u, (cuuint64_t)g.plane * 4u};
+    const cuuint32_t box[3] = {(cuuint32_t)TMA_BOX_ROWS, (cuuint32_t)TMA_BOX_COLS, 1u};
+    const cuuint32_t estr[3] = {1u, 1u, 1u};
+    return enc(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(f), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // the RK stage is a template parameter of the tiled kernel (its combination and whether it
 // reads the step-start field are then fixed at compile time); the ENORK2 kinds have two
-template <int KIND> void launch_stage_kind(int stage, dim3 gr, dim3 bl, cudaStream_t s, const TiledArgs &a)
+template <int KIND, bool TMA>
+void launch_stage_kind_as(int stage, dim3 gr, dim3 bl, cudaStream_t s, const TiledArgs &a, const CUtensorMap &tm)
 {
-    if (stage == 0) {
-        k_stage_tiled<KIND, 0><<<gr, bl, 0, s>>>(a);
+    if constexpr (KIND == SK_VELOCITY) {
+        k_stage_tiled<KIND, 0, TMA><<<gr, bl, 0, s>>>(a, tm);  // a single pass, not an RK stage
+    } else if (stage == 0) {
+        k_stage_tiled<KIND, 0, TMA><<<gr, bl, 0, s>>>(a, tm);
     } else if constexpr (KIND == SK_ENO2 || KIND == SK_ENO2R) {
-        k_stage_tiled<KIND, 1><<<gr, bl, 0, s>>>(a);
+        k_stage_tiled<KIND, 1, TMA><<<gr, bl, 0, s>>>(a, tm);
     } else {
         if (stage == 1)
-            k_stage_tiled<KIND, 1><<<gr, bl, 0, s>>>(a);
+            k_stage_tiled<KIND, 1, TMA><<<gr, bl, 0, s>>>(a, tm);
         else
-            k_stage_tiled<KIND, 2><<<gr, bl, 0, s>>>(a);
+            k_stage_tiled<KIND, 2, TMA><<<gr, bl, 0, s>>>(a, tm);
     }
+}
+
+template <int KIND> void launch_stage_kind(int stage, dim3 gr, dim3 bl, cudaStream_t s, const TiledArgs &a)
+{
+    CUtensorMap tm{};
+    if (encode_plane_map(tm, a.phi_s, a.g))
+        launch_stage_kind_as<KIND, true>(stage, gr, bl, s, a, tm);
+    else
+        launch_stage_kind_as<KIND, false>(stage, gr, bl, s, a, tm);
 }
 
 cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const Grid &g, cudaStream_t s)
@@ -809,7 +1002,7 @@ cudaError_t launch_velocity_tiled(const float *phi, const uint8_t *flags, Ptr3<f
     a.w = v;
     a.floor = floor;
     a.kz = tile_pages(g, SK_VELOCITY);
-    k_stage_tiled<SK_VELOCITY, 0><<<tiled_grid(g, a.kz), dim3(TY, TX), 0, s>>>(a);
+    launch_stage_kind<SK_VELOCITY>(0, tiled_grid(g, a.kz), dim3(TY, TX), s, a);
     return cudaGetLastError();
 }
 

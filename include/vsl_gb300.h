@@ -200,6 +200,21 @@ enum {
 int vsl_set_tile_pages(int rows, int cols, int pges, int kind, int pages);
 int vsl_tile_pages(int rows, int cols, int pges, int kind);
 
+/* Plane loads of the FP32 tiled stage kernels (no counterpart in the reference), process-wide:
+ * mode 0 (the default) loads every plane through registers; mode 1 loads them by TMA tensor
+ * copies (grids with rows a multiple of 4 and 16-byte aligned fields; other grids keep the
+ * register loads).  The planes are the same; the two kernels are compiled apart and fuse
+ * multiply-adds differently, so results agree to a few ulp, not bit for bit (mode 0 is the
+ * one the bitwise tests pin; mode 1 measured slower on GB300).  A launch takes the mode in
+ * effect when it is issued (a CUDA graph keeps it).  vsl_set_plane_loads
+ * returns VSL_ERR_VALUE for another mode; vsl_plane_loads returns the mode in effect.
+ * vsl_tma_wait_timeouts reads how many bounded waits for a tensor copy have given up since
+ * the library was loaded (0 unless a copy failed to complete; the kernel then goes on,
+ * every access in bounds, with the plane's earlier contents). */
+int vsl_set_plane_loads(int mode);
+int vsl_plane_loads(void);
+int vsl_tma_wait_timeouts(unsigned *count);
+
 /* Bytes of workspace operation `op` needs on a rows x cols x pges grid of elements of
  * `elem_bytes` (8 for _f64, 4 for _f32); 0 for an unknown op or bad shape. */
 size_t vsl_workspace_bytes(int op, int rows, int cols, int pges, int elem_bytes);

@@ -116,6 +116,17 @@ def test_workspace_sizes(vsl):
     assert vsl.lib.vsl_workspace_bytes(1, 0, 8, 8, 8) == 0
 
 
+def test_plane_loads_switch(vsl):
+    """The process-wide plane-load mode of the tiled kernels (1 TMA, 0 registers) and the
+    argument checks of its entry points (host only, no launch)."""
+    call = vsl.raw
+    assert call("vsl_plane_loads") == 0  # the default: registers
+    assert call("vsl_set_plane_loads", 1) == 0 and call("vsl_plane_loads") == 1
+    assert call("vsl_set_plane_loads", 2) == 3 and call("vsl_plane_loads") == 1  # VSL_ERR_VALUE, unchanged
+    assert call("vsl_set_plane_loads", 0) == 0 and call("vsl_plane_loads") == 0
+    assert call("vsl_tma_wait_timeouts", None) == 1  # VSL_ERR_NULL before any CUDA call
+
+
 def test_tile_pages_table(vsl):
     """The pages-per-block table of the tiled kernels: default 20, set / replace / remove,
     argument checks (host only, no launch)."""
