@@ -716,16 +716,39 @@ __device__ __forceinline__ void interface_pair_gaps(const T p[7], T r1, T rc, T 
 }
 
 // Godunov |grad phi| for the reinitialization Hamiltonian; `neg` is the mask (phi0 < 0)
-// (re_step.cu:382-392).
+// (re_step.cu:382-392).  Per axis max(max(0, D-)^2, min(0, D+)^2) is formed as
+// max(0, D-, -D+)^2 (and with both derivatives negated where neg): the squares of non-negative
+// numbers keep their order, also when rounded, so the square of the maximum is the maximum
+// of the squares, bit for bit, with one square per axis instead of two.  The sums are
+// explicitly rounded (no multiply-add contraction), as the maxima between squares and sums
+// kept them before.
+template <typename T> __device__ __forceinline__ T add_rn(T x, T y);
+template <> __device__ __forceinline__ float add_rn<float>(float x, float y) { return __fadd_rn(x, y); }
+template <> __device__ __forceinline__ double add_rn<double>(double x, double y) { return __dadd_rn(x, y); }
+// square root of the norm: FP32 by the bare PTX sqrt.approx.ftz.f32 (the sums are normal
+// or zero; checked bitwise on the GPU against sqrtf of the fast-math build)
+template <typename T> __device__ __forceinline__ T norm_root(T x) { return sqrt(x); }
+template <> __device__ __forceinline__ float norm_root<float>(float x)
+{
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 template <typename T>
 __device__ __forceinline__ T godunov_norm(bool neg, T xR, T xL, T yF, T yB, T zU, T zD)
 {
     const T z = T(0);
-    if (neg)
-        return sqrt(vmax(sqr(vmin(z, xL)), sqr(vmax(z, xR))) + vmax(sqr(vmin(z, yB)), sqr(vmax(z, yF))) +
-                    vmax(sqr(vmin(z, zD)), sqr(vmax(z, zU))));
-    return sqrt(vmax(sqr(vmax(z, xL)), sqr(vmin(z, xR))) + vmax(sqr(vmax(z, yB)), sqr(vmin(z, yF))) +
-                vmax(sqr(vmax(z, zD)), sqr(vmin(z, zU))));
+    T a, b, c;
+    if (neg) {
+        a = vmax(z, vmax(-xL, xR));
+        b = vmax(z, vmax(-yB, yF));
+        c = vmax(z, vmax(-zD, zU));
+    } else {
+        a = vmax(z, vmax(xL, -xR));
+        b = vmax(z, vmax(yB, -yF));
+        c = vmax(z, vmax(zD, -zU));
+    }
+    return norm_root(add_rn(add_rn(sqr(a), sqr(b)), sqr(c)));
 }
 
 // Upwind transport term sum_a min(0,v_a) D+_a + max(0,v_a) D-_a (extend_step.cu:121-123).
