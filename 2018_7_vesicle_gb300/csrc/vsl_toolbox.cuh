@@ -46,20 +46,129 @@ template <typename T> __device__ __forceinline__ T fourth(T x);
 template <> __device__ __forceinline__ double fourth<double>(double x) { return pow_cr<4>(x); }
 template <> __device__ __forceinline__ float fourth<float>(float x) { return (x * x) * (x * x); }
 
-// reciprocals of the spacings for the mixed form's FP64 area and volume terms
+// reciprocals of the spacings for the mixed form: FP64 for its area and volume terms, FP32
+// for its stencils
 struct Recips {
     double i2x, i2y, i2z, ixx, iyy, izz;  // 1 / (2 d), 1 / d^2 per axis
+    float f2x, f2y, f2z, fxx, fyy, fzz, f4ds;  // the same in FP32, and 1 / (4 Ds^2)
 };
 
-// One node of the toolbox (set_calculus_toolbox.cu:9-107): F(a, b, e) gives the field at
-// row a, column b, page e (clamped coordinates), c the node's offset.  Adds the node's FP64
-// area and volume terms to area / vol and counts a volume term of exactly 1 in units.
-template <typename T, class Get>
-__device__ __forceinline__ void toolbox_point(Get F, int i, int j, int k, int im, int ip, int jm, int jp, int km,
-                                              int kp, long long c, const ToolboxOut<T> &o, const Grid &g,
-                                              double ds_, T thr2ds, const Recips &rc, double &area, double &vol,
-                                              int &units)
+// One node of the mixed form's toolbox: the expressions of toolbox_point in FP32 with the
+// divisions by the spacings as products with their FP32 reciprocals and one reciprocal of
+// |grad F| (the reference's quotients, rounded differently within a few ulp); the fields
+// that only an output needs (Gaussian curvature, Heaviside, Dirac delta) are formed only
+// when that output is requested.  The area and volume terms are FP64 on the promoted FP32
+// values over the band (see below).
+template <class Get>
+__device__ __forceinline__ void toolbox_point_f32(Get F, int i, int j, int k, int im, int ip, int jm, int jp, int km,
+                                                  int kp, long long c, const ToolboxOut<float> &o, float thr2ds,
+                                                  const Recips &rc, double &area, double &vol, int &units)
 {
+    bool unit = false;
+    const float fc = F(i, j, k);
+    const float fxp = F(i, jp, k), fxm = F(i, jm, k), fyp = F(ip, j, k), fym = F(im, j, k);
+    const float fzp = F(i, j, kp), fzm = F(i, j, km);
+    const float fx = (fxp - fxm) * rc.f2x, fy = (fyp - fym) * rc.f2y, fz = (fzp - fzm) * rc.f2z;
+    const float gm = vmax(sqrtf(fx * fx + fy * fy + fz * fz), 1e-14f);
+    const float ig = rcp_ftz(gm);  // gm >= 1e-14: a normal number
+    // The area and volume terms in FP64 on the promoted FP32 values: FP32 quotients and
+    // second differences carry a relative error of ~1e-7 per node that does not average out
+    // in the sums (4e-8 of the area at 256^3).  Only nodes with a positive value among the
+    // seven carry a nonzero term, so the FP64 arithmetic runs on the interface band alone.
+    const bool pos =
+        fc > 0.f || fxp > 0.f || fxm > 0.f || fyp > 0.f || fym > 0.f || fzp > 0.f || fzm > 0.f;
+    if (fc < thr2ds && pos) {
+        // FP64 divisions and square roots are slow on this GPU: reciprocals of the spacings
+        // from the host, |grad|^2 clamped instead of |grad|, one division
+        const double c0 = fc, xp = fxp, xm = fxm, yp = fyp, ym = fym, zp = fzp, zm = fzm;
+        const double gx = (xp - xm) * rc.i2x, gy = (yp - ym) * rc.i2y, gz = (zp - zm) * rc.i2z;
+        const double gg = fmax(gx * gx + gy * gy + gz * gz, 1e-28);
+        const double l = (xp - 2 * c0 + xm) * rc.ixx + (yp - 2 * c0 + ym) * rc.iyy + (zp - 2 * c0 + zm) * rc.izz;
+        const double q0 = fmax(c0, 0.0);
+        const double qxp = fmax(xp, 0.0), qxm = fmax(xm, 0.0), qyp = fmax(yp, 0.0), qym = fmax(ym, 0.0);
+        const double qzp = fmax(zp, 0.0), qzm = fmax(zm, 0.0);
+        const double d = (qxp - qxm) * rc.i2x * gx + (qyp - qym) * rc.i2y * gy + (qzp - qzm) * rc.i2z * gz;
+        const double pl =
+            (qxp - 2 * q0 + qxm) * rc.ixx + (qyp - 2 * q0 + qym) * rc.iyy + (qzp - 2 * q0 + qzm) * rc.izz;
+        const double igg = 1.0 / gg;
+        const double h64 = d * igg;
+        if (fabsf(fc) < thr2ds) area += (pl - d * l * igg) * igg;
+        if (h64 == 0.0) {
+            unit = true;
+        } else {
+            const double v1 = 1 - h64;
+            if (v1 == 1.0)
+                unit = true;
+            else
+                vol += v1;
+        }
+    } else if (fc < thr2ds) {
+        unit = true;  // no positive value among the seven: Heaviside 0, Dirac 0
+    }
+    units += unit ? 1 : 0;
+    if (o.f[0]) o.f[0][c] = fx;
+    if (o.f[1]) o.f[1][c] = fy;
+    if (o.f[2]) o.f[2][c] = fz;
+    if (o.f[3]) o.f[3][c] = gm;
+    if (o.f[4]) o.f[4][c] = fx * ig;
+    if (o.f[5]) o.f[5][c] = fy * ig;
+    if (o.f[6]) o.f[6][c] = fz * ig;
+    const bool second = o.f[7] || o.f[8] || o.f[9] || o.f[10] || o.f[11] || o.f[12] || o.f[13] || o.f[14] ||
+                        o.f[15] || o.f[17];
+    if (!second && !o.f[16]) return;
+    const float fxx = (fxp - 2.f * fc + fxm) * rc.fxx;
+    const float fyy = (fyp - 2.f * fc + fym) * rc.fyy;
+    const float fzz = (fzp - 2.f * fc + fzm) * rc.fzz;
+    const float lap = fxx + fyy + fzz;
+    const float ig2 = ig * ig;
+    if (second) {
+        const float fxy = (F(ip, jp, k) + F(im, jm, k) - F(ip, jm, k) - F(im, jp, k)) * rc.f4ds;
+        const float fyz = (F(ip, j, kp) + F(im, j, km) - F(ip, j, km) - F(im, j, kp)) * rc.f4ds;
+        const float fzx = (F(i, jp, kp) + F(i, jm, km) - F(i, jp, km) - F(i, jm, kp)) * rc.f4ds;
+        if (o.f[7]) o.f[7][c] = fxx;
+        if (o.f[8]) o.f[8][c] = fyy;
+        if (o.f[9]) o.f[9][c] = fzz;
+        if (o.f[10]) o.f[10][c] = fxy;
+        if (o.f[11]) o.f[11][c] = fyz;
+        if (o.f[12]) o.f[12][c] = fzx;
+        if (o.f[13]) o.f[13][c] = lap;
+        if (o.f[14]) {
+            const float r1 = fxx * fx + fxy * fy + fzx * fz;
+            const float r2 = fxy * fx + fyy * fy + fyz * fz;
+            const float r3 = fzx * fx + fyz * fy + fzz * fz;
+            o.f[14][c] = -lap * ig + (fx * r1 + fy * r2 + fz * r3) * (ig2 * ig);
+        }
+        if (o.f[15]) {
+            const float q1 = (fyy * fzz - fyz * fyz) * fx + (fzx * fyz - fxy * fzz) * fy + (fxy * fyz - fzx * fyy) * fz;
+            const float q2 = (fyz * fzx - fxy * fzz) * fx + (fxx * fzz - fzx * fzx) * fy + (fzx * fxy - fxx * fyz) * fz;
+            const float q3 = (fxy * fyz - fyy * fzx) * fx + (fzx * fxy - fxx * fyz) * fy + (fxx * fyy - fxy * fxy) * fz;
+            o.f[15][c] = (fx * q1 + fy * q2 + fz * q3) * (ig2 * ig2);
+        }
+    }
+    if (o.f[16] || o.f[17]) {
+        auto H = [&](int a, int b, int e) { return vmax(F(a, b, e), 0.f); };
+        const float hc = vmax(fc, 0.f);
+        const float hxp = H(i, jp, k), hxm = H(i, jm, k), hyp = H(ip, j, k), hym = H(im, j, k);
+        const float hzp = H(i, j, kp), hzm = H(i, j, km);
+        const float dot = (hxp - hxm) * rc.f2x * fx + (hyp - hym) * rc.f2y * fy + (hzp - hzm) * rc.f2z * fz;
+        if (o.f[16]) o.f[16][c] = dot * ig2;
+        if (o.f[17]) {
+            const float plap = (hxp - 2.f * hc + hxm) * rc.fxx + (hyp - 2.f * hc + hym) * rc.fyy +
+                               (hzp - 2.f * hc + hzm) * rc.fzz;
+            o.f[17][c] = plap * ig2 - dot * lap * (ig2 * ig2);
+        }
+    }
+}
+
+// One node of the plain FP64 toolbox (set_calculus_toolbox.cu:9-107), the reference's
+// expressions in its order.
+template <class Get>
+__device__ __forceinline__ void toolbox_point_f64(Get F, int i, int j, int k, int im, int ip, int jm, int jp,
+                                                  int km, int kp, long long c, const ToolboxOut<double> &o,
+                                                  const Grid &g, double ds_, double thr2ds, double &area,
+                                                  double &vol, int &units)
+{
+    using T = double;
     bool unit = false;
     auto H = [&](int a, int b, int e) { return vmax(F(a, b, e), T(0)); };
     const T dx = (T)g.dx, dy = (T)g.dy, dz = (T)g.dz, ds = (T)ds_;
@@ -94,55 +203,17 @@ __device__ __forceinline__ void toolbox_point(Get F, int i, int j, int k, int im
     T plap = pxx + pyy + pzz;
     T heav = dot / gm2;
     T delta = plap / gm2 - dot * lap / gm4;
-    if constexpr (std::is_same<T, float>::value) {
-        // The mixed form's area and volume terms in FP64 on the promoted FP32 values:
-        // the FP32 quotients and second differences above carry a relative error of
-        // ~1e-7 per node that does not average out in the sums (4e-8 of the area at
-        // 256^3).  Only nodes with a positive value among the seven carry a nonzero
-        // term, so the FP64 arithmetic runs on the interface band alone.
-        const bool pos = hc > T(0) || hxp > T(0) || hxm > T(0) || hyp > T(0) || hym > T(0) || hzp > T(0) ||
-                         hzm > T(0);
-        if (fc < thr2ds && pos) {
-            // FP64 divisions and square roots are slow on this GPU: reciprocals of the
-            // spacings from the host, |grad|^2 clamped instead of |grad|, one division
-            const double c0 = fc, xp = fxp, xm = fxm, yp = fyp, ym = fym, zp = fzp, zm = fzm;
-            const double gx = (xp - xm) * rc.i2x, gy = (yp - ym) * rc.i2y, gz = (zp - zm) * rc.i2z;
-            const double gg = fmax(gx * gx + gy * gy + gz * gz, 1e-28);
-            const double l = (xp - 2 * c0 + xm) * rc.ixx + (yp - 2 * c0 + ym) * rc.iyy + (zp - 2 * c0 + zm) * rc.izz;
-            const double q0 = fmax(c0, 0.0);
-            const double qxp = fmax(xp, 0.0), qxm = fmax(xm, 0.0), qyp = fmax(yp, 0.0), qym = fmax(ym, 0.0);
-            const double qzp = fmax(zp, 0.0), qzm = fmax(zm, 0.0);
-            const double d = (qxp - qxm) * rc.i2x * gx + (qyp - qym) * rc.i2y * gy + (qzp - qzm) * rc.i2z * gz;
-            const double pl = (qxp - 2 * q0 + qxm) * rc.ixx + (qyp - 2 * q0 + qym) * rc.iyy +
-                              (qzp - 2 * q0 + qzm) * rc.izz;
-            const double ig = 1.0 / gg;
-            const double h64 = d * ig;
-            if (fabs(fc) < thr2ds) area += (pl - d * l * ig) * ig;
-            if (h64 == 0.0) {
+    if (fabs(fc) < thr2ds) area += delta;
+    if (fc < thr2ds) {
+        // heav == 0 (no positive neighbour) gives a volume term of exactly 1
+        if (heav == T(0)) {
+            unit = true;
+        } else {
+            const double v1 = 1 - heav;
+            if (v1 == 1.0)
                 unit = true;
-            } else {
-                const double v1 = 1 - h64;
-                if (v1 == 1.0)
-                    unit = true;
-                else
-                    vol += v1;
-            }
-        } else if (fc < thr2ds) {
-            unit = true;  // no positive value among the seven: Heaviside 0, Dirac 0
-        }
-    } else {
-        if (fabs(fc) < thr2ds) area += (double)delta;
-        if (fc < thr2ds) {
-            // 1 - heav in FP64; heav == 0 (no positive neighbour) gives exactly 1
-            if (heav == T(0)) {
-                unit = true;
-            } else {
-                const double v1 = 1 - (double)heav;
-                if (v1 == 1.0)
-                    unit = true;
-                else
-                    vol += v1;
-            }
+            else
+                vol += v1;
         }
     }
     if (o.f[0]) o.f[0][c] = fx;
@@ -169,6 +240,21 @@ __device__ __forceinline__ void toolbox_point(Get F, int i, int j, int k, int im
     if (o.f[16]) o.f[16][c] = heav;
     if (o.f[17]) o.f[17][c] = delta;
     units += unit ? 1 : 0;
+}
+
+// One node of the toolbox: F(a, b, e) gives the field at row a, column b, page e (clamped
+// coordinates), c the node's offset.  Adds the node's FP64 area and volume terms to area /
+// vol and counts a volume term of exactly 1 in units.
+template <typename T, class Get>
+__device__ __forceinline__ void toolbox_point(Get F, int i, int j, int k, int im, int ip, int jm, int jp, int km,
+                                              int kp, long long c, const ToolboxOut<T> &o, const Grid &g,
+                                              double ds_, T thr2ds, const Recips &rc, double &area, double &vol,
+                                              int &units)
+{
+    if constexpr (std::is_same<T, float>::value)
+        toolbox_point_f32(F, i, j, k, im, ip, jm, jp, km, kp, c, o, thr2ds, rc, area, vol, units);
+    else
+        toolbox_point_f64(F, i, j, k, im, ip, jm, jp, km, kp, c, o, g, ds_, thr2ds, area, vol, units);
 }
 
 // thr2ds: 2 Ds as the smallest T not below it, so that x < thr2ds in T is exactly
@@ -358,8 +444,20 @@ template <typename T>
 cudaError_t launch_toolbox(const T *phi, ToolboxOut<T> out, const Grid &g, double ds, double *partials,
                            int *nblocks, cudaStream_t s)
 {
-    const Recips rc{1 / (2 * g.dx), 1 / (2 * g.dy), 1 / (2 * g.dz), 1 / (g.dx * g.dx), 1 / (g.dy * g.dy),
-                    1 / (g.dz * g.dz)};
+    const double ds2 = ds * ds;
+    const Recips rc{1 / (2 * g.dx),
+                    1 / (2 * g.dy),
+                    1 / (2 * g.dz),
+                    1 / (g.dx * g.dx),
+                    1 / (g.dy * g.dy),
+                    1 / (g.dz * g.dz),
+                    (float)(1 / (2 * g.dx)),
+                    (float)(1 / (2 * g.dy)),
+                    (float)(1 / (2 * g.dz)),
+                    (float)(1 / (g.dx * g.dx)),
+                    (float)(1 / (g.dy * g.dy)),
+                    (float)(1 / (g.dz * g.dz)),
+                    (float)(1 / (4 * ds2))};
     if constexpr (std::is_same<T, float>::value) {
         // pages per block: a function of the grid alone (the partials, and so the sums, do
         // not depend on the device), about 2400 blocks where the grid allows, 16 pages at most
