@@ -79,6 +79,9 @@ struct TiledArgs {
     int kz;            // pages per block
     Ptr3<float> w;     // SK_VELOCITY: the velocity written
     float floor;       // SK_VELOCITY: the floor of |grad phi|
+    BandShadow sh;     // static-band kinds: the FP64 shadows and crossing values of the band
+    int band_z;        // static-band kinds: page slabs of band blocks after the tile blocks
+    int eno3;          // the extension's band takes the ENO3 (WENORK3) interface scheme
 };
 
 constexpr int PER_THREAD = (PLANE + TY * TX - 1) / (TY * TX);  // halo elements per thread
@@ -443,33 +446,6 @@ __device__ __forceinline__ void stage_tile(const TiledArgs &a, float *smem, int 
     for (int r = 0; k < k1; ++k, ++r) page(r, (r + 3) % RING, (r + 4) % RING, k);
 }
 
-// The ENORK2 extension kind, whose uniform path is light, is latency-bound at 4 blocks per SM
-// (long-scoreboard stalls, DRAM 35% of peak): 5 blocks (47 registers, no spills) took 100
-// pseudo-steps at 256^3 from 26.7 to 23.6 ms.  The ENORK2 reinitialization was slower at 5
-// (25.7 -> 27.7 ms) and keeps 4 with the WENO5 kinds.
-//
-// TMA: the planes by tensor copies (the launch's tensor map of phi_s), else through registers.
-template <int KIND, int STAGE, bool TMA>
-__global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_BLOCKS))
-    k_stage_tiled(const __grid_constant__ TiledArgs a, const __grid_constant__ CUtensorMap tm)
-{
-    static_assert(SH == TMA_BOX_COLS && PLANE <= TMA_SLOT_FLOATS, "ring layouts");
-    if constexpr (TMA) {
-        __shared__ __align__(128) float smem[RING * TMA_SLOT_FLOATS];
-        __shared__ __align__(8) uint64_t bars[RING];
-        __shared__ unsigned fixtab[TMA_FIX * TY * TX];
-        if (threadIdx.x == 0 && threadIdx.y == 0) {
-            for (int s = 0; s < RING; ++s) mbar_init(&bars[s], 1);
-            mbar_init_fence();
-        }
-        __syncthreads();
-        stage_tile<KIND, STAGE, true>(a, smem, blockIdx.x, blockIdx.y, blockIdx.z, &tm, bars, fixtab);
-    } else {
-        __shared__ float smem[RING * PLANE];
-        stage_tile<KIND, STAGE, false>(a, smem, blockIdx.x, blockIdx.y, blockIdx.z);
-    }
-}
-
 // ---------------------------------------------------------------------------------------
 // Extension band of the mixed form with FP64 interface data.  Next to a crossing at a
 // short distance from a node, the one-sided divided difference between the node (or its
@@ -582,16 +558,76 @@ __device__ __forceinline__ void enork2_extend_node_mixed(const TiledArgs &a, con
     sh.s_out[c] = val;
 }
 
-// Band nodes of one stage: the generic per-node update (interface-aware stencils),
-// grid-stride over the queue (reinitialization: also clears the other stage's counter for
-// its next use) or over the static flagged list (extension).
-// The static-band kinds' kernel runs beside the tiled stage: at 8 blocks per SM (64
-// registers) it leaves the tiled kernel more room (256^3: 30 extension pseudo-steps
-// 15.53 -> 15.34 ms); the reinitialization's, which runs alone, has no occupancy target
-// (75 registers; 8 blocks per SM gained nothing there).
-template <int KIND, bool ENO3>
-__global__ void __launch_bounds__(128, (KIND == SK_REINIT ? 0 : 8))
-    k_band_stage(TiledArgs a, BandShadow sh, unsigned *next_counter)
+// one node (offset c) of the static band of a stage of a static-band kind
+template <int KIND>
+__device__ __forceinline__ void static_band_node(const TiledArgs &a, long long c)
+{
+    const Grid &g = a.g;
+    const int k = (int)(c / g.plane);
+    const long long r = c - (long long)k * g.plane;
+    const int j = (int)(r / g.rows);
+    const int i = (int)(r - (long long)j * g.rows);
+    if constexpr (KIND == SK_ENO2)
+        enork2_extend_node_mixed(a, a.sh, i, j, k);
+    else if constexpr (KIND == SK_ENO2R)
+        enork2_reinit_node<float>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
+    else if (a.eno3)
+        extend_node_mixed<true>(a, a.sh, i, j, k);
+    else
+        extend_node_mixed<false>(a, a.sh, i, j, k);
+}
+
+// The ENORK2 extension kind, whose uniform path is light, is latency-bound at 4 blocks per SM
+// (long-scoreboard stalls, DRAM 35% of peak): 5 blocks (47 registers, no spills) took 100
+// pseudo-steps at 256^3 from 26.7 to 23.6 ms.  The ENORK2 reinitialization was slower at 5
+// (25.7 -> 27.7 ms) and keeps 4 with the WENO5 kinds.
+//
+// TMA: the planes by tensor copies (the launch's tensor map of phi_s), else through registers.
+//
+// Static-band kinds: the last a.band_z page slabs of the launch are band blocks, which
+// update the nodes of the classification's flagged list (grid-stride over the list) instead
+// of a tile.  They are dispatched after the tile blocks and fill the SMs as tile blocks
+// retire, in the same launch; every node still has exactly one writer.
+template <int KIND, int STAGE, bool TMA>
+__global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_BLOCKS))
+    k_stage_tiled(const __grid_constant__ TiledArgs a, const __grid_constant__ CUtensorMap tm)
+{
+    static_assert(SH == TMA_BOX_COLS && PLANE <= TMA_SLOT_FLOATS, "ring layouts");
+    if constexpr (static_band_kind(KIND)) {
+        const int bz0 = (int)gridDim.z - a.band_z;
+        if ((int)blockIdx.z >= bz0) {
+            const unsigned nt = TY * TX;
+            const unsigned nb = gridDim.x * gridDim.y * (unsigned)a.band_z;
+            const unsigned b = ((blockIdx.z - (unsigned)bz0) * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+            const unsigned n = *a.counter;
+            for (unsigned t = b * nt + threadIdx.y * TY + threadIdx.x; t < n; t += nb * nt)
+                static_band_node<KIND>(a, a.queue[t]);
+            return;
+        }
+    }
+    if constexpr (TMA) {
+        __shared__ __align__(128) float smem[RING * TMA_SLOT_FLOATS];
+        __shared__ __align__(8) uint64_t bars[RING];
+        __shared__ unsigned fixtab[TMA_FIX * TY * TX];
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            for (int s = 0; s < RING; ++s) mbar_init(&bars[s], 1);
+            mbar_init_fence();
+        }
+        __syncthreads();
+        stage_tile<KIND, STAGE, true>(a, smem, blockIdx.x, blockIdx.y, blockIdx.z, &tm, bars, fixtab);
+    } else {
+        __shared__ float smem[RING * PLANE];
+        stage_tile<KIND, STAGE, false>(a, smem, blockIdx.x, blockIdx.y, blockIdx.z);
+    }
+}
+
+// Band nodes of one reinitialization stage: the generic per-node update (interface-aware
+// stencils), grid-stride over the queue the tiled kernel filled; also clears the other
+// stage's counter for its next use.  (The static bands of the other kinds run in band
+// blocks of the tiled launch itself, k_stage_tiled.)  No occupancy target (75 registers;
+// 8 blocks per SM gained nothing).
+template <bool ENO3>
+__global__ void __launch_bounds__(128) k_band_stage(TiledArgs a, unsigned *next_counter)
 {
     const unsigned n = *a.counter;
     if (next_counter && blockIdx.x == 0 && threadIdx.x == 0) *next_counter = 0u;
@@ -602,14 +638,7 @@ __global__ void __launch_bounds__(128, (KIND == SK_REINIT ? 0 : 8))
         const long long r = c - (long long)k * g.plane;
         const int j = (int)(r / g.rows);
         const int i = (int)(r - (long long)j * g.rows);
-        if (KIND == SK_REINIT)
-            reinit_node<float, ENO3, true>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
-        else if (KIND == SK_ENO2)
-            enork2_extend_node_mixed(a, sh, i, j, k);
-        else if (KIND == SK_ENO2R)
-            enork2_reinit_node<float>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
-        else
-            extend_node_mixed<ENO3>(a, sh, i, j, k);
+        reinit_node<float, ENO3, true>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
     }
 }
 
@@ -734,6 +763,15 @@ inline TiledArgs tiled_args(const Grid &g)
 
 // the band kernels run latency-bound per-node code: 16 blocks of 128 threads per SM
 inline int band_blocks() { return list_blocks() * 4; }
+
+// page slabs of band blocks appended to a static-band kind's tile grid gr: as many threads
+// as the separate band kernel had (band_blocks() x 128), in blocks of the tile kernel's shape
+inline int static_band_slabs(const dim3 &gr)
+{
+    const long long want = (long long)band_blocks() * 128 / (TY * TX);
+    const long long per_slab = (long long)gr.x * gr.y;
+    return (int)std::max<long long>(1, (want + per_slab - 1) / per_slab);
+}
 
 inline dim3 tiled_grid(const Grid &g, int kz)
 {
@@ -945,37 +983,18 @@ cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const 
     a.kz = tile_pages(g, kind);
     dim3 gr = tiled_grid(g, a.kz), bl(TY, TX);
     if (static_band_kind(kind)) {
-        // the tiled kernel is submitted first so that its blocks are dispatched ahead of the
-        // band kernel's (a grid-stride kernel whose blocks mostly find no work)
-        SideLane *ln = side_lane(s);
-        cudaError_t e;
-        if (ln && (e = cudaEventRecord(ln->fork, s)) != cudaSuccess) return e;
+        // the static band in the same launch: band blocks after the tile blocks
+        a.sh = st.shadow;
+        a.eno3 = eno3 ? 1 : 0;
+        a.band_z = static_band_slabs(gr);
+        gr.z += (unsigned)a.band_z;
         if (kind == SK_ENO2)
             launch_stage_kind<SK_ENO2>(a.stage, gr, bl, s, a);
         else if (kind == SK_ENO2R)
             launch_stage_kind<SK_ENO2R>(a.stage, gr, bl, s, a);
         else
             launch_stage_kind<SK_EXTEND>(a.stage, gr, bl, s, a);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        cudaStream_t bs = s;
-        if (ln) {
-            if ((e = cudaStreamWaitEvent(ln->side, ln->fork, 0)) != cudaSuccess) return e;
-            bs = ln->side;
-        }
-        if (kind == SK_ENO2)
-            k_band_stage<SK_ENO2, false><<<band_blocks(), 128, 0, bs>>>(a, st.shadow, next);
-        else if (kind == SK_ENO2R)
-            k_band_stage<SK_ENO2R, false><<<band_blocks(), 128, 0, bs>>>(a, st.shadow, next);
-        else if (eno3)
-            k_band_stage<SK_EXTEND, true><<<band_blocks(), 128, 0, bs>>>(a, st.shadow, next);
-        else
-            k_band_stage<SK_EXTEND, false><<<band_blocks(), 128, 0, bs>>>(a, st.shadow, next);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        if (ln) {
-            if ((e = cudaEventRecord(ln->join, bs)) != cudaSuccess) return e;
-            if ((e = cudaStreamWaitEvent(s, ln->join, 0)) != cudaSuccess) return e;
-        }
-        return cudaSuccess;
+        return cudaGetLastError();
     }
     if (kind == SK_REINIT)
         launch_stage_kind<SK_REINIT>(a.stage, gr, bl, s, a);
@@ -985,9 +1004,9 @@ cudaError_t launch_tiled_stage(int kind, bool eno3, const TiledStage &st, const 
     if (e != cudaSuccess || kind == SK_ADVECT) return e;
     // the reinitialization's band is queued by the tiled kernel, so its kernel follows it
     if (eno3)
-        k_band_stage<SK_REINIT, true><<<band_blocks(), 128, 0, s>>>(a, st.shadow, next);
+        k_band_stage<true><<<band_blocks(), 128, 0, s>>>(a, next);
     else
-        k_band_stage<SK_REINIT, false><<<band_blocks(), 128, 0, s>>>(a, st.shadow, next);
+        k_band_stage<false><<<band_blocks(), 128, 0, s>>>(a, next);
     return cudaGetLastError();
 }
 
@@ -1072,6 +1091,8 @@ cudaError_t launch_tiled_batch(int kind, bool eno3, const TiledStage *st, const 
         }
         a.stage = st[v].stage;
         a.kz = tile_pages(g, kind);
+        a.sh = st[v].shadow;
+        a.eno3 = eno3 ? 1 : 0;
         const dim3 gr = tiled_grid(g, a.kz);
         B.v[v] = a;
         B.nx[v] = (int)gr.x;
@@ -1087,6 +1108,9 @@ cudaError_t launch_tiled_batch(int kind, bool eno3, const TiledStage *st, const 
     const int bgrid = band_blocks();
     cudaError_t e;
     if (static_band_kind(kind)) {
+        // the band kernel beside the persistent tiled kernel (measured faster than band work
+        // items appended to the persistent kernel's list: 168 against 181 ms per step of the
+        // 64-vesicle batch, whose bands are large)
         SideLane *ln = side_lane(s);
         if (ln && (e = cudaEventRecord(ln->fork, s)) != cudaSuccess) return e;
         if (kind == SK_ENO2)

@@ -50,11 +50,11 @@ W64 = 8
 BYTES_PER_NODE_STEP64 = EXT * 56 * W64 + ADV * 17 * W64 + RE * (29 * W64 + 3) + (7 + 10 + 13 + 1 + 7) * W64
 BYTES_REINIT64 = 29 * W64 + 3
 # kernels launched per vesicle step: toolbox, sum, classify, velocity (uniform nodes and
-# the flagged list), crossing values, the band's FP64 shadow, 3*EXT extension stages each
-# with its band kernel, band max, time step, 3 advection stages, setDistance (scan +
-# roots), classify, 3*RE reinitialization stages each with its band kernel (memsets of the
-# list counters are not kernels)
-LAUNCHES_PER_STEP = 1 + 1 + 1 + 2 + 1 + 1 + 2 * 3 * EXT + 1 + 1 + 3 * ADV + 2 + 1 + 2 * 3 * RE
+# the flagged list), crossing values, the band's FP64 shadow, 3*EXT extension stages (the
+# band in band blocks of the same launch), band max, time step, 3 advection stages,
+# setDistance (scan + roots), classify, 3*RE reinitialization stages each with its band
+# kernel (memsets of the list counters are not kernels)
+LAUNCHES_PER_STEP = 1 + 1 + 1 + 2 + 1 + 1 + 3 * EXT + 1 + 1 + 3 * ADV + 2 + 1 + 2 * 3 * RE
 
 
 def replica_seed(rank: int) -> int:
@@ -948,8 +948,8 @@ def main():
     hbm, peak_kind = peaks()
     sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
     sm_mhz = clk.summary()["sm_mhz"]
-    ext_roof = stage_roofline("extension", "one FP32 WENO5 RK3 extension stage: k_stage_tiled<SK_EXTEND> + "
-                              "k_band_stage<SK_EXTEND> (side stream)", stage_ms, BYTES_EXTEND / 3 * N**3,
+    ext_roof = stage_roofline("extension", "one FP32 WENO5 RK3 extension stage: k_stage_tiled<SK_EXTEND>, its "
+                              "band blocks in the same launch", stage_ms, BYTES_EXTEND / 3 * N**3,
                               "extend_stage_f32_256.md", hbm, peak_kind, sm_mhz, sms)
     re_roof = stage_roofline("reinitialization", "one FP32 WENO5 RK3 reinitialization stage: k_stage_tiled<SK_REINIT> "
                              "+ k_band_stage<SK_REINIT>", re_stage_ms, BYTES_REINIT / 3 * N**3,

@@ -15,9 +15,9 @@ def test_step_counts():
     assert (bench.EXT, bench.ADV, bench.RE) == (30, 1, 20)
     w = 4
     assert bench.BYTES_PER_NODE_STEP == 30 * 56 * w + 17 * w + 20 * (29 * w + 3) + 38 * w
-    # toolbox, sum, classify, velocity (2), crossing, shadow, 90 x (tiled + band), band max,
+    # toolbox, sum, classify, velocity (2), crossing, shadow, 90 tiled (band blocks inside), band max,
     # time step, 3 advection stages, setDistance (2), classify, 60 x (tiled + band)
-    assert bench.LAUNCHES_PER_STEP == 315
+    assert bench.LAUNCHES_PER_STEP == 225
 
 
 def test_profiled_figures_match_summaries():
