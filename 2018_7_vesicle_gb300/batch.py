@@ -2,7 +2,7 @@
 
 Two batch steps:
 
-* `step_batched` (FP32): vsl_vesicle_step_batch_f32, one persistent launch per RK stage
+* `step_batched` (FP32): vsl_vesicle_step_batch_f32, one launch per RK stage
   running that stage of every vesicle (a work list of all the vesicles' tiles), with the
   per-vesicle set-up passes between them; recorded once as a CUDA graph and replayed.  A
   batch step of 64 vesicles is then ~1,300 launches instead of ~20,000, and the small
@@ -49,7 +49,7 @@ class VesicleBatch:
         return arr
 
     def step_batched(self, ext_iters: int = 30, reinit_iters: int = 20, cfl: float = 0.5, graph: bool = True):
-        """One batch step with each RK stage of all the vesicles as one persistent launch
+        """One batch step with each RK stage of all the vesicles as one launch
         (vsl_vesicle_step_batch_f32; FP32 vesicles only).  graph=True records the step's
         launches once as a CUDA graph and replays it (re-recorded when the arguments
         change); bitwise the results of `step_loop`."""

@@ -842,7 +842,7 @@ int op_reinit_tol(T *F, int max_iters, double tol, double band, const T *xpr, co
 
 // ---------------------------------------------------------------------------------------
 // a batch of vesicle steps (FP32): the composite step of op_vesicle_step for every vesicle,
-// with each RK stage of all the vesicles as one persistent launch (launch_tiled_batch); the
+// with each RK stage of all the vesicles as one launch (launch_tiled_batch); the
 // per-vesicle set-up passes (toolbox, extension velocity and crossing values, time step,
 // setDistance, classification) stay per vesicle, spread over BATCH_LANES streams forked
 // from and joined back into the caller's stream (parallel branches under stream capture).

@@ -182,7 +182,7 @@ cudaError_t tma_timeouts(unsigned *count);
 cudaError_t launch_velocity_tiled(const float *phi, const uint8_t *flags, Ptr3<float> v, const Grid &g, float floor,
                                   cudaStream_t s);
 // the same stage (same kind and RK stage) of `count` <= TILED_BATCH_MAX grids as one
-// persistent launch over all their tiles, and one launch for all their band nodes
+// launch over all their tiles, and one launch for all their band nodes
 constexpr int TILED_BATCH_MAX = 64;
 cudaError_t launch_tiled_batch(int kind, bool eno3, const TiledStage *st, const Grid *grids, int count, cudaStream_t s);
 // the mixed form's extension set-up at the listed (flagged) nodes: FP64 crossing values on

@@ -643,10 +643,11 @@ __global__ void __launch_bounds__(128) k_band_stage(TiledArgs a, unsigned *next_
 }
 
 // ---------------------------------------------------------------------------------------
-// Batched stages: one persistent launch runs one RK stage of up to BATCH_MAX grids (a batch
-// of vesicles).  The work list is every grid's tiles (tile x, tile y, page slab) in order;
-// the launch's blocks walk it grid-stride, so small grids that could not fill the GPU alone
-// share its SMs, and a batch step issues one launch per stage instead of one per vesicle.
+// Batched stages: one launch runs one RK stage of up to BATCH_MAX grids (a batch of
+// vesicles).  The work list is every grid's tiles (tile x, tile y, page slab) in order, one
+// block per item (the kernel walks the list grid-stride, so a smaller grid of blocks also
+// covers it), so small grids that could not fill the GPU alone share its SMs, and a batch
+// step issues one launch per stage instead of one per vesicle.
 // The stages' order is the launches' order on the stream: no block waits for another.
 // Every grid's arguments travel in the kernel parameter (a __grid_constant__ table indexed
 // by the block-uniform grid number).
@@ -1029,33 +1030,23 @@ cudaError_t launch_velocity_tiled(const float *phi, const uint8_t *flags, Ptr3<f
 // batched stages (k_stage_tiled_batch, k_band_stage_batch)
 // ---------------------------------------------------------------------------------------
 namespace {
-// resident blocks per SM of a batched stage kernel (its occupancy; the persistent grid)
-template <int KIND, int STAGE> int batch_blocks()
-{
-    static int n = 0;
-    if (n == 0) {
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_stage_tiled_batch<KIND, STAGE>, TY * TX, 0);
-        n = (sms > 0 ? sms : 132) * (per > 0 ? per : 1);
-    }
-    return n;
-}
-
+// One block per work item: the hardware block scheduler hands items to SMs as blocks retire.
+// (A persistent grid of the resident blocks walking the list grid-stride measured slower,
+// 168 against 158 ms per step of the 64-vesicle batch: its static split left SMs idle at
+// the end of each launch.)
 template <int KIND> cudaError_t launch_batch_kind(int stage, const TiledBatch &B, int total, cudaStream_t s)
 {
     const dim3 bl(TY, TX);
-    auto go = [&](auto kernel, int blocks) {
-        kernel<<<std::min(total, blocks), bl, 0, s>>>(B);
+    auto go = [&](auto kernel) {
+        kernel<<<total, bl, 0, s>>>(B);
         return cudaGetLastError();
     };
-    if (stage == 0) return go(k_stage_tiled_batch<KIND, 0>, batch_blocks<KIND, 0>());
+    if (stage == 0) return go(k_stage_tiled_batch<KIND, 0>);
     if constexpr (KIND == SK_ENO2 || KIND == SK_ENO2R) {
-        return go(k_stage_tiled_batch<KIND, 1>, batch_blocks<KIND, 1>());
+        return go(k_stage_tiled_batch<KIND, 1>);
     } else {
-        if (stage == 1) return go(k_stage_tiled_batch<KIND, 1>, batch_blocks<KIND, 1>());
-        return go(k_stage_tiled_batch<KIND, 2>, batch_blocks<KIND, 2>());
+        if (stage == 1) return go(k_stage_tiled_batch<KIND, 1>);
+        return go(k_stage_tiled_batch<KIND, 2>);
     }
 }
 }  // namespace
@@ -1108,8 +1099,8 @@ cudaError_t launch_tiled_batch(int kind, bool eno3, const TiledStage *st, const 
     const int bgrid = band_blocks();
     cudaError_t e;
     if (static_band_kind(kind)) {
-        // the band kernel beside the persistent tiled kernel (measured faster than band work
-        // items appended to the persistent kernel's list: 168 against 181 ms per step of the
+        // the band kernel beside the batched tiled kernel (measured faster than band work
+        // items appended to a persistent kernel's list: 168 against 181 ms per step of the
         // 64-vesicle batch, whose bands are large)
         SideLane *ln = side_lane(s);
         if (ln && (e = cudaEventRecord(ln->fork, s)) != cudaSuccess) return e;

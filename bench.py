@@ -452,7 +452,7 @@ def profile_case(which, m, torch):
 def batched_measure(torch, pkg, S, steps: int, seed: int = 0, tune: bool = True):
     """The batched workload: 64 vesicles with node counts per axis drawn from
     {48, 64, 96, 128, 160} and half axes U[0.4, 1.0], FP32, advanced `steps` vesicle steps
-    with each RK stage of all the vesicles as one persistent launch (step_batched, a graph
+    with each RK stage of all the vesicles as one launch (step_batched, a graph
     per batch step) and, for comparison, as one CUDA graph of parallel per-vesicle branches
     and by the per-vesicle launch loop.  With `tune`, pages per block of the tiled kernels
     are first autotuned for the batched step (VesicleBatch.autotune, mode "batched"); the

@@ -355,7 +355,7 @@ int vsl_vesicle_step_f32(float *F, float *xpr, float *xpl, float *ypf, float *yp
  * advances one vesicle per MATLAB process).  Every vesicle gets the step of
  * vsl_vesicle_step_f32 (its own field, cached distances, info output and workspace of
  * vsl_workspace_bytes(VSL_OP_VESICLE_STEP, its grid, 4)); each RK stage of all the
- * vesicles runs as one persistent launch over all their tiles, 64 vesicles at a time, and
+ * vesicles runs as one launch over all their tiles, 64 vesicles at a time, and
  * the per-vesicle set-up passes stay per vesicle.  Results are bitwise those of
  * vsl_vesicle_step_f32 called per vesicle.  `vesicles` is a HOST array read during the
  * call; the pointers in it are device pointers. */

@@ -123,7 +123,7 @@ def test_edge_mix_with_tuned_pages(pkg, vsl, oracle_mod):
 
 @pytest.mark.parametrize("count,edges,iters", [(5, (24, 32, 40), (8, 5)), (66, (16, 20, 24), (4, 3))])
 def test_batched_stages_match_loop(pkg, vsl, count, edges, iters):
-    """vsl_vesicle_step_batch_f32 (each RK stage of all the vesicles as one persistent launch;
+    """vsl_vesicle_step_batch_f32 (each RK stage of all the vesicles as one launch;
     66 vesicles run as two launches' worth, 64 + 2) gives bitwise the per-vesicle steps,
     as a graph replay and as direct launches, over two batch steps."""
     loop = B.VesicleBatch(make_batch_edges(pkg, count, edges), streams=2)
