@@ -691,17 +691,18 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
 }
 
 // The band nodes of one stage of every grid of a batch (k_band_stage per grid, all the
-// grids' band nodes as one work list in one launch).
+// grids' band nodes as one work list in one launch).  8 blocks per SM (64 registers) for
+// every kind: the batch's bands are large and latency-bound (64-vesicle batch step 158.0 ->
+// 157.0 ms with the reinitialization's held to 64 registers too).
 struct BandBatch {
-    TiledArgs v[BATCH_MAX];
-    BandShadow sh[BATCH_MAX];
+    TiledArgs v[BATCH_MAX];     // with each grid's band shadows (static-band kinds)
     unsigned *next[BATCH_MAX];  // reinitialization: the other stage's counter, zeroed here
     int count;
 };
 static_assert(sizeof(BandBatch) <= 32000, "kernel parameter space");
 
 template <int KIND, bool ENO3>
-__global__ void __launch_bounds__(128, (KIND == SK_REINIT ? 0 : 8)) k_band_stage_batch(const __grid_constant__ BandBatch B)
+__global__ void __launch_bounds__(128, 8) k_band_stage_batch(const __grid_constant__ BandBatch B)
 {
     // one work list of every grid's band nodes: the grids' counts, prefix-summed per block,
     // place work item t at node t - first[v] of grid v (first[v] <= t < first[v + 1]), so the
@@ -737,11 +738,11 @@ __global__ void __launch_bounds__(128, (KIND == SK_REINIT ? 0 : 8)) k_band_stage
         if (KIND == SK_REINIT)
             reinit_node<float, ENO3, true>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
         else if (KIND == SK_ENO2)
-            enork2_extend_node_mixed(a, B.sh[lo], i, j, k);
+            enork2_extend_node_mixed(a, a.sh, i, j, k);
         else if (KIND == SK_ENO2R)
             enork2_reinit_node<float>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
         else
-            extend_node_mixed<ENO3>(a, B.sh[lo], i, j, k);
+            extend_node_mixed<ENO3>(a, a.sh, i, j, k);
     }
 }
 
@@ -1091,7 +1092,6 @@ cudaError_t launch_tiled_batch(int kind, bool eno3, const TiledStage *st, const 
         B.start[v] = total;
         total += (int)(gr.x * gr.y * gr.z);
         BB.v[v] = a;
-        BB.sh[v] = st[v].shadow;
         BB.next[v] = next;
     }
     B.start[count] = total;

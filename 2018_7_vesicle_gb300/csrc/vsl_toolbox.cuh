@@ -53,59 +53,73 @@ struct Recips {
     float f2x, f2y, f2z, fxx, fyy, fzz, f4ds;  // the same in FP32, and 1 / (4 Ds^2)
 };
 
+// The FP64 area and volume terms of one band node of the mixed form from its seven FP32
+// values v[0..6] (centre, x+, x-, y+, y-, z+, z-) and v[7] != 0 where the node is in the
+// area band: FP32 quotients and second differences carry a relative error of ~1e-7 per
+// node that does not average out in the sums (4e-8 of the area at 256^3), so the terms are
+// FP64 on the promoted values.  FP64 divisions and square roots are slow on this GPU:
+// reciprocals of the spacings from the host, |grad|^2 clamped instead of |grad|, one
+// division.
+__device__ __forceinline__ void band_terms_f64(const float v[8], const Recips &rc, double &area, double &vol,
+                                               int &units)
+{
+    const double c0 = v[0], xp = v[1], xm = v[2], yp = v[3], ym = v[4], zp = v[5], zm = v[6];
+    const double gx = (xp - xm) * rc.i2x, gy = (yp - ym) * rc.i2y, gz = (zp - zm) * rc.i2z;
+    const double gg = fmax(gx * gx + gy * gy + gz * gz, 1e-28);
+    const double l = (xp - 2 * c0 + xm) * rc.ixx + (yp - 2 * c0 + ym) * rc.iyy + (zp - 2 * c0 + zm) * rc.izz;
+    const double q0 = fmax(c0, 0.0);
+    const double qxp = fmax(xp, 0.0), qxm = fmax(xm, 0.0), qyp = fmax(yp, 0.0), qym = fmax(ym, 0.0);
+    const double qzp = fmax(zp, 0.0), qzm = fmax(zm, 0.0);
+    const double d = (qxp - qxm) * rc.i2x * gx + (qyp - qym) * rc.i2y * gy + (qzp - qzm) * rc.i2z * gz;
+    const double pl = (qxp - 2 * q0 + qxm) * rc.ixx + (qyp - 2 * q0 + qym) * rc.iyy + (qzp - 2 * q0 + qzm) * rc.izz;
+    const double igg = 1.0 / gg;
+    const double h64 = d * igg;
+    if (v[7] != 0.f) area += (pl - d * l * igg) * igg;
+    if (h64 == 0.0) {
+        units += 1;
+    } else {
+        const double v1 = 1 - h64;
+        if (v1 == 1.0)
+            units += 1;
+        else
+            vol += v1;
+    }
+}
+
 // One node of the mixed form's toolbox: the expressions of toolbox_point in FP32 with the
 // divisions by the spacings as products with their FP32 reciprocals and one reciprocal of
 // |grad F| (the reference's quotients, rounded differently within a few ulp); the fields
 // that only an output needs (Gaussian curvature, Heaviside, Dirac delta) are formed only
-// when that output is requested.  The area and volume terms are FP64 on the promoted FP32
-// values over the band (see below).
+// when that output is requested.  Returns whether the node carries FP64 area and volume
+// terms (a node of the volume band, F < 2 Ds, with a positive value among its seven), with
+// the inputs of band_terms_f64 in v; a node of the volume band without a positive value
+// has a volume term of exactly 1 (Heaviside 0, Dirac 0) and is counted in units here.
 template <class Get>
-__device__ __forceinline__ void toolbox_point_f32(Get F, int i, int j, int k, int im, int ip, int jm, int jp, int km,
+__device__ __forceinline__ bool toolbox_point_f32(Get F, int i, int j, int k, int im, int ip, int jm, int jp, int km,
                                                   int kp, long long c, const ToolboxOut<float> &o, float thr2ds,
-                                                  const Recips &rc, double &area, double &vol, int &units)
+                                                  const Recips &rc, float v[8], int &units)
 {
-    bool unit = false;
     const float fc = F(i, j, k);
     const float fxp = F(i, jp, k), fxm = F(i, jm, k), fyp = F(ip, j, k), fym = F(im, j, k);
     const float fzp = F(i, j, kp), fzm = F(i, j, km);
     const float fx = (fxp - fxm) * rc.f2x, fy = (fyp - fym) * rc.f2y, fz = (fzp - fzm) * rc.f2z;
     const float gm = vmax(sqrtf(fx * fx + fy * fy + fz * fz), 1e-14f);
     const float ig = rcp_ftz(gm);  // gm >= 1e-14: a normal number
-    // The area and volume terms in FP64 on the promoted FP32 values: FP32 quotients and
-    // second differences carry a relative error of ~1e-7 per node that does not average out
-    // in the sums (4e-8 of the area at 256^3).  Only nodes with a positive value among the
-    // seven carry a nonzero term, so the FP64 arithmetic runs on the interface band alone.
     const bool pos =
         fc > 0.f || fxp > 0.f || fxm > 0.f || fyp > 0.f || fym > 0.f || fzp > 0.f || fzm > 0.f;
-    if (fc < thr2ds && pos) {
-        // FP64 divisions and square roots are slow on this GPU: reciprocals of the spacings
-        // from the host, |grad|^2 clamped instead of |grad|, one division
-        const double c0 = fc, xp = fxp, xm = fxm, yp = fyp, ym = fym, zp = fzp, zm = fzm;
-        const double gx = (xp - xm) * rc.i2x, gy = (yp - ym) * rc.i2y, gz = (zp - zm) * rc.i2z;
-        const double gg = fmax(gx * gx + gy * gy + gz * gz, 1e-28);
-        const double l = (xp - 2 * c0 + xm) * rc.ixx + (yp - 2 * c0 + ym) * rc.iyy + (zp - 2 * c0 + zm) * rc.izz;
-        const double q0 = fmax(c0, 0.0);
-        const double qxp = fmax(xp, 0.0), qxm = fmax(xm, 0.0), qyp = fmax(yp, 0.0), qym = fmax(ym, 0.0);
-        const double qzp = fmax(zp, 0.0), qzm = fmax(zm, 0.0);
-        const double d = (qxp - qxm) * rc.i2x * gx + (qyp - qym) * rc.i2y * gy + (qzp - qzm) * rc.i2z * gz;
-        const double pl =
-            (qxp - 2 * q0 + qxm) * rc.ixx + (qyp - 2 * q0 + qym) * rc.iyy + (qzp - 2 * q0 + qzm) * rc.izz;
-        const double igg = 1.0 / gg;
-        const double h64 = d * igg;
-        if (fabsf(fc) < thr2ds) area += (pl - d * l * igg) * igg;
-        if (h64 == 0.0) {
-            unit = true;
-        } else {
-            const double v1 = 1 - h64;
-            if (v1 == 1.0)
-                unit = true;
-            else
-                vol += v1;
-        }
+    const bool need = fc < thr2ds && pos;
+    if (need) {
+        v[0] = fc;
+        v[1] = fxp;
+        v[2] = fxm;
+        v[3] = fyp;
+        v[4] = fym;
+        v[5] = fzp;
+        v[6] = fzm;
+        v[7] = fabsf(fc) < thr2ds ? 1.f : 0.f;
     } else if (fc < thr2ds) {
-        unit = true;  // no positive value among the seven: Heaviside 0, Dirac 0
+        units += 1;
     }
-    units += unit ? 1 : 0;
     if (o.f[0]) o.f[0][c] = fx;
     if (o.f[1]) o.f[1][c] = fy;
     if (o.f[2]) o.f[2][c] = fz;
@@ -115,7 +129,7 @@ __device__ __forceinline__ void toolbox_point_f32(Get F, int i, int j, int k, in
     if (o.f[6]) o.f[6][c] = fz * ig;
     const bool second = o.f[7] || o.f[8] || o.f[9] || o.f[10] || o.f[11] || o.f[12] || o.f[13] || o.f[14] ||
                         o.f[15] || o.f[17];
-    if (!second && !o.f[16]) return;
+    if (!second && !o.f[16]) return need;
     const float fxx = (fxp - 2.f * fc + fxm) * rc.fxx;
     const float fyy = (fyp - 2.f * fc + fym) * rc.fyy;
     const float fzz = (fzp - 2.f * fc + fzm) * rc.fzz;
@@ -158,6 +172,7 @@ __device__ __forceinline__ void toolbox_point_f32(Get F, int i, int j, int k, in
             o.f[17][c] = plap * ig2 - dot * lap * (ig2 * ig2);
         }
     }
+    return need;
 }
 
 // One node of the plain FP64 toolbox (set_calculus_toolbox.cu:9-107), the reference's
@@ -251,10 +266,8 @@ __device__ __forceinline__ void toolbox_point(Get F, int i, int j, int k, int im
                                               double ds_, T thr2ds, const Recips &rc, double &area, double &vol,
                                               int &units)
 {
-    if constexpr (std::is_same<T, float>::value)
-        toolbox_point_f32(F, i, j, k, im, ip, jm, jp, km, kp, c, o, thr2ds, rc, area, vol, units);
-    else
-        toolbox_point_f64(F, i, j, k, im, ip, jm, jp, km, kp, c, o, g, ds_, thr2ds, area, vol, units);
+    static_assert(std::is_same<T, double>::value, "the mixed form's toolbox is k_toolbox_tiled");
+    toolbox_point_f64(F, i, j, k, im, ip, jm, jp, km, kp, c, o, g, ds_, thr2ds, area, vol, units);
 }
 
 // thr2ds: 2 Ds as the smallest T not below it, so that x < thr2ds in T is exactly
@@ -363,18 +376,60 @@ __global__ void __launch_bounds__(NT, 4) k_toolbox_tiled(const T *__restrict__ f
     double area = 0.0, vol = 0.0;
     int units = 0;
     const long long col = (long long)clampi(j, g.cols) * g.rows + clampi(i, g.rows);
+    // Per warp, the band nodes waiting for their FP64 area and volume terms (their eight
+    // inputs, one column per node), evaluated 32 at a time, one node per lane: a warp with
+    // one band node would otherwise issue the FP64 block (1/64 of the FP32 rate on this
+    // GPU) for all its lanes.  The queue's order (page, then lane) and each lane's sum are
+    // fixed, so the sums stay reproducible.
+    __shared__ float q64[NW][8][64];
+    float(*Q)[64] = q64[tid >> 5];
+    const unsigned lane = tid & 31;
+    int qn = 0;  // queued nodes of this warp (warp-uniform)
+    auto evaluate = [&](int n) {  // the first n <= 32 queued nodes, lane l the l-th
+        if ((int)lane < n) {
+            float v[8];
+#pragma unroll
+            for (int m = 0; m < 8; ++m) v[m] = Q[m][lane];
+            band_terms_f64(v, rc, area, vol, units);
+        }
+    };
     for (int k = k0; k < k1; ++k) {
         // plane k+1 is stored, and no warp reads the slot of page k-2 any more
         __syncthreads();
         fetch(k + 2);
+        bool need = false;
+        float v[8];
         if (active) {
             const int km = clampi(k - 1, g.pges), kp = clampi(k + 1, g.pges);
-            toolbox_point<T>(F, i, j, k, im, ip, jm, jp, km, kp, col + (long long)k * g.plane, o, g, ds_, thr2ds, rc,
-                             area, vol, units);
+            need = toolbox_point_f32(F, i, j, k, im, ip, jm, jp, km, kp, col + (long long)k * g.plane, o, thr2ds, rc, v,
+                                     units);
+        }
+        if (partials) {
+            const unsigned m = __ballot_sync(0xffffffffu, need);
+            if (m) {
+                if (need) {
+                    const int r = qn + __popc(m & ((1u << lane) - 1u));
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) Q[e][r] = v[e];
+                }
+                qn += __popc(m);
+                __syncwarp();
+                if (qn >= 32) {
+                    evaluate(32);
+                    __syncwarp();
+                    if ((int)lane < qn - 32) {
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) Q[e][lane] = Q[e][lane + 32];
+                    }
+                    __syncwarp();
+                    qn -= 32;
+                }
+            }
         }
         store(k + 2);
     }
     if (!partials) return;
+    if (qn > 0) evaluate(qn);
     __shared__ double sa[NW], sv[NW];
     __shared__ int sc[NW];
     const int ones = __reduce_add_sync(0xffffffffu, units);
