@@ -10,13 +10,13 @@
 // both the forward derivative at k and the backward derivative at k+1.
 //
 // Nodes whose update needs the interface-aware (nonuniform) stencil -- the "band" -- are
-// not computed here; k_band_stage processes them with the generic per-node code, so the
-// uniform WENO5 path runs without divergence.  For the reinitialization a node is band
-// when the sign of phi changes on one of its stencil edges (the reference's trigger); the
-// tiled kernel queues those (warp-aggregated atomics) and the band kernel follows it.  For
-// the extension a node is band when one of its distances differs from the spacing (a
-// superset of the reference's trigger r1 < h || l1 < h; the band kernel applies the exact
-// test): a static list, so the band kernel runs beside the tiled kernel on a side stream.
+// not computed by the tile code; the generic per-node code updates them, so the uniform
+// WENO5 path runs without divergence.  For the reinitialization a node is band when the
+// sign of phi changes on one of its stencil edges (the reference's trigger); the tiled
+// kernel queues those (warp-aggregated atomics) and k_band_stage follows it.  For the
+// extension a node is band when one of its distances differs from the spacing (a superset
+// of the reference's trigger r1 < h || l1 < h; the band code applies the exact test): a
+// static list, which band blocks of the tiled launch itself update.
 #pragma once
 
 #include <algorithm>
@@ -657,6 +657,8 @@ struct TiledBatch {
     TiledArgs v[BATCH_MAX];
     int start[BATCH_MAX + 1];  // first work item of each grid; start[count] = all items
     int nx[BATCH_MAX], ny[BATCH_MAX];  // tiles along rows and columns
+    int tiles[BATCH_MAX];  // tile items of each grid; its band blocks follow them
+    int nb[BATCH_MAX];     // static-band kinds: band blocks of each grid
     int count;
 };
 static_assert(sizeof(TiledBatch) <= 32000, "kernel parameter space");
@@ -684,16 +686,30 @@ __global__ void __launch_bounds__(TY *TX, (KIND == SK_ENO2 ? 5 : VSL_TILED_MIN_B
     for (int w = blockIdx.x; w < total; w += gridDim.x) {
         const int v = batch_member(B.start, B.count, w);
         const int local = w - B.start[v];
-        const int rest = local / B.nx[v];
-        stage_tile<KIND, STAGE>(B.v[v], smem, local - rest * B.nx[v], rest % B.ny[v], rest / B.ny[v]);
-        __syncthreads();  // the next item's prologue rewrites the plane ring
+        if (local < B.tiles[v]) {
+            const int rest = local / B.nx[v];
+            stage_tile<KIND, STAGE>(B.v[v], smem, local - rest * B.nx[v], rest % B.ny[v], rest / B.ny[v]);
+            __syncthreads();  // the next item's prologue rewrites the plane ring
+            continue;
+        }
+        if constexpr (static_band_kind(KIND)) {
+            // band block of grid v: its static band grid-stride, right after its tiles (its
+            // planes still in L2)
+            const TiledArgs &a = B.v[v];
+            const unsigned nt = TY * TX, nb = (unsigned)B.nb[v];
+            const unsigned n = *a.counter;
+            for (unsigned t = (unsigned)(local - B.tiles[v]) * nt + threadIdx.y * TY + threadIdx.x; t < n; t += nb * nt)
+                static_band_node<KIND>(a, a.queue[t]);
+        }
     }
 }
 
-// The band nodes of one stage of every grid of a batch (k_band_stage per grid, all the
-// grids' band nodes as one work list in one launch).  8 blocks per SM (64 registers) for
-// every kind: the batch's bands are large and latency-bound (64-vesicle batch step 158.0 ->
-// 157.0 ms with the reinitialization's held to 64 registers too).
+// The reinitialization's band nodes of one stage of every grid of a batch (k_band_stage per
+// grid, all the grids' queued band nodes as one work list in one launch, which follows the
+// batched tiled launch that fills the queues).  8 blocks per SM (64 registers): the batch's
+// bands are large and latency-bound (64-vesicle batch step 158.0 -> 157.0 ms against 75
+// registers).  The static bands of the other kinds run as band blocks of the batched tiled
+// launch, each grid's right after its tiles.
 struct BandBatch {
     TiledArgs v[BATCH_MAX];     // with each grid's band shadows (static-band kinds)
     unsigned *next[BATCH_MAX];  // reinitialization: the other stage's counter, zeroed here
@@ -701,7 +717,7 @@ struct BandBatch {
 };
 static_assert(sizeof(BandBatch) <= 32000, "kernel parameter space");
 
-template <int KIND, bool ENO3>
+template <bool ENO3>
 __global__ void __launch_bounds__(128, 8) k_band_stage_batch(const __grid_constant__ BandBatch B)
 {
     // one work list of every grid's band nodes: the grids' counts, prefix-summed per block,
@@ -735,14 +751,7 @@ __global__ void __launch_bounds__(128, 8) k_band_stage_batch(const __grid_consta
         const long long r = c - (long long)k * g.plane;
         const int j = (int)(r / g.rows);
         const int i = (int)(r - (long long)j * g.rows);
-        if (KIND == SK_REINIT)
-            reinit_node<float, ENO3, true>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
-        else if (KIND == SK_ENO2)
-            enork2_extend_node_mixed(a, a.sh, i, j, k);
-        else if (KIND == SK_ENO2R)
-            enork2_reinit_node<float>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
-        else
-            extend_node_mixed<ENO3>(a, a.sh, i, j, k);
+        reinit_node<float, ENO3, true>(a.phi_s, a.phi_n, a.out, a.flags, a.d, g, a.stage, i, j, k);
     }
 }
 
@@ -825,53 +834,6 @@ int set_tile_pages(int rows, int cols, int pges, int kind, int pages)
     return VSL_OK;
 }
 
-// ---------------------------------------------------------------------------------------
-// side lanes: the extension's band kernel reads only the stage input and writes only the
-// nodes of the static list, which the tiled kernel leaves alone, so it runs beside the
-// tiled kernel on a second stream (forked from and joined back into the caller's stream
-// by events; under stream capture the two launches become parallel graph branches).
-// One lane per (device, caller stream), created on first use with this thread's capture
-// mode relaxed for the creation calls, so a first use inside a capture sequence is legal.
-// With the pool full, or if creation fails, the band kernel follows the tiled kernel on
-// the caller's stream.
-// ---------------------------------------------------------------------------------------
-namespace {
-struct SideLane {
-    int device;
-    cudaStream_t user;
-    cudaStream_t side;
-    cudaEvent_t fork, join;
-};
-constexpr int MAX_LANES = 256;
-std::mutex lane_mutex;
-SideLane lanes[MAX_LANES];
-int n_lanes = 0;
-
-SideLane *side_lane(cudaStream_t s)
-{
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
-    std::lock_guard<std::mutex> lock(lane_mutex);
-    for (int e = 0; e < n_lanes; ++e)
-        if (lanes[e].device == dev && lanes[e].user == s) return &lanes[e];
-    if (n_lanes == MAX_LANES) return nullptr;
-    SideLane ln{dev, s, nullptr, nullptr, nullptr};
-    cudaStreamCaptureMode mode = cudaStreamCaptureModeRelaxed;
-    if (cudaThreadExchangeStreamCaptureMode(&mode) != cudaSuccess) return nullptr;
-    bool ok = cudaStreamCreateWithFlags(&ln.side, cudaStreamNonBlocking) == cudaSuccess;
-    ok = ok && cudaEventCreateWithFlags(&ln.fork, cudaEventDisableTiming) == cudaSuccess;
-    ok = ok && cudaEventCreateWithFlags(&ln.join, cudaEventDisableTiming) == cudaSuccess;
-    cudaThreadExchangeStreamCaptureMode(&mode);
-    if (!ok) {
-        if (ln.join) cudaEventDestroy(ln.join);
-        if (ln.fork) cudaEventDestroy(ln.fork);
-        if (ln.side) cudaStreamDestroy(ln.side);
-        return nullptr;
-    }
-    lanes[n_lanes] = ln;
-    return &lanes[n_lanes++];
-}
-}  // namespace
 
 // ---------------------------------------------------------------------------------------
 // TMA plane loads: the driver's tensor-map encoder (looked up once through the runtime) and
@@ -1090,7 +1052,12 @@ cudaError_t launch_tiled_batch(int kind, bool eno3, const TiledStage *st, const 
         B.nx[v] = (int)gr.x;
         B.ny[v] = (int)gr.y;
         B.start[v] = total;
-        total += (int)(gr.x * gr.y * gr.z);
+        B.tiles[v] = (int)(gr.x * gr.y * gr.z);
+        // static-band kinds: band blocks for a band of about 3% of the nodes, one node per
+        // thread (a larger band is walked grid-stride)
+        const long long nodes = (long long)g.rows * g.cols * g.pges;
+        B.nb[v] = static_band_kind(kind) ? (int)std::max<long long>(1, (nodes * 3 / 100 + TY * TX - 1) / (TY * TX)) : 0;
+        total += B.tiles[v] + B.nb[v];
         BB.v[v] = a;
         BB.next[v] = next;
     }
@@ -1099,44 +1066,16 @@ cudaError_t launch_tiled_batch(int kind, bool eno3, const TiledStage *st, const 
     const int bgrid = band_blocks();
     cudaError_t e;
     if (static_band_kind(kind)) {
-        // the band kernel beside the batched tiled kernel (measured faster than band work
-        // items appended to a persistent kernel's list: 168 against 181 ms per step of the
-        // 64-vesicle batch, whose bands are large)
-        SideLane *ln = side_lane(s);
-        if (ln && (e = cudaEventRecord(ln->fork, s)) != cudaSuccess) return e;
-        if (kind == SK_ENO2)
-            e = launch_batch_kind<SK_ENO2>(stage, B, total, s);
-        else if (kind == SK_ENO2R)
-            e = launch_batch_kind<SK_ENO2R>(stage, B, total, s);
-        else
-            e = launch_batch_kind<SK_EXTEND>(stage, B, total, s);
-        if (e != cudaSuccess) return e;
-        cudaStream_t bs = s;
-        if (ln) {
-            if ((e = cudaStreamWaitEvent(ln->side, ln->fork, 0)) != cudaSuccess) return e;
-            bs = ln->side;
-        }
-        if (kind == SK_ENO2)
-            k_band_stage_batch<SK_ENO2, false><<<bgrid, 128, 0, bs>>>(BB);
-        else if (kind == SK_ENO2R)
-            k_band_stage_batch<SK_ENO2R, false><<<bgrid, 128, 0, bs>>>(BB);
-        else if (eno3)
-            k_band_stage_batch<SK_EXTEND, true><<<bgrid, 128, 0, bs>>>(BB);
-        else
-            k_band_stage_batch<SK_EXTEND, false><<<bgrid, 128, 0, bs>>>(BB);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        if (ln) {
-            if ((e = cudaEventRecord(ln->join, bs)) != cudaSuccess) return e;
-            if ((e = cudaStreamWaitEvent(s, ln->join, 0)) != cudaSuccess) return e;
-        }
-        return cudaSuccess;
+        if (kind == SK_ENO2) return launch_batch_kind<SK_ENO2>(stage, B, total, s);
+        if (kind == SK_ENO2R) return launch_batch_kind<SK_ENO2R>(stage, B, total, s);
+        return launch_batch_kind<SK_EXTEND>(stage, B, total, s);
     }
     e = kind == SK_REINIT ? launch_batch_kind<SK_REINIT>(stage, B, total, s) : launch_batch_kind<SK_ADVECT>(stage, B, total, s);
     if (e != cudaSuccess || kind == SK_ADVECT) return e;
     if (eno3)
-        k_band_stage_batch<SK_REINIT, true><<<bgrid, 128, 0, s>>>(BB);
+        k_band_stage_batch<true><<<bgrid, 128, 0, s>>>(BB);
     else
-        k_band_stage_batch<SK_REINIT, false><<<bgrid, 128, 0, s>>>(BB);
+        k_band_stage_batch<false><<<bgrid, 128, 0, s>>>(BB);
     return cudaGetLastError();
 }
 
