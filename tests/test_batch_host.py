@@ -1,0 +1,53 @@
+"""Argument checks of the batch of vesicle steps (vsl_vesicle_step_batch_f32) without a GPU:
+every check runs on the host before any CUDA call, so bad descriptors and arguments are
+rejected with their status codes and an empty batch is a no-op."""
+import ctypes
+import importlib
+
+from conftest import ROOT  # noqa: F401  (puts the repository on sys.path)
+
+L = importlib.import_module("2018_7_vesicle_gb300._lib")
+
+VSL_OK, VSL_ERR_NULL, VSL_ERR_SHAPE, VSL_ERR_VALUE, VSL_ERR_WORKSPACE = 0, 1, 2, 3, 4
+FAKE = 0x1000  # never dereferenced: every call below fails its checks first (or has no work)
+
+
+def descriptor(rows=40, cols=36, pges=32, h=0.05, ws=FAKE * 16, nbytes=1 << 30, **over):
+    d = L.VesicleF32()
+    d.F = d.xpr = d.xpl = d.ypf = d.ypb = d.zpu = d.zpd = d.info = FAKE
+    d.rows, d.cols, d.pges = rows, cols, pges
+    d.dx = d.dy = d.dz = h
+    d.workspace, d.workspace_bytes = ws, nbytes
+    for k, v in over.items():
+        setattr(d, k, v)
+    return d
+
+
+def call(vsl, arr, count, ext=30, re=20, cfl=0.5):
+    ptr = ctypes.addressof(arr) if arr is not None else None
+    return vsl.raw("vsl_vesicle_step_batch_f32", ptr, count, ext, re, cfl, None)
+
+
+def test_batch_rejects_bad_arguments(vsl):
+    arr = (L.VesicleF32 * 1)(descriptor())
+    assert call(vsl, None, 1) == VSL_ERR_NULL
+    assert call(vsl, arr, -1) == VSL_ERR_VALUE
+    assert call(vsl, arr, 1, ext=-1) == VSL_ERR_VALUE
+    assert call(vsl, arr, 1, re=-1) == VSL_ERR_VALUE
+    assert call(vsl, arr, 1, cfl=0.0) == VSL_ERR_VALUE
+    assert call(vsl, arr, 1, cfl=float("nan")) == VSL_ERR_VALUE
+
+
+def test_batch_rejects_bad_descriptors(vsl):
+    good = descriptor()
+    for bad, status in ((descriptor(F=None), VSL_ERR_NULL), (descriptor(info=None), VSL_ERR_NULL),
+                        (descriptor(rows=0), VSL_ERR_SHAPE), (descriptor(dx=0.0), VSL_ERR_VALUE),
+                        (descriptor(ws=None), VSL_ERR_WORKSPACE), (descriptor(nbytes=16), VSL_ERR_WORKSPACE),
+                        (descriptor(ws=FAKE + 1), VSL_ERR_WORKSPACE)):
+        # the bad member is found wherever it sits, before any vesicle is stepped
+        arr = (L.VesicleF32 * 3)(good, bad, good)
+        assert call(vsl, arr, 3) == status
+
+
+def test_empty_batch_is_a_no_op(vsl):
+    assert call(vsl, None, 0) == VSL_OK
