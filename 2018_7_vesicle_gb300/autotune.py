@@ -19,7 +19,10 @@ from .sdf3 import SDF3, colmajor_full
 KINDS = {"reinit": 0, "extend": 1, "advect": 2, "enork2_extend": 3, "enork2_reinit": 4}
 CANDIDATES = (4, 8, 10, 15, 16, 20, 25, 30, 32, 40, 64)
 DEFAULT_PAGES = 20  # pages per block of a shape not in the table
-TILE_ROWS, TILE_COLS = 32, 8  # tile of one block of the tiled kernels
+# tile of one block of the tiled kernels, fixed at compile time: 32x4, 32x16 and 64x4 tiles
+# gave bitwise the same results and ran -1 % / +4 % / +1 % on the 256^3 vesicle step and
+# +1 % / +3 % / +10 % on a batch of 64 vesicles of 48..160 nodes per axis
+TILE_ROWS, TILE_COLS = 32, 8
 BLOCKS_PER_SM = 4  # resident blocks per SM of the tiled kernels (launch bounds; 5 for the ENORK2 extension)
 
 
