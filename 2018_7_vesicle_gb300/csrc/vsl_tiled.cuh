@@ -388,9 +388,9 @@ __device__ __forceinline__ void stage_tile(const TiledArgs &a, float *smem, int 
                 step = KIND == SK_EXTEND ? tr * a.dt_uniform : dt_adv * tr;
             }
             if (!band && KIND == SK_VELOCITY) {
-                // k_velocity_uniform's arithmetic: each axis reconstructs the side it keeps
-                // (D+ where |p4| < |p2|, else D-), x and y as the lanes of one packed WENO5,
-                // z with itself in both lanes, so the velocity is the same to the bit
+                // the unit normal of a node away from the interface: each axis reconstructs
+                // the side it keeps (D+ where |p4| < |p2|, else D-), x and y as the lanes of
+                // one packed WENO5, z with itself in both lanes
                 const bool bx = !(fabsf(px[4]) < fabsf(px[2])), by = !(fabsf(py[4]) < fabsf(py[2]));
                 const bool bz = !(fabsf(q[4]) < fabsf(q[2]));
                 const float2 dxy =
