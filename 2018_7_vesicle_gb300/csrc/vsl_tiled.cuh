@@ -489,22 +489,39 @@ __device__ __forceinline__ void extend_node_mixed(const TiledArgs &a, const Band
                 crossing_gaps(L, ax, a.d, c, r1, l1, h, rc, lc);
                 float G[6], pv[7];
                 insert_interface_gaps(p, r1, rc, l1, lc, h, 0.f, 0.f, G, pv);
-                double hs[7];
-#pragma unroll
-                for (int m = 0; m < 7; ++m) hs[m] = (double)pv[m];
-                hs[3] = cs;
-                if (r1 < h) {
-                    hs[4] = __ldg(sh.cp.p[2 * ax] + c);
-                    hs[5] = shadow_or(sh, a.flags, c + L.stride, p[4]);
+                // The line hs[0..6] in FP64: pv, with the node's shadow cs at 3, and on each
+                // side with a crossing the crossing value (2 / 4) and the shadow of the
+                // neighbour beyond it (1 / 5).  The differences are taken in FP64 where an
+                // end is such a value (the digits cancel there), the quotients in FP32.  A
+                // segment between two FP32 values takes the FP32 difference instead: the FP64
+                // difference of two FP32 values is exact unless their exponents lie more than
+                // 28 apart, and then it lies far from an FP32 rounding boundary, so rounded to
+                // FP32 it is the FP32 difference.  Same bits, with 4 of the 6 segments in FP64
+                // on a one-sided crossing (FP64 runs at 1/64 of the FP32 rate here).
+                const bool rs = r1 < h, both = rs && l1 < h;
+                // the side with the crossing (the right one when both have one): the chain
+                // e0 .. e4 = hs[2..6] (right) or hs[0..4] (left) and its four segments
+                const double cx = __ldg(sh.cp.p[rs ? 2 * ax : 2 * ax + 1] + c);
+                const double sn = shadow_or(sh, a.flags, rs ? c + L.stride : c - L.stride, rs ? p[4] : p[2]);
+                double e0 = (double)(rs ? pv[2] : pv[0]);
+                float x0 = 0.f, x1 = 0.f;  // both sides: segments 0 and 1 in FP64 as well
+                if (both) {
+                    const double cl = __ldg(sh.cp.p[2 * ax + 1] + c);
+                    const double sl = shadow_or(sh, a.flags, c - L.stride, p[2]);
+                    x0 = (float)(sl - (double)pv[0]);
+                    x1 = (float)(cl - sl);
+                    e0 = cl;
                 }
-                if (l1 < h) {
-                    hs[2] = __ldg(sh.cp.p[2 * ax + 1] + c);
-                    hs[1] = shadow_or(sh, a.flags, c - L.stride, p[2]);
-                }
-                // the differences in FP64 (where the digits cancel), the quotients in FP32
-                float dd[6];
+                const double e1 = rs ? cs : sn, e3 = rs ? sn : cs, e4 = (double)(rs ? pv[6] : pv[4]);
+                const float f0 = (float)(e1 - e0), f1 = (float)(cx - e1), f2 = (float)(e3 - cx),
+                            f3 = (float)(e4 - e3);
+                // the other side's two segments, between FP32 values
+                const float u0 = rs ? pv[0] : pv[4], u1 = rs ? pv[1] : pv[5], u2 = rs ? pv[2] : pv[6];
+                const float g0 = __fsub_rn(u1, u0), g1 = __fsub_rn(u2, u1);
+                float dd[6] = {rs ? (both ? x0 : g0) : f0, rs ? (both ? x1 : g1) : f1, rs ? f0 : f2,
+                               rs ? f1 : f3, rs ? f2 : g0, rs ? f3 : g1};
 #pragma unroll
-                for (int m = 0; m < 6; ++m) dd[m] = (float)(hs[m + 1] - hs[m]) / G[m];
+                for (int m = 0; m < 6; ++m) dd[m] = dd[m] / G[m];
                 if (ENO3)
                     eno3_nonuniform_pair_dd(G, dd, df[ax], db[ax]);
                 else
