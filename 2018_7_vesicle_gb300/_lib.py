@@ -69,6 +69,7 @@ for _suf in ("f64", "f32"):
             f"vsl_weno5_rk3_extend_{_suf}": "pip" + "pppppp" + _G + "pz" + "s",
             f"vsl_wenork3_extend_{_suf}": "pip" + _G + "pz" + "s",
             f"vsl_weno5_rk3_surface_redistance_{_suf}": "piip" + _G + "pz" + "s",
+            f"vsl_wenork3_surface_redistance_{_suf}": "piip" + _G + "pz" + "s",
             f"vsl_area_volume_{_suf}": "pp" + _G + "pz" + "s",
             f"vsl_weno5_rk3_advection_{_suf}": "pppppi" + _G + "pz" + "s",
             f"vsl_vesicle_step_{_suf}": "p" + "pppppp" + "iid" + "p" + _G + "pz" + "s",
@@ -105,6 +106,7 @@ OP = {
     "aux_toolbox": 17,
     "masked_integral": 18,
     "reinit_tol": 19,
+    "surface_redistance_eno3": 20,
 }
 
 

@@ -264,7 +264,8 @@ size_t measure(int op, const Grid &g, int elem)
         case VSL_OP_REINIT_ENO3: carve_reinit<T>(w, g, true); break;
         case VSL_OP_EXTEND_WENO5: carve_extend<T>(w, g, false); break;
         case VSL_OP_EXTEND_ENO3: carve_extend<T>(w, g, true); break;
-        case VSL_OP_SURFACE_REDISTANCE: carve_redist<T>(w, g); break;
+        case VSL_OP_SURFACE_REDISTANCE:
+        case VSL_OP_SURFACE_REDISTANCE_ENO3: carve_redist<T>(w, g); break;
         case VSL_OP_AREA_VOLUME: carve_reduce(w, g, 2); break;
         case VSL_OP_ADVECTION: carve_reinit<T>(w, g, false); break;
         case VSL_OP_VESICLE_STEP: carve_step<T>(w, g); break;
@@ -547,46 +548,51 @@ int op_extend_eno3(T *C, int iteration, const T *F, int rows, int cols, int pges
     return extend_loop<T>(C, iteration, d, w, g, true, s);
 }
 
+// WENO5RK3ClosetPointSurfaceRedistance.m:4-157 (eno3 = false) and its WENORK3 form,
+// WENORK3ClosetPointSurfaceRedistance.m:4-152 (eno3 = true): the same composition with
+// the cubic distances, the WENORK3 upwind normals, crossing values and extension step and
+// the ENO3 interface scheme of the reinitialization
 template <typename T>
 int op_redistance(T *A, int iter1, int iter2, const T *F, int rows, int cols, int pges, double dx, double dy,
-                  double dz, void *ws, size_t bytes, cudaStream_t s)
+                  double dz, bool eno3, void *ws, size_t bytes, cudaStream_t s)
 {
     if (any_null(A, F)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     if (iter1 < 0 || iter2 < 0) return VSL_ERR_VALUE;
     Grid g = make_grid(rows, cols, pges, dx, dy, dz);
-    if (int st = check_ws(VSL_OP_SURFACE_REDISTANCE, g, sizeof(T), ws, bytes)) return st;
+    const int op = eno3 ? VSL_OP_SURFACE_REDISTANCE_ENO3 : VSL_OP_SURFACE_REDISTANCE;
+    if (int st = check_ws(op, g, sizeof(T), ws, bytes)) return st;
     Bump b(ws);
     RedistWork<T> w = carve_redist<T>(b, g);
     // reinitialization part: distances of A, mask A < 0 (ClosetPointSurfaceRedistance.m:15-25)
-    VSL_TRY(launch_set_distance<T>(A, w.re.dist, g, true, w.re.edges, s));
+    VSL_TRY(launch_set_distance<T>(A, w.re.dist, g, !eno3, w.re.edges, s));
     Ptr6<const T> dA = cview(w.re.dist);
     VSL_TRY(launch_classify<T>(A, dA, w.re.flags, NodeList{nullptr, nullptr}, g, s));
     // extension part: distances and upwind normals of F, floor 1e-14 (:37-74)
-    VSL_TRY(launch_set_distance<T>(F, w.ext.dist, g, true, w.ext.edges, s));
+    VSL_TRY(launch_set_distance<T>(F, w.ext.dist, g, !eno3, w.ext.edges, s));
     Ptr6<const T> dF = cview(w.ext.dist);
-    if (int st = extend_setup<T>(F, dF, w.ext, g, false, 1e-14, s)) return st;
+    if (int st = extend_setup<T>(F, dF, w.ext, g, eno3, 1e-14, s)) return st;
     const bool fast = fast_form<T>();
     if (int st = band_reset(w.re.band, s)) return st;
     // one reinitialization stage of A's pseudo-time loop (tiled kernels for FP32)
     auto re_stage = [&](const T *in, T *out, int stage) -> cudaError_t {
         if constexpr (std::is_same<T, float>::value)
-            return tiled(0, false, w.re.band, in, A, out, w.re.flags, dA, BandShadow{}, Ptr3<const float>{},
+            return tiled(0, eno3, w.re.band, in, A, out, w.re.flags, dA, BandShadow{}, Ptr3<const float>{},
                          nullptr, nullptr, stage, g, s);
         else
-            return launch_reinit_stage<T>(in, A, out, w.re.flags, dA, g, stage, false, fast, s);
+            return launch_reinit_stage<T>(in, A, out, w.re.flags, dA, g, stage, eno3, fast, s);
     };
     // the reinit stages need their own temporaries: the extension uses w.ext.b/c
     T *t1 = w.re.b, *t2 = w.re.c;
     for (int it = 0; it < iter1; ++it) {
-        if (int st = extend_loop<T>(A, iter2, dF, w.ext, g, false, s)) return st;
+        if (int st = extend_loop<T>(A, iter2, dF, w.ext, g, eno3, s)) return st;
         VSL_TRY(re_stage(A, t1, 0));
-        if (int st = extend_loop<T>(t1, iter2, dF, w.ext, g, false, s)) return st;
+        if (int st = extend_loop<T>(t1, iter2, dF, w.ext, g, eno3, s)) return st;
         VSL_TRY(re_stage(t1, t2, 1));
-        if (int st = extend_loop<T>(t2, iter2, dF, w.ext, g, false, s)) return st;
+        if (int st = extend_loop<T>(t2, iter2, dF, w.ext, g, eno3, s)) return st;
         VSL_TRY(re_stage(t2, A, 2));
     }
-    return extend_loop<T>(A, iter2, dF, w.ext, g, false, s);
+    return extend_loop<T>(A, iter2, dF, w.ext, g, eno3, s);
 }
 
 template <typename T>
@@ -1504,7 +1510,13 @@ size_t vsl_workspace_bytes(int op, int rows, int cols, int pges, int elem_bytes)
                                                int pges, double dx, double dy, double dz, void *ws, size_t bytes,  \
                                                vsl_stream_t stream)                                                \
     {                                                                                                              \
-        return op_redistance<T>(A, iter1, iter2, F, rows, cols, pges, dx, dy, dz, ws, bytes, stream);              \
+        return op_redistance<T>(A, iter1, iter2, F, rows, cols, pges, dx, dy, dz, false, ws, bytes, stream);       \
+    }                                                                                                              \
+    int vsl_wenork3_surface_redistance_##SUF(T *A, int iter1, int iter2, const T *F, int rows, int cols, int pges, \
+                                             double dx, double dy, double dz, void *ws, size_t bytes,              \
+                                             vsl_stream_t stream)                                                  \
+    {                                                                                                              \
+        return op_redistance<T>(A, iter1, iter2, F, rows, cols, pges, dx, dy, dz, true, ws, bytes, stream);        \
     }                                                                                                              \
     int vsl_area_volume_##SUF(const T *F, double *area_volume, int rows, int cols, int pges, double dx, double dy, \
                               double dz, void *ws, size_t bytes, vsl_stream_t stream)                              \

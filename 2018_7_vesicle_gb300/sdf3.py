@@ -288,6 +288,16 @@ class SDF3:
                    *self.GD3.args(), _ptr(ws), ws.numel(), _stream())
         return out
 
+    def WENORK3ClosetPointSurfaceRedistance(self, A, iter1: int, iter2: int):
+        """WENORK3ClosetPointSurfaceRedistance.m:4-152: the WENO5 method's composition with
+        the cubic distances, the WENORK3 normals, crossing values and extension step and the
+        ENO3 interface scheme of the reinitialization."""
+        out = self._field(A).clone()
+        ws = self.workspace("surface_redistance_eno3")
+        lib().call(self._fn("vsl_wenork3_surface_redistance"), _ptr(out), int(iter1), int(iter2), _ptr(self.F),
+                   *self.GD3.args(), _ptr(ws), ws.numel(), _stream())
+        return out
+
     def ENORK2ClosetPointSurfaceRedistance(self, A, iter1: int, iter2: int):
         """ENORK2ClosetPointSurfaceRedistance.m:4-128 (second-order ENO, Heun RK2)."""
         out = self._field(A).clone()

@@ -186,7 +186,8 @@ enum {
     VSL_OP_RELAX_STEP = 16,
     VSL_OP_AUX_TOOLBOX = 17,
     VSL_OP_MASKED_INTEGRAL = 18,
-    VSL_OP_REINIT_TOL = 19
+    VSL_OP_REINIT_TOL = 19,
+    VSL_OP_SURFACE_REDISTANCE_ENO3 = 20
 };
 
 /* Tuning of the FP32 tiled stage kernels (no counterpart in the reference).  Each block
@@ -297,6 +298,16 @@ int vsl_weno5_rk3_surface_redistance_f64(double *A, int iter1, int iter2, const 
 int vsl_weno5_rk3_surface_redistance_f32(float *A, int iter1, int iter2, const float *F, int rows, int cols,
                                          int pges, double dx, double dy, double dz, void *workspace,
                                          size_t workspace_bytes, vsl_stream_t stream);
+/* ref: +SD/@SDF3/WENORK3ClosetPointSurfaceRedistance.m:4-152.  The WENORK3 form of the
+ * same composition: cubic distances of A and F, the WENORK3 upwind normals of F (1e-14
+ * floor), crossing values and extension step, and the reinitialization with the ENO3
+ * interface scheme.  Workspace op VSL_OP_SURFACE_REDISTANCE_ENO3. */
+int vsl_wenork3_surface_redistance_f64(double *A, int iter1, int iter2, const double *F, int rows, int cols,
+                                       int pges, double dx, double dy, double dz, void *workspace,
+                                       size_t workspace_bytes, vsl_stream_t stream);
+int vsl_wenork3_surface_redistance_f32(float *A, int iter1, int iter2, const float *F, int rows, int cols,
+                                       int pges, double dx, double dy, double dz, void *workspace,
+                                       size_t workspace_bytes, vsl_stream_t stream);
 
 /* ref: +SD/@SDF3/SDF3.m:73-80 (calArea, calVolume) after GPUsetCalculusToolBox.m:2-42.
  * area_volume: device pointer to 2 doubles, written with the FP64 sums

@@ -410,22 +410,28 @@ def extend_eno3(K, g: Grid, F, C, iteration: int):
 # ---------------------------------------------------------------------------------------
 
 
-def surface_redistance(K, g: Grid, F, A, iter1: int, iter2: int):
+def surface_redistance(K, g: Grid, F, A, iter1: int, iter2: int, eno3: bool = False):
+    """WENO5RK3ClosetPointSurfaceRedistance(A, iter1, iter2); eno3=True gives
+    WENORK3ClosetPointSurfaceRedistance (V/+SD/@SDF3/WENORK3ClosetPointSurfaceRedistance.m:4-152),
+    the same composition with cubic_boundary_correction for both distance sets (:16, :39),
+    WENORK3_upwind_normal (:55), WENORK3_reinitialization_step (:85-101),
+    WENORK3_boundary_interpolate (:118) and WENORK3_extend_step (:126-141)."""
     A = F64(A).copy(order="F")
-    dA = set_distance(K, g, A)
+    dA = set_distance(K, g, A, cubic=eno3)
     deltat = F64(0.3 * dA.min_dist)
     mask = np.asfortranarray(A < 0)
-    dF = set_distance(K, g, F)
+    dF = set_distance(K, g, F, cubic=eno3)
     fdeltat = F64(0.3 * dF.min_dist)
-    v = extension_velocity(K, g, F, dF, floor=1e-14)
+    v = extension_velocity(K, g, F, dF, eno3=eno3, floor=1e-14)
     step = zeros(g)
+    re_step = K.re_step_eno3 if eno3 else K.re_step
 
     def ext(C):
-        cp = crossing_values(K, g, C, dF)
-        return extend_loop(K, g, C, iter2, dF, v, fdeltat, cp)
+        cp = crossing_values(K, g, C, dF, eno3=eno3)
+        return extend_loop(K, g, C, iter2, dF, v, fdeltat, cp, eno3=eno3)
 
     def re(Cs):
-        K.re_step(step, F64(Cs), mask, deltat, *dA.six(), *g.args(), g.num_ele)
+        re_step(step, F64(Cs), mask, deltat, *dA.six(), *g.args(), g.num_ele)
         return step.copy(order="F")
 
     new = A

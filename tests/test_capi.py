@@ -100,6 +100,7 @@ def test_workspace_sizes(vsl):
     ext32 = 5 * 4 + 9 * 8 + 1
     for op, per_node_min, min32 in (("reinit_weno5", 2 * 8 + 1, None), ("reinit_eno3", 8 * 8 + 1, None),
                                     ("extend_weno5", 11 * 8 + 1, ext32), ("surface_redistance", 25 * 8 + 2, ext32),
+                                    ("surface_redistance_eno3", 25 * 8 + 2, ext32),
                                     ("advection", 2 * 8, None), ("vesicle_step", 15 * 8 + 1, ext32),
                                     ("reinit_tol", 2 * 8 + 1, None)):
         n = vsl.workspace_bytes(op, 32, 24, 16, 8)

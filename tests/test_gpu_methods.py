@@ -138,15 +138,19 @@ def test_extend_config1(pkg, oracles, config1, eno3):
         assert max_rel(got, O.extend_weno5(K, g, F, O.set_distance(K, g, F), C, 30)) <= TOL
 
 
-def test_surface_redistance(pkg, oracles):
+@pytest.mark.parametrize("eno3", [False, True])
+def test_surface_redistance(pkg, oracles, eno3):
+    """WENO5RK3ClosetPointSurfaceRedistance and its WENORK3 form (cubic distances, WENORK3
+    normals, crossing values and extension, ENO3 reinitialization)."""
     O, K, KC = oracles
     x, y, z = S.cube_grid(28, -1.0, 1.0)
     F = np.asfortranarray(np.sqrt(x**2 + y**2 + z**2) - 0.6)
     A = np.asfortranarray(np.exp(z) - 1)
     m = make(pkg, x, y, z, F)
-    got = host(m.WENO5RK3ClosetPointSurfaceRedistance(dev(A), 3, 6))
-    assert same(got, O.surface_redistance(KC, ograd(O, x, y, z), F, A, 3, 6))
-    assert max_rel(got, O.surface_redistance(K, ograd(O, x, y, z), F, A, 3, 6)) <= TOL_REDIST_LIBM
+    method = m.WENORK3ClosetPointSurfaceRedistance if eno3 else m.WENO5RK3ClosetPointSurfaceRedistance
+    got = host(method(dev(A), 3, 6))
+    assert same(got, O.surface_redistance(KC, ograd(O, x, y, z), F, A, 3, 6, eno3=eno3))
+    assert max_rel(got, O.surface_redistance(K, ograd(O, x, y, z), F, A, 3, 6, eno3=eno3)) <= TOL_REDIST_LIBM
 
 
 def test_area_volume_and_toolbox(pkg, oracles, config1):

@@ -130,14 +130,16 @@ def test_golden_cases_fp32(pkg, vsl, name):
     assert rel_err(host(m.WENORK3Extend(C, 3)), G["extend3_it3"]) <= 5e-5
 
 
-def test_surface_redistance(pkg, oracle_mod):
+@pytest.mark.parametrize("eno3", [False, True])
+def test_surface_redistance(pkg, oracle_mod, eno3):
     O = oracle_mod
     x, y, z = S.cube_grid(28, -1.0, 1.0)
     F = np.asfortranarray(np.sqrt(x**2 + y**2 + z**2) - 0.6)
     A = np.asfortranarray(np.exp(z) - 1)
     m = f32(pkg, x, y, z, F)
-    got = host(m.WENO5RK3ClosetPointSurfaceRedistance(dev(A), 3, 6))
-    ref = O.surface_redistance(O.kernels("port"), O.grid_from_mesh(x, y, z), F, A, 3, 6)
+    method = m.WENORK3ClosetPointSurfaceRedistance if eno3 else m.WENO5RK3ClosetPointSurfaceRedistance
+    got = host(method(dev(A), 3, 6))
+    ref = O.surface_redistance(O.kernels("port"), O.grid_from_mesh(x, y, z), F, A, 3, 6, eno3=eno3)
     assert rel_err(got, ref) <= 5e-5
 
 

@@ -38,6 +38,8 @@ def test_bit_identical_on_seeded_inputs(both, seed):
     v = [O.F64(rng.standard_normal(g.size)) for _ in range(3)]
     assert np.array_equal(O.weno_dot_grad(P, g, *v, F), O.weno_dot_grad(R, g, *v, F))
     assert np.array_equal(O.surface_redistance(P, g, F, C, 1, 2), O.surface_redistance(R, g, F, C, 1, 2))
+    assert np.array_equal(O.surface_redistance(P, g, F, C, 1, 2, eno3=True),
+                          O.surface_redistance(R, g, F, C, 1, 2, eno3=True))
     # ENORK2 (second-order ENO, Heun RK2): distances, reinitialization, extension
     assert all(np.array_equal(a, b) for a, b in zip(O.set_distance_enork2(P, g, F).six(),
                                                      O.set_distance_enork2(R, g, F).six()))
