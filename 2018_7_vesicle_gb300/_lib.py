@@ -77,6 +77,7 @@ for _suf in ("f64", "f32"):
             f"vsl_enork2_extend_{_suf}": "pip" + _G + "pz" + "s",
             f"vsl_enork2_surface_redistance_{_suf}": "piip" + _G + "pz" + "s",
             f"vsl_laplacian_{_suf}": "pp" + _G + "s",
+            f"vsl_gradient_{_suf}": "pppp" + _G + "s",
             f"vsl_smooth_bilaplacian_{_suf}": "pppdi" + _G + "pz" + "s",
             f"vsl_relax_step_{_suf}": "p" + "pppppp" + "dddddd" + "ii" + "p" + _G + "pz" + "s",
             f"vsl_weno5_rk3_advection_adjoint_{_suf}": "ppppp" + "pppp" + _G + "pz" + "s",

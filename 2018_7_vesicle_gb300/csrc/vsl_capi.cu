@@ -1199,6 +1199,16 @@ int op_laplacian(const T *f, T *out, int rows, int cols, int pges, double dx, do
 }
 
 template <typename T>
+int op_gradient(const T *f, T *fx, T *fy, T *fz, int rows, int cols, int pges, double dx, double dy, double dz,
+                cudaStream_t s)
+{
+    if (any_null(f, fx, fy, fz)) return VSL_ERR_NULL;
+    if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
+    VSL_TRY(launch_gradient<T>(f, fx, fy, fz, make_grid(rows, cols, pges, dx, dy, dz), s));
+    return VSL_OK;
+}
+
+template <typename T>
 int op_smooth(const T *rhs, T *out, const double *dt, double alpha, int exact, int rows, int cols, int pges, double dx,
               double dy, double dz, void *ws, size_t bytes, cudaStream_t s)
 {
@@ -1556,6 +1566,11 @@ size_t vsl_workspace_bytes(int op, int rows, int cols, int pges, int elem_bytes)
                             vsl_stream_t stream)                                                                   \
     {                                                                                                              \
         return op_laplacian<T>(field, out, rows, cols, pges, dx, dy, dz, stream);                                  \
+    }                                                                                                              \
+    int vsl_gradient_##SUF(const T *field, T *fx, T *fy, T *fz, int rows, int cols, int pges, double dx,          \
+                           double dy, double dz, vsl_stream_t stream)                                              \
+    {                                                                                                              \
+        return op_gradient<T>(field, fx, fy, fz, rows, cols, pges, dx, dy, dz, stream);                            \
     }                                                                                                              \
     int vsl_smooth_bilaplacian_##SUF(const T *rhs, T *out, const double *dt, double alpha, int exact, int rows,    \
                                      int cols, int pges, double dx, double dy, double dz, void *ws, size_t bytes,  \

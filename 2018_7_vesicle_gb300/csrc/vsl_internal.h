@@ -118,6 +118,8 @@ cudaError_t launch_enork2_extend_stage(const T *c_s, const T *c_n, T *out, const
 // ---- the relaxation step (vsl_relax.cuh, vsl_spectral.cu), T in {float, double} ------
 template <typename T> cudaError_t launch_laplacian(const T *f, T *out, const Grid &g, cudaStream_t s);
 template <typename T>
+cudaError_t launch_gradient(const T *f, T *fx, T *fy, T *fz, const Grid &g, cudaStream_t s);
+template <typename T>
 cudaError_t launch_bending_speed(const T *H, const T *K, T *out, const Grid &g, double kappa, double c0,
                                  cudaStream_t s);
 // per-block partials of the surface integrals over |F| < band: 4 (H^2, H, H NSB, NSB) or,

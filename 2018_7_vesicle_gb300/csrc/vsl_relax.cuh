@@ -63,6 +63,23 @@ __global__ void __launch_bounds__(RNT) k_laplacian(const T *__restrict__ f, T *_
     out[c] = periodic_laplacian(f, g, i, j, k, c, dx2, dy2, dz2);
 }
 
+// GD3.Gradient (GD3.m:314-318): Fx = (F(oXo) - F(oxo)) / (2 Dx), Fy, Fz alike (GD3.m:218-240),
+// with the periodic neighbours of the Laplacian
+template <typename T>
+__global__ void __launch_bounds__(RNT) k_gradient(const T *__restrict__ f, T *__restrict__ fx, T *__restrict__ fy,
+                                                  T *__restrict__ fz, Grid g, T dx2, T dy2, T dz2)
+{
+    int i, j, k;
+    long long c;
+    if (!relax_node(g, i, j, k, c)) return;
+    const int jp = j + 1 == g.cols ? 0 : j + 1, jm = j == 0 ? g.cols - 1 : j - 1;
+    const int ip = i + 1 == g.rows ? 0 : i + 1, im = i == 0 ? g.rows - 1 : i - 1;
+    const int kp = k + 1 == g.pges ? 0 : k + 1, km = k == 0 ? g.pges - 1 : k - 1;
+    fx[c] = (__ldg(f + node_index(g, i, jp, k)) - __ldg(f + node_index(g, i, jm, k))) / dx2;
+    fy[c] = (__ldg(f + node_index(g, ip, j, k)) - __ldg(f + node_index(g, im, j, k))) / dy2;
+    fz[c] = (__ldg(f + node_index(g, i, j, kp)) - __ldg(f + node_index(g, i, j, km))) / dz2;
+}
+
 // NormalSpeedBend = Kappa * (Lap H + 0.5 H (H^2 - 4 K) + 2 c0 K - 0.5 c0^2 H)
 // (p00_test_singlephase_relax.m:80-84), H the extended mean curvature, K the Gaussian
 // curvature, c0 the spontaneous curvature
@@ -196,6 +213,14 @@ template <> inline float relax_round_up<float>(double x)
 
 }  // namespace
 
+// the divisors 2 Dx, 2 Dy, 2 Dz formed in FP64 (GD3.m:219) and rounded once to T
+template <typename T> cudaError_t launch_gradient(const T *f, T *fx, T *fy, T *fz, const Grid &g, cudaStream_t s)
+{
+    k_gradient<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(f, fx, fy, fz, g, (T)(2 * g.dx), (T)(2 * g.dy),
+                                                       (T)(2 * g.dz));
+    return cudaGetLastError();
+}
+
 template <typename T> cudaError_t launch_laplacian(const T *f, T *out, const Grid &g, cudaStream_t s)
 {
     k_laplacian<T><<<node_grid(g), dim3(BX, BY), 0, s>>>(f, out, g, (T)(g.dx * g.dx), (T)(g.dy * g.dy),
@@ -244,6 +269,7 @@ template <typename T> cudaError_t launch_euler(T *F, const T *v, const double *d
 
 #define VSL_INSTANTIATE_RELAX(T)                                                                                   \
     template cudaError_t launch_laplacian<T>(const T *, T *, const Grid &, cudaStream_t);                          \
+    template cudaError_t launch_gradient<T>(const T *, T *, T *, T *, const Grid &, cudaStream_t);                 \
     template cudaError_t launch_bending_speed<T>(const T *, const T *, T *, const Grid &, double, double,          \
                                                  cudaStream_t);                                                    \
     template cudaError_t launch_relax_moments<T>(const T *, const T *, const T *, const T *, const T *, double,    \

@@ -116,6 +116,15 @@ class GD3:
         lib().call(f"vsl_laplacian_{precision}", _ptr(f), _ptr(out), *self.args(), _stream())
         return out
 
+    def Gradient(self, field, precision: str = "f64"):
+        """GD3.Gradient (GD3.m:314-318): central differences with periodic neighbours;
+        returns (fx, fy, fz)."""
+        dtype = _DTYPES[precision]
+        f = as_field(field, dtype)
+        out = [colmajor_empty(self.Size, dtype) for _ in range(3)]
+        lib().call(f"vsl_gradient_{precision}", _ptr(f), *[_ptr(o) for o in out], *self.args(), _stream())
+        return tuple(out)
+
     def _smooth(self, rhs, Dt, Alpha, exact: int, precision: str):
         dtype = _DTYPES[precision]
         f = as_field(rhs, dtype)

@@ -416,6 +416,14 @@ int vsl_laplacian_f64(const double *field, double *out, int rows, int cols, int 
 int vsl_laplacian_f32(const float *field, float *out, int rows, int cols, int pges, double dx, double dy, double dz,
                       vsl_stream_t stream);
 
+/* ref: +SD/@GD3/GD3.m:314-318 (Gradient) of Fx, Fy, Fz (GD3.m:218-240) with the same
+ * circshift neighbours: fx = (F(x+dx) - F(x-dx)) / (2 Dx), fy and fz alike, periodic in
+ * every axis. */
+int vsl_gradient_f64(const double *field, double *fx, double *fy, double *fz, int rows, int cols, int pges, double dx,
+                     double dy, double dz, vsl_stream_t stream);
+int vsl_gradient_f32(const float *field, float *fx, float *fy, float *fz, int rows, int cols, int pges, double dx,
+                     double dy, double dz, vsl_stream_t stream);
+
 /* ref: +SD/@GD3/GD3.m:434-485 (smoothGMRES, smoothFFT).  out = real(ifftn(fftn(rhs) ./ S))
  * with S = 1 + alpha * (*dt) * symbol: exact = 1 takes the symbol of the periodic discrete
  * bi-Laplacian (lambda^2, lambda = sum (2 cos(2 pi m/n) - 2) / h^2), which makes out the

@@ -651,6 +651,16 @@ def laplacian(g: Grid, f):
     return F64(fxx + fyy + fzz)
 
 
+def gradient(g: Grid, f):
+    """GD3.Gradient (GD3.m:314-318): Fx = (F(oXo) - F(oxo)) / (2 Dx) (GD3.m:218-220), Fy and
+    Fz alike, circshift neighbours; arrays are (rows = y, cols = x, pges = z)."""
+    f = F64(f)
+    fx = (np.roll(f, -1, axis=1) - np.roll(f, 1, axis=1)) / (2 * g.dx)
+    fy = (np.roll(f, -1, axis=0) - np.roll(f, 1, axis=0)) / (2 * g.dy)
+    fz = (np.roll(f, -1, axis=2) - np.roll(f, 1, axis=2)) / (2 * g.dz)
+    return F64(fx), F64(fy), F64(fz)
+
+
 def wave_numbers(g: Grid):
     """GD3.m:195-207: kx, ky, kz from fftshift(2 pi (-n/2 : n/2-1) / (n h)) on meshgrid."""
     def axis(n, h):

@@ -1,7 +1,8 @@
 """The single-phase relaxation step of the vesicle driver (p00_test_singlephase_relax.m:
 60-196) and its SD.GD3 operators on the GPU, against the oracle.
 
-* GD3.Laplacian (periodic 7-point): bitwise equal to the oracle's numpy restatement;
+* GD3.Laplacian (periodic 7-point) and GD3.Gradient (periodic central differences):
+  bitwise equal to the oracle's numpy restatement;
 * GD3.smoothGMRES: the GPU's exact spectral solve of (I + alpha Dt L^2) x = rhs against
   the reference's own algorithm, GMRES with the FFT preconditioner to relative
   tolerance 1e-12 (scipy), within 1e-9 of max|x|, and against a numpy direct spectral
@@ -45,6 +46,21 @@ def test_periodic_laplacian(pkg, vsl, oracle_mod):
     got32 = host(gd.Laplacian(dev(f), precision="f32"))
     ref = O.laplacian(g, f)
     assert np.abs(got32 - ref).max() <= 1e-5 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("size", [(28, 26, 24), (3, 2, 5)])
+def test_periodic_gradient(pkg, vsl, oracle_mod, size):
+    """GD3.Gradient: bitwise the oracle in FP64 (grids down to 2 nodes on an axis, where both
+    periodic neighbours are the same node), within 1e-6 of max|grad| in FP32."""
+    O = oracle_mod
+    gd, x, y, z, F = grid_and_field(pkg, size)
+    g = O.grid_from_mesh(x, y, z)
+    f = np.asfortranarray(np.sin(3 * x) * np.cos(2 * y + z) + F)
+    ref = O.gradient(g, f)
+    for got, r in zip(gd.Gradient(dev(f)), ref):
+        assert np.array_equal(host(got), r)
+    for got, r in zip(gd.Gradient(dev(f), precision="f32"), ref):
+        assert np.abs(host(got) - r).max() <= 1e-6 * max(np.abs(r).max(), 1.0)
 
 
 @pytest.mark.parametrize("size", [(28, 26, 24), (21, 19, 17)])
