@@ -12,6 +12,9 @@ Two batch steps:
   round-robin.
 
 The vesicles share nothing: each has its own field, distances and workspace.
+
+`reinitialize_batched` (FP32) runs WENO5RK3Reinitialization on a list of level sets the same
+way (vsl_weno5_rk3_reinitialization_batch_f32), bitwise the per-object calls.
 """
 from __future__ import annotations
 
@@ -19,7 +22,7 @@ import ctypes
 
 import torch
 
-from ._lib import VesicleF32, lib
+from ._lib import ReinitF32, VesicleF32, lib
 from .sdf3 import SDF3
 
 
@@ -170,3 +173,30 @@ class VesicleBatch:
             self._graph, self._key = g, key
         self._graph.replay()
         return self.infos
+
+
+def reinitialize_batched(maps: list[SDF3], fields, iteration: int):
+    """WENO5RK3Reinitialization(F, iteration) of every (level set, field) pair, each RK stage
+    of all of them as one launch (vsl_weno5_rk3_reinitialization_batch_f32; FP32 objects,
+    cached distances of setDistance).  Returns new fields, bitwise those of
+    `m.WENO5RK3Reinitialization(F, iteration)` per object."""
+    maps = list(maps)
+    if len(maps) != len(fields):
+        raise ValueError("one field per level set")
+    if any(m.precision != "f32" for m in maps):
+        raise ValueError("reinitialize_batched runs the FP32 mixed form")
+    outs = [m._field(F).clone() for m, F in zip(maps, fields)]
+    arr = (ReinitF32 * len(maps))()
+    keep = []
+    for d, m, out in zip(arr, maps, outs):
+        ws = m.workspace("reinit_weno5")
+        dist = m._dist()
+        keep.append((ws, dist))
+        d.F = out.data_ptr()
+        d.xpr, d.xpl, d.ypf, d.ypb, d.zpu, d.zpd = (t.data_ptr() for t in dist)
+        d.rows, d.cols, d.pges = m.GD3.Size
+        d.dx, d.dy, d.dz = m.GD3.Dx, m.GD3.Dy, m.GD3.Dz
+        d.workspace, d.workspace_bytes = ws.data_ptr(), ws.numel()
+    lib().call("vsl_weno5_rk3_reinitialization_batch_f32", ctypes.addressof(arr), len(maps), int(iteration),
+               torch.cuda.current_stream().cuda_stream)
+    return outs

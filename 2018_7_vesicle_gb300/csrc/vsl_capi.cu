@@ -1062,6 +1062,63 @@ int op_vesicle_step_batch(const vsl_vesicle_f32 *ves, int count, int ext_iters, 
     return VSL_OK;
 }
 
+// A batch of WENO5RK3Reinitialization calls (op_reinit_weno5 per member): each member's
+// classification on its lane, then each RK stage of all members as one launch
+int check_reinit_member(const vsl_reinit_f32 &r)
+{
+    if (any_null(r.F, r.xpr, r.xpl, r.ypf, r.ypb, r.zpu, r.zpd)) return VSL_ERR_NULL;
+    if (int st = check_grid(r.rows, r.cols, r.pges, r.dx, r.dy, r.dz)) return st;
+    const Grid g = make_grid(r.rows, r.cols, r.pges, r.dx, r.dy, r.dz);
+    return check_ws(VSL_OP_REINIT_WENO5, g, sizeof(float), r.workspace, r.workspace_bytes);
+}
+
+int reinit_batch_chunk(const vsl_reinit_f32 *mem, int n, int iteration, cudaStream_t s)
+{
+    ReinitWork<float> w[TILED_BATCH_MAX];
+    Ptr6<const float> d[TILED_BATCH_MAX];
+    TiledStage st[TILED_BATCH_MAX];
+    Grid grids[TILED_BATCH_MAX];
+    for (int v = 0; v < n; ++v) {
+        const vsl_reinit_f32 &r = mem[v];
+        grids[v] = make_grid(r.rows, r.cols, r.pges, r.dx, r.dy, r.dz);
+        Bump bump(r.workspace);
+        w[v] = carve_reinit<float>(bump, grids[v], false);
+        d[v] = six(r.xpr, r.xpl, r.ypf, r.ypb, r.zpu, r.zpd);
+    }
+    Fan fan{batch_lanes(s), s};
+    VSL_TRY(fan.open());
+    for (int v = 0; v < n; ++v) {
+        const cudaStream_t ls = fan.lane(v);
+        VSL_TRY(launch_classify<float>(mem[v].F, d[v], w[v].flags, NodeList{nullptr, nullptr}, grids[v], ls));
+        if (int r = band_reset(w[v].band, ls)) return r;
+    }
+    VSL_TRY(fan.close());
+    for (int it = 0; it < iteration; ++it) {
+        for (int stage = 0; stage < 3; ++stage) {
+            for (int v = 0; v < n; ++v) {
+                float *F = mem[v].F;
+                float *in = stage == 0 ? F : (stage == 1 ? w[v].b : w[v].c);
+                float *out = stage == 0 ? w[v].b : (stage == 1 ? w[v].c : F);
+                st[v] = TiledStage{in, F, out, w[v].flags, d[v], BandShadow{}, Ptr3<const float>{}, nullptr, nullptr,
+                                   w[v].band.q, NodeList{nullptr, nullptr}, stage, w[v].band.seq++};
+            }
+            VSL_TRY(launch_tiled_batch(0, false, st, grids, n, s));
+        }
+    }
+    return VSL_OK;
+}
+
+int op_reinit_batch(const vsl_reinit_f32 *mem, int count, int iteration, cudaStream_t s)
+{
+    if (mem == nullptr && count > 0) return VSL_ERR_NULL;
+    if (count < 0 || iteration < 0) return VSL_ERR_VALUE;
+    for (int v = 0; v < count; ++v)
+        if (int st = check_reinit_member(mem[v])) return st;
+    for (int v0 = 0; v0 < count; v0 += TILED_BATCH_MAX)
+        if (int st = reinit_batch_chunk(mem + v0, std::min(TILED_BATCH_MAX, count - v0), iteration, s)) return st;
+    return VSL_OK;
+}
+
 // ---------------------------------------------------------------------------------------
 // ENORK2 (ENORK2Reinitialization.m:3-45, ENORK2Extend.m:9-81)
 // ---------------------------------------------------------------------------------------
@@ -1427,6 +1484,12 @@ int vsl_vesicle_step_batch_f32(const vsl_vesicle_f32 *vesicles, int count, int e
                                double cfl, vsl_stream_t stream)
 {
     return op_vesicle_step_batch(vesicles, count, ext_iters, reinit_iters, cfl, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int vsl_weno5_rk3_reinitialization_batch_f32(const vsl_reinit_f32 *members, int count, int iteration,
+                                             vsl_stream_t stream)
+{
+    return op_reinit_batch(members, count, iteration, reinterpret_cast<cudaStream_t>(stream));
 }
 
 const char *vsl_status_string(int status)

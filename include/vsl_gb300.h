@@ -382,6 +382,24 @@ typedef struct {
 int vsl_vesicle_step_batch_f32(const vsl_vesicle_f32 *vesicles, int count, int ext_iters, int reinit_iters,
                                double cfl, vsl_stream_t stream);
 
+/* A batch of WENO5RK3Reinitialization calls, FP32 mixed form (ref, per member:
+ * +SD/@SDF3/WENO5RK3Reinitialization.m:3-43 with the member's cached distances, as
+ * vsl_weno5_rk3_reinitialization_f32).  Each member has its own field, distances and
+ * workspace of vsl_workspace_bytes(VSL_OP_REINIT_WENO5, its grid, 4); each RK stage of all
+ * the members runs as one launch over all their tiles, 64 members at a time.  Results are
+ * bitwise those of vsl_weno5_rk3_reinitialization_f32 called per member.  `members` is a
+ * HOST array read during the call; the pointers in it are device pointers. */
+typedef struct {
+    float *F;
+    const float *xpr, *xpl, *ypf, *ypb, *zpu, *zpd;
+    int rows, cols, pges;
+    double dx, dy, dz;
+    void *workspace;
+    size_t workspace_bytes;
+} vsl_reinit_f32;
+int vsl_weno5_rk3_reinitialization_batch_f32(const vsl_reinit_f32 *members, int count, int iteration,
+                                             vsl_stream_t stream);
+
 /* ref: +SD/@SDF3/ENORK2Reinitialization.m:3-45.  Quadratic-ENO distances recomputed from
  * F, then `iteration` Heun RK2 pseudo-steps F1 = F - step(F), F = (F + F1 - step(F1)) / 2
  * with the mask and dt = 0.3 min(distances) of F at the start. */

@@ -1,4 +1,5 @@
-"""Argument checks of the batch of vesicle steps (vsl_vesicle_step_batch_f32) without a GPU:
+"""Argument checks of the batch of vesicle steps (vsl_vesicle_step_batch_f32) and of the batch
+of WENO5 RK3 reinitializations (vsl_weno5_rk3_reinitialization_batch_f32) without a GPU:
 every check runs on the host before any CUDA call, so bad descriptors and arguments are
 rejected with their status codes and an empty batch is a no-op."""
 import ctypes
@@ -51,3 +52,36 @@ def test_batch_rejects_bad_descriptors(vsl):
 
 def test_empty_batch_is_a_no_op(vsl):
     assert call(vsl, None, 0) == VSL_OK
+
+
+# ---- the batch of WENO5 RK3 reinitializations (vsl_weno5_rk3_reinitialization_batch_f32) ----
+
+
+def reinit_member(rows=40, cols=36, pges=32, h=0.05, ws=FAKE * 16, nbytes=1 << 30, **over):
+    d = L.ReinitF32()
+    d.F = d.xpr = d.xpl = d.ypf = d.ypb = d.zpu = d.zpd = FAKE
+    d.rows, d.cols, d.pges = rows, cols, pges
+    d.dx = d.dy = d.dz = h
+    d.workspace, d.workspace_bytes = ws, nbytes
+    for k, v in over.items():
+        setattr(d, k, v)
+    return d
+
+
+def reinit_call(vsl, arr, count, iteration=20):
+    ptr = ctypes.addressof(arr) if arr is not None else None
+    return vsl.raw("vsl_weno5_rk3_reinitialization_batch_f32", ptr, count, iteration, None)
+
+
+def test_reinit_batch_rejects_bad_arguments(vsl):
+    arr = (L.ReinitF32 * 1)(reinit_member())
+    assert reinit_call(vsl, None, 1) == VSL_ERR_NULL
+    assert reinit_call(vsl, arr, -1) == VSL_ERR_VALUE
+    assert reinit_call(vsl, arr, 1, iteration=-1) == VSL_ERR_VALUE
+    good = reinit_member()
+    for bad, status in ((reinit_member(F=None), VSL_ERR_NULL), (reinit_member(zpd=None), VSL_ERR_NULL),
+                        (reinit_member(pges=0), VSL_ERR_SHAPE), (reinit_member(dz=-1.0), VSL_ERR_VALUE),
+                        (reinit_member(ws=None), VSL_ERR_WORKSPACE), (reinit_member(nbytes=16), VSL_ERR_WORKSPACE)):
+        arr = (L.ReinitF32 * 3)(good, good, bad)
+        assert reinit_call(vsl, arr, 3) == status
+    assert reinit_call(vsl, None, 0) == VSL_OK

@@ -148,3 +148,22 @@ def make_batch_edges(pkg, n, edges):
         m.setDistance()
         maps.append(m)
     return maps
+
+
+@pytest.mark.parametrize("count", [5, 66])
+def test_reinitialize_batched_matches_per_object(pkg, vsl, count):
+    """vsl_weno5_rk3_reinitialization_batch_f32 (each RK stage of every member as one
+    launch; 66 members run as chunks of 64 and 2) against each object's own
+    WENO5RK3Reinitialization: bitwise."""
+    edges = (24, 32, 40) if count < 10 else (16, 20, 24)
+    maps = []
+    for xv, yv, zv, axes in S.random_vesicles(count, seed=4, edges=edges):
+        x, y, z, F = S.ellipsoid_field(xv, yv, zv, axes)
+        m = pkg.SDF3(pkg.GD3(x, y, z), Val=F, precision="f32")
+        m.setDistance()
+        maps.append(m)
+    fields = [m.F for m in maps]
+    got = B.reinitialize_batched(maps, fields, 6)
+    for m, F, g in zip(maps, fields, got):
+        assert np.array_equal(host(g), host(m.WENO5RK3Reinitialization(F, 6)))
+    assert len({m.GD3.Size for m in maps}) > 1
