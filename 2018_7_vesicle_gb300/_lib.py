@@ -50,7 +50,19 @@ SIGNATURES = {
     "vsl_vesicle_step_batch_f32": "piiid" + "s",
     # a batch of WENO5 RK3 reinitializations: host array of ReinitF32, count, pseudo-steps
     "vsl_weno5_rk3_reinitialization_batch_f32": "pii" + "s",
+    # a batch of WENO5 RK3 extensions: host array of ExtendF32, count, pseudo-steps
+    "vsl_weno5_rk3_extend_batch_f32": "pii" + "s",
 }
+
+
+class ExtendF32(ctypes.Structure):
+    """vsl_extend_f32 of the C ABI: one member of vsl_weno5_rk3_extend_batch_f32."""
+
+    _fields_ = [("C", ctypes.c_void_p), ("F", ctypes.c_void_p), ("xpr", ctypes.c_void_p), ("xpl", ctypes.c_void_p),
+                ("ypf", ctypes.c_void_p), ("ypb", ctypes.c_void_p), ("zpu", ctypes.c_void_p), ("zpd", ctypes.c_void_p),
+                ("rows", ctypes.c_int), ("cols", ctypes.c_int), ("pges", ctypes.c_int),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
+                ("workspace", ctypes.c_void_p), ("workspace_bytes", ctypes.c_size_t)]
 
 
 class ReinitF32(ctypes.Structure):

@@ -13,8 +13,9 @@ Two batch steps:
 
 The vesicles share nothing: each has its own field, distances and workspace.
 
-`reinitialize_batched` (FP32) runs WENO5RK3Reinitialization on a list of level sets the same
-way (vsl_weno5_rk3_reinitialization_batch_f32), bitwise the per-object calls.
+`reinitialize_batched` and `extend_batched` (FP32) run WENO5RK3Reinitialization and
+WENO5RK3Extend on a list of level sets the same way (vsl_weno5_rk3_reinitialization_batch_f32,
+vsl_weno5_rk3_extend_batch_f32), bitwise the per-object calls.
 """
 from __future__ import annotations
 
@@ -22,7 +23,7 @@ import ctypes
 
 import torch
 
-from ._lib import ReinitF32, VesicleF32, lib
+from ._lib import ExtendF32, ReinitF32, VesicleF32, lib
 from .sdf3 import SDF3
 
 
@@ -198,5 +199,32 @@ def reinitialize_batched(maps: list[SDF3], fields, iteration: int):
         d.dx, d.dy, d.dz = m.GD3.Dx, m.GD3.Dy, m.GD3.Dz
         d.workspace, d.workspace_bytes = ws.data_ptr(), ws.numel()
     lib().call("vsl_weno5_rk3_reinitialization_batch_f32", ctypes.addressof(arr), len(maps), int(iteration),
+               torch.cuda.current_stream().cuda_stream)
+    return outs
+
+
+def extend_batched(maps: list[SDF3], fields, iteration: int):
+    """WENO5RK3Extend(C, iteration) of every (level set, field) pair off the level set's zero
+    set, each RK stage of all of them as one launch (vsl_weno5_rk3_extend_batch_f32; FP32
+    objects, cached distances of setDistance).  Returns new fields, bitwise those of
+    `m.WENO5RK3Extend(C, iteration)` per object."""
+    maps = list(maps)
+    if len(maps) != len(fields):
+        raise ValueError("one field per level set")
+    if any(m.precision != "f32" for m in maps):
+        raise ValueError("extend_batched runs the FP32 mixed form")
+    outs = [m._field(C).clone() for m, C in zip(maps, fields)]
+    arr = (ExtendF32 * len(maps))()
+    keep = []
+    for d, m, out in zip(arr, maps, outs):
+        ws = m.workspace("extend_weno5")
+        dist = m._dist()
+        keep.append((ws, dist))
+        d.C, d.F = out.data_ptr(), m.F.data_ptr()
+        d.xpr, d.xpl, d.ypf, d.ypb, d.zpu, d.zpd = (t.data_ptr() for t in dist)
+        d.rows, d.cols, d.pges = m.GD3.Size
+        d.dx, d.dy, d.dz = m.GD3.Dx, m.GD3.Dy, m.GD3.Dz
+        d.workspace, d.workspace_bytes = ws.data_ptr(), ws.numel()
+    lib().call("vsl_weno5_rk3_extend_batch_f32", ctypes.addressof(arr), len(maps), int(iteration),
                torch.cuda.current_stream().cuda_stream)
     return outs

@@ -1108,6 +1108,69 @@ int reinit_batch_chunk(const vsl_reinit_f32 *mem, int n, int iteration, cudaStre
     return VSL_OK;
 }
 
+// A batch of WENO5RK3Extend calls (op_extend_weno5 per member): each member's velocity,
+// classification, FP64 crossing values and shadow on its lane, then each RK stage of all
+// members as one launch (the extension's band blocks inside it, per member)
+int check_extend_member(const vsl_extend_f32 &e)
+{
+    if (any_null(e.C, e.F, e.xpr, e.xpl, e.ypf, e.ypb, e.zpu, e.zpd)) return VSL_ERR_NULL;
+    if (int st = check_grid(e.rows, e.cols, e.pges, e.dx, e.dy, e.dz)) return st;
+    const Grid g = make_grid(e.rows, e.cols, e.pges, e.dx, e.dy, e.dz);
+    return check_ws(VSL_OP_EXTEND_WENO5, g, sizeof(float), e.workspace, e.workspace_bytes);
+}
+
+int extend_batch_chunk(const vsl_extend_f32 *mem, int n, int iteration, cudaStream_t s)
+{
+    ExtendWork<float> w[TILED_BATCH_MAX];
+    Ptr6<const float> d[TILED_BATCH_MAX];
+    TiledStage st[TILED_BATCH_MAX];
+    Grid grids[TILED_BATCH_MAX];
+    for (int v = 0; v < n; ++v) {
+        const vsl_extend_f32 &e = mem[v];
+        grids[v] = make_grid(e.rows, e.cols, e.pges, e.dx, e.dy, e.dz);
+        Bump bump(e.workspace);
+        w[v] = carve_extend<float>(bump, grids[v], false);
+        d[v] = six(e.xpr, e.xpl, e.ypf, e.ypb, e.zpu, e.zpd);
+    }
+    Fan fan{batch_lanes(s), s};
+    VSL_TRY(fan.open());
+    for (int v = 0; v < n; ++v) {
+        const cudaStream_t ls = fan.lane(v);
+        ExtendWork<float> &e = w[v];
+        if (int r = extend_setup<float>(mem[v].F, d[v], e, grids[v], false, 1e-6, ls)) return r;
+        VSL_TRY(launch_crossing_mixed(mem[v].C, d[v], e.cp64, e.flagged, grids[v], false, ls));
+        VSL_TRY(launch_shadow_init(mem[v].C, e.sh[0], e.flagged, ls));
+        if (int r = band_reset(e.band, ls)) return r;
+    }
+    VSL_TRY(fan.close());
+    for (int it = 0; it < iteration; ++it) {
+        for (int stage = 0; stage < 3; ++stage) {
+            for (int v = 0; v < n; ++v) {
+                ExtendWork<float> &e = w[v];
+                float *C = mem[v].C;
+                float *in = stage == 0 ? C : (stage == 1 ? e.b : e.c);
+                float *out = stage == 0 ? e.b : (stage == 1 ? e.c : C);
+                double *s_out = e.sh[stage == 2 ? 0 : stage + 1];
+                st[v] = TiledStage{in, C, out, e.flags, d[v], BandShadow{e.sh[stage], e.sh[0], s_out, cview(e.cp64)},
+                                   cview3(e.v), nullptr, nullptr, e.band.q, e.flagged, stage, e.band.seq++};
+            }
+            VSL_TRY(launch_tiled_batch(1, false, st, grids, n, s));
+        }
+    }
+    return VSL_OK;
+}
+
+int op_extend_batch(const vsl_extend_f32 *mem, int count, int iteration, cudaStream_t s)
+{
+    if (mem == nullptr && count > 0) return VSL_ERR_NULL;
+    if (count < 0 || iteration < 0) return VSL_ERR_VALUE;
+    for (int v = 0; v < count; ++v)
+        if (int st = check_extend_member(mem[v])) return st;
+    for (int v0 = 0; v0 < count; v0 += TILED_BATCH_MAX)
+        if (int st = extend_batch_chunk(mem + v0, std::min(TILED_BATCH_MAX, count - v0), iteration, s)) return st;
+    return VSL_OK;
+}
+
 int op_reinit_batch(const vsl_reinit_f32 *mem, int count, int iteration, cudaStream_t s)
 {
     if (mem == nullptr && count > 0) return VSL_ERR_NULL;
@@ -1490,6 +1553,11 @@ int vsl_weno5_rk3_reinitialization_batch_f32(const vsl_reinit_f32 *members, int 
                                              vsl_stream_t stream)
 {
     return op_reinit_batch(members, count, iteration, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int vsl_weno5_rk3_extend_batch_f32(const vsl_extend_f32 *members, int count, int iteration, vsl_stream_t stream)
+{
+    return op_extend_batch(members, count, iteration, reinterpret_cast<cudaStream_t>(stream));
 }
 
 const char *vsl_status_string(int status)

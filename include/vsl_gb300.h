@@ -400,6 +400,25 @@ typedef struct {
 int vsl_weno5_rk3_reinitialization_batch_f32(const vsl_reinit_f32 *members, int count, int iteration,
                                              vsl_stream_t stream);
 
+/* A batch of WENO5RK3Extend calls, FP32 mixed form (ref, per member:
+ * +SD/@SDF3/WENO5RK3Extend.m:9-76 with F's cached distances, as vsl_weno5_rk3_extend_f32).
+ * Each member has its own field C (extended in place), level set F, F's distances and
+ * workspace of vsl_workspace_bytes(VSL_OP_EXTEND_WENO5, its grid, 4); each RK stage of all
+ * the members runs as one launch over all their tiles and band blocks, 64 members at a
+ * time.  Results are bitwise those of vsl_weno5_rk3_extend_f32 called per member.
+ * `members` is a HOST array read during the call; the pointers in it are device
+ * pointers. */
+typedef struct {
+    float *C;
+    const float *F;
+    const float *xpr, *xpl, *ypf, *ypb, *zpu, *zpd;
+    int rows, cols, pges;
+    double dx, dy, dz;
+    void *workspace;
+    size_t workspace_bytes;
+} vsl_extend_f32;
+int vsl_weno5_rk3_extend_batch_f32(const vsl_extend_f32 *members, int count, int iteration, vsl_stream_t stream);
+
 /* ref: +SD/@SDF3/ENORK2Reinitialization.m:3-45.  Quadratic-ENO distances recomputed from
  * F, then `iteration` Heun RK2 pseudo-steps F1 = F - step(F), F = (F + F1 - step(F1)) / 2
  * with the mask and dt = 0.3 min(distances) of F at the start. */

@@ -1,5 +1,6 @@
 """Argument checks of the batch of vesicle steps (vsl_vesicle_step_batch_f32) and of the batch
-of WENO5 RK3 reinitializations (vsl_weno5_rk3_reinitialization_batch_f32) without a GPU:
+of WENO5 RK3 reinitializations and extensions (vsl_weno5_rk3_reinitialization_batch_f32,
+vsl_weno5_rk3_extend_batch_f32) without a GPU:
 every check runs on the host before any CUDA call, so bad descriptors and arguments are
 rejected with their status codes and an empty batch is a no-op."""
 import ctypes
@@ -85,3 +86,36 @@ def test_reinit_batch_rejects_bad_arguments(vsl):
         arr = (L.ReinitF32 * 3)(good, good, bad)
         assert reinit_call(vsl, arr, 3) == status
     assert reinit_call(vsl, None, 0) == VSL_OK
+
+
+# ---- the batch of WENO5 RK3 extensions (vsl_weno5_rk3_extend_batch_f32) ----
+
+
+def extend_member(rows=40, cols=36, pges=32, h=0.05, ws=FAKE * 16, nbytes=1 << 30, **over):
+    d = L.ExtendF32()
+    d.C = d.F = d.xpr = d.xpl = d.ypf = d.ypb = d.zpu = d.zpd = FAKE
+    d.rows, d.cols, d.pges = rows, cols, pges
+    d.dx = d.dy = d.dz = h
+    d.workspace, d.workspace_bytes = ws, nbytes
+    for k, v in over.items():
+        setattr(d, k, v)
+    return d
+
+
+def extend_call(vsl, arr, count, iteration=30):
+    ptr = ctypes.addressof(arr) if arr is not None else None
+    return vsl.raw("vsl_weno5_rk3_extend_batch_f32", ptr, count, iteration, None)
+
+
+def test_extend_batch_rejects_bad_arguments(vsl):
+    arr = (L.ExtendF32 * 1)(extend_member())
+    assert extend_call(vsl, None, 2) == VSL_ERR_NULL
+    assert extend_call(vsl, arr, -1) == VSL_ERR_VALUE
+    assert extend_call(vsl, arr, 1, iteration=-1) == VSL_ERR_VALUE
+    good = extend_member()
+    for bad, status in ((extend_member(C=None), VSL_ERR_NULL), (extend_member(F=None), VSL_ERR_NULL),
+                        (extend_member(xpl=None), VSL_ERR_NULL), (extend_member(cols=-3), VSL_ERR_SHAPE),
+                        (extend_member(dx=float("nan")), VSL_ERR_VALUE), (extend_member(nbytes=0), VSL_ERR_WORKSPACE)):
+        arr = (L.ExtendF32 * 3)(bad, good, good)
+        assert extend_call(vsl, arr, 3) == status
+    assert extend_call(vsl, None, 0) == VSL_OK

@@ -5,7 +5,7 @@ import importlib
 import numpy as np
 import pytest
 
-from gpu_util import host
+from gpu_util import dev, host
 
 pytestmark = pytest.mark.gpu
 
@@ -167,3 +167,21 @@ def test_reinitialize_batched_matches_per_object(pkg, vsl, count):
     for m, F, g in zip(maps, fields, got):
         assert np.array_equal(host(g), host(m.WENO5RK3Reinitialization(F, 6)))
     assert len({m.GD3.Size for m in maps}) > 1
+
+
+@pytest.mark.parametrize("count", [5, 66])
+def test_extend_batched_matches_per_object(pkg, vsl, count):
+    """vsl_weno5_rk3_extend_batch_f32 (each RK stage of every member, band blocks included,
+    as one launch; 66 members run as chunks of 64 and 2) against each object's own
+    WENO5RK3Extend: bitwise."""
+    edges = (24, 32, 40) if count < 10 else (16, 20, 24)
+    maps, fields = [], []
+    for xv, yv, zv, axes in S.random_vesicles(count, seed=6, edges=edges):
+        x, y, z, F = S.ellipsoid_field(xv, yv, zv, axes)
+        m = pkg.SDF3(pkg.GD3(x, y, z), Val=F, precision="f32")
+        m.setDistance()
+        maps.append(m)
+        fields.append(dev(np.sin(3 * x) * np.cos(2 * y) + z))
+    got = B.extend_batched(maps, fields, 8)
+    for m, C, g in zip(maps, fields, got):
+        assert np.array_equal(host(g), host(m.WENO5RK3Extend(C, 8)))
