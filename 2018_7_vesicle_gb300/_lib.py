@@ -52,7 +52,18 @@ SIGNATURES = {
     "vsl_weno5_rk3_reinitialization_batch_f32": "pii" + "s",
     # a batch of WENO5 RK3 extensions: host array of ExtendF32, count, pseudo-steps
     "vsl_weno5_rk3_extend_batch_f32": "pii" + "s",
+    # a batch of WENO5 RK3 advections: host array of AdvectF32, count, steps
+    "vsl_weno5_rk3_advection_batch_f32": "pii" + "s",
 }
+
+
+class AdvectF32(ctypes.Structure):
+    """vsl_advect_f32 of the C ABI: one member of vsl_weno5_rk3_advection_batch_f32."""
+
+    _fields_ = [("F", ctypes.c_void_p), ("vx", ctypes.c_void_p), ("vy", ctypes.c_void_p), ("vz", ctypes.c_void_p),
+                ("dt", ctypes.c_void_p), ("rows", ctypes.c_int), ("cols", ctypes.c_int), ("pges", ctypes.c_int),
+                ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
+                ("workspace", ctypes.c_void_p), ("workspace_bytes", ctypes.c_size_t)]
 
 
 class ExtendF32(ctypes.Structure):

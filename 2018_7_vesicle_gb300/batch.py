@@ -13,9 +13,10 @@ Two batch steps:
 
 The vesicles share nothing: each has its own field, distances and workspace.
 
-`reinitialize_batched` and `extend_batched` (FP32) run WENO5RK3Reinitialization and
-WENO5RK3Extend on a list of level sets the same way (vsl_weno5_rk3_reinitialization_batch_f32,
-vsl_weno5_rk3_extend_batch_f32), bitwise the per-object calls.
+`reinitialize_batched`, `extend_batched` and `advect_batched` (FP32) run
+WENO5RK3Reinitialization, WENO5RK3Extend and WENO5RK3Advection on a list of level sets the
+same way (vsl_weno5_rk3_{reinitialization,extend,advection}_batch_f32), bitwise the
+per-object calls.
 """
 from __future__ import annotations
 
@@ -23,7 +24,7 @@ import ctypes
 
 import torch
 
-from ._lib import ExtendF32, ReinitF32, VesicleF32, lib
+from ._lib import AdvectF32, ExtendF32, ReinitF32, VesicleF32, lib
 from .sdf3 import SDF3
 
 
@@ -226,5 +227,35 @@ def extend_batched(maps: list[SDF3], fields, iteration: int):
         d.dx, d.dy, d.dz = m.GD3.Dx, m.GD3.Dy, m.GD3.Dz
         d.workspace, d.workspace_bytes = ws.data_ptr(), ws.numel()
     lib().call("vsl_weno5_rk3_extend_batch_f32", ctypes.addressof(arr), len(maps), int(iteration),
+               torch.cuda.current_stream().cuda_stream)
+    return outs
+
+
+def advect_batched(maps: list[SDF3], fields, velocities, dts, steps: int = 1):
+    """WENO5RK3Advection(F, vx, vy, vz, dt, steps) of every level set's grid, each RK stage of
+    all of them as one launch (vsl_weno5_rk3_advection_batch_f32; FP32 objects).
+    velocities: one (vx, vy, vz) per object; dts: one time step per object (a float or a
+    device tensor of one double).  Returns new fields, bitwise those of
+    `m.WENO5RK3Advection(F, vx, vy, vz, dt, steps)` per object."""
+    maps = list(maps)
+    if not (len(maps) == len(fields) == len(velocities) == len(dts)):
+        raise ValueError("one field, velocity and time step per level set")
+    if any(m.precision != "f32" for m in maps):
+        raise ValueError("advect_batched runs the FP32 mixed form")
+    outs = [m._field(F).clone() for m, F in zip(maps, fields)]
+    arr = (AdvectF32 * len(maps))()
+    keep = []
+    for d, m, out, vel, dt in zip(arr, maps, outs, velocities, dts):
+        v = [m._field(a) for a in vel]
+        dtt = dt if isinstance(dt, torch.Tensor) else torch.tensor([float(dt)], dtype=torch.float64, device="cuda")
+        ws = m.workspace("advection")
+        keep.append((v, dtt, ws))
+        d.F = out.data_ptr()
+        d.vx, d.vy, d.vz = (t.data_ptr() for t in v)
+        d.dt = dtt.data_ptr()
+        d.rows, d.cols, d.pges = m.GD3.Size
+        d.dx, d.dy, d.dz = m.GD3.Dx, m.GD3.Dy, m.GD3.Dz
+        d.workspace, d.workspace_bytes = ws.data_ptr(), ws.numel()
+    lib().call("vsl_weno5_rk3_advection_batch_f32", ctypes.addressof(arr), len(maps), int(steps),
                torch.cuda.current_stream().cuda_stream)
     return outs

@@ -1171,6 +1171,54 @@ int op_extend_batch(const vsl_extend_f32 *mem, int count, int iteration, cudaStr
     return VSL_OK;
 }
 
+// A batch of WENO5 RK3 advections (op_advection per member): each RK stage of all members as
+// one launch, `steps` steps of each member's device time step
+int check_advect_member(const vsl_advect_f32 &a)
+{
+    if (any_null(a.F, a.vx, a.vy, a.vz, a.dt)) return VSL_ERR_NULL;
+    if (int st = check_grid(a.rows, a.cols, a.pges, a.dx, a.dy, a.dz)) return st;
+    const Grid g = make_grid(a.rows, a.cols, a.pges, a.dx, a.dy, a.dz);
+    return check_ws(VSL_OP_ADVECTION, g, sizeof(float), a.workspace, a.workspace_bytes);
+}
+
+int advect_batch_chunk(const vsl_advect_f32 *mem, int n, int steps, cudaStream_t s)
+{
+    ReinitWork<float> w[TILED_BATCH_MAX];
+    TiledStage st[TILED_BATCH_MAX];
+    Grid grids[TILED_BATCH_MAX];
+    for (int v = 0; v < n; ++v) {
+        const vsl_advect_f32 &a = mem[v];
+        grids[v] = make_grid(a.rows, a.cols, a.pges, a.dx, a.dy, a.dz);
+        Bump bump(a.workspace);
+        w[v] = carve_reinit<float>(bump, grids[v], false);
+    }
+    for (int it = 0; it < steps; ++it) {
+        for (int stage = 0; stage < 3; ++stage) {
+            for (int v = 0; v < n; ++v) {
+                const vsl_advect_f32 &a = mem[v];
+                float *in = stage == 0 ? a.F : (stage == 1 ? w[v].b : w[v].c);
+                float *out = stage == 0 ? w[v].b : (stage == 1 ? w[v].c : a.F);
+                st[v] = TiledStage{in, a.F, out, nullptr, Ptr6<const float>{}, BandShadow{},
+                                   Ptr3<const float>{{a.vx, a.vy, a.vz}}, nullptr, a.dt, w[v].band.q,
+                                   NodeList{nullptr, nullptr}, stage, w[v].band.seq++};
+            }
+            VSL_TRY(launch_tiled_batch(2, false, st, grids, n, s));
+        }
+    }
+    return VSL_OK;
+}
+
+int op_advect_batch(const vsl_advect_f32 *mem, int count, int steps, cudaStream_t s)
+{
+    if (mem == nullptr && count > 0) return VSL_ERR_NULL;
+    if (count < 0 || steps < 0) return VSL_ERR_VALUE;
+    for (int v = 0; v < count; ++v)
+        if (int st = check_advect_member(mem[v])) return st;
+    for (int v0 = 0; v0 < count; v0 += TILED_BATCH_MAX)
+        if (int st = advect_batch_chunk(mem + v0, std::min(TILED_BATCH_MAX, count - v0), steps, s)) return st;
+    return VSL_OK;
+}
+
 int op_reinit_batch(const vsl_reinit_f32 *mem, int count, int iteration, cudaStream_t s)
 {
     if (mem == nullptr && count > 0) return VSL_ERR_NULL;
@@ -1558,6 +1606,11 @@ int vsl_weno5_rk3_reinitialization_batch_f32(const vsl_reinit_f32 *members, int 
 int vsl_weno5_rk3_extend_batch_f32(const vsl_extend_f32 *members, int count, int iteration, vsl_stream_t stream)
 {
     return op_extend_batch(members, count, iteration, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int vsl_weno5_rk3_advection_batch_f32(const vsl_advect_f32 *members, int count, int steps, vsl_stream_t stream)
+{
+    return op_advect_batch(members, count, steps, reinterpret_cast<cudaStream_t>(stream));
 }
 
 const char *vsl_status_string(int status)

@@ -419,6 +419,24 @@ typedef struct {
 } vsl_extend_f32;
 int vsl_weno5_rk3_extend_batch_f32(const vsl_extend_f32 *members, int count, int iteration, vsl_stream_t stream);
 
+/* A batch of WENO5 RK3 advections, FP32 mixed form (per member as
+ * vsl_weno5_rk3_advection_f32: `steps` steps of the member's device time step *dt along its
+ * velocity).  Each member has its own field F (advanced in place), velocity, time step and
+ * workspace of vsl_workspace_bytes(VSL_OP_ADVECTION, its grid, 4); each RK stage of all
+ * the members runs as one launch, 64 members at a time.  Results are bitwise those of
+ * vsl_weno5_rk3_advection_f32 called per member.  `members` is a HOST array read during
+ * the call; the pointers in it are device pointers. */
+typedef struct {
+    float *F;
+    const float *vx, *vy, *vz;
+    const double *dt;
+    int rows, cols, pges;
+    double dx, dy, dz;
+    void *workspace;
+    size_t workspace_bytes;
+} vsl_advect_f32;
+int vsl_weno5_rk3_advection_batch_f32(const vsl_advect_f32 *members, int count, int steps, vsl_stream_t stream);
+
 /* ref: +SD/@SDF3/ENORK2Reinitialization.m:3-45.  Quadratic-ENO distances recomputed from
  * F, then `iteration` Heun RK2 pseudo-steps F1 = F - step(F), F = (F + F1 - step(F1)) / 2
  * with the mask and dt = 0.3 min(distances) of F at the start. */

@@ -1,6 +1,6 @@
 """Argument checks of the batch of vesicle steps (vsl_vesicle_step_batch_f32) and of the batch
-of WENO5 RK3 reinitializations and extensions (vsl_weno5_rk3_reinitialization_batch_f32,
-vsl_weno5_rk3_extend_batch_f32) without a GPU:
+of WENO5 RK3 reinitializations, extensions and advections
+(vsl_weno5_rk3_{reinitialization,extend,advection}_batch_f32) without a GPU:
 every check runs on the host before any CUDA call, so bad descriptors and arguments are
 rejected with their status codes and an empty batch is a no-op."""
 import ctypes
@@ -119,3 +119,36 @@ def test_extend_batch_rejects_bad_arguments(vsl):
         arr = (L.ExtendF32 * 3)(bad, good, good)
         assert extend_call(vsl, arr, 3) == status
     assert extend_call(vsl, None, 0) == VSL_OK
+
+
+# ---- the batch of WENO5 RK3 advections (vsl_weno5_rk3_advection_batch_f32) ----
+
+
+def advect_member(rows=40, cols=36, pges=32, h=0.05, ws=FAKE * 16, nbytes=1 << 30, **over):
+    d = L.AdvectF32()
+    d.F = d.vx = d.vy = d.vz = d.dt = FAKE
+    d.rows, d.cols, d.pges = rows, cols, pges
+    d.dx = d.dy = d.dz = h
+    d.workspace, d.workspace_bytes = ws, nbytes
+    for k, v in over.items():
+        setattr(d, k, v)
+    return d
+
+
+def advect_call(vsl, arr, count, steps=1):
+    ptr = ctypes.addressof(arr) if arr is not None else None
+    return vsl.raw("vsl_weno5_rk3_advection_batch_f32", ptr, count, steps, None)
+
+
+def test_advect_batch_rejects_bad_arguments(vsl):
+    arr = (L.AdvectF32 * 1)(advect_member())
+    assert advect_call(vsl, None, 1) == VSL_ERR_NULL
+    assert advect_call(vsl, arr, -2) == VSL_ERR_VALUE
+    assert advect_call(vsl, arr, 1, steps=-1) == VSL_ERR_VALUE
+    good = advect_member()
+    for bad, status in ((advect_member(F=None), VSL_ERR_NULL), (advect_member(vy=None), VSL_ERR_NULL),
+                        (advect_member(dt=None), VSL_ERR_NULL), (advect_member(rows=-1), VSL_ERR_SHAPE),
+                        (advect_member(dy=0.0), VSL_ERR_VALUE), (advect_member(ws=None), VSL_ERR_WORKSPACE)):
+        arr = (L.AdvectF32 * 2)(good, bad)
+        assert advect_call(vsl, arr, 2) == status
+    assert advect_call(vsl, None, 0) == VSL_OK

@@ -185,3 +185,22 @@ def test_extend_batched_matches_per_object(pkg, vsl, count):
     got = B.extend_batched(maps, fields, 8)
     for m, C, g in zip(maps, fields, got):
         assert np.array_equal(host(g), host(m.WENO5RK3Extend(C, 8)))
+
+
+@pytest.mark.parametrize("count", [5, 66])
+def test_advect_batched_matches_per_object(pkg, vsl, count):
+    """vsl_weno5_rk3_advection_batch_f32 (each RK stage of every member as one launch; 66
+    members run as chunks of 64 and 2) against each object's own WENO5RK3Advection, two steps
+    of a rotation-plus-shear velocity with each member's own time step: bitwise."""
+    edges = (24, 32, 40) if count < 10 else (16, 20, 24)
+    maps, vels, dts = [], [], []
+    for q, (xv, yv, zv, axes) in enumerate(S.random_vesicles(count, seed=8, edges=edges)):
+        x, y, z, F = S.ellipsoid_field(xv, yv, zv, axes)
+        m = pkg.SDF3(pkg.GD3(x, y, z), Val=F, precision="f32")
+        maps.append(m)
+        vels.append((dev(-y + 0.2 * z), dev(x), dev(0.3 * np.sin(2 * x))))
+        dts.append(0.3 * float(xv[1] - xv[0]) * (1 + 0.01 * q))
+    fields = [m.F for m in maps]
+    got = B.advect_batched(maps, fields, vels, dts, 2)
+    for m, F, v, dt, g in zip(maps, fields, vels, dts, got):
+        assert np.array_equal(host(g), host(m.WENO5RK3Advection(F, *v, dt, 2)))
