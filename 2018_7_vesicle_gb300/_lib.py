@@ -54,7 +54,18 @@ SIGNATURES = {
     "vsl_weno5_rk3_extend_batch_f32": "pii" + "s",
     # a batch of WENO5 RK3 advections: host array of AdvectF32, count, steps
     "vsl_weno5_rk3_advection_batch_f32": "pii" + "s",
+    # batches of closest-point surface redistances: host array of RedistanceF32, count, iter1, iter2
+    "vsl_weno5_rk3_surface_redistance_batch_f32": "piii" + "s",
+    "vsl_wenork3_surface_redistance_batch_f32": "piii" + "s",
 }
+
+
+class RedistanceF32(ctypes.Structure):
+    """vsl_redistance_f32 of the C ABI: one member of vsl_*_surface_redistance_batch_f32."""
+
+    _fields_ = [("A", ctypes.c_void_p), ("F", ctypes.c_void_p), ("rows", ctypes.c_int), ("cols", ctypes.c_int),
+                ("pges", ctypes.c_int), ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dz", ctypes.c_double),
+                ("workspace", ctypes.c_void_p), ("workspace_bytes", ctypes.c_size_t)]
 
 
 class AdvectF32(ctypes.Structure):

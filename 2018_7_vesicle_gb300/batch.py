@@ -13,10 +13,11 @@ Two batch steps:
 
 The vesicles share nothing: each has its own field, distances and workspace.
 
-`reinitialize_batched`, `extend_batched` and `advect_batched` (FP32) run
-WENO5RK3Reinitialization, WENO5RK3Extend and WENO5RK3Advection on a list of level sets the
-same way (vsl_weno5_rk3_{reinitialization,extend,advection}_batch_f32), bitwise the
-per-object calls.
+`reinitialize_batched`, `extend_batched`, `advect_batched` and `redistance_batched` (FP32)
+run WENO5RK3Reinitialization, WENO5RK3Extend, WENO5RK3Advection and the closest-point
+surface redistance (WENO5 or WENORK3 form) on a list of level sets the same way
+(vsl_weno5_rk3_{reinitialization,extend,advection}_batch_f32,
+vsl_{weno5_rk3,wenork3}_surface_redistance_batch_f32), bitwise the per-object calls.
 """
 from __future__ import annotations
 
@@ -24,7 +25,7 @@ import ctypes
 
 import torch
 
-from ._lib import AdvectF32, ExtendF32, ReinitF32, VesicleF32, lib
+from ._lib import AdvectF32, ExtendF32, RedistanceF32, ReinitF32, VesicleF32, lib
 from .sdf3 import SDF3
 
 
@@ -258,4 +259,30 @@ def advect_batched(maps: list[SDF3], fields, velocities, dts, steps: int = 1):
         d.workspace, d.workspace_bytes = ws.data_ptr(), ws.numel()
     lib().call("vsl_weno5_rk3_advection_batch_f32", ctypes.addressof(arr), len(maps), int(steps),
                torch.cuda.current_stream().cuda_stream)
+    return outs
+
+
+def redistance_batched(maps: list[SDF3], fields, iter1: int, iter2: int, eno3: bool = False):
+    """WENO5RK3ClosetPointSurfaceRedistance(A, iter1, iter2) (eno3: the WENORK3 form) of every
+    (level set, field) pair on the level set's zero set, each RK stage of all of them as one
+    launch (vsl_weno5_rk3_surface_redistance_batch_f32 / vsl_wenork3_surface_redistance_batch_f32;
+    FP32 objects).  Returns new fields, bitwise those of the per-object method."""
+    maps = list(maps)
+    if len(maps) != len(fields):
+        raise ValueError("one field per level set")
+    if any(m.precision != "f32" for m in maps):
+        raise ValueError("redistance_batched runs the FP32 mixed form")
+    op = "surface_redistance_eno3" if eno3 else "surface_redistance"
+    fn = "vsl_wenork3_surface_redistance_batch_f32" if eno3 else "vsl_weno5_rk3_surface_redistance_batch_f32"
+    outs = [m._field(A).clone() for m, A in zip(maps, fields)]
+    arr = (RedistanceF32 * len(maps))()
+    keep = []
+    for d, m, out in zip(arr, maps, outs):
+        ws = m.workspace(op)
+        keep.append(ws)
+        d.A, d.F = out.data_ptr(), m.F.data_ptr()
+        d.rows, d.cols, d.pges = m.GD3.Size
+        d.dx, d.dy, d.dz = m.GD3.Dx, m.GD3.Dy, m.GD3.Dz
+        d.workspace, d.workspace_bytes = ws.data_ptr(), ws.numel()
+    lib().call(fn, ctypes.addressof(arr), len(maps), int(iter1), int(iter2), torch.cuda.current_stream().cuda_stream)
     return outs

@@ -1219,6 +1219,110 @@ int op_advect_batch(const vsl_advect_f32 *mem, int count, int steps, cudaStream_
     return VSL_OK;
 }
 
+// A batch of closest-point surface redistances (op_redistance per member, WENO5 or WENORK3
+// form): the set-up passes and each extension loop's crossing values and shadow per member
+// on its lane; each RK stage of the extensions and of the reinitialization of all members
+// as one launch
+int check_redistance_member(const vsl_redistance_f32 &r, int op)
+{
+    if (any_null(r.A, r.F)) return VSL_ERR_NULL;
+    if (int st = check_grid(r.rows, r.cols, r.pges, r.dx, r.dy, r.dz)) return st;
+    const Grid g = make_grid(r.rows, r.cols, r.pges, r.dx, r.dy, r.dz);
+    return check_ws(op, g, sizeof(float), r.workspace, r.workspace_bytes);
+}
+
+int redistance_batch_chunk(const vsl_redistance_f32 *mem, int n, int iter1, int iter2, bool eno3, cudaStream_t s)
+{
+    RedistWork<float> w[TILED_BATCH_MAX];
+    TiledStage st[TILED_BATCH_MAX];
+    Grid grids[TILED_BATCH_MAX];
+    float *src[TILED_BATCH_MAX];
+    for (int v = 0; v < n; ++v) {
+        const vsl_redistance_f32 &r = mem[v];
+        grids[v] = make_grid(r.rows, r.cols, r.pges, r.dx, r.dy, r.dz);
+        Bump bump(r.workspace);
+        w[v] = carve_redist<float>(bump, grids[v]);
+    }
+    Fan fan{batch_lanes(s), s};
+    // set-up (ClosetPointSurfaceRedistance.m:15-74): A's distances and classes, F's distances,
+    // normals and classes
+    VSL_TRY(fan.open());
+    for (int v = 0; v < n; ++v) {
+        const cudaStream_t ls = fan.lane(v);
+        RedistWork<float> &rw = w[v];
+        VSL_TRY(launch_set_distance<float>(mem[v].A, rw.re.dist, grids[v], !eno3, rw.re.edges, ls));
+        VSL_TRY(launch_classify<float>(mem[v].A, cview(rw.re.dist), rw.re.flags, NodeList{nullptr, nullptr},
+                                       grids[v], ls));
+        VSL_TRY(launch_set_distance<float>(mem[v].F, rw.ext.dist, grids[v], !eno3, rw.ext.edges, ls));
+        if (int r = extend_setup<float>(mem[v].F, cview(rw.ext.dist), rw.ext, grids[v], eno3, 1e-14, ls)) return r;
+        if (int r = band_reset(rw.re.band, ls)) return r;
+    }
+    VSL_TRY(fan.close());
+    // iter2 extension pseudo-steps of every member's src[v] off F (extend_loop per member)
+    auto extend_all = [&]() -> int {
+        VSL_TRY(fan.open());
+        for (int v = 0; v < n; ++v) {
+            const cudaStream_t ls = fan.lane(v);
+            ExtendWork<float> &e = w[v].ext;
+            VSL_TRY(launch_crossing_mixed(src[v], cview(e.dist), e.cp64, e.flagged, grids[v], eno3, ls));
+            VSL_TRY(launch_shadow_init(src[v], e.sh[0], e.flagged, ls));
+            if (int r = band_reset(e.band, ls)) return r;
+        }
+        VSL_TRY(fan.close());
+        for (int it = 0; it < iter2; ++it) {
+            for (int stage = 0; stage < 3; ++stage) {
+                for (int v = 0; v < n; ++v) {
+                    ExtendWork<float> &e = w[v].ext;
+                    float *C = src[v];
+                    float *in = stage == 0 ? C : (stage == 1 ? e.b : e.c);
+                    float *out = stage == 0 ? e.b : (stage == 1 ? e.c : C);
+                    double *s_out = e.sh[stage == 2 ? 0 : stage + 1];
+                    st[v] = TiledStage{in, C, out, e.flags, cview(e.dist),
+                                       BandShadow{e.sh[stage], e.sh[0], s_out, cview(e.cp64)}, cview3(e.v), nullptr,
+                                       nullptr, e.band.q, e.flagged, stage, e.band.seq++};
+                }
+                VSL_TRY(launch_tiled_batch(1, eno3, st, grids, n, s));
+            }
+        }
+        return VSL_OK;
+    };
+    // one reinitialization stage of every member: stage input src[v] into out(v)
+    auto reinit_all = [&](int stage) -> int {
+        for (int v = 0; v < n; ++v) {
+            ReinitWork<float> &re = w[v].re;
+            float *A = mem[v].A;
+            float *out = stage == 0 ? re.b : (stage == 1 ? re.c : A);
+            st[v] = TiledStage{src[v], A, out, re.flags, cview(re.dist), BandShadow{}, Ptr3<const float>{}, nullptr,
+                               nullptr, re.band.q, NodeList{nullptr, nullptr}, stage, re.band.seq++};
+        }
+        VSL_TRY(launch_tiled_batch(0, eno3, st, grids, n, s));
+        return VSL_OK;
+    };
+    for (int it = 0; it < iter1; ++it) {
+        for (int stage = 0; stage < 3; ++stage) {
+            for (int v = 0; v < n; ++v)
+                src[v] = stage == 0 ? mem[v].A : (stage == 1 ? w[v].re.b : w[v].re.c);
+            if (int r = extend_all()) return r;
+            if (int r = reinit_all(stage)) return r;
+        }
+    }
+    for (int v = 0; v < n; ++v) src[v] = mem[v].A;
+    return extend_all();
+}
+
+int op_redistance_batch(const vsl_redistance_f32 *mem, int count, int iter1, int iter2, bool eno3, cudaStream_t s)
+{
+    if (mem == nullptr && count > 0) return VSL_ERR_NULL;
+    if (count < 0 || iter1 < 0 || iter2 < 0) return VSL_ERR_VALUE;
+    const int op = eno3 ? VSL_OP_SURFACE_REDISTANCE_ENO3 : VSL_OP_SURFACE_REDISTANCE;
+    for (int v = 0; v < count; ++v)
+        if (int st = check_redistance_member(mem[v], op)) return st;
+    for (int v0 = 0; v0 < count; v0 += TILED_BATCH_MAX)
+        if (int st = redistance_batch_chunk(mem + v0, std::min(TILED_BATCH_MAX, count - v0), iter1, iter2, eno3, s))
+            return st;
+    return VSL_OK;
+}
+
 int op_reinit_batch(const vsl_reinit_f32 *mem, int count, int iteration, cudaStream_t s)
 {
     if (mem == nullptr && count > 0) return VSL_ERR_NULL;
@@ -1611,6 +1715,18 @@ int vsl_weno5_rk3_extend_batch_f32(const vsl_extend_f32 *members, int count, int
 int vsl_weno5_rk3_advection_batch_f32(const vsl_advect_f32 *members, int count, int steps, vsl_stream_t stream)
 {
     return op_advect_batch(members, count, steps, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int vsl_weno5_rk3_surface_redistance_batch_f32(const vsl_redistance_f32 *members, int count, int iter1, int iter2,
+                                               vsl_stream_t stream)
+{
+    return op_redistance_batch(members, count, iter1, iter2, false, reinterpret_cast<cudaStream_t>(stream));
+}
+
+int vsl_wenork3_surface_redistance_batch_f32(const vsl_redistance_f32 *members, int count, int iter1, int iter2,
+                                             vsl_stream_t stream)
+{
+    return op_redistance_batch(members, count, iter1, iter2, true, reinterpret_cast<cudaStream_t>(stream));
 }
 
 const char *vsl_status_string(int status)

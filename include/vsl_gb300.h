@@ -437,6 +437,29 @@ typedef struct {
 } vsl_advect_f32;
 int vsl_weno5_rk3_advection_batch_f32(const vsl_advect_f32 *members, int count, int steps, vsl_stream_t stream);
 
+/* A batch of closest-point surface redistances, FP32 mixed form (ref, per member:
+ * +SD/@SDF3/WENO5RK3ClosetPointSurfaceRedistance.m:4-157, or for the _wenork3_ entry
+ * +SD/@SDF3/WENORK3ClosetPointSurfaceRedistance.m:4-152; as
+ * vsl_weno5_rk3_surface_redistance_f32 / vsl_wenork3_surface_redistance_f32).  Each member
+ * has its own A (redistanced in place), F and workspace of vsl_workspace_bytes(
+ * VSL_OP_SURFACE_REDISTANCE or VSL_OP_SURFACE_REDISTANCE_ENO3, its grid, 4); each RK
+ * stage of the extensions and of the reinitialization of all the members runs as one
+ * launch, 64 members at a time.  Results are bitwise those of the per-member calls.
+ * `members` is a HOST array read during the call; the pointers in it are device
+ * pointers. */
+typedef struct {
+    float *A;
+    const float *F;
+    int rows, cols, pges;
+    double dx, dy, dz;
+    void *workspace;
+    size_t workspace_bytes;
+} vsl_redistance_f32;
+int vsl_weno5_rk3_surface_redistance_batch_f32(const vsl_redistance_f32 *members, int count, int iter1, int iter2,
+                                               vsl_stream_t stream);
+int vsl_wenork3_surface_redistance_batch_f32(const vsl_redistance_f32 *members, int count, int iter1, int iter2,
+                                             vsl_stream_t stream);
+
 /* ref: +SD/@SDF3/ENORK2Reinitialization.m:3-45.  Quadratic-ENO distances recomputed from
  * F, then `iteration` Heun RK2 pseudo-steps F1 = F - step(F), F = (F + F1 - step(F1)) / 2
  * with the mask and dt = 0.3 min(distances) of F at the start. */

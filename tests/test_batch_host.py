@@ -1,6 +1,7 @@
 """Argument checks of the batch of vesicle steps (vsl_vesicle_step_batch_f32) and of the batch
-of WENO5 RK3 reinitializations, extensions and advections
-(vsl_weno5_rk3_{reinitialization,extend,advection}_batch_f32) without a GPU:
+of WENO5 RK3 reinitializations, extensions, advections and surface redistances
+(vsl_weno5_rk3_{reinitialization,extend,advection}_batch_f32,
+vsl_{weno5_rk3,wenork3}_surface_redistance_batch_f32) without a GPU:
 every check runs on the host before any CUDA call, so bad descriptors and arguments are
 rejected with their status codes and an empty batch is a no-op."""
 import ctypes
@@ -152,3 +153,37 @@ def test_advect_batch_rejects_bad_arguments(vsl):
         arr = (L.AdvectF32 * 2)(good, bad)
         assert advect_call(vsl, arr, 2) == status
     assert advect_call(vsl, None, 0) == VSL_OK
+
+
+# ---- the batches of surface redistances (vsl_{weno5_rk3,wenork3}_surface_redistance_batch_f32) ----
+
+
+def redistance_member(rows=40, cols=36, pges=32, h=0.05, ws=FAKE * 16, nbytes=1 << 30, **over):
+    d = L.RedistanceF32()
+    d.A = d.F = FAKE
+    d.rows, d.cols, d.pges = rows, cols, pges
+    d.dx = d.dy = d.dz = h
+    d.workspace, d.workspace_bytes = ws, nbytes
+    for k, v in over.items():
+        setattr(d, k, v)
+    return d
+
+
+def test_redistance_batches_reject_bad_arguments(vsl):
+    for fn in ("vsl_weno5_rk3_surface_redistance_batch_f32", "vsl_wenork3_surface_redistance_batch_f32"):
+        def call(arr, count, it1=2, it2=3):
+            ptr = ctypes.addressof(arr) if arr is not None else None
+            return vsl.raw(fn, ptr, count, it1, it2, None)
+
+        arr = (L.RedistanceF32 * 1)(redistance_member())
+        assert call(None, 1) == VSL_ERR_NULL
+        assert call(arr, -1) == VSL_ERR_VALUE
+        assert call(arr, 1, it1=-1) == VSL_ERR_VALUE
+        assert call(arr, 1, it2=-1) == VSL_ERR_VALUE
+        good = redistance_member()
+        for bad, status in ((redistance_member(A=None), VSL_ERR_NULL), (redistance_member(F=None), VSL_ERR_NULL),
+                            (redistance_member(pges=0), VSL_ERR_SHAPE), (redistance_member(dx=0.0), VSL_ERR_VALUE),
+                            (redistance_member(nbytes=64), VSL_ERR_WORKSPACE)):
+            arr = (L.RedistanceF32 * 2)(good, bad)
+            assert call(arr, 2) == status
+        assert call(None, 0) == VSL_OK

@@ -204,3 +204,21 @@ def test_advect_batched_matches_per_object(pkg, vsl, count):
     got = B.advect_batched(maps, fields, vels, dts, 2)
     for m, F, v, dt, g in zip(maps, fields, vels, dts, got):
         assert np.array_equal(host(g), host(m.WENO5RK3Advection(F, *v, dt, 2)))
+
+
+@pytest.mark.parametrize("eno3", [False, True])
+@pytest.mark.parametrize("count", [5, 66])
+def test_redistance_batched_matches_per_object(pkg, vsl, count, eno3):
+    """vsl_{weno5_rk3,wenork3}_surface_redistance_batch_f32 (each RK stage of every member's
+    extensions and reinitialization as one launch; 66 members run as chunks of 64 and 2)
+    against each object's own closest-point surface redistance: bitwise."""
+    edges = (24, 32, 40) if count < 10 else (16, 20, 24)
+    maps, fields = [], []
+    for xv, yv, zv, axes in S.random_vesicles(count, seed=10, edges=edges):
+        x, y, z, F = S.ellipsoid_field(xv, yv, zv, axes)
+        maps.append(pkg.SDF3(pkg.GD3(x, y, z), Val=F, precision="f32"))
+        fields.append(dev(np.exp(z) - 1 + 0.1 * x))
+    got = B.redistance_batched(maps, fields, 2, 3, eno3=eno3)
+    for m, A, g in zip(maps, fields, got):
+        method = m.WENORK3ClosetPointSurfaceRedistance if eno3 else m.WENO5RK3ClosetPointSurfaceRedistance
+        assert np.array_equal(host(g), host(method(A, 2, 3)))
