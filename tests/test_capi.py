@@ -28,6 +28,21 @@ def test_header_declares_entry_points():
     assert len(d) >= 30
 
 
+def test_header_is_plain_c(tmp_path):
+    """The header serves C callers (a MEX gateway, cgo): it compiles as strict C99."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "use_header.c"
+    src.write_text('#include "vsl_gb300.h"\nint main(void) { return VSL_OP_SURFACE_REDISTANCE_ENO3 == 20 ? 0 : 1; }\n')
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I" + os.path.dirname(HEADER),
+                        "-c", str(src), "-o", str(tmp_path / "use_header.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_library_exports_every_declared_symbol(vsl):
     lib = ctypes.CDLL(vsl.path)
     for name in declared():
