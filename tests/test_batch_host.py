@@ -187,3 +187,29 @@ def test_redistance_batches_reject_bad_arguments(vsl):
             arr = (L.RedistanceF32 * 2)(good, bad)
             assert call(arr, 2) == status
         assert call(None, 0) == VSL_OK
+
+
+def test_python_batch_wrappers_check_their_arguments():
+    """batch.*_batched reject mismatched lists and FP64 objects before any device work."""
+    import types
+
+    import pytest
+
+    Bm = importlib.import_module("2018_7_vesicle_gb300.batch")
+    f32, f64 = types.SimpleNamespace(precision="f32"), types.SimpleNamespace(precision="f64")
+    with pytest.raises(ValueError, match="one field"):
+        Bm.reinitialize_batched([f32, f32], [None], 3)
+    with pytest.raises(ValueError, match="FP32"):
+        Bm.reinitialize_batched([f64], [None], 3)
+    with pytest.raises(ValueError, match="one field"):
+        Bm.extend_batched([f32], [None, None], 3)
+    with pytest.raises(ValueError, match="FP32"):
+        Bm.extend_batched([f32, f64], [None, None], 3)
+    with pytest.raises(ValueError, match="one field, velocity and time step"):
+        Bm.advect_batched([f32], [None], [], [0.1])
+    with pytest.raises(ValueError, match="FP32"):
+        Bm.advect_batched([f64], [None], [None], [0.1])
+    with pytest.raises(ValueError, match="one field"):
+        Bm.redistance_batched([f32], [], 2, 3)
+    with pytest.raises(ValueError, match="FP32"):
+        Bm.redistance_batched([f64], [None], 2, 3, eno3=True)
