@@ -2,6 +2,10 @@
 and linked into ``lib/libvsl_gb300.so`` (in-tree, git-ignored).
 
     __graft_entry__.build()  (or the package's build())
+
+``python 2018_7_vesicle_gb300/_build.py --nvtx`` rebuilds every object with NVTX ranges around
+the C-ABI operations (-DVSL_NVTX, for timeline profilers); run it without ``--nvtx`` (it
+rebuilds every object too) to return to the default library.
 """
 from __future__ import annotations
 
@@ -80,8 +84,10 @@ def build(force: bool = False, extra_flags=()) -> str:
     if _stale(LIB, objs):
         tmp = LIB + ".tmp"
         cuda_lib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc()))), "lib64")
-        r = subprocess.run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcufft", "-Xlinker", "-rpath," + cuda_lib],
-                           capture_output=True, text=True)
+        # the NVTX ranges' loader of a profiler's injection library needs dlopen
+        libdl = ["-ldl"] if "-DVSL_NVTX" in extra_flags else []
+        r = subprocess.run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcufft", *libdl, "-Xlinker",
+                            "-rpath," + cuda_lib], capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")
         os.replace(tmp, LIB)
@@ -89,4 +95,11 @@ def build(force: bool = False, extra_flags=()) -> str:
 
 
 if __name__ == "__main__":
-    print(build())
+    import sys
+
+    if len(sys.argv) > 1:
+        # an explicit variant: rebuild every object with its flags
+        shutil.rmtree(os.path.join(OUT_DIR, "obj"), ignore_errors=True)
+        print(build(force=True, extra_flags=["-DVSL_NVTX"] if "--nvtx" in sys.argv[1:] else []))
+    else:
+        print(build())

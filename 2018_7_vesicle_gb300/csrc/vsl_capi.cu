@@ -470,6 +470,7 @@ template <typename T>
 int op_set_distance(const T *F, T *xpr, T *xpl, T *ypf, T *ypb, T *zpu, T *zpd, int rows, int cols, int pges,
                     double dx, double dy, double dz, void *ws, size_t bytes, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(F, xpr, xpl, ypf, ypb, zpu, zpd)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     Grid g = make_grid(rows, cols, pges, dx, dy, dz);
@@ -485,6 +486,7 @@ int op_reinit_weno5(T *F, int iteration, const T *xpr, const T *xpl, const T *yp
                     const T *zpd, int rows, int cols, int pges, double dx, double dy, double dz, void *ws,
                     size_t bytes, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(F, xpr, xpl, ypf, ypb, zpu, zpd)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     if (iteration < 0) return VSL_ERR_VALUE;
@@ -501,6 +503,7 @@ template <typename T>
 int op_reinit_eno3(T *F, int iteration, int rows, int cols, int pges, double dx, double dy, double dz, void *ws,
                    size_t bytes, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(F)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     if (iteration < 0) return VSL_ERR_VALUE;
@@ -519,6 +522,7 @@ int op_extend_weno5(T *C, int iteration, const T *F, const T *xpr, const T *xpl,
                     const T *zpu, const T *zpd, int rows, int cols, int pges, double dx, double dy, double dz,
                     void *ws, size_t bytes, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(C, F, xpr, xpl, ypf, ypb, zpu, zpd)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     if (iteration < 0) return VSL_ERR_VALUE;
@@ -535,6 +539,7 @@ template <typename T>
 int op_extend_eno3(T *C, int iteration, const T *F, int rows, int cols, int pges, double dx, double dy, double dz,
                    void *ws, size_t bytes, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(C, F)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     if (iteration < 0) return VSL_ERR_VALUE;
@@ -556,6 +561,7 @@ template <typename T>
 int op_redistance(T *A, int iter1, int iter2, const T *F, int rows, int cols, int pges, double dx, double dy,
                   double dz, bool eno3, void *ws, size_t bytes, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(A, F)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     if (iter1 < 0 || iter2 < 0) return VSL_ERR_VALUE;
@@ -599,6 +605,7 @@ template <typename T>
 int op_area_volume(const T *F, double *av, int rows, int cols, int pges, double dx, double dy, double dz, void *ws,
                    size_t bytes, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(F, av)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     Grid g = make_grid(rows, cols, pges, dx, dy, dz);
@@ -620,6 +627,7 @@ template <typename T>
 int op_aux_toolbox(const T *A, const T *F, T *const *out, int rows, int cols, int pges, double dx, double dy,
                    double dz, void *ws, size_t bytes, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(A, F, out)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     Grid g = make_grid(rows, cols, pges, dx, dy, dz);
@@ -647,6 +655,7 @@ int op_masked_integral(const T *F, const T *A, const T *f0, const T *f1, const T
                        double *result, int rows, int cols, int pges, double dx, double dy, double dz, void *ws,
                        size_t bytes, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(F, result)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     Grid g = make_grid(rows, cols, pges, dx, dy, dz);
@@ -664,6 +673,7 @@ template <typename T>
 int op_advection(T *F, const T *vx, const T *vy, const T *vz, const double *dt, int steps, int rows, int cols,
                  int pges, double dx, double dy, double dz, void *ws, size_t bytes, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(F, vx, vy, vz, dt)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     if (steps < 0) return VSL_ERR_VALUE;
@@ -679,6 +689,7 @@ int op_vesicle_step(T *F, T *xpr, T *xpl, T *ypf, T *ypb, T *zpu, T *zpd, int ex
                     double cfl, double *info, int rows, int cols, int pges, double dx, double dy, double dz, void *ws,
                     size_t bytes, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(F, xpr, xpl, ypf, ypb, zpu, zpd, info)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     if (ext_iters < 0 || reinit_iters < 0 || !(cfl > 0)) return VSL_ERR_VALUE;
@@ -816,6 +827,7 @@ int op_reinit_tol(T *F, int max_iters, double tol, double band, const T *xpr, co
                   const T *ypb, const T *zpu, const T *zpd, int rows, int cols, int pges, double dx, double dy,
                   double dz, int *status, double *history, void *ws, size_t bytes, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(F, xpr, xpl, ypf, ypb, zpu, zpd, status)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     if (max_iters < 0 || !(tol >= 0) || !(band > 0)) return VSL_ERR_VALUE;
@@ -1052,6 +1064,7 @@ int batch_chunk(const vsl_vesicle_f32 *ves, int n, int ext_iters, int reinit_ite
 int op_vesicle_step_batch(const vsl_vesicle_f32 *ves, int count, int ext_iters, int reinit_iters, double cfl,
                           cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (ves == nullptr && count > 0) return VSL_ERR_NULL;
     if (count < 0 || ext_iters < 0 || reinit_iters < 0 || !(cfl > 0)) return VSL_ERR_VALUE;
     for (int v = 0; v < count; ++v)
@@ -1162,6 +1175,7 @@ int extend_batch_chunk(const vsl_extend_f32 *mem, int n, int iteration, cudaStre
 
 int op_extend_batch(const vsl_extend_f32 *mem, int count, int iteration, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (mem == nullptr && count > 0) return VSL_ERR_NULL;
     if (count < 0 || iteration < 0) return VSL_ERR_VALUE;
     for (int v = 0; v < count; ++v)
@@ -1210,6 +1224,7 @@ int advect_batch_chunk(const vsl_advect_f32 *mem, int n, int steps, cudaStream_t
 
 int op_advect_batch(const vsl_advect_f32 *mem, int count, int steps, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (mem == nullptr && count > 0) return VSL_ERR_NULL;
     if (count < 0 || steps < 0) return VSL_ERR_VALUE;
     for (int v = 0; v < count; ++v)
@@ -1312,6 +1327,7 @@ int redistance_batch_chunk(const vsl_redistance_f32 *mem, int n, int iter1, int 
 
 int op_redistance_batch(const vsl_redistance_f32 *mem, int count, int iter1, int iter2, bool eno3, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (mem == nullptr && count > 0) return VSL_ERR_NULL;
     if (count < 0 || iter1 < 0 || iter2 < 0) return VSL_ERR_VALUE;
     const int op = eno3 ? VSL_OP_SURFACE_REDISTANCE_ENO3 : VSL_OP_SURFACE_REDISTANCE;
@@ -1325,6 +1341,7 @@ int op_redistance_batch(const vsl_redistance_f32 *mem, int count, int iter1, int
 
 int op_reinit_batch(const vsl_reinit_f32 *mem, int count, int iteration, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (mem == nullptr && count > 0) return VSL_ERR_NULL;
     if (count < 0 || iteration < 0) return VSL_ERR_VALUE;
     for (int v = 0; v < count; ++v)
@@ -1361,6 +1378,7 @@ template <typename T>
 int op_reinit_enork2(T *F, int iteration, int rows, int cols, int pges, double dx, double dy, double dz, void *ws,
                      size_t bytes, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(F)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     if (iteration < 0) return VSL_ERR_VALUE;
@@ -1411,6 +1429,7 @@ template <typename T>
 int op_extend_enork2(T *C, int iteration, const T *F, int rows, int cols, int pges, double dx, double dy, double dz,
                      void *ws, size_t bytes, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(C, F)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     if (iteration < 0) return VSL_ERR_VALUE;
@@ -1430,6 +1449,7 @@ template <typename T>
 int op_redistance_enork2(T *A, int iter1, int iter2, const T *F, int rows, int cols, int pges, double dx, double dy,
                          double dz, void *ws, size_t bytes, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(A, F)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     if (iter1 < 0 || iter2 < 0) return VSL_ERR_VALUE;
@@ -1464,6 +1484,7 @@ int op_redistance_enork2(T *A, int iter1, int iter2, const T *F, int rows, int c
 template <typename T>
 int op_laplacian(const T *f, T *out, int rows, int cols, int pges, double dx, double dy, double dz, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(f, out)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     VSL_TRY(launch_laplacian<T>(f, out, make_grid(rows, cols, pges, dx, dy, dz), s));
@@ -1474,6 +1495,7 @@ template <typename T>
 int op_gradient(const T *f, T *fx, T *fy, T *fz, int rows, int cols, int pges, double dx, double dy, double dz,
                 cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(f, fx, fy, fz)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     VSL_TRY(launch_gradient<T>(f, fx, fy, fz, make_grid(rows, cols, pges, dx, dy, dz), s));
@@ -1484,6 +1506,7 @@ template <typename T>
 int op_smooth(const T *rhs, T *out, const double *dt, double alpha, int exact, int rows, int cols, int pges, double dx,
               double dy, double dz, void *ws, size_t bytes, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(rhs, out, dt)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     if (!(alpha >= 0)) return VSL_ERR_VALUE;
@@ -1521,6 +1544,7 @@ int op_relax_step(T *F, T *xpr, T *xpl, T *ypf, T *ypb, T *zpu, T *zpd, double A
                   double spon_c, double cfl, double alpha, int ext_iters, int reinit_iters, double *info, int rows,
                   int cols, int pges, double dx, double dy, double dz, void *ws, size_t bytes, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(F, xpr, xpl, ypf, ypb, zpu, zpd, info)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     if (!(cfl > 0) || !(alpha >= 0) || ext_iters < 0 || reinit_iters < 0) return VSL_ERR_VALUE;
@@ -1633,6 +1657,7 @@ int op_advection_adjoint(const T *F, const T *vx, const T *vy, const T *vz, cons
                          T *gvz, int rows, int cols, int pges, double dx, double dy, double dz, void *ws, size_t bytes,
                          cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(F, vx, vy, vz, dt, lam, gvx, gvy, gvz)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     Grid g = make_grid(rows, cols, pges, dx, dy, dz);
@@ -1652,6 +1677,7 @@ template <typename T>
 int op_reinit_adjoint(const T *F0, int iteration, T *lam, T *tape, int rows, int cols, int pges, double dx, double dy,
                       double dz, void *ws, size_t bytes, cudaStream_t s)
 {
+    VSL_RANGE(__func__);
     if (any_null(F0, lam, tape)) return VSL_ERR_NULL;
     if (int st = check_grid(rows, cols, pges, dx, dy, dz)) return st;
     if (iteration < 0) return VSL_ERR_VALUE;

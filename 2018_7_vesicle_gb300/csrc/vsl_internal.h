@@ -8,6 +8,23 @@
 #include "../../include/vsl_gb300.h"
 #include "vsl_device.cuh"
 
+// NVTX ranges around the C-ABI operations (named after the operation) for timeline
+// profilers; compiled in only with -DVSL_NVTX, a no-op statement otherwise
+#if defined(VSL_NVTX) && __has_include(<nvtx3/nvToolsExt.h>)
+#include <nvtx3/nvToolsExt.h>
+namespace vsl {
+struct TraceRange {
+    explicit TraceRange(const char *name) { nvtxRangePushA(name); }
+    ~TraceRange() { nvtxRangePop(); }
+    TraceRange(const TraceRange &) = delete;
+    TraceRange &operator=(const TraceRange &) = delete;
+};
+}  // namespace vsl
+#define VSL_RANGE(name) ::vsl::TraceRange vsl_trace_range_(name)
+#else
+#define VSL_RANGE(name) (void)0
+#endif
+
 namespace vsl {
 
 // thread block used by the node-parallel kernels: 32 rows x 8 columns of one page
