@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(RNT) k_laplacian(const T *__restrict__ f, T *_
 // with the periodic neighbours of the Laplacian
 template <typename T>
 __global__ void __launch_bounds__(RNT) k_gradient(const T *__restrict__ f, T *__restrict__ fx, T *__restrict__ fy,
-                                                  T *__restrict__ fz, Grid g, T dx2, T dy2, T dz2)
+                                                  T *__restrict__ fz, Grid g, T two_dx, T two_dy, T two_dz)
 {
     int i, j, k;
     long long c;
@@ -75,9 +75,9 @@ __global__ void __launch_bounds__(RNT) k_gradient(const T *__restrict__ f, T *__
     const int jp = j + 1 == g.cols ? 0 : j + 1, jm = j == 0 ? g.cols - 1 : j - 1;
     const int ip = i + 1 == g.rows ? 0 : i + 1, im = i == 0 ? g.rows - 1 : i - 1;
     const int kp = k + 1 == g.pges ? 0 : k + 1, km = k == 0 ? g.pges - 1 : k - 1;
-    fx[c] = (__ldg(f + node_index(g, i, jp, k)) - __ldg(f + node_index(g, i, jm, k))) / dx2;
-    fy[c] = (__ldg(f + node_index(g, ip, j, k)) - __ldg(f + node_index(g, im, j, k))) / dy2;
-    fz[c] = (__ldg(f + node_index(g, i, j, kp)) - __ldg(f + node_index(g, i, j, km))) / dz2;
+    fx[c] = (__ldg(f + node_index(g, i, jp, k)) - __ldg(f + node_index(g, i, jm, k))) / two_dx;
+    fy[c] = (__ldg(f + node_index(g, ip, j, k)) - __ldg(f + node_index(g, im, j, k))) / two_dy;
+    fz[c] = (__ldg(f + node_index(g, i, j, kp)) - __ldg(f + node_index(g, i, j, km))) / two_dz;
 }
 
 // NormalSpeedBend = Kappa * (Lap H + 0.5 H (H^2 - 4 K) + 2 c0 K - 0.5 c0^2 H)
